@@ -1,0 +1,179 @@
+/*
+ * picgb.h -- C ABI of the GB300 particle-in-cell step library (libpicgb.so).
+ *
+ * One run handle (`pgb_run`) owns the device state of one 2D electrostatic PIC
+ * simulation: electrons and one ion species, the charge/potential/field grids,
+ * the multigrid levels and the per-step counters.  The entry points mirror the
+ * per-step call sequence of the reference driver pic::pic_run
+ * (pic.cpp:1069-1250) and the class methods it calls, so that a host driver
+ * written against the reference can call them one for one.  Every function
+ * returns 0 on success or a negative PGB_ERR_* code; pgb_last_error() then
+ * holds a message.  No exception crosses this boundary, no torch type appears
+ * in it, and every pointer argument is a plain host pointer borrowed for the
+ * duration of the call.
+ *
+ * Units and layouts are the reference's: SI units; energies in eV where the
+ * reference uses eV; particles as 6 doubles {x, y, vx, vy, vz, weight}
+ * (particleVec.h:26-35); charge grids q as ny*nx doubles, row = y index
+ * (particle.cpp:663-858); rho and phi as [ny][nx] (fields.cpp:42-62); E grids
+ * as (nx+1)*(ny+1) doubles addressed with stride nx (fields.cpp:65-76,
+ * 230-268).
+ */
+#ifndef PICGB_H
+#define PICGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PGB_OK            0
+#define PGB_ERR_ARG      -1   /* invalid argument or parameter set            */
+#define PGB_ERR_CUDA     -2   /* a CUDA call failed (message names it)         */
+#define PGB_ERR_NOMEM    -3   /* device or host allocation failed              */
+#define PGB_ERR_CAPACITY -4   /* a particle or scratch capacity was exceeded   */
+#define PGB_ERR_STATE    -5   /* call not valid in the handle's current state  */
+#define PGB_ERR_IO       -6   /* file could not be read or written             */
+
+/* ---- enumerations (string-valued macros of parameters.h) ---- */
+enum { PGB_ELECTRONS = 0, PGB_IONS = 1 };
+enum { PGB_ARGON = 0, PGB_HYDROGEN = 1 };                 /* SPECIES            */
+enum { PGB_SIGMA_CONSTANT = 0, PGB_SIGMA_ENERGY_DEPENDENT = 1 };
+enum { PGB_GRID_Q_E = 0, PGB_GRID_Q_I = 1, PGB_GRID_RHO = 2, PGB_GRID_PHI = 3,
+       PGB_GRID_EX = 4, PGB_GRID_EY = 5 };
+/* Poisson solver: the reference's one-pass full multigrid (mglin.cpp:21-196)
+ * in FP64 with the same schedule, or FP32 full multigrid wrapped in an FP64
+ * defect-correction loop that converges to the exact discrete solution.     */
+enum { PGB_POISSON_FMG_REF = 0, PGB_POISSON_FP32_DC = 1 };
+/* boundary selector for pgb_boundary(): the two member-function pointers
+ * implement_i_boundary / implement_e_boundary (boundary.h:372-383)          */
+enum { PGB_BOUNDARY_IONS = 0, PGB_BOUNDARY_ELECTRONS = 1 };
+
+/*
+ * Run parameters.  Field names follow the parameters.h macros
+ * (parameters.h:41-366, constants.h) and pic.cpp's initialize_* methods
+ * (pic.cpp:226-529); pgb_params_default() fills in the reference's defaults.
+ */
+typedef struct pgb_params {
+    int32_t x_no_of_cells;         /* X_NO_OF_CELLS (grid nodes, 2^k+1)          */
+    int32_t y_no_of_cells;         /* Y_NO_OF_CELLS (must equal x_no_of_cells)   */
+    double  xlength, ylength;      /* XLENGTH, YLENGTH [m]                        */
+    double  dt, dti;               /* DT, DTI [s]; DT_DTI = (int)(dti/dt)         */
+    double  electron_mass;         /* ELECTRON_MASS [kg]                          */
+    double  ion_mass;              /* ION_MASS [kg]                               */
+    double  q_over_me, q_over_mi;  /* Q_OVER_ME, Q_OVER_MI [C/kg]                 */
+    double  qce, qci;              /* QCE, QCI: macro-particle charge [C]         */
+    double  vte, vti, vtn;         /* VTE, VTI, VTN [m/s]                         */
+    double  magnetic_field;        /* MAGNETIC_FIELD [T]                          */
+    double  angle;                 /* ANGLE [rad]                                 */
+    double  phi_left, phi_right, phi_bottom, phi_top;  /* wall potentials [V]    */
+    double  phi_period;            /* PHI_PERIOD: right wall = phi_right*cos(phi_period*t) */
+    double  neutral_density;       /* NEUTRAL_DENSITY [1/m^3]                     */
+    double  threshold;             /* THRESHOLD: ionization threshold [eV]        */
+    double  work_function;         /* WORK_FUNCTION [eV]                          */
+    int32_t have_collisions;       /* HAVE_COLLISIONS                             */
+    int32_t species;               /* SPECIES: PGB_ARGON / PGB_HYDROGEN           */
+    int32_t sigma_cx_mode;         /* SIGMA            (CONSTANT/ENERGY_DEPENDENT) */
+    int32_t sigma_elastic_mode;    /* SIGMA_ELASTIC                               */
+    int32_t sigma_ionization_mode; /* SIGMA_IONIZATION                            */
+    double  sigma_value;           /* SIGMA_VALUE [1e-20 m^2]                     */
+    double  elastic_sigma_value;   /* ELASTIC_SIGMA_VALUE                         */
+    double  ionization_sigma_value;/* IONIZATION_SIGMA_VALUE                      */
+    int32_t e_impact_see;          /* E_IMPACT_SEE  (1 = "YES")                   */
+    int32_t ion_impact_see;        /* ION_IMPACT_SEE                              */
+    int32_t reflection;            /* REFLECTION                                  */
+    int32_t backscatter;           /* BACKSCATTER                                 */
+    int32_t steadystate;           /* STEADYSTATE                                 */
+    int32_t number_to_inject;      /* NUMBER_TO_INJECT per species per step       */
+    int32_t init_no_neutrals;      /* INIT_NO_NEUTRALS (neutral velocity table)   */
+    double  see_e0, see_max_yield, see_emax0;  /* Vaughan constants (pic.cpp:459-477) */
+    /* Kunhardt population control (parameters.h:339-366, pic.cpp:257-327)    */
+    int32_t no_groups;             /* NO_GROUPS (<= 3)                            */
+    double  v_limit_e[3], v_limit_i[3];
+    int32_t group_limit_e[3], group_limit_i[3];
+    int32_t new_group_size_e[3], new_group_size_i[3];
+    int64_t size_to_check_e, size_to_check_i;  /* SIZE_TO_CHECK_E, SIZE_TO_CHECK */
+    /* GB300 run controls (no reference counterpart)                          */
+    uint64_t seed;                 /* Philox key for every random draw            */
+    int32_t poisson_mode;          /* PGB_POISSON_*                               */
+    int32_t dc_max_iters;          /* FP32_DC: max defect-correction passes       */
+    double  dc_tolerance;          /* FP32_DC: stop when max|r| <= tol*max|f|     */
+    int32_t sort_interval;         /* cell-sort particles every k steps (0 = off) */
+    int64_t capacity_e, capacity_i;/* particle slots to reserve (0 = automatic)   */
+} pgb_params;
+
+/* Per-run counters, cumulative since pgb_create (read with pgb_get_counters). */
+typedef struct pgb_counters {
+    int64_t n_e, n_i;              /* live particles now                          */
+    int64_t step;                  /* time steps taken (the reference's time_step) */
+    int64_t absorbed_e, absorbed_i;/* removed at walls                            */
+    int64_t plopped;               /* steady-state e-ion pairs re-inserted        */
+    int64_t reflected, backscattered, see_events, see_emitted;  /* electron walls */
+    int64_t ion_see_emitted;       /* electrons emitted by ion impact             */
+    int64_t elastic, ionization, charge_exchange;  /* collisions                  */
+    int64_t injected_e, injected_i;
+    int64_t reductions_e, reductions_i;  /* Kunhardt reductions (count_reduce)    */
+} pgb_counters;
+
+typedef struct pgb_run pgb_run;
+
+/* Fill *p with the reference's default parameters.h values (Ar, 257x257,
+ * steady state, no collisions) and this library's run controls.           */
+int pgb_params_default(pgb_params* p);
+
+/* pic::pic (pic.cpp:55-221) minus particle loading: allocate the device
+ * state, build the neutral velocity tables (collisions.cpp:66-89).          */
+int pgb_create(const pgb_params* p, pgb_run** out);
+/* pic::~pic (pic.cpp:1297-1340) */
+int pgb_destroy(pgb_run* run);
+/* Message for the last failing call on this handle (never NULL). */
+const char* pgb_last_error(const pgb_run* run);
+
+/* particle::load_particles (particle.cpp:359-401): replace the species'
+ * particles with n records of 6 doubles (the dataDump_*.txt columns).       */
+int pgb_load_species(pgb_run* run, int species, const double* aos6, int64_t n);
+/* particle::dump_data (particle.cpp:1361-1382) without the text formatting:
+ * copy the live particles out as 6 doubles each.  *n_out = live count; at
+ * most cap records are written.                                             */
+int pgb_dump_species(pgb_run* run, int species, double* aos6, int64_t cap, int64_t* n_out);
+/* particle::particle_size */
+int pgb_species_count(pgb_run* run, int species, int64_t* n_out);
+
+/* Set the reference's time_step counter (used by the right-wall potential
+ * and the random streams).  pgb_step advances it.                           */
+int pgb_set_time_step(pgb_run* run, int64_t time_step);
+
+/* The two boundary calls pic_run makes before its loop (pic.cpp:1049-1057). */
+int pgb_initial_boundary(pgb_run* run);
+/* nsteps iterations of the pic_run loop body (pic.cpp:1069-1250) with fused
+ * kernels; same physics and call order as the per-phase entry points.      */
+int pgb_step(pgb_run* run, int32_t nsteps);
+
+/* ---- per-phase entry points, in pic_run order ---- */
+int pgb_collide_electrons(pgb_run* run);        /* e_collisions::collision (e_collisions.cpp:480-597) */
+int pgb_inject(pgb_run* run);                   /* particle::inject_more_particles, e then ions (particle.cpp:491-510) */
+int pgb_gather_push(pgb_run* run, int species); /* get_particle_electric_field + move_particles (particle.cpp:870-1341, pic.cl:56-149) */
+int pgb_collide_ions(pgb_run* run);             /* ion_collisions::collision (ion_collisions.cpp:255-308) */
+int pgb_boundary(pgb_run* run, int which);      /* implement_i_boundary / implement_e_boundary (boundary.cpp:581-1103) */
+int pgb_contain_growth(pgb_run* run, int species); /* particle::contain_particle_growth (particle.cpp:541-653) */
+int pgb_deposit(pgb_run* run, int species);     /* particle::collect_charge (particle.cpp:663-858, pic.cl:22-52) */
+int pgb_grid_rho(pgb_run* run);                 /* fields::grid_rho (fields.cpp:100-143) */
+int pgb_poisson(pgb_run* run, int64_t time_step); /* fields::grid_potential + Mglin (fields.cpp:169-220, mglin.cpp:21-196) */
+int pgb_efield(pgb_run* run);                   /* fields::grid_electric_field (fields.cpp:230-268) */
+
+/* Copy a grid out in the reference layout (see the header comment).
+ * n = number of doubles the caller's buffer holds.                        */
+int pgb_get_grid(pgb_run* run, int which, double* out, int64_t n);
+/* Overwrite rho ([ny][nx]) before pgb_poisson, e.g. to solve a given
+ * charge density without particles.                                       */
+int pgb_set_rho(pgb_run* run, const double* rho, int64_t n);
+int pgb_get_counters(pgb_run* run, pgb_counters* out);
+/* Wait for all work queued on the handle's stream. */
+int pgb_sync(pgb_run* run);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PICGB_H */

@@ -1,0 +1,401 @@
+"""Python host mirror of the reference PIC driver over the libpicgb C ABI.
+
+The reference configures a run with compile-time macros in parameters.h
+(parameters.h:41-366) and drives it with pic::pic_run (pic.cpp:1040-1279).
+This module offers the same inputs as keyword arguments named after those
+macros (`make_params`), derives the dependent quantities with the
+reference's formulas, and wraps libpicgb.so (include/picgb.h) with ctypes so
+that tests and benchmarks can call the exact C entry points a C++ or FFI
+caller would use.  No computation happens here: every physics call goes to
+the CUDA library, and a missing library raises instead of falling back.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+
+# constants.h:17-26
+PI = 3.141592654
+CHARGE = 1.602177e-19
+ELECTRON_CHARGE2 = 2.566971e-38
+ELECTRON_MASS = 9.10939e-31
+AMU = 1.66054e-27
+EPSILON = 8.854e-12
+
+PGB_ELECTRONS, PGB_IONS = 0, 1
+PGB_ARGON, PGB_HYDROGEN = 0, 1
+PGB_SIGMA_CONSTANT, PGB_SIGMA_ENERGY_DEPENDENT = 0, 1
+GRID = {"q_e": 0, "q_i": 1, "rho": 2, "phi": 3, "ex": 4, "ey": 5}
+PGB_POISSON_FMG_REF, PGB_POISSON_FP32_DC = 0, 1
+PGB_BOUNDARY_IONS, PGB_BOUNDARY_ELECTRONS = 0, 1
+
+
+class PgbParams(C.Structure):
+    """ctypes image of `pgb_params` (include/picgb.h)."""
+
+    _fields_ = [
+        ("x_no_of_cells", C.c_int32), ("y_no_of_cells", C.c_int32),
+        ("xlength", C.c_double), ("ylength", C.c_double),
+        ("dt", C.c_double), ("dti", C.c_double),
+        ("electron_mass", C.c_double), ("ion_mass", C.c_double),
+        ("q_over_me", C.c_double), ("q_over_mi", C.c_double),
+        ("qce", C.c_double), ("qci", C.c_double),
+        ("vte", C.c_double), ("vti", C.c_double), ("vtn", C.c_double),
+        ("magnetic_field", C.c_double), ("angle", C.c_double),
+        ("phi_left", C.c_double), ("phi_right", C.c_double),
+        ("phi_bottom", C.c_double), ("phi_top", C.c_double), ("phi_period", C.c_double),
+        ("neutral_density", C.c_double), ("threshold", C.c_double), ("work_function", C.c_double),
+        ("have_collisions", C.c_int32), ("species", C.c_int32),
+        ("sigma_cx_mode", C.c_int32), ("sigma_elastic_mode", C.c_int32),
+        ("sigma_ionization_mode", C.c_int32),
+        ("sigma_value", C.c_double), ("elastic_sigma_value", C.c_double),
+        ("ionization_sigma_value", C.c_double),
+        ("e_impact_see", C.c_int32), ("ion_impact_see", C.c_int32), ("reflection", C.c_int32),
+        ("backscatter", C.c_int32), ("steadystate", C.c_int32),
+        ("number_to_inject", C.c_int32), ("init_no_neutrals", C.c_int32),
+        ("see_e0", C.c_double), ("see_max_yield", C.c_double), ("see_emax0", C.c_double),
+        ("no_groups", C.c_int32),
+        ("v_limit_e", C.c_double * 3), ("v_limit_i", C.c_double * 3),
+        ("group_limit_e", C.c_int32 * 3), ("group_limit_i", C.c_int32 * 3),
+        ("new_group_size_e", C.c_int32 * 3), ("new_group_size_i", C.c_int32 * 3),
+        ("size_to_check_e", C.c_int64), ("size_to_check_i", C.c_int64),
+        ("seed", C.c_uint64), ("poisson_mode", C.c_int32), ("dc_max_iters", C.c_int32),
+        ("dc_tolerance", C.c_double), ("sort_interval", C.c_int32),
+        ("capacity_e", C.c_int64), ("capacity_i", C.c_int64),
+    ]
+
+
+class PgbCounters(C.Structure):
+    """ctypes image of `pgb_counters` (include/picgb.h)."""
+
+    _fields_ = [(name, C.c_int64) for name in (
+        "n_e", "n_i", "step", "absorbed_e", "absorbed_i", "plopped", "reflected",
+        "backscattered", "see_events", "see_emitted", "ion_see_emitted", "elastic",
+        "ionization", "charge_exchange", "injected_e", "injected_i",
+        "reductions_e", "reductions_i")]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+
+def _yes(v) -> int:
+    if isinstance(v, str):
+        return 1 if v.upper() == "YES" else 0
+    return 1 if v else 0
+
+
+def make_params(**kw) -> PgbParams:
+    """Build run parameters from parameters.h-style inputs.
+
+    Keyword names are the parameters.h macros (upper case); the derived
+    quantities use the reference's formulas (parameters.h:71-262):
+    NEUTRAL_DENSITY from GAS_PRESSURE_TORR, VTE/VTI/VTN from TEMPERATURE,
+    XLENGTH = NO_OF_DEBYE_LENGTHS * DEBYE_LENGTH, DX = XLENGTH/(X_NO_OF_CELLS-1),
+    DT = 0.1/PLASMA_FREQUENCY (scale DT_SCALE), DTI = DTI_RATIO*DT.
+    Defaults are those of the reference's parameters.h.
+    """
+    g = dict(
+        X_NO_OF_CELLS=257, TEMPERATURE=1.5, GAS_PRESSURE_TORR=0.2, ION_MASS_AMU=39.948,
+        THRESHOLD=15.75, WORK_FUNCTION=4.6, HAVE_COLLISIONS=False, SPECIES="ARGON",
+        SIGMA="CONSTANT", SIGMA_VALUE=0.0, SIGMA_ELASTIC="CONSTANT", ELASTIC_SIGMA_VALUE=0.0,
+        SIGMA_IONIZATION="CONSTANT", IONIZATION_SIGMA_VALUE=0.0, E_IMPACT_SEE="NO",
+        ION_IMPACT_SEE="NO", REFLECTION="NO", BACKSCATTER="NO", STEADYSTATE="YES",
+        NUMBER_TO_INJECT=0, INIT_NO_NEUTRALS=10000, NO_OF_DEBYE_LENGTHS=64,
+        ELECTRON_PARTICLE_DENSITY=1.0e15, DT_SCALE=0.1, DTI_RATIO=1.0, MAGNETIC_FIELD=0.0,
+        ANGLE_DEG=30.0, PHI_LEFT=0.0, PHI_RIGHT=0.0, PHI_PERIOD=0.0, PHI_TOP=0.0,
+        PHI_BOTTOM=0.0, E_MACROPARTICLE_SIZE=1.0e6, ION_MACROPARTICLE_SIZE=1.0e6,
+        SIZE_TO_CHECK=1000001, SIZE_TO_CHECK_E=None, RAND_SEED=1, POISSON="FMG_REF",
+        DC_MAX_ITERS=8, DC_TOLERANCE=1e-10, SORT_INTERVAL=0, CAPACITY_E=0, CAPACITY_I=0,
+    )
+    for k, v in kw.items():
+        if k not in g:
+            raise KeyError(f"unknown parameter {k}")
+        g[k] = v
+    T = float(g["TEMPERATURE"])
+    ion_mass = float(g["ION_MASS_AMU"]) * AMU
+    gas_pressure = float(g["GAS_PRESSURE_TORR"]) * 133.32
+    n_e = float(g["ELECTRON_PARTICLE_DENSITY"])
+    debye = math.sqrt((EPSILON * T) / (n_e * CHARGE))
+    xlength = float(int(g["NO_OF_DEBYE_LENGTHS"])) * debye
+    plasma_frequency = math.sqrt((n_e * ELECTRON_CHARGE2) / (EPSILON * ELECTRON_MASS))
+    dt = float(g["DT_SCALE"]) / plasma_frequency
+    vte = math.sqrt(T * CHARGE / ELECTRON_MASS)
+    vti = math.sqrt(T * CHARGE / ion_mass)
+    p = PgbParams()
+    n = int(g["X_NO_OF_CELLS"])
+    p.x_no_of_cells = p.y_no_of_cells = n
+    p.xlength = p.ylength = xlength
+    p.dt = dt
+    p.dti = float(g["DTI_RATIO"]) * dt
+    p.electron_mass = ELECTRON_MASS
+    p.ion_mass = ion_mass
+    p.q_over_me = -CHARGE / ELECTRON_MASS
+    p.q_over_mi = CHARGE / ion_mass
+    p.qce = float(g["E_MACROPARTICLE_SIZE"]) * -CHARGE
+    p.qci = float(g["ION_MACROPARTICLE_SIZE"]) * CHARGE
+    p.vte, p.vti = vte, vti
+    p.vtn = math.sqrt(0.025 * CHARGE / ion_mass)
+    p.magnetic_field = float(g["MAGNETIC_FIELD"])
+    p.angle = float(g["ANGLE_DEG"]) * PI / 180.0
+    p.phi_left, p.phi_right = float(g["PHI_LEFT"]), float(g["PHI_RIGHT"])
+    p.phi_bottom, p.phi_top = float(g["PHI_BOTTOM"]), float(g["PHI_TOP"])
+    p.phi_period = float(g["PHI_PERIOD"])
+    p.neutral_density = gas_pressure / (0.025 * CHARGE)
+    p.threshold = float(g["THRESHOLD"])
+    p.work_function = float(g["WORK_FUNCTION"])
+    p.have_collisions = 1 if g["HAVE_COLLISIONS"] else 0
+    p.species = PGB_ARGON if str(g["SPECIES"]).upper() == "ARGON" else PGB_HYDROGEN
+    mode = lambda s: PGB_SIGMA_CONSTANT if str(s).upper() == "CONSTANT" else PGB_SIGMA_ENERGY_DEPENDENT
+    p.sigma_cx_mode = mode(g["SIGMA"])
+    p.sigma_elastic_mode = mode(g["SIGMA_ELASTIC"])
+    p.sigma_ionization_mode = mode(g["SIGMA_IONIZATION"])
+    p.sigma_value = float(g["SIGMA_VALUE"])
+    p.elastic_sigma_value = float(g["ELASTIC_SIGMA_VALUE"])
+    p.ionization_sigma_value = float(g["IONIZATION_SIGMA_VALUE"])
+    p.e_impact_see = _yes(g["E_IMPACT_SEE"])
+    p.ion_impact_see = _yes(g["ION_IMPACT_SEE"])
+    p.reflection = _yes(g["REFLECTION"])
+    p.backscatter = _yes(g["BACKSCATTER"])
+    p.steadystate = _yes(g["STEADYSTATE"])
+    p.number_to_inject = int(g["NUMBER_TO_INJECT"])
+    p.init_no_neutrals = int(g["INIT_NO_NEUTRALS"])
+    p.see_e0, p.see_max_yield, p.see_emax0 = 4.32, 1.4, 650.0
+    # Kunhardt groups (parameters.h:339-366, pic.cpp:257-327)
+    p.no_groups = 3
+    for k, v in enumerate((2.0 * vte, 3.0 * vte, 1000.0 * vte)):
+        p.v_limit_e[k] = v
+    for k, v in enumerate((2.0 * vti, 3.0 * vti, 1000.0 * vti)):
+        p.v_limit_i[k] = v
+    for k in range(3):
+        p.group_limit_e[k] = 400000
+        p.new_group_size_e[k] = 200000
+    p.group_limit_i[0], p.group_limit_i[1], p.group_limit_i[2] = 400000, 100000, 100000
+    p.new_group_size_i[0], p.new_group_size_i[1], p.new_group_size_i[2] = 200000, 50000, 50000
+    stc = int(g["SIZE_TO_CHECK"])
+    p.size_to_check_i = stc
+    p.size_to_check_e = int(g["SIZE_TO_CHECK_E"]) if g["SIZE_TO_CHECK_E"] is not None else stc
+    p.seed = int(g["RAND_SEED"])
+    p.poisson_mode = PGB_POISSON_FMG_REF if g["POISSON"] == "FMG_REF" else PGB_POISSON_FP32_DC
+    p.dc_max_iters = int(g["DC_MAX_ITERS"])
+    p.dc_tolerance = float(g["DC_TOLERANCE"])
+    p.sort_interval = int(g["SORT_INTERVAL"])
+    p.capacity_e = int(g["CAPACITY_E"])
+    p.capacity_i = int(g["CAPACITY_I"])
+    return p
+
+
+def grid_shape(p: PgbParams, which: str) -> tuple:
+    nx, ny = p.x_no_of_cells, p.y_no_of_cells
+    if which in ("ex", "ey"):
+        return ((nx + 1) * (ny + 1),)
+    return (ny, nx)
+
+
+# ---------------------------------------------------------------- library
+def library_path() -> str:
+    return os.path.join(PKG_DIR, "libpicgb.so")
+
+
+_LIB = None
+
+
+def load_library():
+    """Load libpicgb.so; raise if it was not built (no fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libpicgb.so not built at {path}: run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    R = C.c_void_p
+    i32, i64, dp = C.c_int32, C.c_int64, C.POINTER(C.c_double)
+    sig = {
+        "pgb_params_default": (C.c_int, [C.POINTER(PgbParams)]),
+        "pgb_create": (C.c_int, [C.POINTER(PgbParams), C.POINTER(R)]),
+        "pgb_destroy": (C.c_int, [R]),
+        "pgb_last_error": (C.c_char_p, [R]),
+        "pgb_load_species": (C.c_int, [R, C.c_int, dp, i64]),
+        "pgb_dump_species": (C.c_int, [R, C.c_int, dp, i64, C.POINTER(i64)]),
+        "pgb_species_count": (C.c_int, [R, C.c_int, C.POINTER(i64)]),
+        "pgb_set_time_step": (C.c_int, [R, i64]),
+        "pgb_initial_boundary": (C.c_int, [R]),
+        "pgb_step": (C.c_int, [R, i32]),
+        "pgb_collide_electrons": (C.c_int, [R]),
+        "pgb_inject": (C.c_int, [R]),
+        "pgb_gather_push": (C.c_int, [R, C.c_int]),
+        "pgb_collide_ions": (C.c_int, [R]),
+        "pgb_boundary": (C.c_int, [R, C.c_int]),
+        "pgb_contain_growth": (C.c_int, [R, C.c_int]),
+        "pgb_deposit": (C.c_int, [R, C.c_int]),
+        "pgb_grid_rho": (C.c_int, [R]),
+        "pgb_poisson": (C.c_int, [R, i64]),
+        "pgb_efield": (C.c_int, [R]),
+        "pgb_get_grid": (C.c_int, [R, C.c_int, dp, i64]),
+        "pgb_set_rho": (C.c_int, [R, dp, i64]),
+        "pgb_get_counters": (C.c_int, [R, C.POINTER(PgbCounters)]),
+        "pgb_sync": (C.c_int, [R]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class PicError(RuntimeError):
+    pass
+
+
+class Run:
+    """One simulation on the GPU (a `pgb_run` handle).
+
+    Method names follow the reference's pic / particle / fields calls so that
+    a test reads like the reference's step sequence (pic.cpp:1069-1250).
+    """
+
+    def __init__(self, params: PgbParams):
+        self.lib = load_library()
+        self.params = params
+        h = C.c_void_p()
+        rc = self.lib.pgb_create(C.byref(params), C.byref(h))
+        if rc != 0:
+            raise PicError(f"pgb_create failed ({rc}): {self.lib.pgb_last_error(None).decode()}")
+        self.h = h
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            raise PicError(f"{what} failed ({rc}): {self.lib.pgb_last_error(self.h).decode()}")
+
+    def close(self):
+        if self.h:
+            self.lib.pgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # particles
+    def load_particles(self, species: int, aos6: np.ndarray):
+        a = np.ascontiguousarray(aos6, dtype=np.float64).reshape(-1, 6)
+        self._check(self.lib.pgb_load_species(self.h, species, _dptr(a), a.shape[0]), "pgb_load_species")
+
+    def particle_size(self, species: int) -> int:
+        n = C.c_int64()
+        self._check(self.lib.pgb_species_count(self.h, species, C.byref(n)), "pgb_species_count")
+        return int(n.value)
+
+    def get_particles(self, species: int) -> np.ndarray:
+        n = self.particle_size(species)
+        out = np.empty((max(n, 1), 6), dtype=np.float64)
+        got = C.c_int64()
+        self._check(self.lib.pgb_dump_species(self.h, species, _dptr(out), n, C.byref(got)), "pgb_dump_species")
+        return out[: got.value].copy()
+
+    # driver
+    def set_time_step(self, t: int):
+        self._check(self.lib.pgb_set_time_step(self.h, t), "pgb_set_time_step")
+
+    def initial_boundary(self):
+        self._check(self.lib.pgb_initial_boundary(self.h), "pgb_initial_boundary")
+
+    def step(self, n: int = 1):
+        self._check(self.lib.pgb_step(self.h, n), "pgb_step")
+
+    # phases
+    def collide_electrons(self):
+        self._check(self.lib.pgb_collide_electrons(self.h), "pgb_collide_electrons")
+
+    def inject(self):
+        self._check(self.lib.pgb_inject(self.h), "pgb_inject")
+
+    def gather_push(self, species: int):
+        self._check(self.lib.pgb_gather_push(self.h, species), "pgb_gather_push")
+
+    def collide_ions(self):
+        self._check(self.lib.pgb_collide_ions(self.h), "pgb_collide_ions")
+
+    def boundary(self, which: int):
+        self._check(self.lib.pgb_boundary(self.h, which), "pgb_boundary")
+
+    def contain_growth(self, species: int):
+        self._check(self.lib.pgb_contain_growth(self.h, species), "pgb_contain_growth")
+
+    def deposit(self, species: int):
+        self._check(self.lib.pgb_deposit(self.h, species), "pgb_deposit")
+
+    def grid_rho(self):
+        self._check(self.lib.pgb_grid_rho(self.h), "pgb_grid_rho")
+
+    def poisson(self, t: int):
+        self._check(self.lib.pgb_poisson(self.h, t), "pgb_poisson")
+
+    def efield(self):
+        self._check(self.lib.pgb_efield(self.h), "pgb_efield")
+
+    # grids / counters
+    def get_grid(self, which: str) -> np.ndarray:
+        shape = grid_shape(self.params, which)
+        out = np.empty(shape, dtype=np.float64)
+        self._check(self.lib.pgb_get_grid(self.h, GRID[which], _dptr(out), out.size), "pgb_get_grid")
+        return out
+
+    def set_rho(self, rho: np.ndarray):
+        a = np.ascontiguousarray(rho, dtype=np.float64)
+        self._check(self.lib.pgb_set_rho(self.h, _dptr(a), a.size), "pgb_set_rho")
+
+    def counters(self) -> dict:
+        c = PgbCounters()
+        self._check(self.lib.pgb_get_counters(self.h, C.byref(c)), "pgb_get_counters")
+        return c.as_dict()
+
+    def sync(self):
+        self._check(self.lib.pgb_sync(self.h), "pgb_sync")
+
+
+# ------------------------------------------------------------- dataDump I/O
+def read_datadump(path: str) -> np.ndarray:
+    """particle::load_particles (particle.cpp:359-401): whitespace-separated
+    records `x y vx vy vz weight`, read until the first incomplete record."""
+    with open(path, "rb") as f:
+        vals = np.array(f.read().split(), dtype=np.float64)
+    n = vals.size // 6
+    return vals[: n * 6].reshape(n, 6)
+
+
+def write_datadump(path: str, aos6: np.ndarray):
+    """particle::dump_data (particle.cpp:1361-1382): `ofstream <<` of each
+    double at the default precision (6 significant digits, %g style)."""
+    a = np.asarray(aos6, dtype=np.float64).reshape(-1, 6)
+    with open(path, "w") as f:
+        for row in a:
+            f.write(" ".join(_ostream_double(v) for v in row) + "\n")
+
+
+def _ostream_double(v: float) -> str:
+    if v != v:
+        return "nan" if math.copysign(1.0, v) > 0 else "-nan"
+    if v in (math.inf, -math.inf):
+        return "inf" if v > 0 else "-inf"
+    return "%g" % v
