@@ -24,6 +24,12 @@
 
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define PGB_API __attribute__((visibility("default")))
+#else
+#define PGB_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -121,57 +127,57 @@ typedef struct pgb_run pgb_run;
 
 /* Fill *p with the reference's default parameters.h values (Ar, 257x257,
  * steady state, no collisions) and this library's run controls.           */
-int pgb_params_default(pgb_params* p);
+PGB_API int pgb_params_default(pgb_params* p);
 
 /* pic::pic (pic.cpp:55-221) minus particle loading: allocate the device
  * state, build the neutral velocity tables (collisions.cpp:66-89).          */
-int pgb_create(const pgb_params* p, pgb_run** out);
+PGB_API int pgb_create(const pgb_params* p, pgb_run** out);
 /* pic::~pic (pic.cpp:1297-1340) */
-int pgb_destroy(pgb_run* run);
+PGB_API int pgb_destroy(pgb_run* run);
 /* Message for the last failing call on this handle (never NULL). */
-const char* pgb_last_error(const pgb_run* run);
+PGB_API const char* pgb_last_error(const pgb_run* run);
 
 /* particle::load_particles (particle.cpp:359-401): replace the species'
  * particles with n records of 6 doubles (the dataDump_*.txt columns).       */
-int pgb_load_species(pgb_run* run, int species, const double* aos6, int64_t n);
+PGB_API int pgb_load_species(pgb_run* run, int species, const double* aos6, int64_t n);
 /* particle::dump_data (particle.cpp:1361-1382) without the text formatting:
  * copy the live particles out as 6 doubles each.  *n_out = live count; at
  * most cap records are written.                                             */
-int pgb_dump_species(pgb_run* run, int species, double* aos6, int64_t cap, int64_t* n_out);
+PGB_API int pgb_dump_species(pgb_run* run, int species, double* aos6, int64_t cap, int64_t* n_out);
 /* particle::particle_size */
-int pgb_species_count(pgb_run* run, int species, int64_t* n_out);
+PGB_API int pgb_species_count(pgb_run* run, int species, int64_t* n_out);
 
 /* Set the reference's time_step counter (used by the right-wall potential
  * and the random streams).  pgb_step advances it.                           */
-int pgb_set_time_step(pgb_run* run, int64_t time_step);
+PGB_API int pgb_set_time_step(pgb_run* run, int64_t time_step);
 
 /* The two boundary calls pic_run makes before its loop (pic.cpp:1049-1057). */
-int pgb_initial_boundary(pgb_run* run);
+PGB_API int pgb_initial_boundary(pgb_run* run);
 /* nsteps iterations of the pic_run loop body (pic.cpp:1069-1250) with fused
  * kernels; same physics and call order as the per-phase entry points.      */
-int pgb_step(pgb_run* run, int32_t nsteps);
+PGB_API int pgb_step(pgb_run* run, int32_t nsteps);
 
 /* ---- per-phase entry points, in pic_run order ---- */
-int pgb_collide_electrons(pgb_run* run);        /* e_collisions::collision (e_collisions.cpp:480-597) */
-int pgb_inject(pgb_run* run);                   /* particle::inject_more_particles, e then ions (particle.cpp:491-510) */
-int pgb_gather_push(pgb_run* run, int species); /* get_particle_electric_field + move_particles (particle.cpp:870-1341, pic.cl:56-149) */
-int pgb_collide_ions(pgb_run* run);             /* ion_collisions::collision (ion_collisions.cpp:255-308) */
-int pgb_boundary(pgb_run* run, int which);      /* implement_i_boundary / implement_e_boundary (boundary.cpp:581-1103) */
-int pgb_contain_growth(pgb_run* run, int species); /* particle::contain_particle_growth (particle.cpp:541-653) */
-int pgb_deposit(pgb_run* run, int species);     /* particle::collect_charge (particle.cpp:663-858, pic.cl:22-52) */
-int pgb_grid_rho(pgb_run* run);                 /* fields::grid_rho (fields.cpp:100-143) */
-int pgb_poisson(pgb_run* run, int64_t time_step); /* fields::grid_potential + Mglin (fields.cpp:169-220, mglin.cpp:21-196) */
-int pgb_efield(pgb_run* run);                   /* fields::grid_electric_field (fields.cpp:230-268) */
+PGB_API int pgb_collide_electrons(pgb_run* run);        /* e_collisions::collision (e_collisions.cpp:480-597) */
+PGB_API int pgb_inject(pgb_run* run);                   /* particle::inject_more_particles, e then ions (particle.cpp:491-510) */
+PGB_API int pgb_gather_push(pgb_run* run, int species); /* get_particle_electric_field + move_particles (particle.cpp:870-1341, pic.cl:56-149) */
+PGB_API int pgb_collide_ions(pgb_run* run);             /* ion_collisions::collision (ion_collisions.cpp:255-308) */
+PGB_API int pgb_boundary(pgb_run* run, int which);      /* implement_i_boundary / implement_e_boundary (boundary.cpp:581-1103) */
+PGB_API int pgb_contain_growth(pgb_run* run, int species); /* particle::contain_particle_growth (particle.cpp:541-653) */
+PGB_API int pgb_deposit(pgb_run* run, int species);     /* particle::collect_charge (particle.cpp:663-858, pic.cl:22-52) */
+PGB_API int pgb_grid_rho(pgb_run* run);                 /* fields::grid_rho (fields.cpp:100-143) */
+PGB_API int pgb_poisson(pgb_run* run, int64_t time_step); /* fields::grid_potential + Mglin (fields.cpp:169-220, mglin.cpp:21-196) */
+PGB_API int pgb_efield(pgb_run* run);                   /* fields::grid_electric_field (fields.cpp:230-268) */
 
 /* Copy a grid out in the reference layout (see the header comment).
  * n = number of doubles the caller's buffer holds.                        */
-int pgb_get_grid(pgb_run* run, int which, double* out, int64_t n);
+PGB_API int pgb_get_grid(pgb_run* run, int which, double* out, int64_t n);
 /* Overwrite rho ([ny][nx]) before pgb_poisson, e.g. to solve a given
  * charge density without particles.                                       */
-int pgb_set_rho(pgb_run* run, const double* rho, int64_t n);
-int pgb_get_counters(pgb_run* run, pgb_counters* out);
+PGB_API int pgb_set_rho(pgb_run* run, const double* rho, int64_t n);
+PGB_API int pgb_get_counters(pgb_run* run, pgb_counters* out);
 /* Wait for all work queued on the handle's stream. */
-int pgb_sync(pgb_run* run);
+PGB_API int pgb_sync(pgb_run* run);
 
 #ifdef __cplusplus
 }

@@ -1231,3 +1231,9 @@ void orc_get_counters(orc_run* r, pgb_counters* out) {
     out->n_i = r->sp[1].n;
     out->step = r->time_step;
 }
+
+/* Philox4x32-10 block, exposed for the known-answer test of the shared generator */
+void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    pgb_u32x4 r = pgb_philox4x32_10(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1]);
+    for (int k = 0; k < 4; ++k) out[k] = r.v[k];
+}

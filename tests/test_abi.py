@@ -1,0 +1,93 @@
+"""The C ABI boundary: exported symbols, parameter defaults, loud failure.
+
+These run without a GPU: loading libpicgb.so and calling the functions that
+do not touch the device is enough to check the boundary.
+"""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+HEADER = os.path.join(REPO, "include", "picgb.h")
+
+
+def header_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^PGB_API\s+[\w\s\*]+?\b(pgb_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_the_entry_points():
+    names = header_functions()
+    for required in ("pgb_create", "pgb_destroy", "pgb_step", "pgb_load_species", "pgb_dump_species",
+                     "pgb_gather_push", "pgb_deposit", "pgb_poisson", "pgb_efield", "pgb_boundary",
+                     "pgb_collide_electrons", "pgb_collide_ions"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    import picgb
+    for name in header_functions():
+        assert hasattr(lib, name), f"libpicgb.so does not export {name}"
+    out = subprocess.run(["nm", "-D", "--defined-only", picgb.library_path()], capture_output=True, text=True).stdout
+    exported = sorted(set(re.findall(r"\bT (pgb_\w+)", out)))
+    assert exported == header_functions(), "exports and header differ"
+
+
+def test_params_default_matches_parameters_h(lib):
+    """pgb_params_default (C) and make_params() (Python) restate the same
+    parameters.h defaults (parameters.h:41-366)."""
+    import picgb
+    a = picgb.PgbParams()
+    assert lib.pgb_params_default(C.byref(a)) == 0
+    b = picgb.make_params()
+    for name, _ in picgb.PgbParams._fields_:
+        va, vb = getattr(a, name), getattr(b, name)
+        if hasattr(va, "__len__"):
+            assert list(va) == list(vb), name
+        else:
+            assert va == vb, name
+
+
+def test_create_rejects_bad_grid(lib):
+    import picgb
+    p = picgb.make_params(X_NO_OF_CELLS=100)
+    h = C.c_void_p()
+    rc = lib.pgb_create(C.byref(p), C.byref(h))
+    assert rc == -1 and not h.value
+    assert b"power of 2" in lib.pgb_last_error(None)
+
+
+def test_no_silent_cpu_fallback_without_a_gpu(lib):
+    """Without a usable GPU the library reports a CUDA error; it never
+    computes on the host instead."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import picgb
+    p = picgb.make_params(X_NO_OF_CELLS=33)
+    h = C.c_void_p()
+    rc = lib.pgb_create(C.byref(p), C.byref(h))
+    assert rc == -2 and not h.value
+    assert lib.pgb_last_error(None)
+
+
+def test_datadump_text_format_matches_reference():
+    """particle::dump_data writes each double with `ofstream <<` at the
+    default precision (particle.cpp:1361-1382); write_datadump reproduces
+    the reference's own dump byte for byte."""
+    import tempfile
+    import picgb
+    from conftest import load_golden
+    g = load_golden("core33")
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "dataDump_e.txt")
+        picgb.write_datadump(path, g["e_out"])
+        head = "".join(open(path).readlines()[:20])
+        assert head == str(g["dump_e_head"])
+        back = picgb.read_datadump(path)
+        np.testing.assert_allclose(back, g["e_out"], rtol=5e-6)

@@ -1,0 +1,91 @@
+"""Pin the CPU oracle (oracle/picport.c) to the reference's own outputs.
+
+The golden fixtures were written by the reference's C++ code
+(pic::pic_run, particle, fields, Mglin, collision and boundary classes,
+built unchanged by oracle/Makefile; see tests/golden/gen_golden.py).  With
+the reference's random source (rand()) and removal order (swap with last),
+the oracle must reproduce every particle and grid value.  On x86-64 -- the
+host the fixtures were written on -- the match is exact; elsewhere the C
+library's transcendental functions may differ in the last bit, so a 1e-9
+relative tolerance applies there.
+"""
+import platform
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+import orc
+
+EXACT = platform.machine() in ("x86_64", "AMD64")
+
+
+def _close(a, b, what):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape, f"{what}: shape {a.shape} vs {b.shape}"
+    if EXACT:
+        same = (a == b) | (np.isnan(a) & np.isnan(b))
+        assert same.all(), f"{what}: {np.count_nonzero(~same)} values differ, max |d| {np.nanmax(np.abs(a - b))}"
+    else:
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-30, equal_nan=True, err_msg=what)
+
+
+@pytest.mark.parametrize("case", golden_cases("run"))
+def test_port_matches_reference_run(case):
+    g = load_golden(case)
+    o = orc.Oracle(g["p"], rng=orc.ORC_RNG_LIBC, order=orc.ORC_ORDER_REF)
+    o.load_particles(0, g["e_in"])
+    o.load_particles(1, g["i_in"])
+    o.initial_boundary()
+    o.step(int(g["nsteps"]))
+    _close(o.get_particles(0), g["e_out"], f"{case} electrons")
+    _close(o.get_particles(1), g["i_out"], f"{case} ions")
+    for grid in ("q_e", "q_i", "rho", "phi", "ex", "ey"):
+        _close(o.get_grid(grid).ravel(), g[grid], f"{case} {grid}")
+
+
+@pytest.mark.parametrize("case", golden_cases("fields"))
+def test_port_matches_reference_fields(case):
+    g = load_golden(case)
+    o = orc.Oracle(g["p"], rng=orc.ORC_RNG_LIBC, order=orc.ORC_ORDER_REF)
+    o.set_rho(g["rho"])
+    o.poisson(0)
+    o.efield()
+    for grid in ("phi", "ex", "ey"):
+        _close(o.get_grid(grid).ravel(), g[grid], f"{case} {grid}")
+
+
+def test_golden_cases_exercise_the_paths():
+    """The fixtures must cover walls, collisions, emission and re-insertion."""
+    seen = {}
+    for case in golden_cases("run"):
+        g = load_golden(case)
+        o = orc.Oracle(g["p"], rng=orc.ORC_RNG_LIBC, order=orc.ORC_ORDER_REF)
+        o.load_particles(0, g["e_in"])
+        o.load_particles(1, g["i_in"])
+        o.initial_boundary()
+        o.step(int(g["nsteps"]))
+        for k, v in o.counters().items():
+            seen[k] = seen.get(k, 0) + v
+    for k in ("absorbed_e", "absorbed_i", "plopped", "reflected", "backscattered", "see_events",
+              "ion_see_emitted", "elastic", "ionization", "charge_exchange", "injected_e"):
+        assert seen[k] > 0, f"no golden case exercises {k}"
+
+
+def test_philox_known_answers():
+    """Philox4x32-10 vectors published with the Random123 library."""
+    import ctypes as C
+    lib = orc.load()
+    kat = [
+        ([0, 0, 0, 0], [0, 0], [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]),
+        ([0xffffffff] * 4, [0xffffffff] * 2, [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]),
+        ([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0],
+         [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]),
+    ]
+    for ctr, key, want in kat:
+        c = (C.c_uint32 * 4)(*ctr)
+        k = (C.c_uint32 * 2)(*key)
+        o = (C.c_uint32 * 4)()
+        lib.orc_philox4x32(c, k, o)
+        assert list(o) == want

@@ -1,0 +1,646 @@
+/*
+ * C ABI of libpicgb (include/picgb.h): run handles, particle I/O and the
+ * host-side sequencing of the per-step kernels.
+ *
+ * pgb_step follows pic::pic_run's loop body (pic.cpp:1069-1250) on one CUDA
+ * stream without host synchronisation inside a step:
+ *   electron collisions + gather + push + deposit + wall list   (one kernel)
+ *   ionization products, injection (+ push of the injected electrons)
+ *   [ion step] charge exchange, ion gather + push + deposit + wall list,
+ *              ion walls, electron walls
+ *   [other steps] ion deposit, electron walls
+ *   charge -> rho -> Poisson right-hand side, full multigrid, E
+ * The per-phase entry points run the same kernels one reference call at a
+ * time.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+#include <algorithm>
+#include <new>
+#include <string>
+#include "pgb_internal.h"
+#include "pgb_physics.cuh"
+#include "pgb_rng.h"
+
+static std::string g_create_error = "no error";
+
+bool pgb_cuda_ok(pgb_run* r, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+    if (r) r->err = msg;
+    else g_create_error = msg;
+    return false;
+}
+
+static int fail(pgb_run* r, int code, const std::string& msg) {
+    if (r) r->err = msg;
+    else g_create_error = msg;
+    return code;
+}
+
+extern "C" const char* pgb_last_error(const pgb_run* r) {
+    return r ? r->err.c_str() : g_create_error.c_str();
+}
+
+/* pgb_params from parameters.h defaults (parameters.h:41-366 and the
+ * boundary constants of pic.cpp:459-484)                               */
+extern "C" int pgb_params_default(pgb_params* p) {
+    if (!p) return PGB_ERR_ARG;
+    memset(p, 0, sizeof(*p));
+    const double CHARGE = 1.602177e-19, EPS = 8.854e-12, ME = 9.10939e-31, AMU = 1.66054e-27, PI = 3.141592654;
+    const double T = 1.5, ne = 1.0e15;
+    double ion_mass = 39.948 * AMU;
+    double xl = (double)64 * sqrt((EPS * T) / (ne * CHARGE));
+    double pf = sqrt((ne * 2.566971e-38) / (EPS * ME));
+    p->x_no_of_cells = p->y_no_of_cells = 257;
+    p->xlength = p->ylength = xl;
+    p->dt = 0.1 / pf;
+    p->dti = 1.0 * p->dt;
+    p->electron_mass = ME;
+    p->ion_mass = ion_mass;
+    p->q_over_me = -CHARGE / ME;
+    p->q_over_mi = CHARGE / ion_mass;
+    p->qce = 1.0e6 * -CHARGE;
+    p->qci = 1.0e6 * CHARGE;
+    p->vte = sqrt(T * CHARGE / ME);
+    p->vti = sqrt(T * CHARGE / ion_mass);
+    p->vtn = sqrt(0.025 * CHARGE / ion_mass);
+    p->angle = 30.0 * PI / 180.0;
+    p->neutral_density = (0.2 * 133.32) / (0.025 * CHARGE);
+    p->threshold = 15.75;
+    p->work_function = 4.6;
+    p->species = PGB_ARGON;
+    p->steadystate = 1;
+    p->init_no_neutrals = 10000;
+    p->see_e0 = 4.32; p->see_max_yield = 1.4; p->see_emax0 = 650.0;
+    p->no_groups = 3;
+    for (int k = 0; k < 3; ++k) {
+        p->v_limit_e[k] = (k == 0 ? 2.0 : k == 1 ? 3.0 : 1000.0) * p->vte;
+        p->v_limit_i[k] = (k == 0 ? 2.0 : k == 1 ? 3.0 : 1000.0) * p->vti;
+        p->group_limit_e[k] = 400000; p->new_group_size_e[k] = 200000;
+        p->group_limit_i[k] = k == 0 ? 400000 : 100000;
+        p->new_group_size_i[k] = k == 0 ? 200000 : 50000;
+    }
+    p->size_to_check_e = p->size_to_check_i = 1000001;
+    p->seed = 1;
+    p->poisson_mode = PGB_POISSON_FMG_REF;
+    p->dc_max_iters = 8;
+    p->dc_tolerance = 1e-10;
+    return 0;
+}
+
+/* collisions::calc_neutral_velocity (collisions.cpp:66-89) on the Philox
+ * stream of entry i; the same host code builds the CPU oracle's table.   */
+static void neutral_table(const pgb_params& p, int which, double* out) {
+    const int n = p.init_no_neutrals;
+    const double PI = 3.141592654, vtn = p.vtn;
+    for (int i = 0; i < n; ++i) {
+        pgb_stream st;
+        pgb_stream_init(&st, p.seed, (uint32_t)i, 0u, which ? PGB_STREAM_NEUTRAL_I : PGB_STREAM_NEUTRAL_E, 0u);
+        double vx, vy, vz;
+        do {
+            double R1 = pgb_u01d(pgb_stream_u32(&st));
+            double R2 = pgb_u01d(pgb_stream_u32(&st));
+            vx = vtn * cos(PI * R2) * sqrt(fabs(log(R1)));
+        } while (fabs(vx) > 10000.0 * vtn);
+        do {
+            double R1 = pgb_u01d(pgb_stream_u32(&st));
+            double R2 = pgb_u01d(pgb_stream_u32(&st));
+            vy = vtn * cos(PI * R2) * sqrt(fabs(log(R1)));
+            vz = vtn * sin(PI * R2) * sqrt(fabs(log(R1)));
+        } while (fabs(vy) > 10000.0 * vtn || fabs(vz) > 10000.0 * vtn);
+        out[i] = vx; out[n + i] = vy; out[2 * n + i] = vz;
+    }
+}
+
+static int validate(const pgb_params* p, std::string& why) {
+    int n = p->x_no_of_cells;
+    if (n < 5 || p->y_no_of_cells != n) { why = "grid must be square with at least 5 nodes"; return 0; }
+    if (((n - 1) & (n - 2)) != 0) { why = "X_NO_OF_CELLS-1 must be a power of 2 (mglin.cpp:26)"; return 0; }
+    if ((n - 1) > 32768) { why = "grid too large"; return 0; }
+    if (!(p->xlength > 0) || !(p->ylength > 0) || !(p->dt > 0) || !(p->dti > 0)) { why = "lengths and time steps must be positive"; return 0; }
+    if (p->init_no_neutrals < 2) { why = "INIT_NO_NEUTRALS must be >= 2"; return 0; }
+    if (p->no_groups < 1 || p->no_groups > 3) { why = "NO_GROUPS must be 1..3"; return 0; }
+    return 1;
+}
+
+static void free_species(Species& S) {
+    cudaFree(S.xv); cudaFree(S.vz); cudaFree(S.w); cudaFree(S.id);
+    cudaFree(S.xv2); cudaFree(S.vz2); cudaFree(S.w2); cudaFree(S.id2);
+    S.xv = nullptr; S.vz = nullptr; S.w = nullptr; S.id = nullptr;
+    S.xv2 = nullptr; S.vz2 = nullptr; S.w2 = nullptr; S.id2 = nullptr;
+    S.cap = 0;
+}
+
+static void free_lists(pgb_run* r) {
+    for (int l = 0; l < 4; ++l) {
+        cudaFree(r->tile_list[l]); cudaFree(r->tile_cnt[l]); cudaFree(r->list[l]);
+        r->tile_list[l] = r->tile_cnt[l] = r->list[l] = nullptr;
+    }
+    cudaFree(r->aux_i); cudaFree(r->aux_j); cudaFree(r->cx_tile_sum);
+    r->aux_i = r->aux_j = nullptr;
+    r->cx_tile_sum = nullptr;
+    r->list_cap = 0;
+    r->ntiles_cap = 0;
+}
+
+/* grow particle storage (keeps contents) and the capacity-sized scratch */
+static int ensure_capacity(pgb_run* r, int s, long long need) {
+    Species& S = r->sp[s];
+    if (need > S.cap) {
+        long long cap = std::max<long long>(need, 1024);
+        Species T = S;
+        T.cap = cap;
+        if (cudaMalloc(&T.xv, sizeof(float4) * cap) != cudaSuccess || cudaMalloc(&T.vz, sizeof(float) * cap) != cudaSuccess ||
+            cudaMalloc(&T.w, sizeof(float) * cap) != cudaSuccess || cudaMalloc(&T.id, sizeof(unsigned) * cap) != cudaSuccess ||
+            cudaMalloc(&T.xv2, sizeof(float4) * cap) != cudaSuccess || cudaMalloc(&T.vz2, sizeof(float) * cap) != cudaSuccess ||
+            cudaMalloc(&T.w2, sizeof(float) * cap) != cudaSuccess || cudaMalloc(&T.id2, sizeof(unsigned) * cap) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(r, PGB_ERR_NOMEM, "device allocation of particle storage failed");
+        }
+        if (S.cap > 0) {
+            long long n = r->hs->n[s];
+            PGB_CK(r, cudaMemcpyAsync(T.xv, S.xv, sizeof(float4) * n, cudaMemcpyDeviceToDevice, r->stream));
+            PGB_CK(r, cudaMemcpyAsync(T.vz, S.vz, sizeof(float) * n, cudaMemcpyDeviceToDevice, r->stream));
+            PGB_CK(r, cudaMemcpyAsync(T.w, S.w, sizeof(float) * n, cudaMemcpyDeviceToDevice, r->stream));
+            PGB_CK(r, cudaMemcpyAsync(T.id, S.id, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, r->stream));
+            PGB_CK(r, cudaStreamSynchronize(r->stream));
+        }
+        free_species(S);
+        S = T;
+    }
+    long long lc = std::max(r->sp[0].cap, r->sp[1].cap);
+    if (lc > r->list_cap) {
+        free_lists(r);
+        long long nt = (lc + PGB_TILE - 1) / PGB_TILE + 1;
+        for (int l = 0; l < 4; ++l) {
+            if (cudaMalloc(&r->tile_list[l], sizeof(int) * nt * PGB_TILE) != cudaSuccess ||
+                cudaMalloc(&r->tile_cnt[l], sizeof(int) * nt) != cudaSuccess ||
+                cudaMalloc(&r->list[l], sizeof(int) * lc) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(r, PGB_ERR_NOMEM, "device allocation of event lists failed");
+            }
+            PGB_CK(r, cudaMemset(r->tile_cnt[l], 0, sizeof(int) * nt));
+        }
+        if (cudaMalloc(&r->aux_i, sizeof(int) * std::max(lc, nt)) != cudaSuccess ||
+            cudaMalloc(&r->aux_j, sizeof(int) * std::max(lc, nt)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(r, PGB_ERR_NOMEM, "device allocation of scratch failed");
+        }
+        long long cxt = (lc + 4096 - 1) / 4096 + 1;
+        if (cudaMalloc(&r->cx_tile_sum, sizeof(long long) * cxt * r->nx) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(r, PGB_ERR_NOMEM, "device allocation of CX scratch failed");
+        }
+        r->list_cap = lc;
+        r->ntiles_cap = nt;
+    }
+    return 0;
+}
+
+static int sync_state(pgb_run* r) {
+    PGB_CK(r, cudaMemcpyAsync(r->hs, r->ds, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
+    PGB_CK(r, cudaStreamSynchronize(r->stream));
+    if (r->hs->err) {
+        int e = r->hs->err;
+        std::string m = "device reported:";
+        if (e & ERR_CAP_E) m += " electron capacity exceeded;";
+        if (e & ERR_CAP_I) m += " ion capacity exceeded;";
+        if (e & ERR_LIST) m += " event list overflow;";
+        r->hs->err = 0;
+        PGB_CK(r, cudaMemsetAsync(&r->ds->err, 0, sizeof(int), r->stream));
+        return fail(r, PGB_ERR_CAPACITY, m);
+    }
+    return 0;
+}
+
+extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
+    if (!p || !out) return fail(nullptr, PGB_ERR_ARG, "null argument");
+    *out = nullptr;
+    std::string why;
+    if (!validate(p, why)) return fail(nullptr, PGB_ERR_ARG, why);
+    pgb_run* r = new (std::nothrow) pgb_run();
+    if (!r) return fail(nullptr, PGB_ERR_NOMEM, "host allocation failed");
+    r->p = *p;
+    r->nx = p->x_no_of_cells;
+    r->ny = p->y_no_of_cells;
+    r->dx = p->xlength / (double)(r->nx - 1);
+    r->dy = p->ylength / (double)(r->ny - 1);
+    r->dt_dti = std::max(1, (int)(p->dti / p->dt));
+    r->sp[0].qc = p->qce; r->sp[0].q_over_m = p->q_over_me; r->sp[0].mass = p->electron_mass;
+    r->sp[0].vt = p->vte; r->sp[0].dt = p->dt;
+    r->sp[1].qc = p->qci; r->sp[1].q_over_m = p->q_over_mi; r->sp[1].mass = p->ion_mass;
+    r->sp[1].vt = p->vti; r->sp[1].dt = p->dti;
+    auto bail = [&](int code) { pgb_destroy(r); return code; };
+    if (!pgb_cuda_ok(nullptr, cudaGetDevice(&r->dev), "cudaGetDevice")) return bail(PGB_ERR_CUDA);
+    if (!pgb_cuda_ok(nullptr, cudaDeviceGetAttribute(&r->sms, cudaDevAttrMultiProcessorCount, r->dev), "sm count"))
+        return bail(PGB_ERR_CUDA);
+    if (!pgb_cuda_ok(nullptr, cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "cudaStreamCreate"))
+        return bail(PGB_ERR_CUDA);
+    const size_t G = (size_t)r->nx * r->ny, GE = (size_t)(r->nx + 1) * (r->ny + 1);
+    bool ok = true;
+    ok = ok && cudaMalloc(&r->ds, sizeof(DevState)) == cudaSuccess;
+    ok = ok && cudaMallocHost(&r->hs, sizeof(DevState)) == cudaSuccess;
+    for (int s = 0; s < 2; ++s) {
+        ok = ok && cudaMalloc(&r->qacc[s], sizeof(unsigned long long) * G) == cudaSuccess;
+        ok = ok && cudaMalloc(&r->q[s], sizeof(double) * G) == cudaSuccess;
+    }
+    ok = ok && cudaMalloc(&r->rho, sizeof(double) * G) == cudaSuccess;
+    ok = ok && cudaMalloc(&r->phi, sizeof(double) * G) == cudaSuccess;
+    ok = ok && cudaMalloc(&r->ex, sizeof(double) * GE) == cudaSuccess;
+    ok = ok && cudaMalloc(&r->ey, sizeof(double) * GE) == cudaSuccess;
+    ok = ok && cudaMalloc(&r->exy, sizeof(float2) * GE) == cudaSuccess;
+    ok = ok && cudaMalloc(&r->prob_cx, sizeof(long long) * r->nx) == cudaSuccess;
+    int ng = 0, nn = r->nx;
+    while (nn >>= 1) ng++;
+    r->ng = ng;
+    nn = r->nx;
+    for (int j = ng - 1; j >= 0; --j) {
+        r->mg_n[j] = nn;
+        size_t s = (size_t)nn * nn * sizeof(double);
+        ok = ok && cudaMalloc(&r->mg_u[j], s) == cudaSuccess && cudaMalloc(&r->mg_f[j], s) == cudaSuccess &&
+             cudaMalloc(&r->mg_v[j], s) == cudaSuccess && cudaMalloc(&r->mg_r[j], s) == cudaSuccess;
+        nn = nn / 2 + 1;
+    }
+    for (int w = 0; w < 2; ++w)
+        ok = ok && cudaMalloc(&r->neut64[w], sizeof(double) * 3 * p->init_no_neutrals) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        fail(nullptr, PGB_ERR_NOMEM, "device allocation failed");
+        return bail(PGB_ERR_NOMEM);
+    }
+    memset(r->hs, 0, sizeof(DevState));
+    if (!pgb_cuda_ok(nullptr, cudaMemset(r->ds, 0, sizeof(DevState)), "memset")) return bail(PGB_ERR_CUDA);
+    cudaMemset(r->q[0], 0, sizeof(double) * G);
+    cudaMemset(r->q[1], 0, sizeof(double) * G);
+    cudaMemset(r->rho, 0, sizeof(double) * G);
+    cudaMemset(r->phi, 0, sizeof(double) * G);
+    cudaMemset(r->ex, 0, sizeof(double) * GE);
+    cudaMemset(r->ey, 0, sizeof(double) * GE);
+    cudaMemset(r->exy, 0, sizeof(float2) * GE);
+    cudaMemset(r->prob_cx, 0, sizeof(long long) * r->nx);
+    /* ion table first, then electron table (pic.cpp:135-138) */
+    double* tab = (double*)malloc(sizeof(double) * 3 * p->init_no_neutrals);
+    for (int w = 1; w >= 0; --w) {
+        neutral_table(*p, w, tab);
+        cudaMemcpy(r->neut64[w], tab, sizeof(double) * 3 * p->init_no_neutrals, cudaMemcpyHostToDevice);
+    }
+    free(tab);
+    if (pgb_mg_setup(r)) { g_create_error = r->err; return bail(PGB_ERR_CUDA); }
+    if (!pgb_cuda_ok(nullptr, cudaDeviceSynchronize(), "create")) return bail(PGB_ERR_CUDA);
+    *out = r;
+    return 0;
+}
+
+extern "C" int pgb_destroy(pgb_run* r) {
+    if (!r) return 0;
+    if (r->stream) cudaStreamSynchronize(r->stream);
+    free_species(r->sp[0]);
+    free_species(r->sp[1]);
+    free_lists(r);
+    cudaFree(r->ds);
+    if (r->hs) cudaFreeHost(r->hs);
+    for (int s = 0; s < 2; ++s) { cudaFree(r->qacc[s]); cudaFree(r->q[s]); }
+    cudaFree(r->rho); cudaFree(r->phi); cudaFree(r->ex); cudaFree(r->ey); cudaFree(r->exy);
+    cudaFree(r->prob_cx);
+    for (int j = 0; j < r->ng; ++j) { cudaFree(r->mg_u[j]); cudaFree(r->mg_f[j]); cudaFree(r->mg_v[j]); cudaFree(r->mg_r[j]); }
+    cudaFree(r->mg_tab);
+    for (int w = 0; w < 2; ++w) cudaFree(r->neut64[w]);
+    if (r->h_stage) cudaFreeHost(r->h_stage);
+    if (r->stream) cudaStreamDestroy(r->stream);
+    delete r;
+    return 0;
+}
+
+static int stage(pgb_run* r, size_t bytes) {
+    if (bytes <= r->h_stage_bytes) return 0;
+    if (r->h_stage) cudaFreeHost(r->h_stage);
+    r->h_stage = nullptr;
+    r->h_stage_bytes = 0;
+    PGB_CK(r, cudaMallocHost(&r->h_stage, bytes));
+    r->h_stage_bytes = bytes;
+    return 0;
+}
+
+extern "C" int pgb_load_species(pgb_run* r, int s, const double* aos6, int64_t n) {
+    if (!r || s < 0 || s > 1 || n < 0 || (n > 0 && !aos6)) return fail(r, PGB_ERR_ARG, "pgb_load_species: bad argument");
+    if (n > 0x7fffffffLL) return fail(r, PGB_ERR_ARG, "pgb_load_species: too many particles");
+    int rc = sync_state(r);
+    if (rc) return rc;
+    long long want = s == 0 ? r->p.capacity_e : r->p.capacity_i;
+    long long cap = std::max<long long>(want, 2 * n + 65536);
+    if (cap > 0x7fffffffLL) cap = 0x7fffffffLL;
+    r->hs->n[s] = 0;
+    if ((rc = ensure_capacity(r, s, cap))) return rc;
+    if ((rc = ensure_capacity(r, 1 - s, std::max<long long>(r->sp[1 - s].cap, 1024)))) return rc;
+    if (n > 0) {
+        double* d = nullptr;
+        PGB_CK(r, cudaMalloc(&d, sizeof(double) * 6 * n));
+        if (cudaMemcpyAsync(d, aos6, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, r->stream) != cudaSuccess ||
+            pgb_launch_load(r, s, d, n) || cudaStreamSynchronize(r->stream) != cudaSuccess) {
+            cudaFree(d);
+            return fail(r, PGB_ERR_CUDA, "pgb_load_species: upload failed");
+        }
+        cudaFree(d);
+    }
+    r->hs->n[s] = n;
+    r->hs->dead[s] = 0;
+    r->hs->next_id[s] = (unsigned)n;
+    PGB_CK(r, cudaMemcpyAsync(&r->ds->n[s], &r->hs->n[s], sizeof(long long), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaMemcpyAsync(&r->ds->dead[s], &r->hs->dead[s], sizeof(long long), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaMemcpyAsync(&r->ds->next_id[s], &r->hs->next_id[s], sizeof(unsigned), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaStreamSynchronize(r->stream));
+    return 0;
+}
+
+extern "C" int pgb_species_count(pgb_run* r, int s, int64_t* n_out) {
+    if (!r || s < 0 || s > 1 || !n_out) return fail(r, PGB_ERR_ARG, "pgb_species_count: bad argument");
+    int rc = sync_state(r);
+    if (rc) return rc;
+    *n_out = r->hs->n[s] - r->hs->dead[s];
+    return 0;
+}
+
+extern "C" int pgb_dump_species(pgb_run* r, int s, double* aos6, int64_t cap, int64_t* n_out) {
+    if (!r || s < 0 || s > 1 || cap < 0 || (cap > 0 && !aos6)) return fail(r, PGB_ERR_ARG, "pgb_dump_species: bad argument");
+    int rc = sync_state(r);
+    if (rc) return rc;
+    long long live = r->hs->n[s] - r->hs->dead[s];
+    if (n_out) *n_out = live;
+    long long m = std::min<long long>(live, cap);
+    if (m <= 0 || r->sp[s].cap == 0) return 0;
+    double* d = nullptr;
+    PGB_CK(r, cudaMalloc(&d, sizeof(double) * 6 * live));
+    if (pgb_launch_dump(r, s, d, live) ||
+        cudaMemcpyAsync(aos6, d, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost, r->stream) != cudaSuccess ||
+        cudaStreamSynchronize(r->stream) != cudaSuccess) {
+        cudaFree(d);
+        return fail(r, PGB_ERR_CUDA, "pgb_dump_species: download failed");
+    }
+    cudaFree(d);
+    return 0;
+}
+
+extern "C" int pgb_set_time_step(pgb_run* r, int64_t t) {
+    if (!r) return PGB_ERR_ARG;
+    r->time_step = t;
+    return 0;
+}
+
+static int need_particles(pgb_run* r) {
+    if (r->sp[0].cap == 0 || r->sp[1].cap == 0) return fail(r, PGB_ERR_STATE, "load both species first");
+    return 0;
+}
+
+/* ---------------------------------------------------- phase entry points */
+static int boundary_phase(pgb_run* r, int which) {
+    if (r->p.steadystate) {
+        if (which != PGB_BOUNDARY_ELECTRONS) return 0;   /* steady_i_boundary is empty */
+        if (pgb_launch_flag_outside(r, 0) || pgb_build_list(r, LIST_OUT_E, 0)) return PGB_ERR_CUDA;
+        if (pgb_launch_flag_outside(r, 1) || pgb_build_list(r, LIST_OUT_I, 1)) return PGB_ERR_CUDA;
+        return pgb_launch_walls(r, which);
+    }
+    int s = which == PGB_BOUNDARY_IONS ? 1 : 0;
+    int l = s ? LIST_OUT_I : LIST_OUT_E;
+    if (pgb_launch_flag_outside(r, s) || pgb_build_list(r, l, s)) return PGB_ERR_CUDA;
+    return pgb_launch_walls(r, which);
+}
+
+extern "C" int pgb_boundary(pgb_run* r, int which) {
+    if (!r || (which != 0 && which != 1)) return fail(r, PGB_ERR_ARG, "pgb_boundary: bad argument");
+    int rc = need_particles(r);
+    if (rc) return rc;
+    /* deposits made by wall events go to the accumulators of the step; in
+     * the phase-by-phase form the charge is recomputed by pgb_deposit     */
+    if ((rc = boundary_phase(r, which))) return rc;
+    return sync_state(r);
+}
+
+extern "C" int pgb_initial_boundary(pgb_run* r) {
+    if (!r) return PGB_ERR_ARG;
+    int rc = need_particles(r);
+    if (rc) return rc;
+    int64_t saved = r->time_step;
+    r->time_step = -1;   /* random streams of the pre-loop boundary pass */
+    rc = boundary_phase(r, PGB_BOUNDARY_IONS);
+    if (!rc) rc = boundary_phase(r, PGB_BOUNDARY_ELECTRONS);
+    r->time_step = saved;
+    if (rc) return rc;
+    return sync_state(r);
+}
+
+extern "C" int pgb_collide_electrons(pgb_run* r) {
+    if (!r) return PGB_ERR_ARG;
+    int rc = need_particles(r);
+    if (rc) return rc;
+    if (pgb_launch_mcc(r) || pgb_build_list(r, LIST_ION_EV, 0) || pgb_launch_ionize_appends(r, 1, 1))
+        return PGB_ERR_CUDA;
+    return sync_state(r);
+}
+
+extern "C" int pgb_inject(pgb_run* r) {
+    if (!r) return PGB_ERR_ARG;
+    int rc = need_particles(r);
+    if (rc) return rc;
+    if (pgb_launch_inject(r, 3, false)) return PGB_ERR_CUDA;
+    return sync_state(r);
+}
+
+extern "C" int pgb_gather_push(pgb_run* r, int s) {
+    if (!r || s < 0 || s > 1) return fail(r, PGB_ERR_ARG, "pgb_gather_push: bad argument");
+    int rc = need_particles(r);
+    if (rc) return rc;
+    if (pgb_launch_push(r, s, false, false, false)) return PGB_ERR_CUDA;
+    return sync_state(r);
+}
+
+extern "C" int pgb_collide_ions(pgb_run* r) {
+    if (!r) return PGB_ERR_ARG;
+    int rc = need_particles(r);
+    if (rc) return rc;
+    if (pgb_launch_cx(r)) return PGB_ERR_CUDA;
+    return sync_state(r);
+}
+
+extern "C" int pgb_contain_growth(pgb_run* r, int s) {
+    if (!r || s < 0 || s > 1) return fail(r, PGB_ERR_ARG, "pgb_contain_growth: bad argument");
+    int rc = sync_state(r);
+    if (rc) return rc;
+    long long live = r->hs->n[s] - r->hs->dead[s];
+    long long lim = s == 0 ? r->p.size_to_check_e : r->p.size_to_check_i;
+    if (live > lim) return pgb_launch_reduce(r, s) ? PGB_ERR_CUDA : sync_state(r);
+    return 0;
+}
+
+extern "C" int pgb_deposit(pgb_run* r, int s) {
+    if (!r || s < 0 || s > 1) return fail(r, PGB_ERR_ARG, "pgb_deposit: bad argument");
+    int rc = need_particles(r);
+    if (rc) return rc;
+    PGB_CK(r, cudaMemsetAsync(r->qacc[s], 0, sizeof(unsigned long long) * r->nx * r->ny, r->stream));
+    if (pgb_launch_deposit(r, s) || pgb_launch_finalize(r, 1 << s, false, 0.0)) return PGB_ERR_CUDA;
+    return sync_state(r);
+}
+
+extern "C" int pgb_grid_rho(pgb_run* r) {
+    if (!r) return PGB_ERR_ARG;
+    if (pgb_launch_finalize(r, 0, false, 0.0)) return PGB_ERR_CUDA;
+    return sync_state(r);
+}
+
+extern "C" int pgb_poisson(pgb_run* r, int64_t t) {
+    if (!r) return PGB_ERR_ARG;
+    double phi_right = r->p.phi_right * cos(r->p.phi_period * (double)t);
+    if (pgb_launch_rhs(r, phi_right) || pgb_poisson_solve(r, t)) return PGB_ERR_CUDA;
+    return sync_state(r);
+}
+
+extern "C" int pgb_efield(pgb_run* r) {
+    if (!r) return PGB_ERR_ARG;
+    if (pgb_launch_efield(r)) return PGB_ERR_CUDA;
+    return sync_state(r);
+}
+
+/* -------------------------------------------------------------- pgb_step */
+static int step_once(pgb_run* r) {
+    const int64_t t = r->time_step;
+    const bool coll = r->p.have_collisions != 0;
+    const bool ion_step = (t % r->dt_dti) == 0;
+    const size_t G = (size_t)r->nx * r->ny;
+    PGB_CK(r, cudaMemsetAsync(r->qacc[0], 0, sizeof(unsigned long long) * G, r->stream));
+    PGB_CK(r, cudaMemsetAsync(r->qacc[1], 0, sizeof(unsigned long long) * G, r->stream));
+    /* e_collisions::collision + get_particle_electric_field + move_particles */
+    if (pgb_launch_push(r, 0, coll, true, coll)) return PGB_ERR_CUDA;
+    if (pgb_build_list(r, LIST_OUT_E, 0)) return PGB_ERR_CUDA;
+    if (coll) {
+        if (pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
+        int store_e = r->p.steadystate ? 1 : 0;
+        int store_i = (r->p.steadystate || !ion_step) ? 1 : 0;
+        if (pgb_launch_ionize_appends(r, store_e, store_i)) return PGB_ERR_CUDA;
+    }
+    /* inject_more_particles: electrons are pushed as they are created */
+    if (r->p.number_to_inject > 0 && pgb_launch_inject(r, 3, true)) return PGB_ERR_CUDA;
+    if (ion_step) {
+        if (coll && pgb_launch_cx(r)) return PGB_ERR_CUDA;
+        if (pgb_launch_push(r, 1, false, true, false)) return PGB_ERR_CUDA;
+        if (pgb_build_list(r, LIST_OUT_I, 1)) return PGB_ERR_CUDA;
+        if (pgb_launch_walls(r, PGB_BOUNDARY_IONS)) return PGB_ERR_CUDA;
+        if (pgb_launch_walls(r, PGB_BOUNDARY_ELECTRONS)) return PGB_ERR_CUDA;
+    } else {
+        if (pgb_launch_deposit(r, 1)) return PGB_ERR_CUDA;
+        if (r->p.steadystate && (pgb_launch_flag_outside(r, 1) || pgb_build_list(r, LIST_OUT_I, 1))) return PGB_ERR_CUDA;
+        if (pgb_launch_walls(r, PGB_BOUNDARY_ELECTRONS)) return PGB_ERR_CUDA;
+    }
+    /* contain_particle_growth: only when a species can exceed its limit */
+    if (!r->p.steadystate) {
+        for (int s = 0; s < 2; ++s) {
+            long long lim = s == 0 ? r->p.size_to_check_e : r->p.size_to_check_i;
+            if (r->sp[s].cap > lim) {
+                int rc = sync_state(r);
+                if (rc) return rc;
+                if (r->hs->n[s] - r->hs->dead[s] > lim) {
+                    if (pgb_launch_reduce(r, s)) return PGB_ERR_CUDA;
+                    /* the reduction changes weights: rebuild both charges */
+                    PGB_CK(r, cudaMemsetAsync(r->qacc[0], 0, sizeof(unsigned long long) * G, r->stream));
+                    PGB_CK(r, cudaMemsetAsync(r->qacc[1], 0, sizeof(unsigned long long) * G, r->stream));
+                    if (pgb_launch_deposit(r, 0) || pgb_launch_deposit(r, 1)) return PGB_ERR_CUDA;
+                }
+            }
+        }
+    }
+    /* collect_charge edge doubling, grid_rho, grid_potential, grid_electric_field */
+    double phi_right = r->p.phi_right * cos(r->p.phi_period * (double)t);
+    if (pgb_launch_finalize(r, 3, true, phi_right)) return PGB_ERR_CUDA;
+    if (pgb_poisson_solve(r, t)) return PGB_ERR_CUDA;
+    if (pgb_launch_efield(r)) return PGB_ERR_CUDA;
+    r->time_step = t + 1;
+    return 0;
+}
+
+extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
+    if (!r || nsteps < 0) return fail(r, PGB_ERR_ARG, "pgb_step: bad argument");
+    int rc = need_particles(r);
+    if (rc) return rc;
+    for (int k = 0; k < nsteps; ++k) {
+        /* compact when tombstones exceed 1/8 of the slots (counts read lazily) */
+        for (int s = 0; s < 2; ++s)
+            if (r->hs->dead[s] * 8 > r->hs->n[s] && r->hs->dead[s] > 0) {
+                if (pgb_launch_compact(r, s)) return PGB_ERR_CUDA;
+                r->hs->dead[s] = 0;
+            }
+        if ((rc = step_once(r))) return rc;
+        PGB_CK(r, cudaMemcpyAsync(r->hs, r->ds, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
+        if ((k & 7) == 7) PGB_CK(r, cudaStreamSynchronize(r->stream));
+    }
+    return sync_state(r);
+}
+
+/* ------------------------------------------------------------ grids */
+extern "C" int pgb_get_grid(pgb_run* r, int which, double* out, int64_t n) {
+    if (!r || !out) return fail(r, PGB_ERR_ARG, "pgb_get_grid: bad argument");
+    int64_t G = (int64_t)r->nx * r->ny, GE = (int64_t)(r->nx + 1) * (r->ny + 1);
+    const double* src = nullptr;
+    int64_t cnt = G;
+    switch (which) {
+        case PGB_GRID_Q_E: src = r->q[0]; break;
+        case PGB_GRID_Q_I: src = r->q[1]; break;
+        case PGB_GRID_RHO: src = r->rho; break;
+        case PGB_GRID_PHI: src = r->phi; break;
+        case PGB_GRID_EX: src = r->ex; cnt = GE; break;
+        case PGB_GRID_EY: src = r->ey; cnt = GE; break;
+        default: return fail(r, PGB_ERR_ARG, "pgb_get_grid: unknown grid");
+    }
+    if (n < cnt) return fail(r, PGB_ERR_ARG, "pgb_get_grid: buffer too small");
+    PGB_CK(r, cudaMemcpyAsync(out, src, sizeof(double) * cnt, cudaMemcpyDeviceToHost, r->stream));
+    PGB_CK(r, cudaStreamSynchronize(r->stream));
+    return 0;
+}
+
+extern "C" int pgb_set_rho(pgb_run* r, const double* rho, int64_t n) {
+    if (!r || !rho) return fail(r, PGB_ERR_ARG, "pgb_set_rho: bad argument");
+    int64_t G = (int64_t)r->nx * r->ny;
+    if (n < G) return fail(r, PGB_ERR_ARG, "pgb_set_rho: buffer too small");
+    PGB_CK(r, cudaMemcpyAsync(r->rho, rho, sizeof(double) * G, cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaStreamSynchronize(r->stream));
+    return 0;
+}
+
+extern "C" int pgb_get_counters(pgb_run* r, pgb_counters* c) {
+    if (!r || !c) return fail(r, PGB_ERR_ARG, "pgb_get_counters: bad argument");
+    int rc = sync_state(r);
+    if (rc) return rc;
+    const DevState& h = *r->hs;
+    memset(c, 0, sizeof(*c));
+    c->n_e = h.n[0] - h.dead[0];
+    c->n_i = h.n[1] - h.dead[1];
+    c->step = r->time_step;
+    c->absorbed_e = h.stats[ST_ABS_E];
+    c->absorbed_i = h.stats[ST_ABS_I];
+    c->plopped = h.stats[ST_PLOP];
+    c->reflected = h.stats[ST_REFL];
+    c->backscattered = h.stats[ST_BACK];
+    c->see_events = h.stats[ST_SEE_EV];
+    c->see_emitted = h.stats[ST_SEE_EM];
+    c->ion_see_emitted = h.stats[ST_ISEE_EM];
+    c->elastic = h.stats[ST_ELASTIC];
+    c->ionization = h.stats[ST_IONIZE];
+    c->charge_exchange = h.stats[ST_CX];
+    c->injected_e = h.stats[ST_INJ_E];
+    c->injected_i = h.stats[ST_INJ_I];
+    c->reductions_e = h.stats[ST_RED_E];
+    c->reductions_i = h.stats[ST_RED_I];
+    return 0;
+}
+
+extern "C" int pgb_sync(pgb_run* r) {
+    if (!r) return PGB_ERR_ARG;
+    return sync_state(r);
+}
+
+/* Kunhardt reduction: not yet on the device; report instead of guessing */
+int pgb_launch_reduce(pgb_run* r, int s) {
+    (void)s;
+    fail(r, PGB_ERR_STATE, "population reduction (SIZE_TO_CHECK exceeded) is not implemented on the device yet");
+    return PGB_ERR_STATE;
+}

@@ -1,0 +1,469 @@
+/*
+ * Grid kernels: charge finalisation and rho, the Poisson right-hand side,
+ * the full-multigrid solve and the electric field.
+ *
+ * Reference path: particle::collect_charge edge doubling
+ * (particle.cpp:829-845), fields::grid_rho (fields.cpp:100-143),
+ * fields::grid_potential (fields.cpp:169-220) with Mglin (mglin.cpp:21-196),
+ * fields::grid_electric_field (fields.cpp:230-268).
+ *
+ * This file is compiled with --fmad=false: the FP64 multigrid performs the
+ * reference's additions and multiplications one by one, in its order, so
+ * that from the same right-hand side it returns the reference's potential
+ * bit for bit.  Within one colour of the red-black sweep every update reads
+ * only the other colour, so the order of updates inside a colour does not
+ * change the result.
+ *
+ * Schedule (one call): restrict the right-hand side to every level, solve
+ * the 3x3 grid, then for each finer level prolong and run two V(1,1)
+ * cycles.  Levels with n <= PGB_MG_SMALL (65) run inside one CTA with all
+ * their arrays in shared memory (one launch per coarse sub-solve); finer
+ * levels use one launch per grid operation.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include "pgb_internal.h"
+
+/* ------------------------------------------------ charge, rho, rhs */
+struct FinalizeArgs {
+    const unsigned long long* acc[2];
+    double* q[2];
+    double* rho;
+    double* f;            /* Poisson right-hand side, or null */
+    int nx, ny;
+    double qcdxdy[2];     /* qc/(DX*DY) per species */
+    int mask;             /* species whose q is rebuilt from acc */
+    double coef;          /* 1/EPSILON */
+    double divdxdy;       /* 1/(DX*DY) */
+    double phi0x, phirx, phi0y, phily;
+};
+
+__device__ __forceinline__ double edge_factor(int i, int j, int nx, int ny) {
+    bool ex = (i == 0 || i == nx - 1), ey = (j == 0 || j == ny - 1);
+    /* columns doubled, rows doubled, corners doubled again (particle.cpp:830-845) */
+    return (ex ? 2.0 : 1.0) * (ey ? 2.0 : 1.0) * ((ex && ey) ? 2.0 : 1.0);
+}
+
+/* RHS of fields::grid_potential (fields.cpp:184-204) for node (j, i) */
+__device__ __forceinline__ double rhs_node(double rho, int i, int j, const FinalizeArgs& a) {
+    double f = -a.coef * rho;
+    if (i == 1) f = f - a.phi0x * a.divdxdy;
+    if (i == a.nx - 2) f = f - a.phirx * a.divdxdy;
+    if (j == 1) f = f - a.phi0y * a.divdxdy;
+    if (j == a.ny - 2) f = f - a.phily * a.divdxdy;
+    return f;
+}
+
+__global__ void k_finalize(FinalizeArgs a) {
+    const int G = a.nx * a.ny;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x) {
+        int j = k / a.nx, i = k - j * a.nx;
+        double ef = edge_factor(i, j, a.nx, a.ny);
+        for (int s = 0; s < 2; ++s)
+            if (a.mask & (1 << s)) {
+                double v = (double)(long long)a.acc[s][k] * (1.0 / PGB_FIX_SCALE);
+                a.q[s][k] = (v * a.qcdxdy[s]) * ef;
+            }
+        double rho = a.q[1][k] + a.q[0][k];
+        a.rho[k] = rho;
+        if (a.f) a.f[k] = rhs_node(rho, i, j, a);
+    }
+}
+
+__global__ void k_rhs(FinalizeArgs a) {
+    const int G = a.nx * a.ny;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x) {
+        int j = k / a.nx, i = k - j * a.nx;
+        a.f[k] = rhs_node(a.rho[k], i, j, a);
+    }
+}
+
+/* ------------------------------------------------------ multigrid ops */
+/* red-black Gauss-Seidel update of one point (mglin.cpp:116-127) */
+template <class T>
+__device__ __forceinline__ T gs_point(const T* u, const T* f, int n, int i, int j, T h2) {
+    return (T)0.25 * (u[(i + 1) * n + j] + u[(i - 1) * n + j] + u[i * n + j + 1] + u[i * n + j - 1] - h2 * f[i * n + j]);
+}
+/* minus the residual at an interior point (mglin.cpp:133-141) */
+template <class T>
+__device__ __forceinline__ T resid_point(const T* u, const T* f, int n, int i, int j, T h2i) {
+    return -h2i * (u[(i + 1) * n + j] + u[(i - 1) * n + j] + u[i * n + j + 1] + u[i * n + j - 1] - (T)4.0 * u[i * n + j]) +
+           f[i * n + j];
+}
+/* half-weighting of the fine residual onto coarse interior point (ic,jc)
+ * (mglin.cpp:151-160 applied to resid's output)                         */
+template <class T>
+__device__ __forceinline__ T restrict_resid_point(const T* u, const T* f, int nf, int ic, int jc, T h2i) {
+    int i = 2 * ic, j = 2 * jc;
+    T c = resid_point(u, f, nf, i, j, h2i);
+    T n1 = resid_point(u, f, nf, i + 1, j, h2i), n2 = resid_point(u, f, nf, i - 1, j, h2i);
+    T n3 = resid_point(u, f, nf, i, j + 1, h2i), n4 = resid_point(u, f, nf, i, j - 1, h2i);
+    return (T)0.5 * c + (T)0.125 * (n1 + n2 + n3 + n4);
+}
+template <class T>
+__device__ __forceinline__ T restrict_point(const T* uf, int nf, int ic, int jc) {
+    int i = 2 * ic, j = 2 * jc;
+    return (T)0.5 * uf[i * nf + j] + (T)0.125 * (uf[(i + 1) * nf + j] + uf[(i - 1) * nf + j] + uf[i * nf + j + 1] + uf[i * nf + j - 1]);
+}
+/* bilinear prolongation value at fine point (i,j) (mglin.cpp:70-82) */
+template <class T>
+__device__ __forceinline__ T prolong_point(const T* uc, int nc, int i, int j) {
+    if ((j & 1) == 0) {
+        if ((i & 1) == 0) return uc[(i >> 1) * nc + (j >> 1)];
+        return (T)0.5 * (uc[((i + 1) >> 1) * nc + (j >> 1)] + uc[((i - 1) >> 1) * nc + (j >> 1)]);
+    }
+    T a, b;   /* values of the two even columns next to j, in row i */
+    if ((i & 1) == 0) {
+        a = uc[(i >> 1) * nc + ((j + 1) >> 1)];
+        b = uc[(i >> 1) * nc + ((j - 1) >> 1)];
+    } else {
+        a = (T)0.5 * (uc[((i + 1) >> 1) * nc + ((j + 1) >> 1)] + uc[((i - 1) >> 1) * nc + ((j + 1) >> 1)]);
+        b = (T)0.5 * (uc[((i + 1) >> 1) * nc + ((j - 1) >> 1)] + uc[((i - 1) >> 1) * nc + ((j - 1) >> 1)]);
+    }
+    return (T)0.5 * (a + b);
+}
+
+/* ------------------------------------------------ grid-wide launches */
+/* generic indexer: covers every interior point of the colour */
+template <class T>
+__global__ void k_relax_rows(T* u, const T* f, int n, T h2, int color) {
+    const int m = n - 2, per_row = (m + 1) / 2;
+    const long long tot = (long long)m * per_row;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+        int r = (int)(t / per_row), c = (int)(t - (long long)r * per_row);
+        int i = r + 1;
+        int j0 = 1 + ((i + 1 + color) & 1);
+        int j = j0 + 2 * c;
+        if (j > n - 2) continue;
+        u[i * n + j] = gs_point(u, f, n, i, j, h2);
+    }
+}
+template <class T>
+__global__ void k_resid_restrict(T* rc, const T* u, const T* f, int nf, T h2i) {
+    const int nc = (nf + 1) / 2;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc * nc; k += gridDim.x * blockDim.x) {
+        int ic = k / nc, jc = k - ic * nc;
+        T v = (T)0;
+        if (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) v = restrict_resid_point(u, f, nf, ic, jc, h2i);
+        rc[k] = v;
+    }
+}
+template <class T>
+__global__ void k_restrict(T* uc, const T* uf, int nc) {
+    const int nf = 2 * nc - 1;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc * nc; k += gridDim.x * blockDim.x) {
+        int ic = k / nc, jc = k - ic * nc;
+        T v;
+        if (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) v = restrict_point(uf, nf, ic, jc);
+        else v = uf[(2 * ic) * nf + 2 * jc];   /* injected boundary (mglin.cpp:161-168) */
+        uc[k] = v;
+    }
+}
+template <class T>
+__global__ void k_prolong(T* uf, const T* uc, int nf, int add) {
+    const int nc = nf / 2 + 1;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nf * nf; k += gridDim.x * blockDim.x) {
+        int i = k / nf, j = k - i * nf;
+        T v = prolong_point(uc, nc, i, j);
+        uf[k] = add ? uf[k] + v : v;
+    }
+}
+
+/* --------------------------------------- one-CTA solver for coarse levels */
+/* Shared-memory image of levels 0..J (n_l = 2^(l+1)+1).  U/F: the current
+ * level's solution and right-hand side at the top, V/R: correction and
+ * restricted residual of the levels below.                              */
+template <class T>
+struct SmallMG {
+    T* U[8];
+    T* F[8];
+    T* V[8];
+    T* R[8];
+    int n[8];
+    T length;
+};
+
+template <class T>
+__device__ void sm_relax(T* u, const T* f, int n, T length) {
+    T h = length / (T)(n - 1), h2 = h * h;
+    const int m = n - 2, per_row = (m + 1) / 2;
+    for (int color = 0; color < 2; ++color) {
+        for (int t = threadIdx.x; t < m * per_row; t += blockDim.x) {
+            int r = t / per_row, c = t - r * per_row;
+            int i = r + 1, j = 1 + ((i + 1 + color) & 1) + 2 * c;
+            if (j <= n - 2) u[i * n + j] = gs_point(u, f, n, i, j, h2);
+        }
+        __syncthreads();
+    }
+}
+template <class T>
+__device__ void sm_coarsest(T* u, const T* f, T length) {
+    if (threadIdx.x == 0) {
+        T h = (T)0.5 * length;
+        for (int k = 0; k < 9; ++k) u[k] = (T)0;
+        u[4] = -h * h * f[4] / (T)4.0;   /* mglin.cpp:103-110 */
+    }
+    __syncthreads();
+}
+/* V-cycle at level j on (u, f) using V/R of the levels below */
+template <class T>
+__device__ void sm_vcycle(SmallMG<T>& s, int j, T* u, const T* f) {
+    if (j == 0) { sm_coarsest(u, f, s.length); return; }
+    for (int l = j; l >= 1; --l) {
+        T* ul = (l == j) ? u : s.V[l];
+        const T* fl = (l == j) ? f : s.R[l];
+        int nf = s.n[l], nc = s.n[l - 1];
+        T h = s.length / (T)(nf - 1), h2i = (T)1.0 / (h * h);
+        sm_relax(ul, fl, nf, s.length);
+        for (int k = threadIdx.x; k < nc * nc; k += blockDim.x) {
+            int ic = k / nc, jc = k - ic * nc;
+            T v = (T)0;
+            if (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) v = restrict_resid_point(ul, fl, nf, ic, jc, h2i);
+            s.R[l - 1][k] = v;
+            s.V[l - 1][k] = (T)0;
+        }
+        __syncthreads();
+    }
+    sm_coarsest(s.V[0], s.R[0], s.length);
+    for (int l = 1; l <= j; ++l) {
+        T* ul = (l == j) ? u : s.V[l];
+        const T* fl = (l == j) ? f : s.R[l];
+        int nf = s.n[l], nc = s.n[l - 1];
+        for (int k = threadIdx.x; k < nf * nf; k += blockDim.x) {
+            int i = k / nf, jj = k - i * nf;
+            ul[k] = ul[k] + prolong_point(s.V[l - 1], nc, i, jj);
+        }
+        __syncthreads();
+        sm_relax(ul, fl, nf, s.length);
+    }
+}
+
+/* mode 0: full multigrid from level 0 to J with rhs levels in g_f[0..J];
+ *         writes u_J to g_u[J].
+ * mode 1: one V-cycle at level J on (g_v[J], g_r[J]) in place.          */
+template <class T>
+__global__ void k_mg_small(int J, int mode, T length, T** g_u, T** g_f, T** g_v, T** g_r) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SmallMG<T> s;
+    s.length = length;
+    T* p = reinterpret_cast<T*>(smem_raw);
+    for (int l = 0; l <= J; ++l) {
+        int n = (1 << (l + 1)) + 1;
+        s.n[l] = n;
+        s.U[l] = p; p += n * n;
+        s.F[l] = p; p += n * n;
+        s.V[l] = p; p += n * n;
+        s.R[l] = p; p += n * n;
+    }
+    if (mode == 0) {
+        for (int l = 0; l <= J; ++l)
+            for (int k = threadIdx.x; k < s.n[l] * s.n[l]; k += blockDim.x) s.F[l][k] = g_f[l][k];
+        __syncthreads();
+        sm_coarsest(s.U[0], s.F[0], length);
+        for (int l = 1; l <= J; ++l) {
+            int nf = s.n[l], nc = s.n[l - 1];
+            for (int k = threadIdx.x; k < nf * nf; k += blockDim.x) {
+                int i = k / nf, jj = k - i * nf;
+                s.U[l][k] = prolong_point(s.U[l - 1], nc, i, jj);
+            }
+            __syncthreads();
+            for (int c = 0; c < 2; ++c) sm_vcycle(s, l, s.U[l], s.F[l]);
+        }
+        for (int k = threadIdx.x; k < s.n[J] * s.n[J]; k += blockDim.x) g_u[J][k] = s.U[J][k];
+    } else {
+        int n = s.n[J];
+        for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+            s.U[J][k] = g_v[J][k];
+            s.F[J][k] = g_r[J][k];
+        }
+        __syncthreads();
+        sm_vcycle(s, J, s.U[J], s.F[J]);
+        for (int k = threadIdx.x; k < n * n; k += blockDim.x) g_v[J][k] = s.U[J][k];
+    }
+}
+
+static size_t small_smem_bytes(int J, size_t elem) {
+    size_t tot = 0;
+    for (int l = 0; l <= J; ++l) {
+        size_t n = (size_t)(1 << (l + 1)) + 1;
+        tot += 4 * n * n;
+    }
+    return tot * elem;
+}
+
+/* ------------------------------------------------------- E field */
+/* fields::grid_electric_field (fields.cpp:230-268) in the stride-nx layout
+ * of an (nx+1)*(ny+1) buffer; also writes the FP32 {Ex,Ey} copy read by
+ * the gather.                                                           */
+__device__ __forceinline__ double ex_interior(const double* phi, int nx, int ny, int j, int i, double twoDX) {
+    if (j < 1 || j > ny - 2 || i < 1 || i > nx - 2) return 0.0;
+    return (phi[j * nx + i - 1] - phi[j * nx + i + 1]) / twoDX;
+}
+__device__ __forceinline__ double ey_interior(const double* phi, int nx, int ny, int j, int i, double twoDX) {
+    if (j < 1 || j > ny - 2 || i < 1 || i > nx - 2) return 0.0;
+    return (phi[(j - 1) * nx + i] - phi[(j + 1) * nx + i]) / twoDX;
+}
+__global__ void k_efield(const double* phi, double* Ex, double* Ey, float2* exy, int nx, int ny, double twoDX) {
+    const int GE = (nx + 1) * (ny + 1);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < GE; k += gridDim.x * blockDim.x) {
+        double ex = 0.0, ey = 0.0;
+        if (k < nx * ny) {
+            int j = k / nx, i = k - j * nx;
+            if (i == 0) ex = 2.0 * ex_interior(phi, nx, ny, j, 1, twoDX) - ex_interior(phi, nx, ny, j, 2, twoDX);
+            else if (i == nx - 1) ex = 2.0 * ex_interior(phi, nx, ny, j, nx - 2, twoDX) - ex_interior(phi, nx, ny, j, nx - 3, twoDX);
+            else ex = ex_interior(phi, nx, ny, j, i, twoDX);
+            if (j == 0) ey = 2.0 * ey_interior(phi, nx, ny, 1, i, twoDX) - ey_interior(phi, nx, ny, 2, i, twoDX);
+            else if (j == ny - 1) ey = 2.0 * ey_interior(phi, nx, ny, ny - 2, i, twoDX) - ey_interior(phi, nx, ny, ny - 3, i, twoDX);
+            else ey = ey_interior(phi, nx, ny, j, i, twoDX);
+        }
+        Ex[k] = ex;
+        Ey[k] = ey;
+        exy[k] = make_float2((float)ex, (float)ey);
+    }
+}
+
+__global__ void k_walls(double* phi, int nx, int ny, double phi0x, double phirx, double phi0y, double phily) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx * ny; k += gridDim.x * blockDim.x) {
+        int j = k / nx, i = k - j * nx;
+        /* fields.cpp:209-219: columns first, then rows overwrite the corners */
+        if (j == 0) phi[k] = phi0y;
+        else if (j == ny - 1) phi[k] = phily;
+        else if (i == 0) phi[k] = phi0x;
+        else if (i == nx - 1) phi[k] = phirx;
+    }
+}
+
+/* ====================================================== host side */
+static FinalizeArgs fin_args(pgb_run* r, int mask, double phi_right, bool rhs) {
+    FinalizeArgs a;
+    a.acc[0] = r->qacc[0]; a.acc[1] = r->qacc[1];
+    a.q[0] = r->q[0]; a.q[1] = r->q[1];
+    a.rho = r->rho; a.f = rhs ? r->mg_f[r->ng - 1] : nullptr;
+    a.nx = r->nx; a.ny = r->ny;
+    a.qcdxdy[0] = r->sp[0].qc / (r->dx * r->dy);
+    a.qcdxdy[1] = r->sp[1].qc / (r->dx * r->dy);
+    a.mask = mask;
+    a.coef = 1.0 / 8.854e-12;
+    a.divdxdy = 1.0 / (r->dx * r->dy);
+    a.phi0x = r->p.phi_left; a.phirx = phi_right; a.phi0y = r->p.phi_bottom; a.phily = r->p.phi_top;
+    return a;
+}
+
+int pgb_launch_finalize(pgb_run* r, int mask, bool make_rhs, double phi_right) {
+    FinalizeArgs a = fin_args(r, mask, phi_right, make_rhs);
+    int G = r->nx * r->ny;
+    k_finalize<<<(G + 255) / 256, 256, 0, r->stream>>>(a);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_rhs(pgb_run* r, double phi_right) {
+    FinalizeArgs a = fin_args(r, 0, phi_right, true);
+    int G = r->nx * r->ny;
+    k_rhs<<<(G + 255) / 256, 256, 0, r->stream>>>(a);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+static int blocks_for(long long work) {
+    long long b = (work + 255) / 256;
+    if (b < 1) b = 1;
+    if (b > 65535) b = 65535;
+    return (int)b;
+}
+
+/* per-level device pointer tables for the small solver */
+struct MgTables {
+    double** u;
+    double** f;
+    double** v;
+    double** r;
+};
+
+static int small_launch(pgb_run* r, double** tab, int J, int mode) {
+    size_t smem = small_smem_bytes(J, sizeof(double));
+    k_mg_small<double><<<1, 1024, smem, r->stream>>>(J, mode, r->p.xlength, tab, tab + PGB_MAX_LEVELS,
+                                                     tab + 2 * PGB_MAX_LEVELS, tab + 3 * PGB_MAX_LEVELS);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+/* V-cycle at level j > small on (u, f) (mglin.cpp:176-196) */
+static int vcycle(pgb_run* r, double** tab, int j, int jsmall, double* u, const double* f) {
+    int nf = r->mg_n[j], nc = r->mg_n[j - 1];
+    double h = r->p.xlength / (nf - 1), h2 = h * h, h2i = 1.0 / (h * h);
+    long long rw = (long long)(nf - 2) * ((nf - 1) / 2);
+    k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
+    k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
+    k_resid_restrict<double><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(r->mg_r[j - 1], u, f, nf, h2i);
+    PGB_CK(r, cudaMemsetAsync(r->mg_v[j - 1], 0, sizeof(double) * nc * nc, r->stream));
+    if (j - 1 <= jsmall) {
+        if (small_launch(r, tab, j - 1, 1)) return PGB_ERR_CUDA;
+    } else {
+        if (vcycle(r, tab, j - 1, jsmall, r->mg_v[j - 1], r->mg_r[j - 1])) return PGB_ERR_CUDA;
+    }
+    k_prolong<double><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(u, r->mg_v[j - 1], nf, 1);
+    k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
+    k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+/* Mglin on the rhs in mg_f[ng-1]; result in mg_u[ng-1] */
+static int fmg(pgb_run* r) {
+    const int ng = r->ng;
+    double** tab = r->mg_tab;   /* device pointer tables, filled at create */
+    for (int j = ng - 2; j >= 0; --j) {
+        int nc = r->mg_n[j];
+        k_restrict<double><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(r->mg_f[j], r->mg_f[j + 1], nc);
+    }
+    int jsmall = 0;
+    while (jsmall + 1 < ng && r->mg_n[jsmall + 1] <= PGB_MG_SMALL) jsmall++;
+    if (small_launch(r, tab, jsmall, 0)) return PGB_ERR_CUDA;
+    for (int j = jsmall + 1; j < ng; ++j) {
+        int nf = r->mg_n[j];
+        k_prolong<double><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(r->mg_u[j], r->mg_u[j - 1], nf, 0);
+        for (int c = 0; c < 2; ++c)
+            if (vcycle(r, tab, j, jsmall, r->mg_u[j], r->mg_f[j])) return PGB_ERR_CUDA;
+    }
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_mg_setup(pgb_run* r) {
+    /* pointer tables: u, f, v, r per level (device array of device pointers) */
+    double* tabs[4 * PGB_MAX_LEVELS] = {};
+    for (int l = 0; l < r->ng; ++l) {
+        tabs[l] = r->mg_u[l];
+        tabs[PGB_MAX_LEVELS + l] = r->mg_f[l];
+        tabs[2 * PGB_MAX_LEVELS + l] = r->mg_v[l];
+        tabs[3 * PGB_MAX_LEVELS + l] = r->mg_r[l];
+    }
+    PGB_CK(r, cudaMalloc(&r->mg_tab, sizeof(tabs)));
+    PGB_CK(r, cudaMemcpy(r->mg_tab, tabs, sizeof(tabs), cudaMemcpyHostToDevice));
+    int jsmall = 0;
+    while (jsmall + 1 < r->ng && r->mg_n[jsmall + 1] <= PGB_MG_SMALL) jsmall++;
+    size_t smem = small_smem_bytes(jsmall, sizeof(double));
+    PGB_CK(r, cudaFuncSetAttribute(k_mg_small<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return 0;
+}
+
+int pgb_poisson_solve(pgb_run* r, int64_t t) {
+    double phi_right = r->p.phi_right * cos(r->p.phi_period * (double)t);
+    if (fmg(r)) return PGB_ERR_CUDA;
+    PGB_CK(r, cudaMemcpyAsync(r->phi, r->mg_u[r->ng - 1], sizeof(double) * r->nx * r->ny, cudaMemcpyDeviceToDevice,
+                              r->stream));
+    k_walls<<<blocks_for((long long)r->nx * r->ny), 256, 0, r->stream>>>(r->phi, r->nx, r->ny, r->p.phi_left, phi_right,
+                                                                         r->p.phi_bottom, r->p.phi_top);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_efield(pgb_run* r) {
+    int GE = (r->nx + 1) * (r->ny + 1);
+    k_efield<<<blocks_for(GE), 256, 0, r->stream>>>(r->phi, r->ex, r->ey, r->exy, r->nx, r->ny, 2.0 * r->dx);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+double pgb_phi_right(pgb_run* r, int64_t t) { return r->p.phi_right * cos(r->p.phi_period * (double)t); }

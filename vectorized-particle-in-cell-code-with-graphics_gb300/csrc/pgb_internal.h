@@ -1,0 +1,146 @@
+/*
+ * Internal definitions shared by the libpicgb translation units.
+ *
+ * Device layout of one species (structure of arrays, slot order):
+ *   xv  float4 {xs, ys, vx, vy}   xs = x/DX, ys = y/DY (cell units), v in m/s
+ *   vz  float                     m/s
+ *   w   float                     macro-particle weight
+ *   id  uint32                    stable identity: keys the random streams
+ * A removed particle keeps its slot with xs = -inf (a tombstone) until the
+ * next compaction, which keeps the surviving slots in order.  Cell units make
+ * the cell index trunc(xs) and the CIC weight xs - trunc(xs) exact in FP32;
+ * the reference computes the same quantities from x/DX in FP64
+ * (pic.cl:31-37).
+ *
+ * Counters that change on the device (slot counts, next id, statistics) live
+ * in one DevState block so that a step never waits for the host.
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include "picgb.h"
+
+#define PGB_TILE 1024          /* particles per tile of the push kernels   */
+#define PGB_PUSH_THREADS 256
+#define PGB_ITEMS (PGB_TILE / PGB_PUSH_THREADS)
+#define PGB_FIX_SCALE 4294967296.0   /* deposit fixed point: 2^32 per unit weight */
+#define PGB_MG_SMALL 65        /* levels with n <= 65 are solved by one CTA  */
+#define PGB_MAX_LEVELS 16
+
+enum { ST_ABS_E = 0, ST_ABS_I, ST_PLOP, ST_REFL, ST_BACK, ST_SEE_EV, ST_SEE_EM, ST_ISEE_EM,
+       ST_ELASTIC, ST_IONIZE, ST_CX, ST_INJ_E, ST_INJ_I, ST_RED_E, ST_RED_I, ST_COUNT };
+
+enum { ERR_CAP_E = 1, ERR_CAP_I = 2, ERR_LIST = 4, ERR_RETRY = 8 };
+
+/* device-resident run state (one allocation) */
+struct DevState {
+    long long n[2];          /* slots in use per species                     */
+    long long dead[2];       /* tombstones among them                        */
+    long long n_mcc;         /* electron slots present before this step's injection */
+    unsigned int next_id[2];
+    unsigned int pad0;
+    long long list_n[4];     /* sizes of the dense event lists               */
+    long long stats[ST_COUNT];
+    int err;
+    int pad1;
+    double cx_acc_dummy;
+};
+
+/* dense event lists (ordered by slot) */
+enum { LIST_OUT_E = 0, LIST_OUT_I = 1, LIST_ION_EV = 2, LIST_SPARE = 3 };
+
+struct Species {
+    float4* xv = nullptr;
+    float* vz = nullptr;
+    float* w = nullptr;
+    unsigned int* id = nullptr;
+    /* compaction targets */
+    float4* xv2 = nullptr;
+    float* vz2 = nullptr;
+    float* w2 = nullptr;
+    unsigned int* id2 = nullptr;
+    long long cap = 0;
+    double qc = 0, q_over_m = 0, mass = 0, vt = 0, dt = 0;
+};
+
+struct PushConsts {
+    int nx, ny;
+    float dtdx, dtdy;      /* dt/DX, dt/DY: cell units per (m/s)            */
+    float coef;            /* 0.5*dt*q/m                                     */
+    float ca, sa, co, so;  /* cos/sin of ANGLE and of omega*dt               */
+    int bfield;            /* MAGNETIC_FIELD > 0                             */
+    int steady;            /* STEADYSTATE wall classification               */
+};
+
+struct pgb_run {
+    pgb_params p;
+    std::string err;
+    int dev = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    int nx = 0, ny = 0, dt_dti = 1;
+    double dx = 0, dy = 0;
+    int64_t time_step = 0;
+    Species sp[2];
+    DevState* ds = nullptr;       /* device */
+    DevState* hs = nullptr;       /* pinned host mirror */
+    /* grids */
+    unsigned long long* qacc[2] = {nullptr, nullptr};   /* fixed-point deposit */
+    double* q[2] = {nullptr, nullptr};
+    double *rho = nullptr, *phi = nullptr, *rhs = nullptr;
+    double *ex = nullptr, *ey = nullptr;
+    float2* exy = nullptr;        /* FP32 {Ex,Ey} per node, stride nx, (nx+1)(ny+1) */
+    /* multigrid */
+    int ng = 0;
+    int mg_n[PGB_MAX_LEVELS];
+    double *mg_u[PGB_MAX_LEVELS], *mg_f[PGB_MAX_LEVELS], *mg_v[PGB_MAX_LEVELS], *mg_r[PGB_MAX_LEVELS];
+    double** mg_tab = nullptr;                       /* device table of the level pointers */
+    double *dc_d = nullptr, *dc_u = nullptr;        /* FP32_DC defect correction (FP64) */
+    float *mg32_u[PGB_MAX_LEVELS], *mg32_f[PGB_MAX_LEVELS], *mg32_v[PGB_MAX_LEVELS], *mg32_r[PGB_MAX_LEVELS];
+    /* event lists */
+    int* tile_list[4] = {nullptr, nullptr, nullptr, nullptr};
+    int* tile_cnt[4] = {nullptr, nullptr, nullptr, nullptr};
+    int* list[4] = {nullptr, nullptr, nullptr, nullptr};
+    long long list_cap = 0;   /* = max particle capacity                       */
+    long long ntiles_cap = 0;
+    int* aux_i = nullptr;     /* scratch ints (wall passes), list_cap entries  */
+    int* aux_j = nullptr;
+    /* collisions */
+    float* neut[2] = {nullptr, nullptr};   /* [which]: 3 x N_neutral, FP32    */
+    double* neut64[2] = {nullptr, nullptr};
+    double* prob_cx = nullptr;             /* per-column CX accumulator       */
+    float* cx_p = nullptr;                 /* per-ion CX probability          */
+    float* cx_tile_sum = nullptr;          /* [tile][column]                  */
+    /* host staging */
+    double* h_stage = nullptr;
+    size_t h_stage_bytes = 0;
+};
+
+/* ------------------------------------------------------------ helpers */
+bool pgb_cuda_ok(pgb_run* r, cudaError_t e, const char* what);
+#define PGB_CK(r, call)                                  \
+    do {                                                 \
+        if (!pgb_cuda_ok((r), (call), #call)) return PGB_ERR_CUDA; \
+    } while (0)
+
+/* kernels launched from the host side (defined in the .cu files) */
+struct CollConsts;
+int pgb_launch_push(pgb_run* r, int s, bool mcc, bool deposit, bool flag_ion);
+int pgb_launch_flag_outside(pgb_run* r, int s);
+int pgb_build_list(pgb_run* r, int which, int species_for_tiles);
+int pgb_launch_deposit(pgb_run* r, int s);
+int pgb_launch_finalize(pgb_run* r, int which_species_mask, bool make_rhs, double phi_right);
+int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e);
+int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i);
+int pgb_launch_mcc(pgb_run* r);
+int pgb_launch_cx(pgb_run* r);
+int pgb_launch_walls(pgb_run* r, int which);
+int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long n);
+int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap);
+int pgb_mg_setup(pgb_run* r);
+CollConsts pgb_coll_consts(pgb_run* r);
+int pgb_launch_compact(pgb_run* r, int s);
+int pgb_launch_reduce(pgb_run* r, int s);
+int pgb_poisson_solve(pgb_run* r, int64_t t);
+int pgb_launch_efield(pgb_run* r);
+int pgb_launch_rhs(pgb_run* r, double phi_right);

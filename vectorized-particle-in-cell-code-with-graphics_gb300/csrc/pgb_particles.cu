@@ -1,0 +1,762 @@
+/*
+ * Particle kernels: fused collision + gather + push + deposit, ordered event
+ * lists, injection, ionization products, compaction, load and dump.
+ *
+ * Reference path: e_collisions::collision (e_collisions.cpp:480-597),
+ * particle::get_particle_electric_field + move_particles
+ * (particle.cpp:870-1341, pic.cl:56-149), particle::collect_charge
+ * (particle.cpp:663-858, pic.cl:22-52), particle::inject_more_particles
+ * (particle.cpp:491-510).
+ *
+ * One pass of k_push reads a particle once (16 B position/velocity, 4 B vz,
+ * 4 B weight, 4 B id when collisions are on), applies the electron-neutral
+ * collision test, gathers E bilinearly from the FP32 node grid (L2
+ * resident), pushes, deposits the new position into the int64 fixed-point
+ * charge grid and records wall crossings and ionization events in per-tile
+ * lists that keep slot order.  Grids are sized from the SM count and loop
+ * over tiles, reading the particle count from device memory, so a step
+ * needs no host round trip.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include "pgb_internal.h"
+#include "pgb_physics.cuh"
+
+/* ------------------------------------------------------------ device state */
+struct PushArgs {
+    float4* xv;
+    float* vz;
+    float* w;
+    const unsigned int* id;
+    const float2* exy;
+    unsigned long long* qacc;
+    DevState* ds;
+    int s;
+    PushConsts pc;
+    CollConsts cc;
+    const double* neut64;       /* electron-neutral table (FP64), 3 x N */
+    int* tl_out;                /* per-tile outside list              */
+    int* tc_out;
+    int* tl_ev;                 /* per-tile ionization-event list     */
+    int* tc_ev;
+    unsigned int step;
+};
+
+/* gather (pic.cl:56-92) + push (pic.cl:95-149) of one particle in cell units */
+__device__ __forceinline__ void gather_push_one(const PushConsts& pc, const float2* exy, float4& p, float& vz,
+                                                bool& moved) {
+    int jp = cellf(p.x), kp = cellf(p.y);
+    moved = false;
+    if (jp < pc.nx && p.x > 0.0f && kp < pc.ny && p.y > 0.0f) {
+        float wj = p.x - (float)jp, wk = p.y - (float)kp;
+        float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
+        float a2 = wk * (1.0f - wj), a1 = wj * wk;
+        const float2* e = exy + (long long)kp * pc.nx + jp;
+        float2 e0 = __ldg(e), e1 = __ldg(e + 1), e2 = __ldg(e + pc.nx), e3 = __ldg(e + pc.nx + 1);
+        float Exp = a4 * e0.x + a3 * e1.x + a2 * e2.x + a1 * e3.x;
+        float Eyp = a4 * e0.y + a3 * e1.y + a2 * e2.y + a1 * e3.y;
+        float vx = p.z + pc.coef * Exp;
+        float vy = p.w + pc.coef * Eyp;
+        if (pc.bfield) {
+            float vpar = pc.ca * vx + pc.sa * vy;
+            float vperp = -pc.sa * vx + pc.ca * vy;
+            float vperp_after = vperp * pc.co + pc.so * vz;
+            vz = -vperp * pc.so + pc.co * vz;
+            vx = pc.ca * vpar - pc.sa * vperp_after;
+            vy = pc.sa * vpar + pc.ca * vperp_after;
+        }
+        vx += pc.coef * Exp;
+        vy += pc.coef * Eyp;
+        p.x += pc.dtdx * vx;
+        p.y += pc.dtdy * vy;
+        p.z = vx;
+        p.w = vy;
+        moved = true;
+    }
+}
+
+/* electron-neutral collision test and event (e_collisions.cpp:504-562).
+ * Returns true if the electron ionized (its velocity is then NaN).        */
+__device__ __forceinline__ bool mcc_one(const CollConsts& cc, const double* neut64, unsigned int id, unsigned int step,
+                                        int nx, int ny, float4& p, float& vz, bool& vchanged, int* stats) {
+    int jp = cellf(p.x), kp = cellf(p.y);
+    if (!(jp >= 0 && jp < nx && kp >= 0 && kp < ny)) return false;
+    float u2 = p.z * p.z + p.w * p.w + vz * vz;
+    float energy = cc.e_energy_coef * u2;
+    float u = sqrtf(u2);
+    float sel = sigma_el(cc, energy), sio = sigma_ion(cc, energy);
+    pgb_stream st;
+    pgb_stream_init(&st, cc.seed, id, step, PGB_STREAM_EMCC, 0);
+    float R = pgb_u01f(pgb_stream_u32(&st));
+    float P = -expm1f(-(u * cc.e_pcoef * sel));
+    bool ion = false;
+    if (P > 2.0f * R) {
+        double vx = p.z, vy = p.w, vzz = vz;
+        double e64 = (0.5 / PGB_CHARGE) * cc.me * (vx * vx + vy * vy + vzz * vzz);
+        scatter_fp64(&st, neut64, cc.n_neutral, e64, cc.reduced_mass, vx, vy, vzz);
+        p.z = (float)vx; p.w = (float)vy; vz = (float)vzz;
+        vchanged = true;
+        stats[0] += 1;
+    }
+    float Pi = -expm1f(-(u * cc.e_pcoef * sio));
+    if (Pi > 0.0f) {
+        pgb_stream si;
+        pgb_stream_init(&si, cc.seed, id, step, PGB_STREAM_IONIZE, 0);
+        /* positions enter only the products; the parent keeps its position */
+        IonizeOut o = ionize_fp64(&si, neut64, cc.n_neutral, cc, 0.0, 0.0, (double)p.z, (double)p.w, (double)vz);
+        p.z = (float)o.evx; p.w = (float)o.evy; vz = (float)o.evz;
+        vchanged = true;
+        ion = true;
+        stats[1] += 1;
+    }
+    return ion;
+}
+
+/* add per-thread event counts (elastic, ionization) with one atomic per warp */
+__device__ __forceinline__ void flush_stats(int (&st)[2], long long* stats) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        int v = st[k];
+        for (int d = 16; d; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd((unsigned long long*)&stats[ST_ELASTIC + k], (unsigned long long)v);
+    }
+}
+
+/* ordered compaction of per-thread flags of one tile into its list.
+ * Item k of thread t is slot tile*TILE + k*THREADS + t, so (k, warp, lane)
+ * order is slot order.                                                    */
+template <int NL>
+__device__ __forceinline__ void tile_lists(const bool (&f)[NL][PGB_ITEMS], long long tile_base, int tile,
+                                           int* const (&tl)[NL], int* const (&tc)[NL]) {
+    __shared__ int s_off[NL][PGB_ITEMS][PGB_PUSH_THREADS / 32];
+    __shared__ int s_tot[NL];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned m[NL][PGB_ITEMS];
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            m[l][k] = __ballot_sync(0xffffffffu, f[l][k]);
+            if (lane == 0) s_off[l][k][warp] = __popc(m[l][k]);
+        }
+    __syncthreads();
+    if (threadIdx.x < NL) {
+        int l = threadIdx.x, acc = 0;
+        for (int k = 0; k < PGB_ITEMS; ++k)
+            for (int w = 0; w < PGB_PUSH_THREADS / 32; ++w) {
+                int c = s_off[l][k][w];
+                s_off[l][k][w] = acc;
+                acc += c;
+            }
+        s_tot[l] = acc;
+        tc[l][tile] = acc;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k)
+            if (f[l][k]) {
+                int pos = s_off[l][k][warp] + __popc(m[l][k] & lt);
+                tl[l][(long long)tile * PGB_TILE + pos] = (int)(tile_base + k * PGB_PUSH_THREADS + threadIdx.x);
+            }
+    __syncthreads();
+}
+
+template <bool MCC, bool DEP, bool FLAG>
+__global__ void __launch_bounds__(PGB_PUSH_THREADS) k_push(PushArgs a) {
+    const long long n = a.ds->n[a.s];
+    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    const PushConsts pc = a.pc;
+    int st_loc[2] = {0, 0};
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long base = (long long)tile * PGB_TILE;
+        bool f[2][PGB_ITEMS];
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            f[0][k] = false;
+            f[1][k] = false;
+            long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+            if (i >= n) continue;
+            float4 p = a.xv[i];
+            if (is_dead(p.x)) continue;
+            float vz = (MCC || pc.bfield) ? a.vz[i] : 0.0f;
+            bool vchanged = false;
+            if (MCC) {
+                unsigned int id = a.id[i];
+                f[1][k] = mcc_one(a.cc, a.neut64, id, a.step, pc.nx, pc.ny, p, vz, vchanged, st_loc);
+            }
+            bool moved;
+            gather_push_one(pc, a.exy, p, vz, moved);
+            if (moved || vchanged) a.xv[i] = p;
+            if ((MCC && vchanged) || (pc.bfield && moved)) a.vz[i] = vz;
+            if (DEP) {
+                if (deposit_ok(p.x, p.y, pc.nx, pc.ny)) deposit_cell(a.qacc, pc.nx, p.x, p.y, a.w[i]);
+            }
+            if (FLAG) f[0][k] = pc.steady ? outside_steady(p.x, p.y, pc.nx, pc.ny)
+                                          : outside_absorbing(p.x, p.y, pc.nx, pc.ny);
+        }
+        if (FLAG) {
+            if (MCC) {
+                int* const tl[2] = {a.tl_out, a.tl_ev};
+                int* const tc[2] = {a.tc_out, a.tc_ev};
+                tile_lists<2>(f, base, tile, tl, tc);
+            } else {
+                bool g[1][PGB_ITEMS];
+#pragma unroll
+                for (int k = 0; k < PGB_ITEMS; ++k) g[0][k] = f[0][k];
+                int* const tl[1] = {a.tl_out};
+                int* const tc[1] = {a.tc_out};
+                tile_lists<1>(g, base, tile, tl, tc);
+            }
+        }
+    }
+    if (MCC) flush_stats(st_loc, a.ds->stats);
+}
+
+/* flag-only pass (wall classification without a push) */
+__global__ void __launch_bounds__(PGB_PUSH_THREADS) k_flag(const float4* xv, DevState* ds, int s, int nx, int ny,
+                                                           int steady, int* tl, int* tc) {
+    const long long n = ds->n[s];
+    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long base = (long long)tile * PGB_TILE;
+        bool f[1][PGB_ITEMS];
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+            f[0][k] = false;
+            if (i >= n) continue;
+            float4 p = xv[i];
+            if (is_dead(p.x)) continue;
+            f[0][k] = steady ? outside_steady(p.x, p.y, nx, ny) : outside_absorbing(p.x, p.y, nx, ny);
+        }
+        int* const tla[1] = {tl};
+        int* const tca[1] = {tc};
+        tile_lists<1>(f, base, tile, tla, tca);
+    }
+}
+
+/* standalone deposit (particle::collect_charge) */
+__global__ void __launch_bounds__(256) k_deposit(const float4* xv, const float* w, DevState* ds, int s, int nx, int ny,
+                                                 unsigned long long* qacc) {
+    const long long n = ds->n[s];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float4 p = xv[i];
+        if (deposit_ok(p.x, p.y, nx, ny)) deposit_cell(qacc, nx, p.x, p.y, w[i]);
+    }
+}
+
+/* standalone electron collisions (e_collisions::collision) */
+__global__ void __launch_bounds__(PGB_PUSH_THREADS) k_mcc(PushArgs a) {
+    const long long n = a.ds->n[0];
+    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    int st_loc[2] = {0, 0};
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long base = (long long)tile * PGB_TILE;
+        bool f[1][PGB_ITEMS];
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            f[0][k] = false;
+            long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+            if (i >= n) continue;
+            float4 p = a.xv[i];
+            if (is_dead(p.x)) continue;
+            float vz = a.vz[i];
+            bool vchanged = false;
+            f[0][k] = mcc_one(a.cc, a.neut64, a.id[i], a.step, a.pc.nx, a.pc.ny, p, vz, vchanged, st_loc);
+            if (vchanged) { a.xv[i] = p; a.vz[i] = vz; }
+        }
+        int* const tla[1] = {a.tl_ev};
+        int* const tca[1] = {a.tc_ev};
+        tile_lists<1>(f, base, tile, tla, tca);
+    }
+    flush_stats(st_loc, a.ds->stats);
+}
+
+/* ------------------------------------------------------------ scans */
+/* exclusive scan of cnt[0..m) (m read from *m_ptr or given) into off[];
+ * total written to *total.  Single block; m up to a few 1e5.             */
+__global__ void __launch_bounds__(1024) k_scan_small(const int* cnt, int* off, const long long* n_ptr, long long m_const,
+                                                     long long* total) {
+    __shared__ long long s_warp[32];
+    __shared__ long long s_carry;
+    /* n_ptr: particle count whose tiles are scanned; else m_const entries */
+    const long long m = n_ptr ? (*n_ptr + PGB_TILE - 1) / PGB_TILE : m_const;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (long long b = 0; b < m; b += 1024) {
+        long long i = b + threadIdx.x;
+        long long v = (i < m) ? cnt[i] : 0;
+        long long x = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            long long t = s_warp[lane];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                long long y = __shfl_up_sync(0xffffffffu, t, d);
+                if (lane >= d) t += y;
+            }
+            s_warp[lane] = t;
+        }
+        __syncthreads();
+        long long excl = s_carry + (warp ? s_warp[warp - 1] : 0) + x - v;
+        if (i < m) off[i] = (int)excl;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += s_warp[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = s_carry;
+}
+
+/* exclusive scan of a list-length array (length read from device memory) */
+__global__ void __launch_bounds__(1024) k_scan_list(const int* cnt, int* off, const long long* m_ptr, long long* total) {
+    __shared__ long long s_warp[32];
+    __shared__ long long s_carry;
+    const long long m = *m_ptr;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (long long b = 0; b < m; b += 1024) {
+        long long i = b + threadIdx.x;
+        long long v = (i < m) ? cnt[i] : 0;
+        long long x = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            long long t = s_warp[lane];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                long long y = __shfl_up_sync(0xffffffffu, t, d);
+                if (lane >= d) t += y;
+            }
+            s_warp[lane] = t;
+        }
+        __syncthreads();
+        long long excl = s_carry + (warp ? s_warp[warp - 1] : 0) + x - v;
+        if (i < m) off[i] = (int)excl;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += s_warp[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = s_carry;
+}
+
+/* gather per-tile lists into one dense list in slot order */
+__global__ void k_gather_lists(const int* tl, const int* tc, const int* toff, const long long* n_ptr, int* out) {
+    const long long n = *n_ptr;
+    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int c = tc[t], o = toff[t];
+        for (int k = threadIdx.x; k < c; k += blockDim.x) out[o + k] = tl[(long long)t * PGB_TILE + k];
+    }
+}
+
+/* ------------------------------------------------------------ inject */
+/* particle::inject_more_particles (particle.cpp:491-510): uniform position
+ * in [DX, L-DX]^2, velocities from get_particle_velocity, weight 0.0.  For
+ * electrons the new particles are pushed here too (they are created before
+ * the electron push in pic_run, after the collision loop).               */
+struct InjectArgs {
+    Species e, i;
+    DevState* ds;
+    int k;                       /* NUMBER_TO_INJECT */
+    double dx, dy, xlength, ylength;
+    uint64_t seed;
+    unsigned int step;
+    PushConsts pce;
+    const float2* exy;
+    unsigned long long* qacc_e;
+    int push_e;                  /* push the new electrons (inside pgb_step) */
+    int species_mask;            /* 1 = electrons, 2 = ions                  */
+    int* list_out_e;             /* append outside electrons (ordered)       */
+    long long list_cap;
+};
+__global__ void k_inject(InjectArgs a) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int s = 0; s < 2; ++s) {
+        if (!(a.species_mask & (1 << s))) continue;
+        const Species& S = s == 0 ? a.e : a.i;
+        for (int j = 0; j < a.k; ++j) {
+            long long slot = a.ds->n[s];
+            if (slot >= S.cap) { a.ds->err |= (s == 0 ? ERR_CAP_E : ERR_CAP_I); break; }
+            unsigned int id = a.ds->next_id[s]++;
+            a.ds->n[s] = slot + 1;
+            pgb_stream st;
+            pgb_stream_init(&st, a.seed, id, a.step, PGB_STREAM_INJECT, (uint32_t)s);
+            double rx = pgb_u01d(pgb_stream_u32(&st));
+            double ry = pgb_u01d(pgb_stream_u32(&st));
+            double x = (a.dx + rx * (a.xlength - 2.0 * a.dx));
+            double y = (a.dy + ry * (a.ylength - 2.0 * a.dy));
+            double vx = maxwell_fp64(&st, S.vt), vy = maxwell_fp64(&st, S.vt), vz = maxwell_fp64(&st, S.vt);
+            float4 p = make_float4((float)(x / a.dx), (float)(y / a.dy), (float)vx, (float)vy);
+            float vzf = (float)vz;
+            if (s == 0 && a.push_e) {
+                bool moved;
+                gather_push_one(a.pce, a.exy, p, vzf, moved);
+                if (deposit_ok(p.x, p.y, a.pce.nx, a.pce.ny)) deposit_cell(a.qacc_e, a.pce.nx, p.x, p.y, 0.0f);
+                bool out = a.pce.steady ? outside_steady(p.x, p.y, a.pce.nx, a.pce.ny)
+                                        : outside_absorbing(p.x, p.y, a.pce.nx, a.pce.ny);
+                if (out) {
+                    long long pos = a.ds->list_n[LIST_OUT_E];
+                    if (pos < a.list_cap) { a.list_out_e[pos] = (int)slot; a.ds->list_n[LIST_OUT_E] = pos + 1; }
+                    else a.ds->err |= ERR_LIST;
+                }
+            }
+            S.xv[slot] = p;
+            S.vz[slot] = vzf;
+            S.w[slot] = 0.0f;
+            S.id[slot] = id;
+            atomicAdd((unsigned long long*)&a.ds->stats[s == 0 ? ST_INJ_E : ST_INJ_I], 1ull);
+        }
+    }
+}
+
+/* ------------------------------------------------- ionization products */
+/* e_collisions::ionization appends one ion and one electron per event
+ * (e_collisions.cpp:406-441); both are NaN (see ionize_fp64).  With
+ * absorbing walls the electron is removed by the wall pass of the same
+ * step, and so is the ion on an ion step, so those are counted without
+ * being stored; otherwise they are stored in event order.                 */
+struct IonizeAppendArgs {
+    Species e, i;
+    DevState* ds;
+    const int* ev;               /* dense event list (electron slots)      */
+    CollConsts cc;
+    const double* neut64;
+    double dx, dy;
+    unsigned int step;
+    int store_e, store_i;
+};
+__global__ void k_ionize_append(IonizeAppendArgs a) {
+    const long long m = a.ds->list_n[LIST_ION_EV];
+    const long long ne0 = a.ds->n[0], ni0 = a.ds->n[1];
+    const unsigned int ide0 = a.ds->next_id[0], idi0 = a.ds->next_id[1];
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < m; r += (long long)gridDim.x * blockDim.x) {
+        if (!a.store_e && !a.store_i) break;
+        int slot = a.ev[r];
+        unsigned int pid = a.e.id[slot];
+        /* recompute the event's products from the parent's stream; the
+         * parent's pre-event velocity is not needed because every product
+         * is NaN (the excess energy is negative)                           */
+        pgb_stream si;
+        pgb_stream_init(&si, a.cc.seed, pid, a.step, PGB_STREAM_IONIZE, 0);
+        float4 pp = a.e.xv[slot];
+        double xe = (double)pp.x * a.dx, ye = (double)pp.y * a.dy;
+        IonizeOut o = ionize_fp64(&si, a.neut64, a.cc.n_neutral, a.cc, xe, ye, 0.0, 0.0, 0.0);
+        if (a.store_i) {
+            long long s2 = ni0 + r;
+            if (s2 < a.i.cap) {
+                a.i.xv[s2] = make_float4((float)(o.ix / a.dx), (float)(o.iy / a.dy), (float)o.ivx, (float)o.ivy);
+                a.i.vz[s2] = (float)o.ivz;
+                a.i.w[s2] = a.e.w[slot];
+                a.i.id[s2] = idi0 + (unsigned int)r;
+            } else {
+                a.ds->err |= ERR_CAP_I;
+            }
+        }
+        if (a.store_e) {
+            long long s2 = ne0 + r;
+            if (s2 < a.e.cap) {
+                a.e.xv[s2] = make_float4((float)(o.nx_ / a.dx), (float)(o.ny_ / a.dy), (float)o.nvx, (float)o.nvy);
+                a.e.vz[s2] = (float)o.nvz;
+                a.e.w[s2] = a.e.w[slot];
+                a.e.id[s2] = ide0 + (unsigned int)r;
+            } else {
+                a.ds->err |= ERR_CAP_E;
+            }
+        }
+    }
+}
+__global__ void k_ionize_commit(DevState* ds, int store_e, int store_i, long long cap_e, long long cap_i) {
+    long long m = ds->list_n[LIST_ION_EV];
+    ds->next_id[0] += (unsigned int)m;
+    ds->next_id[1] += (unsigned int)m;
+    if (store_e) { long long v = ds->n[0] + m; ds->n[0] = v < cap_e ? v : cap_e; }
+    else ds->stats[ST_ABS_E] += m;
+    if (store_i) { long long v = ds->n[1] + m; ds->n[1] = v < cap_i ? v : cap_i; }
+    else ds->stats[ST_ABS_I] += m;
+}
+
+/* ------------------------------------------------------------ compaction */
+__global__ void __launch_bounds__(PGB_PUSH_THREADS) k_alive_count(const float4* xv, DevState* ds, int s, int* tc) {
+    const long long n = ds->n[s];
+    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    __shared__ int s_w[PGB_PUSH_THREADS / 32];
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        int c = 0;
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            long long i = (long long)tile * PGB_TILE + k * PGB_PUSH_THREADS + threadIdx.x;
+            if (i < n && !is_dead(xv[i].x)) c++;
+        }
+        for (int d = 16; d; d >>= 1) c += __shfl_down_sync(0xffffffffu, c, d);
+        if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int w = 0; w < PGB_PUSH_THREADS / 32; ++w) t += s_w[w];
+            tc[tile] = t;
+        }
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(PGB_PUSH_THREADS) k_compact(Species S, DevState* ds, int s, const int* toff) {
+    const long long n = ds->n[s];
+    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    bool f[1][PGB_ITEMS];
+    __shared__ int s_off[PGB_ITEMS][PGB_PUSH_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        unsigned m[PGB_ITEMS];
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            long long i = (long long)tile * PGB_TILE + k * PGB_PUSH_THREADS + threadIdx.x;
+            f[0][k] = (i < n) && !is_dead(S.xv[i].x);
+            m[k] = __ballot_sync(0xffffffffu, f[0][k]);
+            if (lane == 0) s_off[k][warp] = __popc(m[k]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = toff[tile];
+            for (int k = 0; k < PGB_ITEMS; ++k)
+                for (int w = 0; w < PGB_PUSH_THREADS / 32; ++w) { int c = s_off[k][w]; s_off[k][w] = acc; acc += c; }
+        }
+        __syncthreads();
+        for (int k = 0; k < PGB_ITEMS; ++k)
+            if (f[0][k]) {
+                long long i = (long long)tile * PGB_TILE + k * PGB_PUSH_THREADS + threadIdx.x;
+                int pos = s_off[k][warp] + __popc(m[k] & ((1u << lane) - 1u));
+                S.xv2[pos] = S.xv[i];
+                S.vz2[pos] = S.vz[i];
+                S.w2[pos] = S.w[i];
+                S.id2[pos] = S.id[i];
+            }
+        __syncthreads();
+    }
+}
+__global__ void k_compact_commit(DevState* ds, int s, const long long* total) {
+    ds->n[s] = *total;
+    ds->dead[s] = 0;
+}
+
+/* ------------------------------------------------------------ load / dump */
+__global__ void k_load(Species S, const double* aos, long long n, double dx, double dy) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double* r = aos + 6 * i;
+        S.xv[i] = make_float4((float)(r[0] / dx), (float)(r[1] / dy), (float)r[2], (float)r[3]);
+        S.vz[i] = (float)r[4];
+        S.w[i] = (float)r[5];
+        S.id[i] = (unsigned int)i;
+    }
+}
+/* dump live slots in order: out[j] for the j-th live slot; pos[] = exclusive
+ * scan of the per-tile live counts                                        */
+__global__ void __launch_bounds__(PGB_PUSH_THREADS) k_dump(Species S, DevState* ds, int s, const int* toff, double dx,
+                                                           double dy, double* out, long long cap) {
+    const long long n = ds->n[s];
+    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    __shared__ int s_off[PGB_ITEMS][PGB_PUSH_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        bool f[PGB_ITEMS];
+        unsigned m[PGB_ITEMS];
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            long long i = (long long)tile * PGB_TILE + k * PGB_PUSH_THREADS + threadIdx.x;
+            f[k] = (i < n) && !is_dead(S.xv[i].x);
+            m[k] = __ballot_sync(0xffffffffu, f[k]);
+            if (lane == 0) s_off[k][warp] = __popc(m[k]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = toff[tile];
+            for (int k = 0; k < PGB_ITEMS; ++k)
+                for (int w = 0; w < PGB_PUSH_THREADS / 32; ++w) { int c = s_off[k][w]; s_off[k][w] = acc; acc += c; }
+        }
+        __syncthreads();
+        for (int k = 0; k < PGB_ITEMS; ++k)
+            if (f[k]) {
+                long long i = (long long)tile * PGB_TILE + k * PGB_PUSH_THREADS + threadIdx.x;
+                long long pos = s_off[k][warp] + __popc(m[k] & ((1u << lane) - 1u));
+                if (pos < cap) {
+                    float4 p = S.xv[i];
+                    double* o = out + 6 * pos;
+                    o[0] = (double)p.x * dx; o[1] = (double)p.y * dy;
+                    o[2] = p.z; o[3] = p.w; o[4] = S.vz[i]; o[5] = S.w[i];
+                }
+            }
+        __syncthreads();
+    }
+}
+
+/* ====================================================== host launchers */
+static int grid_for(pgb_run* r, int per_sm) { return r->sms * per_sm; }
+
+static PushConsts push_consts(pgb_run* r, int s) {
+    PushConsts pc;
+    const Species& S = r->sp[s];
+    pc.nx = r->nx; pc.ny = r->ny;
+    pc.dtdx = (float)(S.dt / r->dx);
+    pc.dtdy = (float)(S.dt / r->dy);
+    pc.coef = (float)(0.5 * S.dt * S.q_over_m);
+    double omega_dt = S.dt * S.q_over_m * r->p.magnetic_field;
+    pc.ca = (float)cos(r->p.angle); pc.sa = (float)sin(r->p.angle);
+    pc.co = (float)cos(omega_dt); pc.so = (float)sin(omega_dt);
+    pc.bfield = r->p.magnetic_field > 0.0;
+    pc.steady = r->p.steadystate;
+    return pc;
+}
+
+CollConsts pgb_coll_consts(pgb_run* r) {
+    CollConsts c;
+    const pgb_params& p = r->p;
+    c.species = p.species;
+    c.el_const = p.sigma_elastic_mode == PGB_SIGMA_CONSTANT;
+    c.ion_const = p.sigma_ionization_mode == PGB_SIGMA_CONSTANT;
+    c.cx_const = p.sigma_cx_mode == PGB_SIGMA_CONSTANT;
+    c.el_value = (float)p.elastic_sigma_value;
+    c.ion_value = (float)p.ionization_sigma_value;
+    c.cx_value = (float)p.sigma_value;
+    c.e_energy_coef = (float)((0.5 / PGB_CHARGE) * p.electron_mass);
+    c.i_energy_coef = (float)((0.5 / PGB_CHARGE) * p.ion_mass);
+    c.e_pcoef = (float)(p.dt * 1.0e-20 * p.neutral_density);
+    c.i_pcoef = (float)(p.dti * 1.0e-20 * p.neutral_density);
+    c.me = p.electron_mass; c.mi = p.ion_mass; c.dt = p.dt; c.dti = p.dti;
+    c.threshold = p.threshold;
+    c.reduced_mass = p.ion_mass / (p.electron_mass + p.ion_mass);
+    c.n_neutral = p.init_no_neutrals;
+    c.seed = p.seed;
+    return c;
+}
+
+static PushArgs push_args(pgb_run* r, int s) {
+    PushArgs a;
+    Species& S = r->sp[s];
+    a.xv = S.xv; a.vz = S.vz; a.w = S.w; a.id = S.id;
+    a.exy = r->exy; a.qacc = r->qacc[s]; a.ds = r->ds; a.s = s;
+    a.pc = push_consts(r, s);
+    a.cc = pgb_coll_consts(r);
+    a.neut64 = r->neut64[0];
+    a.tl_out = r->tile_list[s == 0 ? LIST_OUT_E : LIST_OUT_I];
+    a.tc_out = r->tile_cnt[s == 0 ? LIST_OUT_E : LIST_OUT_I];
+    a.tl_ev = r->tile_list[LIST_ION_EV];
+    a.tc_ev = r->tile_cnt[LIST_ION_EV];
+    a.step = (unsigned int)r->time_step;
+    return a;
+}
+
+int pgb_launch_push(pgb_run* r, int s, bool mcc, bool deposit, bool flag_ion) {
+    (void)flag_ion;
+    PushArgs a = push_args(r, s);
+    int g = grid_for(r, 8);
+    if (mcc && deposit) k_push<true, true, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    else if (mcc) k_push<true, false, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    else if (deposit) k_push<false, true, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    else k_push<false, false, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_flag_outside(pgb_run* r, int s) {
+    int l = s == 0 ? LIST_OUT_E : LIST_OUT_I;
+    k_flag<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s].xv, r->ds, s, r->nx, r->ny, r->p.steadystate,
+                                                               r->tile_list[l], r->tile_cnt[l]);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_mcc(pgb_run* r) {
+    PushArgs a = push_args(r, 0);
+    k_mcc<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+/* per-tile list `which` (tiles of species s) -> dense list + count */
+int pgb_build_list(pgb_run* r, int which, int s) {
+    int* toff = r->aux_j;
+    k_scan_small<<<1, 1024, 0, r->stream>>>(r->tile_cnt[which], toff, &r->ds->n[s], 0, &r->ds->list_n[which]);
+    k_gather_lists<<<grid_for(r, 4), 256, 0, r->stream>>>(r->tile_list[which], r->tile_cnt[which], toff,
+                                                           &r->ds->n[s], r->list[which]);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_deposit(pgb_run* r, int s) {
+    k_deposit<<<grid_for(r, 8), 256, 0, r->stream>>>(r->sp[s].xv, r->sp[s].w, r->ds, s, r->nx, r->ny, r->qacc[s]);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e) {
+    InjectArgs a;
+    a.e = r->sp[0]; a.i = r->sp[1]; a.ds = r->ds; a.k = r->p.number_to_inject;
+    a.dx = r->dx; a.dy = r->dy; a.xlength = r->p.xlength; a.ylength = r->p.ylength;
+    a.seed = r->p.seed; a.step = (unsigned int)r->time_step;
+    a.pce = push_consts(r, 0); a.exy = r->exy; a.qacc_e = r->qacc[0];
+    a.push_e = push_e; a.species_mask = species_mask;
+    a.list_out_e = r->list[LIST_OUT_E]; a.list_cap = r->list_cap;
+    k_inject<<<1, 32, 0, r->stream>>>(a);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i) {
+    IonizeAppendArgs a;
+    a.e = r->sp[0]; a.i = r->sp[1]; a.ds = r->ds; a.ev = r->list[LIST_ION_EV];
+    a.cc = pgb_coll_consts(r); a.neut64 = r->neut64[0];
+    a.dx = r->dx; a.dy = r->dy; a.step = (unsigned int)r->time_step;
+    a.store_e = store_e;
+    a.store_i = store_i;
+    k_ionize_append<<<r->sms * 2, 256, 0, r->stream>>>(a);
+    PGB_CK(r, cudaGetLastError());
+    k_ionize_commit<<<1, 1, 0, r->stream>>>(r->ds, a.store_e, a.store_i, r->sp[0].cap, r->sp[1].cap);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_compact(pgb_run* r, int s) {
+    Species& S = r->sp[s];
+    int* tc = r->tile_cnt[LIST_SPARE];
+    int* toff = r->aux_j;
+    PGB_CK(r, cudaMemsetAsync(tc, 0, sizeof(int) * r->ntiles_cap, r->stream));
+    k_alive_count<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(S.xv, r->ds, s, tc);
+    k_scan_small<<<1, 1024, 0, r->stream>>>(tc, toff, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]);
+    k_compact<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(S, r->ds, s, toff);
+    k_compact_commit<<<1, 1, 0, r->stream>>>(r->ds, s, &r->ds->list_n[LIST_SPARE]);
+    PGB_CK(r, cudaGetLastError());
+    std::swap(S.xv, S.xv2);
+    std::swap(S.vz, S.vz2);
+    std::swap(S.w, S.w2);
+    std::swap(S.id, S.id2);
+    return 0;
+}
+
+int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long n) {
+    k_load<<<grid_for(r, 4), 256, 0, r->stream>>>(r->sp[s], d_aos, n, r->dx, r->dy);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap) {
+    int* tc = r->tile_cnt[LIST_SPARE];
+    int* toff = r->aux_j;
+    PGB_CK(r, cudaMemsetAsync(tc, 0, sizeof(int) * r->ntiles_cap, r->stream));
+    k_alive_count<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s].xv, r->ds, s, tc);
+    k_scan_small<<<1, 1024, 0, r->stream>>>(tc, toff, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]);
+    k_dump<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s], r->ds, s, toff, r->dx, r->dy, d_out, cap);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+

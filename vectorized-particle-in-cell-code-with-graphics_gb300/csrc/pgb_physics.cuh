@@ -1,0 +1,220 @@
+/*
+ * Device physics shared by the particle, collision and wall kernels.
+ *
+ * Per-particle tests that run for every particle every step (in-domain
+ * checks, energies, cross sections, collision probabilities) are FP32.
+ * The events they select (scattering, ionization, charge exchange, wall
+ * interactions, re-insertion) touch a small fraction of the particles and
+ * are evaluated in FP64 with the reference's formulas and operation order.
+ */
+#pragma once
+#include <math.h>
+#include <stdint.h>
+#include "pgb_internal.h"
+#include "pgb_rng.h"
+
+#define PGB_PI 3.141592654
+#define PGB_CHARGE 1.602177e-19
+#define PGB_AMU 1.66054e-27
+
+/* (int)v with the x86-64 result for NaN and out-of-range values (INT_MIN),
+ * which the reference relies on to treat NaN particles as outside the left
+ * wall (boundary.cpp:595-599)                                              */
+__device__ __forceinline__ int cellf(float v) {
+    return (v >= -2147483648.0f && v < 2147483648.0f) ? __float2int_rz(v) : INT32_MIN;
+}
+__device__ __forceinline__ int celld(double v) {
+    return (v > -2147483649.0 && v < 2147483648.0) ? (int)v : INT32_MIN;
+}
+
+/* tombstone: a removed particle */
+__device__ __forceinline__ bool is_dead(float xs) { return xs == -INFINITY; }
+
+/* CIC deposit of one particle (pic.cl:36-49) as int64 fixed point:
+ * round(a*w*2^32) per node; integer sums are exact and order-free, so the
+ * grid is identical run to run.  Caller checks deposit_ok().             */
+__device__ __forceinline__ void deposit_cell(unsigned long long* qacc, int nx, float xs, float ys, float w) {
+    int jp = cellf(xs), kp = cellf(ys);
+    float wj = xs - (float)jp, wk = ys - (float)kp;
+    float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
+    float a2 = wk * (1.0f - wj), a1 = wj * wk;
+    const float S = 4294967296.0f;
+    long long c4 = __float2ll_rn(a4 * w * S), c3 = __float2ll_rn(a3 * w * S);
+    long long c2 = __float2ll_rn(a2 * w * S), c1 = __float2ll_rn(a1 * w * S);
+    unsigned long long* q = qacc + (long long)kp * nx + jp;
+    atomicAdd(q, (unsigned long long)c4);
+    atomicAdd(q + 1, (unsigned long long)c3);
+    atomicAdd(q + nx, (unsigned long long)c2);
+    atomicAdd(q + nx + 1, (unsigned long long)c1);
+}
+
+__device__ __forceinline__ bool deposit_ok(float xs, float ys, int nx, int ny) {
+    int jp = cellf(xs), kp = cellf(ys);
+    return jp < nx - 1 && xs > 0.0f && kp < ny - 1 && ys > 0.0f;
+}
+
+__device__ __forceinline__ void maybe_deposit(unsigned long long* qacc, int nx, int ny, float xs, float ys, float w) {
+    if (deposit_ok(xs, ys, nx, ny)) deposit_cell(qacc, nx, xs, ys, w);
+}
+
+/* ---------------------------------------------------------- wall classes */
+/* e_boundary / ion_boundary: outside iff jp<0 || jp>=nx || kp<0 || kp>=ny
+ * (boundary.cpp:595-599, 774-778)                                         */
+__device__ __forceinline__ bool outside_absorbing(float xs, float ys, int nx, int ny) {
+    int jp = cellf(xs), kp = cellf(ys);
+    return jp < 0 || jp >= nx || kp < 0 || kp >= ny;
+}
+/* steady walls: x < 0 or (int)(x/DX) >= nx, same for y (boundary.cpp:906-1013) */
+__device__ __forceinline__ bool outside_steady(float xs, float ys, int nx, int ny) {
+    return xs < 0.0f || cellf(xs) >= nx || ys < 0.0f || cellf(ys) >= ny;
+}
+
+/* ------------------------------------------------------- cross sections */
+/* FP32 forms of e_collisions.cpp:205-308 and ion_collisions.cpp:170-199;
+ * values the reference leaves uninitialised on branch edges are 0        */
+__device__ __forceinline__ float p6(float e, float a6, float a5, float a4, float a3, float a2, float a1, float a0) {
+    return ((((((a6 * e + a5) * e + a4) * e + a3) * e + a2) * e + a1) * e + a0);
+}
+__device__ __forceinline__ float sig_ar_el(float e) {
+    if (e < 0.35f) return p6(e, 28019.0f, -32798.0f, 15048.0f, -34312.0f, 4084.0f, -249.0f, 7.576f);
+    if (e < 15.0f && e > 0.35f) return ((-0.013f * e + 0.232f) * e + 1.066f) * e + 0.085f;
+    if (e > 15.0f) return 126.2f * __powf(e, -0.69f);
+    return 0.0f;
+}
+__device__ __forceinline__ float sig_ar_ion(float e) {
+    if (e < 15.755f) return 0.0f;
+    if (e < 100.0f && e > 15.755f) return (((-3.0e-7f * e + 8.0e-5f) * e - 0.008f) * e + 0.416f) * e - 4.758f;
+    if (e > 100.0f) return 130.0f * __powf(e, -0.74f);
+    return 0.0f;
+}
+__device__ __forceinline__ float sig_h_el(float e) {
+    if (e < 1.0e-2f) return (3.834f * e - 20.82f) * e + 40.98f;
+    if (e >= 1.0e-2f && e < 20.0f) return -6.15f * logf(e) + 20.91f;
+    if (e >= 20.0f) return 102.2f * __powf(e, -1.19f);
+    return 0.0f;
+}
+__device__ __forceinline__ float sig_h_ion(float e) {
+    const float I = 13.6f;
+    if (!(e >= I)) return 0.0f;
+    float IE = e / I, C = 1.0f - 1.0f / IE;
+    float poly = ((((2.2986f * C - 2.8115f) * C + 1.4003f) * C - 0.034539f) * C - 0.032226f) * C;
+    return (1.0f / (I * e)) * (0.18450f * logf(IE) + poly);
+}
+__device__ __forceinline__ float sig_ar_cx(float e) {
+    if (e > 4.0f) return (2.0f + 5.5f / sqrtf(e)) * 10.0f;
+    return (-2.95f * sqrtf(e) + 10.65f) * 10.0f;
+}
+/* ion_collisions.cpp:185-199: the energy is divided by 1000 and by AMU */
+__device__ __forceinline__ float sig_h_cx(float e) {
+    double ee = (double)e / 1000.0 / PGB_AMU;
+    if (ee < 1.0e-4) return 0.0f;
+    return (float)((3.2345 * log((235.88 / ee) + 2.3713)) /
+                   (1.0 + 0.038371 * ee + 3.8068e-6 * pow(ee, 3.5) + 1.1832e-10 * pow(ee, 5.4)));
+}
+
+struct CollConsts {
+    int species;              /* PGB_ARGON / PGB_HYDROGEN */
+    int el_const, ion_const, cx_const;
+    float el_value, ion_value, cx_value;
+    float e_energy_coef;      /* (0.5/CHARGE)*ME  */
+    float i_energy_coef;      /* (0.5/CHARGE)*MI  */
+    float e_pcoef;            /* DT*1e-20*NEUTRAL_DENSITY  */
+    float i_pcoef;            /* DTI*1e-20*NEUTRAL_DENSITY */
+    double me, mi, dt, dti, threshold, reduced_mass;
+    int n_neutral;
+    uint64_t seed;
+};
+
+__device__ __forceinline__ float sigma_el(const CollConsts& c, float e) {
+    if (c.el_const) return c.el_value;
+    return c.species == PGB_ARGON ? sig_ar_el(e) : sig_h_el(e);
+}
+__device__ __forceinline__ float sigma_ion(const CollConsts& c, float e) {
+    if (c.ion_const) return c.ion_value;
+    return c.species == PGB_ARGON ? sig_ar_ion(e) : sig_h_ion(e);
+}
+__device__ __forceinline__ float sigma_cx(const CollConsts& c, float e) {
+    if (c.cx_const) return c.cx_value;
+    return c.species == PGB_ARGON ? sig_ar_cx(e) : sig_h_cx(e);
+}
+
+/* ------------------------------------------------ electron collisions */
+/* collisions::scattered_velocity (collisions.cpp:107-171), FP64 */
+__device__ inline void scatter_fp64(pgb_stream* st, const double* neut, int nn, double energy, double cf,
+                                    double& vx, double& vy, double& vz) {
+    const double two_pi = 2.0 * PGB_PI;
+    double R = pgb_u01d(pgb_stream_u32(st)), cosChi;
+    if (energy < 1.0e-2) cosChi = sqrt(1.0 - R);
+    else cosChi = 2.0 * (1.0 - pow((1.0 + energy), R)) / energy + 1.0;
+    double sinChi = sqrt(1.0 - cosChi * cosChi);
+    double cosPhi = cos(two_pi * R), sinPhi = sin(two_pi * R);
+    int index = (int)(pgb_stream_u32(st) % (uint32_t)(nn - 1));
+    double nvx = neut[index], nvy = neut[nn + index], nvz = neut[2 * nn + index];
+    double ux = vx - nvx, uy = vy - nvy, uz = vz - nvz;
+    double uperp = sqrt(uy * uy + uz * uz);
+    double u = sqrt(ux * ux + uperp * uperp);
+    double uyp, uzp;
+    if (uperp < 1.0) { uyp = 1.0; uzp = 1.0; }
+    else { uyp = uy / uperp; uzp = uz / uperp; }
+    vz -= cf * (uz * (1.0 - cosChi) - (ux * uzp * cosPhi - u * uyp * sinPhi) * sinChi);
+    vy -= cf * (uy * (1.0 - cosChi) - (ux * uyp * cosPhi + u * uzp * sinPhi) * sinChi);
+    vx -= cf * (ux * (1.0 - cosChi) + uperp * cosPhi * sinChi);
+}
+
+/* e_collisions::ionization (e_collisions.cpp:319-443), FP64.  The excess
+ * energy mixes J and eV (line 377) and is negative, so every output is NaN
+ * as in the reference.  Returns the parent's new velocity and the new
+ * electron/ion states (positions in metres).                              */
+struct IonizeOut {
+    double evx, evy, evz;             /* parent electron after               */
+    double nx_, ny_, nvx, nvy, nvz;   /* new electron                        */
+    double ix, iy, ivx, ivy, ivz;     /* new ion                             */
+};
+__device__ inline IonizeOut ionize_fp64(pgb_stream* st, const double* neut, int nn, const CollConsts& c,
+                                        double xe, double ye, double vxe, double vye, double vze) {
+    const double me = c.me, mi = c.mi;
+    double reduced_mass = c.reduced_mass * me;
+    double R = pgb_u01d(pgb_stream_u32(st));
+    double Rxe = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
+    double Rye = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
+    double Rze = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
+    double R2xe = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
+    double R2ye = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
+    double R2ze = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
+    int index = (int)(pgb_stream_u32(st) % (uint32_t)(nn - 1));
+    double nvx = neut[index], nvy = neut[nn + index], nvz = neut[2 * nn + index];
+    double Wx = (mi * nvx + me * vxe) / (mi + me);
+    double Wy = (mi * nvy + me * vye) / (mi + me);
+    double Wz = (mi * nvz + me * vze) / (mi + me);
+    double ve = sqrt(vxe * vxe + vye * vye + vze * vze);
+    double vn = sqrt(nvx * nvx + nvy * nvy + nvz * nvz);
+    double excess = (reduced_mass / 2.0) * (ve - vn) * (ve - vn) - c.threshold;
+    double ve_after = sqrt(2.0 * R * excess / me);
+    double v2e_after = sqrt(2.0 * (1.0 - R) * excess / me);
+    double a0 = ve_after * Rxe, a1 = ve_after * Rye, a2 = ve_after * Rze;
+    double b0 = v2e_after * R2xe, b1 = v2e_after * R2ye, b2 = v2e_after * R2ze;
+    IonizeOut o;
+    o.ivx = Wx - (me / mi) * (a0 + b0);
+    o.ivy = Wy - (me / mi) * (a1 + b1);
+    o.ivz = Wz - (me / mi) * (a2 + b2);
+    o.ix = xe + o.ivx * c.dti;
+    o.iy = ye + o.ivy * c.dti;
+    o.evx = a0 + Wx; o.evy = a1 + Wy; o.evz = a2 + Wz;
+    o.nvx = b0 + Wx; o.nvy = b1 + Wy; o.nvz = b2 + Wz;
+    o.nx_ = xe + o.nvx * c.dt;
+    o.ny_ = ye + o.nvy * c.dt;
+    return o;
+}
+
+/* particle::get_particle_velocity / boundary::get_particle_velocity
+ * (particle.cpp:452-464, boundary.cpp:833-845), FP64                     */
+__device__ inline double maxwell_fp64(pgb_stream* st, double vt) {
+    double v = 0.0;
+    for (int k = 0; k < 64; ++k) {
+        double R1 = pgb_u01d(pgb_stream_u32(st));
+        double R2 = pgb_u01d(pgb_stream_u32(st));
+        v = vt * cos(2.0 * PGB_PI * R2) * sqrt(fabs(log(R1)));
+        if (!(fabs(v) > vt * 10000)) break;
+    }
+    return v;
+}

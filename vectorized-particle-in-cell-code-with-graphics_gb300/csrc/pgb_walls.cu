@@ -1,0 +1,587 @@
+/*
+ * Wall kernels and ion-neutral charge exchange.
+ *
+ * Reference path: boundary::ion_boundary (boundary.cpp:765-824),
+ * boundary::e_boundary (boundary.cpp:581-677) with its yields
+ * (boundary.cpp:281-337), reflect_electron, secondary_vel,
+ * secondary_electrons, i_secondary_vel (boundary.cpp:374-756), the
+ * steady-state pair re-insertion (boundary.cpp:854-1097) and
+ * ion_collisions::collision (ion_collisions.cpp:255-308).
+ *
+ * The walls work from the ordered lists of outside particles that the push
+ * kernels produced.  Pass 1 decides each wall event from the particle's own
+ * random stream and applies the ones that modify a particle in place
+ * (absorb, reflect, backscatter); an exclusive scan of the secondary counts
+ * gives every new electron its slot and id in list order; pass 2 writes
+ * the secondaries and removes their parents.  Results therefore do not
+ * depend on thread scheduling.  Event arithmetic is FP64.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include "pgb_internal.h"
+#include "pgb_physics.cuh"
+
+struct WallArgs {
+    Species e, i;
+    DevState* ds;
+    const int* list_e;
+    const int* list_i;
+    int* aux;                  /* per list entry: secondary count  */
+    int* off;                  /* exclusive scan of aux            */
+    unsigned long long* qacc_e;
+    unsigned long long* qacc_i;
+    int nx, ny;
+    double dx, dy, dt;         /* boundary objects use DT (boundary.h:62) */
+    double me, mi;
+    double threshold, work_function;
+    double e0, emax0, max_yield;
+    int e_see, refl, back, ion_see;
+    double vte, vti, xlength, ylength;
+    uint64_t seed;
+    unsigned int step;
+};
+
+__device__ __forceinline__ void store_particle(const Species& S, long long slot, double x, double y, double vx,
+                                               double vy, double vz, double dx, double dy) {
+    S.xv[slot] = make_float4((float)(x / dx), (float)(y / dy), (float)vx, (float)vy);
+    S.vz[slot] = (float)vz;
+}
+
+/* boundary::secondary_vel (boundary.cpp:427-486) on a particle state */
+__device__ void secondary_vel_d(const WallArgs& a, pgb_stream* st, double& x, double& y, double& vx, double& vy,
+                                double& vz, double velocity, int jp, int kp) {
+    const double lengthX = a.dx * a.nx, lengthY = a.dy * a.ny;
+    if (jp < 0 || jp >= a.nx) {
+        double R = pgb_u01d(pgb_stream_u32(st)), Rphi = pgb_u01d(pgb_stream_u32(st)), Rchi = pgb_u01d(pgb_stream_u32(st));
+        double chi = asin(sqrt(Rchi)), phi = 2.0 * PGB_PI * Rphi;
+        vx = fabs(velocity * cos(chi));
+        vy = velocity * sin(chi) * cos(phi);
+        vz = velocity * sin(chi) * sin(phi);
+        x = R * a.dt * fabs(vx);
+        if (jp >= a.nx) { x = lengthX - x; vx = -fabs(velocity * cos(chi)); }
+    }
+    if (kp < 0 || kp >= a.ny) {
+        double R = pgb_u01d(pgb_stream_u32(st)), Rphi = pgb_u01d(pgb_stream_u32(st)), Rchi = pgb_u01d(pgb_stream_u32(st));
+        double chi = asin(sqrt(Rchi)), phi = 2.0 * PGB_PI * Rphi;
+        vy = fabs(velocity * cos(chi));
+        vx = velocity * sin(chi) * cos(phi);
+        vz = velocity * sin(chi) * sin(phi);
+        y = R * a.dt * fabs(vy);
+        if (kp >= a.ny) { y = lengthY - y; vy = -fabs(velocity * cos(chi)); }
+    }
+}
+
+__device__ __forceinline__ double see_velocity(const WallArgs& a, double R) {
+    return sqrt((2.0 * R * PGB_CHARGE * (a.threshold - 2.0 * a.work_function) / a.me));
+}
+
+/* --------------------------------------------------------- ion walls */
+/* i_impact_see_yield_Ar (boundary.cpp:310-317) */
+__device__ __forceinline__ double ion_yield(const WallArgs& a, double energy) {
+    if (!a.ion_see) return 0.0;
+    double y = 0.0;
+    if (energy >= 80.0)
+        y = 0.006 * energy / (1.0 + (energy / 10.0)) + 1.05e-4 * (sqrt((energy - 80.0)) / (1.0 + pow((energy / 8000.0), 1.5)));
+    return y;
+}
+
+__global__ void k_iwall1(WallArgs a) {
+    const long long m = a.ds->list_n[LIST_OUT_I];
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
+        int slot = a.list_i[k];
+        float4 p = a.i.xv[slot];
+        double vx = p.z, vy = p.w, vz = a.i.vz[slot];
+        double energy = (0.5 / PGB_CHARGE) * a.mi * (vx * vx + vy * vy + vz * vz);
+        double yield = ion_yield(a, energy);
+        pgb_stream st;
+        pgb_stream_init(&st, a.seed, a.i.id[slot], a.step, PGB_STREAM_IWALL, 1);
+        double R = pgb_u01d(pgb_stream_u32(&st));
+        a.aux[k] = (R < yield) ? (int)floor(yield) + 1 : 0;
+    }
+}
+
+/* boundary::i_secondary_vel (boundary.cpp:687-756) */
+__global__ void k_iwall2(WallArgs a) {
+    const long long m = a.ds->list_n[LIST_OUT_I];
+    const long long ne0 = a.ds->n[0];
+    const unsigned int id0 = a.ds->next_id[0];
+    const double lengthX = a.dx * a.nx, lengthY = a.dy * a.ny;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
+        int slot = a.list_i[k];
+        float4 p = a.i.xv[slot];
+        int c = a.aux[k];
+        if (c > 0) {
+            double ix = (double)p.x * a.dx, iy = (double)p.y * a.dy, w = a.i.w[slot];
+            int jp = cellf(p.x), kp = cellf(p.y);
+            for (int j = 0; j < c; ++j) {
+                long long es = ne0 + a.off[k] + j;
+                if (es >= a.e.cap) { atomicOr(&a.ds->err, ERR_CAP_E); break; }
+                unsigned int id = id0 + (unsigned int)(a.off[k] + j);
+                pgb_stream st;
+                pgb_stream_init(&st, a.seed, id, a.step, PGB_STREAM_SEE, 0);
+                double x = 0.0, y = 0.0, vx = 0.0, vy = 0.0, vz = 0.0, ww = 1.0;
+                if (jp < 0 || jp >= a.nx) {
+                    double R = pgb_u01d(pgb_stream_u32(&st));
+                    double velocity = see_velocity(a, R);
+                    double Rphi = pgb_u01d(pgb_stream_u32(&st)), Rchi = pgb_u01d(pgb_stream_u32(&st));
+                    double chi = asin(sqrt(Rchi)), phi = 2.0 * PGB_PI * Rphi;
+                    vx = fabs(velocity * cos(chi));
+                    vy = velocity * sin(chi) * cos(phi);
+                    vz = velocity * sin(chi) * sin(phi);
+                    ww = w;
+                    x = R * a.dt * fabs(vx);
+                    if (jp >= a.nx) { x = lengthX - x; vx = -fabs(velocity * cos(chi)); }
+                }
+                if (kp < 0 || kp >= a.ny) {
+                    double R = pgb_u01d(pgb_stream_u32(&st));
+                    double velocity = see_velocity(a, R);
+                    double Rphi = pgb_u01d(pgb_stream_u32(&st)), Rchi = pgb_u01d(pgb_stream_u32(&st));
+                    double chi = asin(sqrt(Rchi)), phi = 2.0 * PGB_PI * Rphi;
+                    vy = fabs(velocity * cos(chi));
+                    vx = velocity * sin(chi) * cos(phi);
+                    vz = velocity * sin(chi) * sin(phi);
+                    ww = w;
+                    y = R * a.dt * fabs(vy);
+                    if (kp >= a.ny) { y = lengthY - y; vy = -fabs(velocity * cos(chi)); }
+                }
+                (void)ix; (void)iy;
+                store_particle(a.e, es, x, y, vx, vy, vz, a.dx, a.dy);
+                a.e.w[es] = (float)ww;
+                a.e.id[es] = id;
+                float4 q = a.e.xv[es];
+                maybe_deposit(a.qacc_e, a.nx, a.ny, q.x, q.y, (float)ww);
+            }
+        }
+        a.i.xv[slot].x = -INFINITY;
+    }
+}
+
+/* ---------------------------------------------------- electron walls */
+struct WallState { double energy, angleX, angleY; int onX; };
+
+/* e_impact_see_yield_v (boundary.cpp:281-300) */
+__device__ __forceinline__ double e_yield(const WallArgs& a, const WallState& w) {
+    if (!a.e_see) return 0.0;
+    double twoPi = 2.0 * PGB_PI;
+    double v = (w.energy - a.e0) / (a.emax0 - a.e0);
+    double k = (v > 1) ? 0.25 : 0.62;
+    double ang = w.onX ? w.angleX : w.angleY;
+    double ww = (w.energy - a.e0) / (a.emax0 * (1.0 + k * (ang * ang / twoPi)) - a.e0);
+    return a.max_yield * (1.0 + k * (ang * ang / twoPi)) * pow((ww * exp((1.0 - ww))), k);
+}
+
+/* outcome codes of one electron wall interaction */
+enum { EW_STAY = 0, EW_ABSORB = 1, EW_SEE = 2, EW_RETRY = -1 };
+
+__device__ int e_wall_event(const WallArgs& a, pgb_stream* st, double& x, double& y, double& vx, double& vy,
+                            double& vz, int jp, int kp, int& nsec, int& kind) {
+    const double lengthX = a.dx * a.nx, lengthY = a.dy * a.ny;
+    WallState w;
+    w.onX = (jp < 0 || jp >= a.nx);
+    double u2 = vx * vx + vy * vy + vz * vz;
+    w.energy = (0.5 / PGB_CHARGE) * a.me * u2;
+    double uu = 2.0 * w.energy / a.me;
+    w.angleX = acos(vx / (sqrt(uu) + 1.0e-6));
+    w.angleY = acos(vy / (sqrt(uu) + 1.0e-6));
+    double yield = e_yield(a, w);
+    double R = pgb_u01d(pgb_stream_u32(st));
+    if (R < yield) {
+        double refl = (a.refl && w.energy > 50.0) ? 0.1 * yield : 0.0;
+        double back = (a.back && w.energy > 50.0) ? 0.1 * yield : 0.0;
+        int no_inject = (int)floor(fabs((yield - refl - back))) + 1;
+        const double offset = 1.0e-6;
+        R = pgb_u01d(pgb_stream_u32(st));
+        if (R < refl / (yield + offset)) {
+            /* reflect_electron (boundary.cpp:374-417) */
+            double Rr = pgb_u01d(pgb_stream_u32(st));
+            if (jp >= a.nx) { vx = -vx; x = lengthX - Rr * a.dt * fabs(vx); }
+            else if (jp < 0) { vx = -vx; x = Rr * a.dt * fabs(vx); }
+            if (kp >= a.ny) { vy = -vy; y = lengthY - Rr * a.dt * fabs(vy); }
+            else if (kp < 0) { vy = -vy; y = Rr * a.dt * fabs(vy); }
+            kind = ST_REFL;
+            return EW_STAY;
+        } else if (R > refl / yield && R < (refl + back) / (yield + offset)) {
+            double R3 = (double)(pgb_stream_u32(st) % 10000u) / 10000.0;
+            double velocity = R3 * sqrt((2.0 * PGB_CHARGE * w.energy) / a.me);
+            secondary_vel_d(a, st, x, y, vx, vy, vz, velocity, jp, kp);
+            kind = ST_BACK;
+            return EW_STAY;
+        } else if (R > (refl + back) / (yield + offset)) {
+            nsec = no_inject;
+            return EW_SEE;
+        }
+        return EW_RETRY;
+    }
+    return EW_ABSORB;
+}
+
+__global__ void k_ewall1(WallArgs a) {
+    const long long m = a.ds->list_n[LIST_OUT_E];
+    int cnt[4] = {0, 0, 0, 0};   /* absorbed, reflected, backscattered, see events */
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
+        int slot = a.list_e[k];
+        float4 p = a.e.xv[slot];
+        double x = (double)p.x * a.dx, y = (double)p.y * a.dy, vx = p.z, vy = p.w, vz = a.e.vz[slot];
+        pgb_stream st;
+        pgb_stream_init(&st, a.seed, a.e.id[slot], a.step, PGB_STREAM_EWALL, 0);
+        int res = EW_RETRY, nsec = 0, kind = 0;
+        const int jp = cellf(p.x), kp = cellf(p.y);
+        for (int attempt = 0; attempt < 64 && res == EW_RETRY; ++attempt)
+            res = e_wall_event(a, &st, x, y, vx, vy, vz, jp, kp, nsec, kind);
+        if (res == EW_RETRY) res = EW_ABSORB;
+        int c = 0;
+        if (res == EW_STAY) {
+            store_particle(a.e, slot, x, y, vx, vy, vz, a.dx, a.dy);
+            float4 q = a.e.xv[slot];
+            maybe_deposit(a.qacc_e, a.nx, a.ny, q.x, q.y, a.e.w[slot]);
+            cnt[kind == ST_REFL ? 1 : 2]++;
+        } else if (res == EW_ABSORB) {
+            a.e.xv[slot].x = -INFINITY;
+            cnt[0]++;
+        } else {
+            c = nsec;
+            cnt[3]++;
+        }
+        a.aux[k] = c;
+    }
+    const int idx[4] = {ST_ABS_E, ST_REFL, ST_BACK, ST_SEE_EV};
+    int dead = cnt[0] + cnt[3];
+    for (int d = 16; d; d >>= 1) dead += __shfl_down_sync(0xffffffffu, dead, d);
+    if ((threadIdx.x & 31) == 0 && dead) atomicAdd((unsigned long long*)&a.ds->dead[0], (unsigned long long)dead);
+    for (int q = 0; q < 4; ++q) {
+        int v = cnt[q];
+        for (int d = 16; d; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd((unsigned long long*)&a.ds->stats[idx[q]], (unsigned long long)v);
+    }
+}
+
+/* boundary::secondary_electrons (boundary.cpp:494-529) */
+__global__ void k_ewall2(WallArgs a) {
+    const long long m = a.ds->list_n[LIST_OUT_E];
+    const long long ne0 = a.ds->n[0];
+    const unsigned int id0 = a.ds->next_id[0];
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
+        int c = a.aux[k];
+        if (c == 0) continue;
+        int slot = a.list_e[k];
+        float4 p = a.e.xv[slot];
+        double px = (double)p.x * a.dx, py = (double)p.y * a.dy;
+        float w = a.e.w[slot];
+        int jpp = cellf(p.x);
+        for (int j = 0; j < c; ++j) {
+            long long es = ne0 + a.off[k] + j;
+            if (es >= a.e.cap) { atomicOr(&a.ds->err, ERR_CAP_E); break; }
+            unsigned int id = id0 + (unsigned int)(a.off[k] + j);
+            double x = 0.0, y = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+            if (jpp < 0 || jpp >= a.nx) x = px;
+            else y = py;
+            pgb_stream st;
+            pgb_stream_init(&st, a.seed, id, a.step, PGB_STREAM_SEE, 0);
+            double R = pgb_u01d(pgb_stream_u32(&st));
+            double velocity = see_velocity(a, R);
+            /* the new electron sits at the parent's x (left/right wall) or y */
+            int jp = (jpp < 0 || jpp >= a.nx) ? jpp : 0;
+            int kp = (jpp < 0 || jpp >= a.nx) ? 0 : cellf(p.y);
+            secondary_vel_d(a, &st, x, y, vx, vy, vz, velocity, jp, kp);
+            store_particle(a.e, es, x, y, vx, vy, vz, a.dx, a.dy);
+            a.e.w[es] = w;
+            a.e.id[es] = id;
+            float4 q = a.e.xv[es];
+            maybe_deposit(a.qacc_e, a.nx, a.ny, q.x, q.y, w);
+        }
+        a.e.xv[slot].x = -INFINITY;
+    }
+}
+
+/* n, next id and statistics after a wall pass that appended `total` electrons */
+__global__ void k_wall_commit(DevState* ds, const long long* total, int which, long long cap_e, int stat_emit) {
+    long long t = *total;
+    long long v = ds->n[0] + t;
+    ds->n[0] = v < cap_e ? v : cap_e;
+    ds->next_id[0] += (unsigned int)t;
+    long long m = ds->list_n[which == 0 ? LIST_OUT_I : LIST_OUT_E];
+    if (which == 0) { ds->stats[ST_ABS_I] += m; ds->dead[1] += m; }
+    ds->stats[stat_emit] += t;
+}
+
+/* ------------------------------------------------- steady-state walls */
+/* boundary::steadyBoundaryX/Y (boundary.cpp:890-1082): per wall, the r-th
+ * outside electron in list order is paired with the r-th outside ion, and
+ * both are re-inserted at one random point (plop_particles,
+ * boundary.cpp:854-878).  One CTA; lists are a small fraction of N.       */
+__device__ __forceinline__ int steady_class(float c, int ncells) {
+    if (c < 0.0f) return 1;                 /* left / bottom  */
+    if (cellf(c) >= ncells) return 2;       /* right / top    */
+    return 0;
+}
+
+__device__ __forceinline__ void block_scan2(int a, int b, int& ea, int& eb, int& ta, int& tb) {
+    /* exclusive scans of two 0/1 flags over the block, plus totals */
+    __shared__ int s_a[32], s_b[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned ma = __ballot_sync(0xffffffffu, a), mb = __ballot_sync(0xffffffffu, b);
+    unsigned lt = (1u << lane) - 1u;
+    if (lane == 0) { s_a[warp] = __popc(ma); s_b[warp] = __popc(mb); }
+    __syncthreads();
+    int pa = 0, pb = 0, sa = 0, sb = 0;
+    for (int w = 0; w < nw; ++w) {
+        if (w < warp) { pa += s_a[w]; pb += s_b[w]; }
+        sa += s_a[w]; sb += s_b[w];
+    }
+    ea = pa + __popc(ma & lt);
+    eb = pb + __popc(mb & lt);
+    ta = sa; tb = sb;
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) k_steady(WallArgs a, int* ion_by_rank) {
+    const long long me_ = a.ds->list_n[LIST_OUT_E], mi_ = a.ds->list_n[LIST_OUT_I];
+    __shared__ int s_plops;
+    if (threadIdx.x == 0) s_plops = 0;
+    for (int axis = 0; axis < 2; ++axis) {
+        const int nc = axis == 0 ? a.nx : a.ny;
+        /* ions: record slots by (class, rank); lo from the front, hi from the back */
+        int cnt_lo = 0, cnt_hi = 0;
+        for (long long b = 0; b < mi_; b += blockDim.x) {
+            long long k = b + threadIdx.x;
+            int cls = 0, slot = -1;
+            if (k < mi_) {
+                slot = a.list_i[k];
+                float4 p = a.i.xv[slot];
+                cls = steady_class(axis == 0 ? p.x : p.y, nc);
+            }
+            int ea, eb, ta, tb;
+            block_scan2(cls == 1, cls == 2, ea, eb, ta, tb);
+            if (cls == 1) ion_by_rank[cnt_lo + ea] = slot;
+            if (cls == 2) ion_by_rank[mi_ - 1 - (cnt_hi + eb)] = slot;
+            cnt_lo += ta;
+            cnt_hi += tb;
+        }
+        __syncthreads();
+        /* electrons: pair by rank */
+        int rlo = 0, rhi = 0;
+        for (long long b = 0; b < me_; b += blockDim.x) {
+            long long k = b + threadIdx.x;
+            int cls = 0, slot = -1;
+            if (k < me_) {
+                slot = a.list_e[k];
+                float4 p = a.e.xv[slot];
+                cls = steady_class(axis == 0 ? p.x : p.y, nc);
+            }
+            int ea, eb, ta, tb;
+            block_scan2(cls == 1, cls == 2, ea, eb, ta, tb);
+            int partner = -1;
+            if (cls == 1 && rlo + ea < cnt_lo) partner = ion_by_rank[rlo + ea];
+            if (cls == 2 && rhi + eb < cnt_hi) partner = ion_by_rank[mi_ - 1 - (rhi + eb)];
+            if (partner >= 0) {
+                pgb_stream st;
+                pgb_stream_init(&st, a.seed, a.e.id[slot], a.step, PGB_STREAM_PLOP, 0);
+                double rx = pgb_u01d(pgb_stream_u32(&st)), ry = pgb_u01d(pgb_stream_u32(&st));
+                double x = (a.dx + rx * (a.xlength - 2.0 * a.dx));
+                double y = (a.dy + ry * (a.ylength - 2.0 * a.dy));
+                double evx = maxwell_fp64(&st, a.vte), ivx = maxwell_fp64(&st, a.vti);
+                double evy = maxwell_fp64(&st, a.vte), ivy = maxwell_fp64(&st, a.vti);
+                double evz = maxwell_fp64(&st, a.vte), ivz = maxwell_fp64(&st, a.vti);
+                store_particle(a.e, slot, x, y, evx, evy, evz, a.dx, a.dy);
+                store_particle(a.i, partner, x, y, ivx, ivy, ivz, a.dx, a.dy);
+                float4 q = a.e.xv[slot];
+                maybe_deposit(a.qacc_e, a.nx, a.ny, q.x, q.y, a.e.w[slot]);
+                q = a.i.xv[partner];
+                maybe_deposit(a.qacc_i, a.nx, a.ny, q.x, q.y, a.i.w[partner]);
+                atomicAdd(&s_plops, 1);
+            }
+            rlo += ta;
+            rhi += tb;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.ds->stats[ST_PLOP] += s_plops;
+}
+
+/* ================================================================ CX */
+/* ion_collisions::collision (ion_collisions.cpp:255-308): per x column jp,
+ * the probabilities of the eligible ions accumulate in slot order; the ion
+ * that takes the column above 1 exchanges charge (its velocity becomes a
+ * random neutral's) and the column restarts from 0.  The accumulator is
+ * kept in fixed point (2^40 per unit), so sums are exact and independent
+ * of summation order.  Pass 1: per tile of CX_TILE slots, per-column sums.
+ * Pass 2: one warp per column walks the tiles, skipping whole tiles whose
+ * sum cannot cross 1 and scanning the others element by element.        */
+#define CX_TILE 4096
+#define CX_ONE (1ll << 40)
+
+struct CxArgs {
+    Species i;
+    DevState* ds;
+    int nx, ny;
+    float pcoef, ecoef;      /* DTI*1e-20*n_g, (0.5/CHARGE)*MI */
+    CollConsts cc;
+    long long* tile_sum;     /* [tile][column] fixed point */
+    long long* col_acc;      /* per-column accumulator carried across steps (fixed point) */
+    const double* neut64_i;  /* ion-neutral table */
+    uint64_t seed;
+    unsigned int step;
+};
+
+__device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, float vz, int& col) {
+    col = -1;
+    if (is_dead(p.x)) return 0;
+    int jp = cellf(p.x), kp = cellf(p.y);
+    if (!(jp >= 0 && jp < a.nx && kp >= 0 && kp < a.ny)) return 0;
+    col = jp;
+    float u2 = __fadd_rn(__fadd_rn(__fmul_rn(p.z, p.z), __fmul_rn(p.w, p.w)), __fmul_rn(vz, vz));
+    float energy = __fmul_rn(a.ecoef, u2);
+    float u = sqrtf(u2);
+    float s = sigma_cx(a.cc, energy);
+    /* no contraction: both CX passes must compute the same bits */
+    float P = -expm1f(-__fmul_rn(__fmul_rn(u, a.pcoef), s));
+    return __double2ll_rn((double)P * (double)CX_ONE);
+}
+
+__global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
+    extern __shared__ unsigned long long s_sum[];
+    const long long n = a.ds->n[1];
+    const int ntiles = (int)((n + CX_TILE - 1) / CX_TILE);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) s_sum[c] = 0ull;
+        __syncthreads();
+        for (int k = threadIdx.x; k < CX_TILE; k += blockDim.x) {
+            long long i = (long long)t * CX_TILE + k;
+            if (i >= n) break;
+            int col;
+            long long pf = cx_prob_fixed(a, a.i.xv[i], a.i.vz[i], col);
+            if (col >= 0 && pf) atomicAdd(&s_sum[col], (unsigned long long)pf);
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) a.tile_sum[(long long)t * a.nx + c] = (long long)s_sum[c];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (col >= a.nx) return;
+    const long long n = a.ds->n[1];
+    const int ntiles = (int)((n + CX_TILE - 1) / CX_TILE);
+    long long acc = a.col_acc[col];
+    int fired = 0;
+    for (int t0 = 0; t0 < ntiles; t0 += 32) {
+        int t = t0 + lane;
+        long long s = (t < ntiles) ? a.tile_sum[(long long)t * a.nx + col] : 0;
+        /* inclusive prefix over the 32 tiles */
+        long long ps = s;
+        for (int d = 1; d < 32; d <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, ps, d);
+            if (lane >= d) ps += y;
+        }
+        unsigned cross = __ballot_sync(0xffffffffu, acc + ps > CX_ONE);
+        if (!cross) {
+            acc += __shfl_sync(0xffffffffu, ps, 31);
+            continue;
+        }
+        /* tiles before the first crossing cannot fire */
+        int first = __ffs(cross) - 1;
+        long long before = first ? __shfl_sync(0xffffffffu, ps, first - 1) : 0;
+        acc += before;
+        /* scan tile t0+first element by element, then continue after it */
+        int tt = t0 + first;
+        for (int b = 0; b < CX_TILE; b += 32) {
+            long long i = (long long)tt * CX_TILE + b + lane;
+            int c = -1;
+            long long pf = 0;
+            if (i < n) pf = cx_prob_fixed(a, a.i.xv[i], a.i.vz[i], c);
+            unsigned match = __ballot_sync(0xffffffffu, c == col && pf > 0);
+            while (match) {
+                int l = __ffs(match) - 1;
+                match &= match - 1;
+                long long v = __shfl_sync(0xffffffffu, pf, l);
+                acc += v;
+                if (acc > CX_ONE) {
+                    acc = 0;
+                    if (lane == l) {
+                        /* charge_exchange_velocity (ion_collisions.cpp:209-221) */
+                        pgb_stream st;
+                        pgb_stream_init(&st, a.seed, a.i.id[i], a.step, PGB_STREAM_CX, 1);
+                        (void)pgb_stream_u32(&st);
+                        int nn = a.cc.n_neutral;
+                        int index = (int)(pgb_stream_u32(&st) % (uint32_t)(nn - 1));
+                        float4 p = a.i.xv[i];
+                        p.z = (float)a.neut64_i[index];
+                        p.w = (float)a.neut64_i[nn + index];
+                        a.i.xv[i] = p;
+                        a.i.vz[i] = (float)a.neut64_i[2 * nn + index];
+                    }
+                    fired++;
+                }
+            }
+        }
+        /* resume with the tiles after tt */
+        t0 = tt + 1 - 32;
+    }
+    if (lane == 0) {
+        a.col_acc[col] = acc;
+        if (fired) atomicAdd((unsigned long long*)&a.ds->stats[ST_CX], (unsigned long long)fired);
+    }
+}
+
+/* =========================================================== launchers */
+static WallArgs wall_args(pgb_run* r) {
+    WallArgs a;
+    a.e = r->sp[0]; a.i = r->sp[1]; a.ds = r->ds;
+    a.list_e = r->list[LIST_OUT_E]; a.list_i = r->list[LIST_OUT_I];
+    a.aux = r->aux_i; a.off = r->aux_j;
+    a.qacc_e = r->qacc[0]; a.qacc_i = r->qacc[1];
+    a.nx = r->nx; a.ny = r->ny; a.dx = r->dx; a.dy = r->dy; a.dt = r->p.dt;
+    a.me = r->p.electron_mass; a.mi = r->p.ion_mass;
+    a.threshold = r->p.threshold; a.work_function = r->p.work_function;
+    a.e0 = r->p.see_e0; a.emax0 = r->p.see_emax0; a.max_yield = r->p.see_max_yield;
+    a.e_see = r->p.e_impact_see; a.refl = r->p.reflection; a.back = r->p.backscatter;
+    a.ion_see = (r->p.species == PGB_ARGON && r->p.ion_impact_see) ? 1 : 0;
+    a.vte = r->p.vte; a.vti = r->p.vti; a.xlength = r->p.xlength; a.ylength = r->p.ylength;
+    a.seed = r->p.seed; a.step = (unsigned int)r->time_step;
+    return a;
+}
+
+__global__ void k_scan_list(const int* cnt, int* off, const long long* m_ptr, long long* total);
+
+int pgb_launch_walls(pgb_run* r, int which) {
+    WallArgs a = wall_args(r);
+    int g = r->sms * 4;
+    if (r->p.steadystate) {
+        if (which == PGB_BOUNDARY_ELECTRONS) {
+            k_steady<<<1, 1024, 0, r->stream>>>(a, r->aux_i);
+            PGB_CK(r, cudaGetLastError());
+        }
+        return 0;
+    }
+    if (which == PGB_BOUNDARY_IONS) {
+        k_iwall1<<<g, 256, 0, r->stream>>>(a);
+        k_scan_list<<<1, 1024, 0, r->stream>>>(r->aux_i, r->aux_j, &r->ds->list_n[LIST_OUT_I], &r->ds->list_n[LIST_SPARE]);
+        k_iwall2<<<g, 256, 0, r->stream>>>(a);
+        k_wall_commit<<<1, 1, 0, r->stream>>>(r->ds, &r->ds->list_n[LIST_SPARE], 0, r->sp[0].cap, ST_ISEE_EM);
+    } else {
+        k_ewall1<<<g, 256, 0, r->stream>>>(a);
+        k_scan_list<<<1, 1024, 0, r->stream>>>(r->aux_i, r->aux_j, &r->ds->list_n[LIST_OUT_E], &r->ds->list_n[LIST_SPARE]);
+        k_ewall2<<<g, 256, 0, r->stream>>>(a);
+        k_wall_commit<<<1, 1, 0, r->stream>>>(r->ds, &r->ds->list_n[LIST_SPARE], 1, r->sp[0].cap, ST_SEE_EM);
+    }
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_cx(pgb_run* r) {
+    CxArgs a;
+    a.i = r->sp[1]; a.ds = r->ds; a.nx = r->nx; a.ny = r->ny;
+    a.cc = pgb_coll_consts(r);
+    a.pcoef = a.cc.i_pcoef; a.ecoef = a.cc.i_energy_coef;
+    a.tile_sum = (long long*)r->cx_tile_sum;
+    a.col_acc = (long long*)r->prob_cx;
+    a.neut64_i = r->neut64[1];
+    a.seed = r->p.seed; a.step = (unsigned int)r->time_step;
+    k_cx_tiles<<<r->sms * 4, 256, sizeof(unsigned long long) * r->nx, r->stream>>>(a);
+    int warps = 8;
+    k_cx_walk<<<(r->nx + warps - 1) / warps, warps * 32, 0, r->stream>>>(a);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
