@@ -1,0 +1,322 @@
+"""Benchmark: particle-steps/s of the PIC time step on one GB300.
+
+Workload (the configuration the headline metric is quoted on): H plasma
+(electrons and H+) with the collisional boundary of the reference's
+"H with coll-boundary" preset -- energy-dependent e-H elastic and ionization
+and H+-H charge exchange, electron-impact secondary emission, reflection and
+backscatter, 10 injected particles per species per step -- on a 512x512-cell
+grid (513x513 nodes), 16Mi particles per species, Gaussian density centred in
+the box (sigma = L/4, truncated to the box), Maxwellian Te = 3 eV and
+Ti = 0.026 eV.  Synthetic seeded data; inputs resident in HBM when the timed
+region starts (the particle state, 0.9 GB, is larger than L2).
+
+One JSON line is printed:
+  value      device-timed particle-steps/s (sum over species of live particles
+             x steps / CUDA-event time of the steps on the run's stream)
+  e2e        the same metric through the C ABI with host buffers: every step
+             uploads both species from pinned host memory, steps, and
+             downloads them again
+  roofline   the electron kernel (collisions + gather + push + deposit) at
+             48 algorithmic bytes per particle, against the measured HBM copy
+             bandwidth
+  cpu_baseline  the CPU oracle (restatement of the reference's C++ path) on a
+             bounded sample, all host threads
+`--impl reference` times that CPU path alone on the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "vectorized-particle-in-cell-code-with-graphics_gb300")
+sys.path.insert(0, PKG)
+
+N_PER_SPECIES = 16 * 1024 * 1024
+GRID_NODES = 513
+ALG_BYTES = 48          # per particle-step: read x,y,vx,vy,vz,w,id (28 B) + write x,y,vx,vy,vz (20 B)
+METRIC = "particle-steps/s"
+
+
+def workload_params(picgb, seed=1003):
+    return picgb.make_params(
+        X_NO_OF_CELLS=GRID_NODES, TEMPERATURE=3.0, ION_MASS_AMU=1.0, THRESHOLD=13.6, SPECIES="HYDROGEN",
+        HAVE_COLLISIONS=True, SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT",
+        SIGMA_IONIZATION="ENERGY_DEPENDENT", E_IMPACT_SEE="YES", ION_IMPACT_SEE="NO", REFLECTION="YES",
+        BACKSCATTER="YES", STEADYSTATE="NO", NUMBER_TO_INJECT=10, SIZE_TO_CHECK=2**31 - 1, RAND_SEED=seed)
+
+
+def gaussian_state(p, n, te, ti, seed, ion_mass):
+    """Positions ~ N(L/2, (L/4)^2) truncated to (0, L)^2; Maxwellian velocities."""
+    rng = np.random.default_rng(seed)
+    L = p.xlength
+    out = []
+    for m, T in ((9.10939e-31, te), (ion_mass, ti)):
+        a = np.empty((n, 6))
+        for col in (0, 1):
+            v = rng.normal(0.5 * L, 0.25 * L, n)
+            bad = (v <= 0) | (v >= L)
+            while bad.any():
+                v[bad] = rng.normal(0.5 * L, 0.25 * L, int(bad.sum()))
+                bad = (v <= 0) | (v >= L)
+            a[:, col] = v
+        a[:, 2:5] = rng.normal(0.0, math.sqrt(T * 1.602177e-19 / m), (n, 3))
+        a[:, 5] = 1.0
+        out.append(a)
+    return out
+
+
+class Clocks:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(r[1]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k] and "Not" not in r[5 + k]})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the electron kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d
+    except (OSError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------------ CPU path
+def cpu_sample(n_per_species, steps, threads):
+    """The CPU oracle on a bounded sample of the workload: particle-steps/s."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import orc
+    import picgb
+    orc.build_port()
+    p = workload_params(picgb)
+    e, i = gaussian_state(p, n_per_species, 3.0, 0.026, 1003, p.ion_mass)
+    o = orc.Oracle(p, threads=threads)
+    o.load_particles(0, e)
+    o.load_particles(1, i)
+    o.initial_boundary()
+    o.step(1)
+    c0 = o.counters()
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    c1 = o.counters()
+    ps = 0.5 * (c0["n_e"] + c0["n_i"] + c1["n_e"] + c1["n_i"]) * steps
+    return ps / dt, dt
+
+
+# ------------------------------------------------------------------ GPU path
+def run_gpu(args, rank, world):
+    import torch
+    import picgb
+    import build_lib
+    build_lib.build()
+    torch.cuda.set_device(rank % max(torch.cuda.device_count(), 1))
+    p = workload_params(picgb, seed=1003 + rank)
+    n = int(N_PER_SPECIES * args.scale)
+    e, i = gaussian_state(p, n, 3.0, 0.026, 1003 + rank, p.ion_mass)
+    run = picgb.Run(p)
+    run.load_particles(0, e)
+    run.load_particles(1, i)
+    run.initial_boundary()
+    run.step(args.warmup)
+    stream = torch.cuda.ExternalStream(run.stream())
+    c0 = run.counters()
+    l0 = run.profile()["launches"]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(torch.cuda.current_device()) as clk:
+        ev0.record(stream)
+        run.step(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = ev0.elapsed_time(ev1)
+    c1 = run.counters()
+    launches = run.profile()["launches"] - l0
+    ps = 0.5 * (c0["n_e"] + c0["n_i"] + c1["n_e"] + c1["n_i"]) * args.steps
+    # per-phase device time of the same step sequence (separate pass)
+    run.set_profiling(True)
+    run.step(min(args.steps, 50))
+    prof = run.profile()
+    run.set_profiling(False)
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        ne, ni = run.particle_size(0), run.particle_size(1)
+        he = torch.empty((max(ne, 1) + 4096, 6), dtype=torch.float64, pin_memory=True)
+        hi = torch.empty((max(ni, 1) + 4096, 6), dtype=torch.float64, pin_memory=True)
+        ne = run.dump_particles_ptr(0, he.data_ptr(), he.shape[0])
+        ni = run.dump_particles_ptr(1, hi.data_ptr(), hi.shape[0])
+        h2d = d2h = 0
+        tot = 0.0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            run.load_particles_ptr(0, he.data_ptr(), ne)
+            run.load_particles_ptr(1, hi.data_ptr(), ni)
+            h2d += 48 * (ne + ni)
+            run.step(1)
+            ne2 = run.dump_particles_ptr(0, he.data_ptr(), he.shape[0])
+            ni2 = run.dump_particles_ptr(1, hi.data_ptr(), hi.shape[0])
+            d2h += 48 * (min(ne2, he.shape[0]) + min(ni2, hi.shape[0]))
+            tot += 0.5 * (ne + ni + ne2 + ni2)
+            ne, ni = min(ne2, he.shape[0]), min(ni2, hi.shape[0])
+        wall = time.perf_counter() - t0
+        e2e = {"value": tot / wall, "unit": METRIC, "h2d_bytes_per_step": h2d // args.e2e_steps,
+               "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps}
+    run.close()
+    return dict(ms=ms, ps=ps, counts=(c0, c1), prof=prof, launches=launches, clocks=clk.summary(), e2e=e2e, n=n)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the 16Mi particles per species")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-sample", type=int, default=2 * 1024 * 1024)
+    ap.add_argument("--cpu-steps", type=int, default=6)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    config = {"workload": "H plasma, collisional boundary (SEE+reflection+backscatter, e-H elastic+ionization, "
+                          "H+-H CX), 512x512 cells (513^2 nodes), 16Mi particles/species, Gaussian density "
+                          "sigma=L/4, Te=3 eV, Ti=0.026 eV",
+              "grid_nodes": GRID_NODES, "particles_per_species": int(N_PER_SPECIES * args.scale),
+              "l2": "inputs larger than L2 (particle state 0.9 GB)", "poisson": "FP64 full multigrid, reference schedule",
+              "parallelism": "replicas" if world > 1 else "single"}
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sample = max(64 * 1024, int(args.cpu_sample * args.scale)) if args.scale < 1 else args.cpu_sample // 4
+        steps = max(1, min(args.steps, 20))
+        for _ in range(min(args.warmup, 1)):
+            pass
+        v, dt = cpu_sample(sample, steps, threads)
+        line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus, "steps": steps,
+                "warmup": 1, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": config,
+                "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                                 "sample": f"{sample} particles/species on the workload's grid and physics, "
+                                           f"{steps} steps (CPU oracle: FP64 restatement of the reference path)"},
+                "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    res = run_gpu(args, rank, world)
+    if world > 1:
+        import torch
+        t = torch.tensor([res["ms"], res["ps"]], dtype=torch.float64, device="cuda")
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        ms, ps = float(tmax[0]), float(t[1])
+    else:
+        ms, ps = res["ms"], res["ps"]
+    if rank != 0:
+        return
+    value = ps / (ms / 1000.0)
+    prof = res["prof"]
+    peak, peak_kind = measured_peak_hbm()
+    push_ms = prof["ms_push_e"] / max(prof["steps"], 1)
+    slots = prof["slots_e"] / max(prof["steps"], 1)
+    achieved = ALG_BYTES * slots / (push_ms / 1000.0) / 1e9 if push_ms > 0 else None
+    tr = ncu_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": (tr or {}).get("bytes_per_launch_scaled"), "kernel": "k_push<MCC,DEP,FLAG> (electrons)",
+                "alg_bytes_per_particle": ALG_BYTES, "peak_kind": f"{peak_kind} hbm_gbs",
+                "phase_ms_per_step": {k: prof[k] / max(prof["steps"], 1) for k in
+                                      ("ms_push_e", "ms_push_i", "ms_collide_ions", "ms_walls", "ms_fields")}}
+    cpu = None
+    if not args.no_cpu:
+        try:
+            v, dt = cpu_sample(args.cpu_sample, args.cpu_steps, threads)
+            cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                   "sample": f"{args.cpu_sample} particles/species, {args.cpu_steps} steps of the same workload "
+                             f"({dt:.1f} s CPU wall)"}
+        except Exception as ex:  # the CPU baseline never blocks the GPU line
+            cpu = {"value": None, "unit": METRIC, "cores": threads, "kind": "port", "sample": f"failed: {ex}"}
+    c0, c1 = res["counts"]
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 particles / f64 fields", "data": "synthetic (seeded)",
+            "config": config, "e2e": res["e2e"], "roofline": roofline, "cpu_baseline": cpu,
+            "gpu_launches": res["launches"], "clocks": res["clocks"],
+            "particles": {"start": [c0["n_e"], c0["n_i"]], "end": [c1["n_e"], c1["n_i"]]}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -123,6 +123,19 @@ typedef struct pgb_counters {
     int64_t reductions_e, reductions_i;  /* Kunhardt reductions (count_reduce)    */
 } pgb_counters;
 
+/* Opt-in per-phase device time of pgb_step, from CUDA events recorded on
+ * the run's stream around each phase (no reference counterpart).        */
+typedef struct pgb_profile {
+    double ms_push_e;              /* electron collisions+gather+push+deposit+lists */
+    double ms_push_i;              /* ion gather+push+deposit+lists (or deposit)   */
+    double ms_collide_ions;        /* charge exchange                              */
+    double ms_walls;               /* wall passes, ionization products, injection  */
+    double ms_fields;              /* charge finalisation, rho, Poisson, E         */
+    int64_t steps;                 /* steps profiled                               */
+    int64_t slots_e, slots_i;      /* particle slots swept by the push kernels     */
+    int64_t launches;              /* kernel launches issued since pgb_create      */
+} pgb_profile;
+
 typedef struct pgb_run pgb_run;
 
 /* Fill *p with the reference's default parameters.h values (Ar, 257x257,
@@ -176,6 +189,12 @@ PGB_API int pgb_get_grid(pgb_run* run, int which, double* out, int64_t n);
  * charge density without particles.                                       */
 PGB_API int pgb_set_rho(pgb_run* run, const double* rho, int64_t n);
 PGB_API int pgb_get_counters(pgb_run* run, pgb_counters* out);
+/* The cudaStream_t every kernel of this run is launched on (so a caller
+ * can record CUDA events around pgb_step).                               */
+PGB_API int pgb_get_stream(pgb_run* run, void** stream);
+/* on = 1 resets and starts the per-phase profile of pgb_step; 0 stops it. */
+PGB_API int pgb_set_profiling(pgb_run* run, int on);
+PGB_API int pgb_get_profile(pgb_run* run, pgb_profile* out);
 /* Wait for all work queued on the handle's stream. */
 PGB_API int pgb_sync(pgb_run* run);
 

@@ -5,7 +5,11 @@ removal order (oracle/picport.h), so random events are drawn from the same
 numbers on both sides and only floating-point precision differs (FP32
 particles on the GPU, FP64 in the oracle).  Tolerances, all stated below:
   fields from the same rho ........ bit-identical (FP64 multigrid, same schedule)
-  charge, rho, phi, E after steps . max|d| <= 1e-5 * max|ref|
+  charge, rho, phi, E after steps . max|d| <= 1e-5 * max|ref| at >= 16 particles
+                                    per cell; 1e-4 in the sparse fixtures (< 1 per
+                                    cell), where a node's charge is one particle's
+                                    and FP32 position rounding (2^-24 x/DX per
+                                    step) is not averaged out
   particle positions .............. |d| <= 2e-4 cell;  velocities |d| <= 1e-4 * vt
   particle and event counts ....... exact, except events decided by an FP32
                                     vs FP64 tie (counted and bounded)
@@ -162,9 +166,33 @@ def test_step_matches_oracle_deterministic_physics(case):
         assert cr[k] == co[k], f"{k}: gpu {cr[k]} oracle {co[k]}"
     compare_particles(r.get_particles(0), o.get_particles(0), p, "electrons", vt=p.vte)
     compare_particles(r.get_particles(1), o.get_particles(1), p, "ions", vt=p.vti)
-    for grid in ("q_e", "q_i", "rho", "phi", "ex", "ey"):
-        e = rel_err(r.get_grid(grid), o.get_grid(grid))
+    errs = {grid: rel_err(r.get_grid(grid), o.get_grid(grid)) for grid in ("q_e", "q_i", "rho", "phi", "ex", "ey")}
+    print(case, {k: f"{v:.2e}" for k, v in errs.items()})
+    for grid, e in errs.items():
+        assert e <= 1e-4, f"{grid}: {e:.3g}"
+    r.close()
+
+
+def test_dense_plasma_fields_within_1e5():
+    """At PIC densities (64 particles per cell) the FP32 particle path keeps
+    q, rho, phi and E within 1e-5 of the FP64 oracle after several steps."""
+    p = picgb.make_params(X_NO_OF_CELLS=33, STEADYSTATE="NO", RAND_SEED=3)
+    rng = np.random.default_rng(5)
+    n = 64 * 32 * 32
+    L = p.xlength
+    st = []
+    for m, T in ((picgb.ELECTRON_MASS, 2.0), (p.ion_mass, 0.5)):
+        x = rng.uniform(0.05 * L, 0.95 * L, n)
+        y = rng.uniform(0.05 * L, 0.95 * L, n)
+        v = rng.normal(0, np.sqrt(T * picgb.CHARGE / m), (n, 3))
+        st.append(np.column_stack([x, y, v, np.ones(n)]))
+    g = {"p": p, "e_in": st[0], "i_in": st[1], "nsteps": 5}
+    o, r = run_pair(g)
+    errs = {grid: rel_err(r.get_grid(grid), o.get_grid(grid)) for grid in ("q_e", "q_i", "rho", "phi", "ex", "ey")}
+    print("dense", {k: f"{v:.2e}" for k, v in errs.items()})
+    for grid, e in errs.items():
         assert e <= 1e-5, f"{grid}: {e:.3g}"
+    assert r.counters()["n_e"] == o.counters()["n_e"]
     r.close()
 
 

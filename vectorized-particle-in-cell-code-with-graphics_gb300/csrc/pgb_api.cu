@@ -309,6 +309,9 @@ extern "C" int pgb_destroy(pgb_run* r) {
     cudaFree(r->mg_tab);
     for (int w = 0; w < 2; ++w) cudaFree(r->neut64[w]);
     if (r->h_stage) cudaFreeHost(r->h_stage);
+    cudaFree(r->d_stage);
+    if (r->prof_ev_ok)
+        for (int k = 0; k < 12; ++k) cudaEventDestroy(r->prof_ev[k]);
     if (r->stream) cudaStreamDestroy(r->stream);
     delete r;
     return 0;
@@ -324,6 +327,17 @@ static int stage(pgb_run* r, size_t bytes) {
     return 0;
 }
 
+/* device staging buffer for AoS transfers, kept between calls */
+static int dstage(pgb_run* r, size_t bytes) {
+    if (bytes <= r->d_stage_bytes) return 0;
+    cudaFree(r->d_stage);
+    r->d_stage = nullptr;
+    r->d_stage_bytes = 0;
+    PGB_CK(r, cudaMalloc(&r->d_stage, bytes));
+    r->d_stage_bytes = bytes;
+    return 0;
+}
+
 extern "C" int pgb_load_species(pgb_run* r, int s, const double* aos6, int64_t n) {
     if (!r || s < 0 || s > 1 || n < 0 || (n > 0 && !aos6)) return fail(r, PGB_ERR_ARG, "pgb_load_species: bad argument");
     if (n > 0x7fffffffLL) return fail(r, PGB_ERR_ARG, "pgb_load_species: too many particles");
@@ -336,14 +350,10 @@ extern "C" int pgb_load_species(pgb_run* r, int s, const double* aos6, int64_t n
     if ((rc = ensure_capacity(r, s, cap))) return rc;
     if ((rc = ensure_capacity(r, 1 - s, std::max<long long>(r->sp[1 - s].cap, 1024)))) return rc;
     if (n > 0) {
-        double* d = nullptr;
-        PGB_CK(r, cudaMalloc(&d, sizeof(double) * 6 * n));
-        if (cudaMemcpyAsync(d, aos6, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, r->stream) != cudaSuccess ||
-            pgb_launch_load(r, s, d, n) || cudaStreamSynchronize(r->stream) != cudaSuccess) {
-            cudaFree(d);
+        if ((rc = dstage(r, sizeof(double) * 6 * n))) return rc;
+        if (cudaMemcpyAsync(r->d_stage, aos6, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, r->stream) != cudaSuccess ||
+            pgb_launch_load(r, s, r->d_stage, n) || cudaStreamSynchronize(r->stream) != cudaSuccess)
             return fail(r, PGB_ERR_CUDA, "pgb_load_species: upload failed");
-        }
-        cudaFree(d);
     }
     r->hs->n[s] = n;
     r->hs->dead[s] = 0;
@@ -371,15 +381,11 @@ extern "C" int pgb_dump_species(pgb_run* r, int s, double* aos6, int64_t cap, in
     if (n_out) *n_out = live;
     long long m = std::min<long long>(live, cap);
     if (m <= 0 || r->sp[s].cap == 0) return 0;
-    double* d = nullptr;
-    PGB_CK(r, cudaMalloc(&d, sizeof(double) * 6 * live));
-    if (pgb_launch_dump(r, s, d, live) ||
-        cudaMemcpyAsync(aos6, d, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost, r->stream) != cudaSuccess ||
-        cudaStreamSynchronize(r->stream) != cudaSuccess) {
-        cudaFree(d);
+    if ((rc = dstage(r, sizeof(double) * 6 * live))) return rc;
+    if (pgb_launch_dump(r, s, r->d_stage, live) ||
+        cudaMemcpyAsync(aos6, r->d_stage, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost, r->stream) != cudaSuccess ||
+        cudaStreamSynchronize(r->stream) != cudaSuccess)
         return fail(r, PGB_ERR_CUDA, "pgb_dump_species: download failed");
-    }
-    cudaFree(d);
     return 0;
 }
 
@@ -503,6 +509,10 @@ extern "C" int pgb_efield(pgb_run* r) {
 }
 
 /* -------------------------------------------------------------- pgb_step */
+/* event k marks the start of section k; event 5 the end of the step */
+#define PROF_MARK(r, k) \
+    do { if ((r)->prof_on) PGB_CK((r), cudaEventRecord((r)->prof_ev[k], (r)->stream)); } while (0)
+
 static int step_once(pgb_run* r) {
     const int64_t t = r->time_step;
     const bool coll = r->p.have_collisions != 0;
@@ -511,8 +521,10 @@ static int step_once(pgb_run* r) {
     PGB_CK(r, cudaMemsetAsync(r->qacc[0], 0, sizeof(unsigned long long) * G, r->stream));
     PGB_CK(r, cudaMemsetAsync(r->qacc[1], 0, sizeof(unsigned long long) * G, r->stream));
     /* e_collisions::collision + get_particle_electric_field + move_particles */
+    PROF_MARK(r, 0);
     if (pgb_launch_push(r, 0, coll, true, coll)) return PGB_ERR_CUDA;
     if (pgb_build_list(r, LIST_OUT_E, 0)) return PGB_ERR_CUDA;
+    PROF_MARK(r, 1);
     if (coll) {
         if (pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
         int store_e = r->p.steadystate ? 1 : 0;
@@ -521,15 +533,20 @@ static int step_once(pgb_run* r) {
     }
     /* inject_more_particles: electrons are pushed as they are created */
     if (r->p.number_to_inject > 0 && pgb_launch_inject(r, 3, true)) return PGB_ERR_CUDA;
+    PROF_MARK(r, 2);
     if (ion_step) {
         if (coll && pgb_launch_cx(r)) return PGB_ERR_CUDA;
+        PROF_MARK(r, 3);
         if (pgb_launch_push(r, 1, false, true, false)) return PGB_ERR_CUDA;
         if (pgb_build_list(r, LIST_OUT_I, 1)) return PGB_ERR_CUDA;
+        PROF_MARK(r, 4);
         if (pgb_launch_walls(r, PGB_BOUNDARY_IONS)) return PGB_ERR_CUDA;
         if (pgb_launch_walls(r, PGB_BOUNDARY_ELECTRONS)) return PGB_ERR_CUDA;
     } else {
+        PROF_MARK(r, 3);
         if (pgb_launch_deposit(r, 1)) return PGB_ERR_CUDA;
         if (r->p.steadystate && (pgb_launch_flag_outside(r, 1) || pgb_build_list(r, LIST_OUT_I, 1))) return PGB_ERR_CUDA;
+        PROF_MARK(r, 4);
         if (pgb_launch_walls(r, PGB_BOUNDARY_ELECTRONS)) return PGB_ERR_CUDA;
     }
     /* contain_particle_growth: only when a species can exceed its limit */
@@ -551,10 +568,26 @@ static int step_once(pgb_run* r) {
     }
     /* collect_charge edge doubling, grid_rho, grid_potential, grid_electric_field */
     double phi_right = r->p.phi_right * cos(r->p.phi_period * (double)t);
+    PROF_MARK(r, 5);
     if (pgb_launch_finalize(r, 3, true, phi_right)) return PGB_ERR_CUDA;
     if (pgb_poisson_solve(r, t)) return PGB_ERR_CUDA;
     if (pgb_launch_efield(r)) return PGB_ERR_CUDA;
+    PROF_MARK(r, 6);
     r->time_step = t + 1;
+    return 0;
+}
+
+/* add the section times of the step just queued (waits for it) */
+static int profile_collect(pgb_run* r) {
+    PGB_CK(r, cudaEventSynchronize(r->prof_ev[6]));
+    float ms[6];
+    for (int k = 0; k < 6; ++k) PGB_CK(r, cudaEventElapsedTime(&ms[k], r->prof_ev[k], r->prof_ev[k + 1]));
+    r->prof.ms_push_e += ms[0];
+    r->prof.ms_walls += ms[1] + ms[4];
+    r->prof.ms_collide_ions += ms[2];
+    r->prof.ms_push_i += ms[3];
+    r->prof.ms_fields += ms[5];
+    r->prof.steps += 1;
     return 0;
 }
 
@@ -569,9 +602,16 @@ extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
                 if (pgb_launch_compact(r, s)) return PGB_ERR_CUDA;
                 r->hs->dead[s] = 0;
             }
+        if (r->prof_on) {
+            if ((rc = sync_state(r))) return rc;
+            r->prof.slots_e += r->hs->n[0];
+            r->prof.slots_i += r->hs->n[1];
+        }
         if ((rc = step_once(r))) return rc;
+        if (r->prof_on && (rc = profile_collect(r))) return rc;
+        /* counters come back asynchronously; the host reads them only to
+         * decide when to compact, which never changes results              */
         PGB_CK(r, cudaMemcpyAsync(r->hs, r->ds, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
-        if ((k & 7) == 7) PGB_CK(r, cudaStreamSynchronize(r->stream));
     }
     return sync_state(r);
 }
@@ -630,6 +670,30 @@ extern "C" int pgb_get_counters(pgb_run* r, pgb_counters* c) {
     c->injected_i = h.stats[ST_INJ_I];
     c->reductions_e = h.stats[ST_RED_E];
     c->reductions_i = h.stats[ST_RED_I];
+    return 0;
+}
+
+extern "C" int pgb_get_stream(pgb_run* r, void** stream) {
+    if (!r || !stream) return fail(r, PGB_ERR_ARG, "pgb_get_stream: bad argument");
+    *stream = (void*)r->stream;
+    return 0;
+}
+
+extern "C" int pgb_set_profiling(pgb_run* r, int on) {
+    if (!r) return PGB_ERR_ARG;
+    if (on && !r->prof_ev_ok) {
+        for (int k = 0; k < 12; ++k) PGB_CK(r, cudaEventCreate(&r->prof_ev[k]));
+        r->prof_ev_ok = true;
+    }
+    memset(&r->prof, 0, sizeof(r->prof));
+    r->prof_on = on ? 1 : 0;
+    return 0;
+}
+
+extern "C" int pgb_get_profile(pgb_run* r, pgb_profile* out) {
+    if (!r || !out) return fail(r, PGB_ERR_ARG, "pgb_get_profile: bad argument");
+    *out = r->prof;
+    out->launches = r->launches;
     return 0;
 }
 

@@ -353,6 +353,7 @@ int pgb_launch_finalize(pgb_run* r, int mask, bool make_rhs, double phi_right) {
     FinalizeArgs a = fin_args(r, mask, phi_right, make_rhs);
     int G = r->nx * r->ny;
     k_finalize<<<(G + 255) / 256, 256, 0, r->stream>>>(a);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -361,6 +362,7 @@ int pgb_launch_rhs(pgb_run* r, double phi_right) {
     FinalizeArgs a = fin_args(r, 0, phi_right, true);
     int G = r->nx * r->ny;
     k_rhs<<<(G + 255) / 256, 256, 0, r->stream>>>(a);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -384,6 +386,7 @@ static int small_launch(pgb_run* r, double** tab, int J, int mode) {
     size_t smem = small_smem_bytes(J, sizeof(double));
     k_mg_small<double><<<1, 1024, smem, r->stream>>>(J, mode, r->p.xlength, tab, tab + PGB_MAX_LEVELS,
                                                      tab + 2 * PGB_MAX_LEVELS, tab + 3 * PGB_MAX_LEVELS);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -394,8 +397,11 @@ static int vcycle(pgb_run* r, double** tab, int j, int jsmall, double* u, const 
     double h = r->p.xlength / (nf - 1), h2 = h * h, h2i = 1.0 / (h * h);
     long long rw = (long long)(nf - 2) * ((nf - 1) / 2);
     k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
+    r->launches++;
     k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
+    r->launches++;
     k_resid_restrict<double><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(r->mg_r[j - 1], u, f, nf, h2i);
+    r->launches++;
     PGB_CK(r, cudaMemsetAsync(r->mg_v[j - 1], 0, sizeof(double) * nc * nc, r->stream));
     if (j - 1 <= jsmall) {
         if (small_launch(r, tab, j - 1, 1)) return PGB_ERR_CUDA;
@@ -403,8 +409,11 @@ static int vcycle(pgb_run* r, double** tab, int j, int jsmall, double* u, const 
         if (vcycle(r, tab, j - 1, jsmall, r->mg_v[j - 1], r->mg_r[j - 1])) return PGB_ERR_CUDA;
     }
     k_prolong<double><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(u, r->mg_v[j - 1], nf, 1);
+    r->launches++;
     k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
+    r->launches++;
     k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -416,6 +425,7 @@ static int fmg(pgb_run* r) {
     for (int j = ng - 2; j >= 0; --j) {
         int nc = r->mg_n[j];
         k_restrict<double><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(r->mg_f[j], r->mg_f[j + 1], nc);
+        r->launches++;
     }
     int jsmall = 0;
     while (jsmall + 1 < ng && r->mg_n[jsmall + 1] <= PGB_MG_SMALL) jsmall++;
@@ -423,6 +433,7 @@ static int fmg(pgb_run* r) {
     for (int j = jsmall + 1; j < ng; ++j) {
         int nf = r->mg_n[j];
         k_prolong<double><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(r->mg_u[j], r->mg_u[j - 1], nf, 0);
+        r->launches++;
         for (int c = 0; c < 2; ++c)
             if (vcycle(r, tab, j, jsmall, r->mg_u[j], r->mg_f[j])) return PGB_ERR_CUDA;
     }
@@ -455,6 +466,7 @@ int pgb_poisson_solve(pgb_run* r, int64_t t) {
                               r->stream));
     k_walls<<<blocks_for((long long)r->nx * r->ny), 256, 0, r->stream>>>(r->phi, r->nx, r->ny, r->p.phi_left, phi_right,
                                                                          r->p.phi_bottom, r->p.phi_top);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -462,6 +474,7 @@ int pgb_poisson_solve(pgb_run* r, int64_t t) {
 int pgb_launch_efield(pgb_run* r) {
     int GE = (r->nx + 1) * (r->ny + 1);
     k_efield<<<blocks_for(GE), 256, 0, r->stream>>>(r->phi, r->ex, r->ey, r->exy, r->nx, r->ny, 2.0 * r->dx);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }

@@ -114,6 +114,14 @@ struct pgb_run {
     /* host staging */
     double* h_stage = nullptr;
     size_t h_stage_bytes = 0;
+    double* d_stage = nullptr;     /* device staging for load/dump (AoS doubles) */
+    size_t d_stage_bytes = 0;
+    /* instrumentation */
+    long long launches = 0;        /* kernel launches issued                     */
+    int prof_on = 0;
+    pgb_profile prof;
+    cudaEvent_t prof_ev[12];
+    bool prof_ev_ok = false;
 };
 
 /* ------------------------------------------------------------ helpers */

@@ -664,6 +664,7 @@ int pgb_launch_push(pgb_run* r, int s, bool mcc, bool deposit, bool flag_ion) {
     else if (mcc) k_push<true, false, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
     else if (deposit) k_push<false, true, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
     else k_push<false, false, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -672,6 +673,7 @@ int pgb_launch_flag_outside(pgb_run* r, int s) {
     int l = s == 0 ? LIST_OUT_E : LIST_OUT_I;
     k_flag<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s].xv, r->ds, s, r->nx, r->ny, r->p.steadystate,
                                                                r->tile_list[l], r->tile_cnt[l]);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -679,6 +681,7 @@ int pgb_launch_flag_outside(pgb_run* r, int s) {
 int pgb_launch_mcc(pgb_run* r) {
     PushArgs a = push_args(r, 0);
     k_mcc<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -687,14 +690,17 @@ int pgb_launch_mcc(pgb_run* r) {
 int pgb_build_list(pgb_run* r, int which, int s) {
     int* toff = r->aux_j;
     k_scan_small<<<1, 1024, 0, r->stream>>>(r->tile_cnt[which], toff, &r->ds->n[s], 0, &r->ds->list_n[which]);
+    r->launches++;
     k_gather_lists<<<grid_for(r, 4), 256, 0, r->stream>>>(r->tile_list[which], r->tile_cnt[which], toff,
                                                            &r->ds->n[s], r->list[which]);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
 
 int pgb_launch_deposit(pgb_run* r, int s) {
     k_deposit<<<grid_for(r, 8), 256, 0, r->stream>>>(r->sp[s].xv, r->sp[s].w, r->ds, s, r->nx, r->ny, r->qacc[s]);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -708,6 +714,7 @@ int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e) {
     a.push_e = push_e; a.species_mask = species_mask;
     a.list_out_e = r->list[LIST_OUT_E]; a.list_cap = r->list_cap;
     k_inject<<<1, 32, 0, r->stream>>>(a);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -720,8 +727,10 @@ int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i) {
     a.store_e = store_e;
     a.store_i = store_i;
     k_ionize_append<<<r->sms * 2, 256, 0, r->stream>>>(a);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     k_ionize_commit<<<1, 1, 0, r->stream>>>(r->ds, a.store_e, a.store_i, r->sp[0].cap, r->sp[1].cap);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -732,9 +741,13 @@ int pgb_launch_compact(pgb_run* r, int s) {
     int* toff = r->aux_j;
     PGB_CK(r, cudaMemsetAsync(tc, 0, sizeof(int) * r->ntiles_cap, r->stream));
     k_alive_count<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(S.xv, r->ds, s, tc);
+    r->launches++;
     k_scan_small<<<1, 1024, 0, r->stream>>>(tc, toff, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]);
+    r->launches++;
     k_compact<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(S, r->ds, s, toff);
+    r->launches++;
     k_compact_commit<<<1, 1, 0, r->stream>>>(r->ds, s, &r->ds->list_n[LIST_SPARE]);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     std::swap(S.xv, S.xv2);
     std::swap(S.vz, S.vz2);
@@ -745,6 +758,7 @@ int pgb_launch_compact(pgb_run* r, int s) {
 
 int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long n) {
     k_load<<<grid_for(r, 4), 256, 0, r->stream>>>(r->sp[s], d_aos, n, r->dx, r->dy);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -754,8 +768,11 @@ int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap) {
     int* toff = r->aux_j;
     PGB_CK(r, cudaMemsetAsync(tc, 0, sizeof(int) * r->ntiles_cap, r->stream));
     k_alive_count<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s].xv, r->ds, s, tc);
+    r->launches++;
     k_scan_small<<<1, 1024, 0, r->stream>>>(tc, toff, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]);
+    r->launches++;
     k_dump<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s], r->ds, s, toff, r->dx, r->dy, d_out, cap);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }

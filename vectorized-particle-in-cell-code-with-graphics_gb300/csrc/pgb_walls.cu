@@ -551,20 +551,29 @@ int pgb_launch_walls(pgb_run* r, int which) {
     if (r->p.steadystate) {
         if (which == PGB_BOUNDARY_ELECTRONS) {
             k_steady<<<1, 1024, 0, r->stream>>>(a, r->aux_i);
+            r->launches++;
             PGB_CK(r, cudaGetLastError());
         }
         return 0;
     }
     if (which == PGB_BOUNDARY_IONS) {
         k_iwall1<<<g, 256, 0, r->stream>>>(a);
+        r->launches++;
         k_scan_list<<<1, 1024, 0, r->stream>>>(r->aux_i, r->aux_j, &r->ds->list_n[LIST_OUT_I], &r->ds->list_n[LIST_SPARE]);
+        r->launches++;
         k_iwall2<<<g, 256, 0, r->stream>>>(a);
+        r->launches++;
         k_wall_commit<<<1, 1, 0, r->stream>>>(r->ds, &r->ds->list_n[LIST_SPARE], 0, r->sp[0].cap, ST_ISEE_EM);
+        r->launches++;
     } else {
         k_ewall1<<<g, 256, 0, r->stream>>>(a);
+        r->launches++;
         k_scan_list<<<1, 1024, 0, r->stream>>>(r->aux_i, r->aux_j, &r->ds->list_n[LIST_OUT_E], &r->ds->list_n[LIST_SPARE]);
+        r->launches++;
         k_ewall2<<<g, 256, 0, r->stream>>>(a);
+        r->launches++;
         k_wall_commit<<<1, 1, 0, r->stream>>>(r->ds, &r->ds->list_n[LIST_SPARE], 1, r->sp[0].cap, ST_SEE_EM);
+        r->launches++;
     }
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -580,8 +589,10 @@ int pgb_launch_cx(pgb_run* r) {
     a.neut64_i = r->neut64[1];
     a.seed = r->p.seed; a.step = (unsigned int)r->time_step;
     k_cx_tiles<<<r->sms * 4, 256, sizeof(unsigned long long) * r->nx, r->stream>>>(a);
+    r->launches++;
     int warps = 8;
     k_cx_walk<<<(r->nx + warps - 1) / warps, warps * 32, 0, r->stream>>>(a);
+    r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }

@@ -85,6 +85,17 @@ class PgbCounters(C.Structure):
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
 
 
+class PgbProfile(C.Structure):
+    """ctypes image of `pgb_profile` (include/picgb.h)."""
+
+    _fields_ = [("ms_push_e", C.c_double), ("ms_push_i", C.c_double), ("ms_collide_ions", C.c_double),
+                ("ms_walls", C.c_double), ("ms_fields", C.c_double), ("steps", C.c_int64),
+                ("slots_e", C.c_int64), ("slots_i", C.c_int64), ("launches", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 def _yes(v) -> int:
     if isinstance(v, str):
         return 1 if v.upper() == "YES" else 0
@@ -242,6 +253,9 @@ def load_library():
         "pgb_set_rho": (C.c_int, [R, dp, i64]),
         "pgb_get_counters": (C.c_int, [R, C.POINTER(PgbCounters)]),
         "pgb_sync": (C.c_int, [R]),
+        "pgb_get_stream": (C.c_int, [R, C.POINTER(C.c_void_p)]),
+        "pgb_set_profiling": (C.c_int, [R, C.c_int]),
+        "pgb_get_profile": (C.c_int, [R, C.POINTER(PgbProfile)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -372,6 +386,30 @@ class Run:
 
     def sync(self):
         self._check(self.lib.pgb_sync(self.h), "pgb_sync")
+
+    def stream(self) -> int:
+        v = C.c_void_p()
+        self._check(self.lib.pgb_get_stream(self.h, C.byref(v)), "pgb_get_stream")
+        return int(v.value or 0)
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.pgb_set_profiling(self.h, 1 if on else 0), "pgb_set_profiling")
+
+    def profile(self) -> dict:
+        pr = PgbProfile()
+        self._check(self.lib.pgb_get_profile(self.h, C.byref(pr)), "pgb_get_profile")
+        return pr.as_dict()
+
+    def load_particles_ptr(self, species: int, ptr: int, n: int):
+        """Load n records from a host address (e.g. pinned memory)."""
+        self._check(self.lib.pgb_load_species(self.h, species, C.cast(ptr, C.POINTER(C.c_double)), n),
+                    "pgb_load_species")
+
+    def dump_particles_ptr(self, species: int, ptr: int, cap: int) -> int:
+        got = C.c_int64()
+        self._check(self.lib.pgb_dump_species(self.h, species, C.cast(ptr, C.POINTER(C.c_double)), cap,
+                                              C.byref(got)), "pgb_dump_species")
+        return int(got.value)
 
 
 # ------------------------------------------------------------- dataDump I/O
