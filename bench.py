@@ -46,12 +46,19 @@ ALG_BYTES = 48          # per particle-step: read x,y,vx,vy,vz,w,id (28 B) + wri
 METRIC = "particle-steps/s"
 
 
-def workload_params(picgb, seed=1003):
-    return picgb.make_params(
-        X_NO_OF_CELLS=GRID_NODES, TEMPERATURE=3.0, ION_MASS_AMU=1.0, THRESHOLD=13.6, SPECIES="HYDROGEN",
-        HAVE_COLLISIONS=True, SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT",
-        SIGMA_IONIZATION="ENERGY_DEPENDENT", E_IMPACT_SEE="YES", ION_IMPACT_SEE="NO", REFLECTION="YES",
-        BACKSCATTER="YES", STEADYSTATE="NO", NUMBER_TO_INJECT=10, SIZE_TO_CHECK=2**31 - 1, RAND_SEED=seed)
+def workload_params(picgb, seed=1003, n_per_species=N_PER_SPECIES, poisson="FMG32"):
+    """H preset ("H with coll-boundary") at 513^2 nodes and Te = 3 eV.  The
+    macro-particle size is set so that the mean density equals the design
+    density ELECTRON_PARTICLE_DENSITY = 1e15 m^-3 (parameters.h:71) for
+    n_per_species particles, as INIT_PARTICLE_NO x 1e6 does in the preset."""
+    kw = dict(X_NO_OF_CELLS=GRID_NODES, TEMPERATURE=3.0, ION_MASS_AMU=1.0, THRESHOLD=13.6, SPECIES="HYDROGEN",
+              HAVE_COLLISIONS=True, SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT",
+              SIGMA_IONIZATION="ENERGY_DEPENDENT", E_IMPACT_SEE="YES", ION_IMPACT_SEE="NO", REFLECTION="YES",
+              BACKSCATTER="YES", STEADYSTATE="NO", NUMBER_TO_INJECT=10, SIZE_TO_CHECK=2**31 - 1, RAND_SEED=seed,
+              POISSON=poisson)
+    L = picgb.make_params(**kw).xlength
+    size = 1.0e15 * L * L / n_per_species
+    return picgb.make_params(E_MACROPARTICLE_SIZE=size, ION_MACROPARTICLE_SIZE=size, **kw)
 
 
 def gaussian_state(p, n, te, ti, seed, ion_mass):
@@ -148,7 +155,7 @@ def cpu_sample(n_per_species, steps, threads):
     import orc
     import picgb
     orc.build_port()
-    p = workload_params(picgb)
+    p = workload_params(picgb, n_per_species=n_per_species, poisson="FMG_REF")
     e, i = gaussian_state(p, n_per_species, 3.0, 0.026, 1003, p.ion_mass)
     o = orc.Oracle(p, threads=threads)
     o.load_particles(0, e)
@@ -171,8 +178,8 @@ def run_gpu(args, rank, world):
     import build_lib
     build_lib.build()
     torch.cuda.set_device(rank % max(torch.cuda.device_count(), 1))
-    p = workload_params(picgb, seed=1003 + rank)
     n = int(N_PER_SPECIES * args.scale)
+    p = workload_params(picgb, seed=1003 + rank, n_per_species=n, poisson=args.poisson)
     e, i = gaussian_state(p, n, 3.0, 0.026, 1003 + rank, p.ion_mass)
     run = picgb.Run(p)
     run.load_particles(0, e)
@@ -242,6 +249,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=2 * 1024 * 1024)
     ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--poisson", default="FMG32", choices=["FMG32", "FMG_REF", "FP32_DC"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -250,7 +258,11 @@ def main():
                           "H+-H CX), 512x512 cells (513^2 nodes), 16Mi particles/species, Gaussian density "
                           "sigma=L/4, Te=3 eV, Ti=0.026 eV",
               "grid_nodes": GRID_NODES, "particles_per_species": int(N_PER_SPECIES * args.scale),
-              "l2": "inputs larger than L2 (particle state 0.9 GB)", "poisson": "FP64 full multigrid, reference schedule",
+              "l2": "inputs larger than L2 (particle state 0.9 GB)",
+              "poisson": {"FMG32": "full multigrid, reference schedule, FP32",
+                          "FMG_REF": "full multigrid, reference schedule, FP64 (bit-identical)",
+                          "FP32_DC": "FP32 full multigrid + FP64 defect correction"}[args.poisson],
+              "macro_particle_size": "mean density 1e15 m^-3",
               "parallelism": "replicas" if world > 1 else "single"}
     threads = os.cpu_count() or 1
     if args.impl == "reference":

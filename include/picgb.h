@@ -49,10 +49,12 @@ enum { PGB_ARGON = 0, PGB_HYDROGEN = 1 };                 /* SPECIES            
 enum { PGB_SIGMA_CONSTANT = 0, PGB_SIGMA_ENERGY_DEPENDENT = 1 };
 enum { PGB_GRID_Q_E = 0, PGB_GRID_Q_I = 1, PGB_GRID_RHO = 2, PGB_GRID_PHI = 3,
        PGB_GRID_EX = 4, PGB_GRID_EY = 5 };
-/* Poisson solver: the reference's one-pass full multigrid (mglin.cpp:21-196)
- * in FP64 with the same schedule, or FP32 full multigrid wrapped in an FP64
- * defect-correction loop that converges to the exact discrete solution.     */
-enum { PGB_POISSON_FMG_REF = 0, PGB_POISSON_FP32_DC = 1 };
+/* Poisson solver.  FMG_REF: the reference's one-pass full multigrid
+ * (mglin.cpp:21-196) in FP64 with the same schedule -- bit-identical to the
+ * reference for the same rho.  FMG32: the same schedule in FP32.  FP32_DC:
+ * FP32 full multigrid inside an FP64 defect-correction loop, which converges
+ * to the exact discrete solution (dc_max_iters passes).                    */
+enum { PGB_POISSON_FMG_REF = 0, PGB_POISSON_FP32_DC = 1, PGB_POISSON_FMG32 = 2 };
 /* boundary selector for pgb_boundary(): the two member-function pointers
  * implement_i_boundary / implement_e_boundary (boundary.h:372-383)          */
 enum { PGB_BOUNDARY_IONS = 0, PGB_BOUNDARY_ELECTRONS = 1 };

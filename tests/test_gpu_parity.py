@@ -270,3 +270,44 @@ def test_phase_entry_points_equal_fused_step():
             assert np.array_equal(a.get_particles(s), b.get_particles(s), equal_nan=True)
         for grid in ("q_e", "q_i", "phi", "ex"):
             assert rel_err(a.get_grid(grid), b.get_grid(grid)) <= 1e-12, grid
+
+
+# ------------------------------------------------------------ solver modes
+@pytest.mark.parametrize("n", [129, 513])
+def test_fmg32_within_1e5_of_reference_schedule(n):
+    """FMG32 runs the reference's schedule in FP32: phi within 1e-5 of the
+    FP64 result (max norm relative to max |phi|)."""
+    rng = np.random.default_rng(n + 1)
+    s = np.linspace(0, 1, n)
+    X, Y = np.meshgrid(s, s)
+    rho = 1e-6 * np.exp(-((X - 0.5) ** 2 + (Y - 0.5) ** 2) / 0.06) + 2e-8 * rng.standard_normal((n, n))
+    out = {}
+    for mode in ("FMG_REF", "FMG32"):
+        p = picgb.make_params(X_NO_OF_CELLS=n, POISSON=mode, PHI_RIGHT=1.0)
+        with picgb.Run(p) as r:
+            r.set_rho(rho)
+            r.poisson(0)
+            r.efield()
+            out[mode] = (r.get_grid("phi"), r.get_grid("ex"))
+    e_phi = rel_err(out["FMG32"][0], out["FMG_REF"][0])
+    e_ex = rel_err(out["FMG32"][1], out["FMG_REF"][1])
+    print(n, "phi", e_phi, "ex", e_ex)
+    assert e_phi <= 1e-5 and e_ex <= 1e-4
+
+
+@pytest.mark.parametrize("n", [65, 257])
+def test_defect_correction_converges_to_exact_solution(n):
+    """FP32_DC: FP32 multigrid in an FP64 defect-correction loop reaches the
+    FP64 converged discrete solution (oracle: 30 FP64 corrections)."""
+    rng = np.random.default_rng(n + 2)
+    rho = 1e-6 * rng.standard_normal((n, n))
+    p = picgb.make_params(X_NO_OF_CELLS=n, POISSON="FP32_DC", DC_MAX_ITERS=8)
+    o = orc.Oracle(p)
+    o.set_rho(rho)
+    o.poisson_converged(0, 30)
+    with picgb.Run(p) as r:
+        r.set_rho(rho)
+        r.poisson(0)
+        e = rel_err(r.get_grid("phi"), o.get_grid("phi"))
+    print(n, "dc err", e)
+    assert e <= 1e-9

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <new>
 #include <string>
+#include <vector>
 #include "pgb_internal.h"
 #include "pgb_physics.cuh"
 #include "pgb_rng.h"
@@ -147,8 +148,11 @@ static void free_lists(pgb_run* r) {
 }
 
 /* grow particle storage (keeps contents) and the capacity-sized scratch */
+static void drop_graphs(pgb_run* r);
+
 static int ensure_capacity(pgb_run* r, int s, long long need) {
     Species& S = r->sp[s];
+    if (need > S.cap || std::max(r->sp[0].cap, r->sp[1].cap) > r->list_cap) drop_graphs(r);
     if (need > S.cap) {
         long long cap = std::max<long long>(need, 1024);
         Species T = S;
@@ -170,6 +174,7 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
         }
         free_species(S);
         S = T;
+        r->orient[s] = 0;
     }
     long long lc = std::max(r->sp[0].cap, r->sp[1].cap);
     if (lc > r->list_cap) {
@@ -253,6 +258,8 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
     ok = ok && cudaMalloc(&r->ey, sizeof(double) * GE) == cudaSuccess;
     ok = ok && cudaMalloc(&r->exy, sizeof(float2) * GE) == cudaSuccess;
     ok = ok && cudaMalloc(&r->prob_cx, sizeof(long long) * r->nx) == cudaSuccess;
+    r->phi_tab_cap = 4096;
+    ok = ok && cudaMalloc(&r->phi_tab, sizeof(double) * r->phi_tab_cap) == cudaSuccess;
     int ng = 0, nn = r->nx;
     while (nn >>= 1) ng++;
     r->ng = ng;
@@ -297,6 +304,8 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
 extern "C" int pgb_destroy(pgb_run* r) {
     if (!r) return 0;
     if (r->stream) cudaStreamSynchronize(r->stream);
+    drop_graphs(r);
+    cudaFree(r->phi_tab);
     free_species(r->sp[0]);
     free_species(r->sp[1]);
     free_lists(r);
@@ -307,6 +316,7 @@ extern "C" int pgb_destroy(pgb_run* r) {
     cudaFree(r->prob_cx);
     for (int j = 0; j < r->ng; ++j) { cudaFree(r->mg_u[j]); cudaFree(r->mg_f[j]); cudaFree(r->mg_v[j]); cudaFree(r->mg_r[j]); }
     cudaFree(r->mg_tab);
+    pgb_mg_free(r);
     for (int w = 0; w < 2; ++w) cudaFree(r->neut64[w]);
     if (r->h_stage) cudaFreeHost(r->h_stage);
     cudaFree(r->d_stage);
@@ -400,6 +410,20 @@ static int need_particles(pgb_run* r) {
     return 0;
 }
 
+/* ds->t = t0 and the right-wall potentials phi_right*cos(phi_period*t) of
+ * steps t0 .. t0+n-1 (fields.cpp:177), computed on the host as the
+ * reference does                                                         */
+static int set_device_step(pgb_run* r, int64_t t0, int n) {
+    if (n > r->phi_tab_cap) return fail(r, PGB_ERR_ARG, "step table too small");
+    std::vector<double> tab((size_t)n);
+    for (int k = 0; k < n; ++k) tab[k] = r->p.phi_right * cos(r->p.phi_period * (double)(t0 + k));
+    long long tt[2] = {(long long)t0, (long long)t0};
+    PGB_CK(r, cudaMemcpyAsync(r->phi_tab, tab.data(), sizeof(double) * n, cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaMemcpyAsync(&r->ds->t, tt, sizeof(tt), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaStreamSynchronize(r->stream));
+    return 0;
+}
+
 /* ---------------------------------------------------- phase entry points */
 static int boundary_phase(pgb_run* r, int which) {
     if (r->p.steadystate) {
@@ -420,6 +444,7 @@ extern "C" int pgb_boundary(pgb_run* r, int which) {
     if (rc) return rc;
     /* deposits made by wall events go to the accumulators of the step; in
      * the phase-by-phase form the charge is recomputed by pgb_deposit     */
+    if ((rc = set_device_step(r, r->time_step, 1))) return rc;
     if ((rc = boundary_phase(r, which))) return rc;
     return sync_state(r);
 }
@@ -428,11 +453,10 @@ extern "C" int pgb_initial_boundary(pgb_run* r) {
     if (!r) return PGB_ERR_ARG;
     int rc = need_particles(r);
     if (rc) return rc;
-    int64_t saved = r->time_step;
-    r->time_step = -1;   /* random streams of the pre-loop boundary pass */
+    /* random streams of the pre-loop boundary pass use step -1 */
+    if ((rc = set_device_step(r, -1, 1))) return rc;
     rc = boundary_phase(r, PGB_BOUNDARY_IONS);
     if (!rc) rc = boundary_phase(r, PGB_BOUNDARY_ELECTRONS);
-    r->time_step = saved;
     if (rc) return rc;
     return sync_state(r);
 }
@@ -441,6 +465,7 @@ extern "C" int pgb_collide_electrons(pgb_run* r) {
     if (!r) return PGB_ERR_ARG;
     int rc = need_particles(r);
     if (rc) return rc;
+    if ((rc = set_device_step(r, r->time_step, 1))) return rc;
     if (pgb_launch_mcc(r) || pgb_build_list(r, LIST_ION_EV, 0) || pgb_launch_ionize_appends(r, 1, 1))
         return PGB_ERR_CUDA;
     return sync_state(r);
@@ -450,6 +475,7 @@ extern "C" int pgb_inject(pgb_run* r) {
     if (!r) return PGB_ERR_ARG;
     int rc = need_particles(r);
     if (rc) return rc;
+    if ((rc = set_device_step(r, r->time_step, 1))) return rc;
     if (pgb_launch_inject(r, 3, false)) return PGB_ERR_CUDA;
     return sync_state(r);
 }
@@ -466,6 +492,7 @@ extern "C" int pgb_collide_ions(pgb_run* r) {
     if (!r) return PGB_ERR_ARG;
     int rc = need_particles(r);
     if (rc) return rc;
+    if ((rc = set_device_step(r, r->time_step, 1))) return rc;
     if (pgb_launch_cx(r)) return PGB_ERR_CUDA;
     return sync_state(r);
 }
@@ -485,26 +512,29 @@ extern "C" int pgb_deposit(pgb_run* r, int s) {
     int rc = need_particles(r);
     if (rc) return rc;
     PGB_CK(r, cudaMemsetAsync(r->qacc[s], 0, sizeof(unsigned long long) * r->nx * r->ny, r->stream));
-    if (pgb_launch_deposit(r, s) || pgb_launch_finalize(r, 1 << s, false, 0.0)) return PGB_ERR_CUDA;
+    if (pgb_launch_deposit(r, s) || pgb_launch_finalize(r, 1 << s, false)) return PGB_ERR_CUDA;
     return sync_state(r);
 }
 
 extern "C" int pgb_grid_rho(pgb_run* r) {
     if (!r) return PGB_ERR_ARG;
-    if (pgb_launch_finalize(r, 0, false, 0.0)) return PGB_ERR_CUDA;
+    int rc;
+    if ((rc = set_device_step(r, r->time_step, 1))) return rc;
+    if (pgb_launch_finalize(r, 0, false)) return PGB_ERR_CUDA;
     return sync_state(r);
 }
 
 extern "C" int pgb_poisson(pgb_run* r, int64_t t) {
     if (!r) return PGB_ERR_ARG;
-    double phi_right = r->p.phi_right * cos(r->p.phi_period * (double)t);
-    if (pgb_launch_rhs(r, phi_right) || pgb_poisson_solve(r, t)) return PGB_ERR_CUDA;
+    int rc = set_device_step(r, t, 1);
+    if (rc) return rc;
+    if (pgb_launch_rhs(r) || pgb_poisson_solve(r)) return PGB_ERR_CUDA;
     return sync_state(r);
 }
 
 extern "C" int pgb_efield(pgb_run* r) {
     if (!r) return PGB_ERR_ARG;
-    if (pgb_launch_efield(r)) return PGB_ERR_CUDA;
+    if (pgb_launch_efield(r, 0)) return PGB_ERR_CUDA;
     return sync_state(r);
 }
 
@@ -513,10 +543,11 @@ extern "C" int pgb_efield(pgb_run* r) {
 #define PROF_MARK(r, k) \
     do { if ((r)->prof_on) PGB_CK((r), cudaEventRecord((r)->prof_ev[k], (r)->stream)); } while (0)
 
-static int step_once(pgb_run* r) {
-    const int64_t t = r->time_step;
+/* one pic_run iteration; the device step counter ds->t selects the random
+ * streams and the right-wall potential, so the same launches can be
+ * replayed as a CUDA graph for every step                               */
+static int step_once(pgb_run* r, bool ion_step) {
     const bool coll = r->p.have_collisions != 0;
-    const bool ion_step = (t % r->dt_dti) == 0;
     const size_t G = (size_t)r->nx * r->ny;
     PGB_CK(r, cudaMemsetAsync(r->qacc[0], 0, sizeof(unsigned long long) * G, r->stream));
     PGB_CK(r, cudaMemsetAsync(r->qacc[1], 0, sizeof(unsigned long long) * G, r->stream));
@@ -567,13 +598,11 @@ static int step_once(pgb_run* r) {
         }
     }
     /* collect_charge edge doubling, grid_rho, grid_potential, grid_electric_field */
-    double phi_right = r->p.phi_right * cos(r->p.phi_period * (double)t);
     PROF_MARK(r, 5);
-    if (pgb_launch_finalize(r, 3, true, phi_right)) return PGB_ERR_CUDA;
-    if (pgb_poisson_solve(r, t)) return PGB_ERR_CUDA;
-    if (pgb_launch_efield(r)) return PGB_ERR_CUDA;
+    if (pgb_launch_finalize(r, 3, true)) return PGB_ERR_CUDA;
+    if (pgb_poisson_solve(r)) return PGB_ERR_CUDA;
+    if (pgb_launch_efield(r, 1)) return PGB_ERR_CUDA;
     PROF_MARK(r, 6);
-    r->time_step = t + 1;
     return 0;
 }
 
@@ -591,27 +620,81 @@ static int profile_collect(pgb_run* r) {
     return 0;
 }
 
+static void drop_graphs(pgb_run* r) {
+    for (int k = 0; k < 8; ++k)
+        if (r->graph[k]) { cudaGraphExecDestroy(r->graph[k]); r->graph[k] = nullptr; }
+}
+
+/* graphs are usable when no step needs a host decision: no profiling and
+ * no species that could reach its reduction limit                       */
+static bool graphs_ok(pgb_run* r) {
+    if (!r->use_graphs || r->prof_on) return false;
+    if (!r->p.steadystate && (r->sp[0].cap > r->p.size_to_check_e || r->sp[1].cap > r->p.size_to_check_i)) return false;
+    return true;
+}
+
+static int launch_step(pgb_run* r, bool ion_step) {
+    if (!graphs_ok(r)) return step_once(r, ion_step);
+    int key = (ion_step ? 4 : 0) | (r->orient[0] << 1) | r->orient[1];
+    if (!r->graph[key]) {
+        cudaGraph_t g = nullptr;
+        PGB_CK(r, cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
+        long long l0 = r->launches;
+        int rc = step_once(r, ion_step);
+        cudaError_t e = cudaStreamEndCapture(r->stream, &g);
+        if (rc || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            r->use_graphs = 0;   /* run the launches directly from now on */
+            r->launches = l0;
+            return step_once(r, ion_step);
+        }
+        r->graph_launches[key] = r->launches - l0;
+        r->launches = l0;
+        e = cudaGraphInstantiate(&r->graph[key], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            r->graph[key] = nullptr;
+            r->use_graphs = 0;
+            return step_once(r, ion_step);
+        }
+    }
+    PGB_CK(r, cudaGraphLaunch(r->graph[key], r->stream));
+    r->launches += r->graph_launches[key];
+    return 0;
+}
+
 extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
     if (!r || nsteps < 0) return fail(r, PGB_ERR_ARG, "pgb_step: bad argument");
     int rc = need_particles(r);
     if (rc) return rc;
-    for (int k = 0; k < nsteps; ++k) {
-        /* compact when tombstones exceed 1/8 of the slots (counts read lazily) */
-        for (int s = 0; s < 2; ++s)
-            if (r->hs->dead[s] * 8 > r->hs->n[s] && r->hs->dead[s] > 0) {
-                if (pgb_launch_compact(r, s)) return PGB_ERR_CUDA;
-                r->hs->dead[s] = 0;
+    int done = 0;
+    while (done < nsteps) {
+        int chunk = std::min<int>(nsteps - done, (int)r->phi_tab_cap);
+        if ((rc = set_device_step(r, r->time_step, chunk))) return rc;
+        for (int k = 0; k < chunk; ++k) {
+            /* compact when tombstones exceed 1/8 of the slots (counts read lazily) */
+            for (int s = 0; s < 2; ++s)
+                if (r->hs->dead[s] * 8 > r->hs->n[s] && r->hs->dead[s] > 0) {
+                    if (pgb_launch_compact(r, s)) return PGB_ERR_CUDA;
+                    r->orient[s] ^= 1;
+                    r->hs->dead[s] = 0;
+                }
+            if (r->prof_on) {
+                if ((rc = sync_state(r))) return rc;
+                r->prof.slots_e += r->hs->n[0];
+                r->prof.slots_i += r->hs->n[1];
             }
-        if (r->prof_on) {
-            if ((rc = sync_state(r))) return rc;
-            r->prof.slots_e += r->hs->n[0];
-            r->prof.slots_i += r->hs->n[1];
+            const bool ion_step = (r->time_step % r->dt_dti) == 0;
+            if ((rc = launch_step(r, ion_step))) return rc;
+            if (r->prof_on && (rc = profile_collect(r))) return rc;
+            r->time_step += 1;
+            /* counters come back asynchronously; the host reads them only to
+             * decide when to compact, which never changes results          */
+            PGB_CK(r, cudaMemcpyAsync(r->hs, r->ds, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
         }
-        if ((rc = step_once(r))) return rc;
-        if (r->prof_on && (rc = profile_collect(r))) return rc;
-        /* counters come back asynchronously; the host reads them only to
-         * decide when to compact, which never changes results              */
-        PGB_CK(r, cudaMemcpyAsync(r->hs, r->ds, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
+        done += chunk;
     }
     return sync_state(r);
 }

@@ -35,7 +35,9 @@ struct FinalizeArgs {
     int mask;             /* species whose q is rebuilt from acc */
     double coef;          /* 1/EPSILON */
     double divdxdy;       /* 1/(DX*DY) */
-    double phi0x, phirx, phi0y, phily;
+    double phi0x, phi0y, phily;
+    const double* phi_tab;   /* right wall: phi_tab[t - t_base] (fields.cpp:177) */
+    const DevState* ds;
 };
 
 __device__ __forceinline__ double edge_factor(int i, int j, int nx, int ny) {
@@ -45,10 +47,10 @@ __device__ __forceinline__ double edge_factor(int i, int j, int nx, int ny) {
 }
 
 /* RHS of fields::grid_potential (fields.cpp:184-204) for node (j, i) */
-__device__ __forceinline__ double rhs_node(double rho, int i, int j, const FinalizeArgs& a) {
+__device__ __forceinline__ double rhs_node(double rho, int i, int j, const FinalizeArgs& a, double phirx) {
     double f = -a.coef * rho;
     if (i == 1) f = f - a.phi0x * a.divdxdy;
-    if (i == a.nx - 2) f = f - a.phirx * a.divdxdy;
+    if (i == a.nx - 2) f = f - phirx * a.divdxdy;
     if (j == 1) f = f - a.phi0y * a.divdxdy;
     if (j == a.ny - 2) f = f - a.phily * a.divdxdy;
     return f;
@@ -56,6 +58,7 @@ __device__ __forceinline__ double rhs_node(double rho, int i, int j, const Final
 
 __global__ void k_finalize(FinalizeArgs a) {
     const int G = a.nx * a.ny;
+    const double phirx = a.phi_tab[a.ds->t - a.ds->t_base];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x) {
         int j = k / a.nx, i = k - j * a.nx;
         double ef = edge_factor(i, j, a.nx, a.ny);
@@ -66,15 +69,16 @@ __global__ void k_finalize(FinalizeArgs a) {
             }
         double rho = a.q[1][k] + a.q[0][k];
         a.rho[k] = rho;
-        if (a.f) a.f[k] = rhs_node(rho, i, j, a);
+        if (a.f) a.f[k] = rhs_node(rho, i, j, a, phirx);
     }
 }
 
 __global__ void k_rhs(FinalizeArgs a) {
     const int G = a.nx * a.ny;
+    const double phirx = a.phi_tab[a.ds->t - a.ds->t_base];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x) {
         int j = k / a.nx, i = k - j * a.nx;
-        a.f[k] = rhs_node(a.rho[k], i, j, a);
+        a.f[k] = rhs_node(a.rho[k], i, j, a, phirx);
     }
 }
 
@@ -303,7 +307,10 @@ __device__ __forceinline__ double ey_interior(const double* phi, int nx, int ny,
     if (j < 1 || j > ny - 2 || i < 1 || i > nx - 2) return 0.0;
     return (phi[(j - 1) * nx + i] - phi[(j + 1) * nx + i]) / twoDX;
 }
-__global__ void k_efield(const double* phi, double* Ex, double* Ey, float2* exy, int nx, int ny, double twoDX) {
+__global__ void k_efield(const double* phi, double* Ex, double* Ey, float2* exy, int nx, int ny, double twoDX,
+                         DevState* ds, int advance) {
+    /* the last kernel of a step moves the device step counter on */
+    if (advance && blockIdx.x == 0 && threadIdx.x == 0) ds->t += 1;
     const int GE = (nx + 1) * (ny + 1);
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < GE; k += gridDim.x * blockDim.x) {
         double ex = 0.0, ey = 0.0;
@@ -322,7 +329,9 @@ __global__ void k_efield(const double* phi, double* Ex, double* Ey, float2* exy,
     }
 }
 
-__global__ void k_walls(double* phi, int nx, int ny, double phi0x, double phirx, double phi0y, double phily) {
+__global__ void k_walls(double* phi, int nx, int ny, double phi0x, const double* phi_tab, const DevState* ds,
+                        double phi0y, double phily) {
+    const double phirx = phi_tab[ds->t - ds->t_base];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx * ny; k += gridDim.x * blockDim.x) {
         int j = k / nx, i = k - j * nx;
         /* fields.cpp:209-219: columns first, then rows overwrite the corners */
@@ -334,7 +343,7 @@ __global__ void k_walls(double* phi, int nx, int ny, double phi0x, double phirx,
 }
 
 /* ====================================================== host side */
-static FinalizeArgs fin_args(pgb_run* r, int mask, double phi_right, bool rhs) {
+static FinalizeArgs fin_args(pgb_run* r, int mask, bool rhs) {
     FinalizeArgs a;
     a.acc[0] = r->qacc[0]; a.acc[1] = r->qacc[1];
     a.q[0] = r->q[0]; a.q[1] = r->q[1];
@@ -345,12 +354,13 @@ static FinalizeArgs fin_args(pgb_run* r, int mask, double phi_right, bool rhs) {
     a.mask = mask;
     a.coef = 1.0 / 8.854e-12;
     a.divdxdy = 1.0 / (r->dx * r->dy);
-    a.phi0x = r->p.phi_left; a.phirx = phi_right; a.phi0y = r->p.phi_bottom; a.phily = r->p.phi_top;
+    a.phi0x = r->p.phi_left; a.phi0y = r->p.phi_bottom; a.phily = r->p.phi_top;
+    a.phi_tab = r->phi_tab; a.ds = r->ds;
     return a;
 }
 
-int pgb_launch_finalize(pgb_run* r, int mask, bool make_rhs, double phi_right) {
-    FinalizeArgs a = fin_args(r, mask, phi_right, make_rhs);
+int pgb_launch_finalize(pgb_run* r, int mask, bool make_rhs) {
+    FinalizeArgs a = fin_args(r, mask, make_rhs);
     int G = r->nx * r->ny;
     k_finalize<<<(G + 255) / 256, 256, 0, r->stream>>>(a);
     r->launches++;
@@ -358,8 +368,8 @@ int pgb_launch_finalize(pgb_run* r, int mask, bool make_rhs, double phi_right) {
     return 0;
 }
 
-int pgb_launch_rhs(pgb_run* r, double phi_right) {
-    FinalizeArgs a = fin_args(r, 0, phi_right, true);
+int pgb_launch_rhs(pgb_run* r) {
+    FinalizeArgs a = fin_args(r, 0, true);
     int G = r->nx * r->ny;
     k_rhs<<<(G + 255) / 256, 256, 0, r->stream>>>(a);
     r->launches++;
@@ -382,101 +392,185 @@ struct MgTables {
     double** r;
 };
 
-static int small_launch(pgb_run* r, double** tab, int J, int mode) {
-    size_t smem = small_smem_bytes(J, sizeof(double));
-    k_mg_small<double><<<1, 1024, smem, r->stream>>>(J, mode, r->p.xlength, tab, tab + PGB_MAX_LEVELS,
-                                                     tab + 2 * PGB_MAX_LEVELS, tab + 3 * PGB_MAX_LEVELS);
+template <class T>
+static int small_launch(pgb_run* r, T** tab, int J, int mode) {
+    size_t smem = small_smem_bytes(J, sizeof(T));
+    k_mg_small<T><<<1, 1024, smem, r->stream>>>(J, mode, (T)r->p.xlength, tab, tab + PGB_MAX_LEVELS,
+                                                tab + 2 * PGB_MAX_LEVELS, tab + 3 * PGB_MAX_LEVELS);
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
+
+/* level arrays of one precision */
+template <class T>
+struct Levels {
+    T** u;
+    T** f;
+    T** v;
+    T** rr;
+    T** tab;   /* device copy: u, f, v, r tables */
+};
+static Levels<double> levels64(pgb_run* r) { return {r->mg_u, r->mg_f, r->mg_v, r->mg_r, r->mg_tab}; }
+static Levels<float> levels32(pgb_run* r) { return {r->mg32_u, r->mg32_f, r->mg32_v, r->mg32_r, r->mg32_tab}; }
 
 /* V-cycle at level j > small on (u, f) (mglin.cpp:176-196) */
-static int vcycle(pgb_run* r, double** tab, int j, int jsmall, double* u, const double* f) {
+template <class T>
+static int vcycle(pgb_run* r, const Levels<T>& L, int j, int jsmall, T* u, const T* f) {
     int nf = r->mg_n[j], nc = r->mg_n[j - 1];
-    double h = r->p.xlength / (nf - 1), h2 = h * h, h2i = 1.0 / (h * h);
+    T h = (T)r->p.xlength / (T)(nf - 1), h2 = h * h, h2i = (T)1.0 / (h * h);
     long long rw = (long long)(nf - 2) * ((nf - 1) / 2);
-    k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
-    r->launches++;
-    k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
-    r->launches++;
-    k_resid_restrict<double><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(r->mg_r[j - 1], u, f, nf, h2i);
-    r->launches++;
-    PGB_CK(r, cudaMemsetAsync(r->mg_v[j - 1], 0, sizeof(double) * nc * nc, r->stream));
+    k_relax_rows<T><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
+    k_relax_rows<T><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
+    k_resid_restrict<T><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(L.rr[j - 1], u, f, nf, h2i);
+    r->launches += 3;
+    PGB_CK(r, cudaMemsetAsync(L.v[j - 1], 0, sizeof(T) * nc * nc, r->stream));
     if (j - 1 <= jsmall) {
-        if (small_launch(r, tab, j - 1, 1)) return PGB_ERR_CUDA;
+        if (small_launch<T>(r, L.tab, j - 1, 1)) return PGB_ERR_CUDA;
     } else {
-        if (vcycle(r, tab, j - 1, jsmall, r->mg_v[j - 1], r->mg_r[j - 1])) return PGB_ERR_CUDA;
+        if (vcycle<T>(r, L, j - 1, jsmall, L.v[j - 1], L.rr[j - 1])) return PGB_ERR_CUDA;
     }
-    k_prolong<double><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(u, r->mg_v[j - 1], nf, 1);
-    r->launches++;
-    k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
-    r->launches++;
-    k_relax_rows<double><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
-    r->launches++;
+    k_prolong<T><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(u, L.v[j - 1], nf, 1);
+    k_relax_rows<T><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
+    k_relax_rows<T><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
+    r->launches += 3;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
 
-/* Mglin on the rhs in mg_f[ng-1]; result in mg_u[ng-1] */
-static int fmg(pgb_run* r) {
+static int small_top(pgb_run* r) {
+    int jsmall = 0;
+    while (jsmall + 1 < r->ng && r->mg_n[jsmall + 1] <= PGB_MG_SMALL) jsmall++;
+    return jsmall;
+}
+
+/* Mglin on the rhs in f[ng-1]; result in u[ng-1] */
+template <class T>
+static int fmg(pgb_run* r, const Levels<T>& L) {
     const int ng = r->ng;
-    double** tab = r->mg_tab;   /* device pointer tables, filled at create */
     for (int j = ng - 2; j >= 0; --j) {
         int nc = r->mg_n[j];
-        k_restrict<double><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(r->mg_f[j], r->mg_f[j + 1], nc);
+        k_restrict<T><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(L.f[j], L.f[j + 1], nc);
         r->launches++;
     }
-    int jsmall = 0;
-    while (jsmall + 1 < ng && r->mg_n[jsmall + 1] <= PGB_MG_SMALL) jsmall++;
-    if (small_launch(r, tab, jsmall, 0)) return PGB_ERR_CUDA;
+    int jsmall = small_top(r);
+    if (small_launch<T>(r, L.tab, jsmall, 0)) return PGB_ERR_CUDA;
     for (int j = jsmall + 1; j < ng; ++j) {
         int nf = r->mg_n[j];
-        k_prolong<double><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(r->mg_u[j], r->mg_u[j - 1], nf, 0);
+        k_prolong<T><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(L.u[j], L.u[j - 1], nf, 0);
         r->launches++;
         for (int c = 0; c < 2; ++c)
-            if (vcycle(r, tab, j, jsmall, r->mg_u[j], r->mg_f[j])) return PGB_ERR_CUDA;
+            if (vcycle<T>(r, L, j, jsmall, L.u[j], L.f[j])) return PGB_ERR_CUDA;
     }
     PGB_CK(r, cudaGetLastError());
     return 0;
+}
+
+/* FP64 defect d = f - L u on the interior (zero on the walls), as FP32 */
+__global__ void k_defect32(const double* u, const double* f, float* d, int n, double h2i) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n * n; k += gridDim.x * blockDim.x) {
+        int i = k / n, j = k - i * n;
+        double v = 0.0;
+        if (i > 0 && j > 0 && i < n - 1 && j < n - 1)
+            v = f[k] - h2i * (u[k + n] + u[k - n] + u[k + 1] + u[k - 1] - 4.0 * u[k]);
+        d[k] = (float)v;
+    }
+}
+__global__ void k_add32(double* u, const float* e, int count) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) u[k] += (double)e[k];
+}
+__global__ void k_to32(float* d, const double* s, int count) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) d[k] = (float)s[k];
+}
+__global__ void k_to64(double* d, const float* s, int count) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) d[k] = (double)s[k];
 }
 
 int pgb_mg_setup(pgb_run* r) {
-    /* pointer tables: u, f, v, r per level (device array of device pointers) */
     double* tabs[4 * PGB_MAX_LEVELS] = {};
+    float* tabs32[4 * PGB_MAX_LEVELS] = {};
     for (int l = 0; l < r->ng; ++l) {
+        size_t n2 = (size_t)r->mg_n[l] * r->mg_n[l];
+        PGB_CK(r, cudaMalloc(&r->mg32_u[l], n2 * sizeof(float)));
+        PGB_CK(r, cudaMalloc(&r->mg32_f[l], n2 * sizeof(float)));
+        PGB_CK(r, cudaMalloc(&r->mg32_v[l], n2 * sizeof(float)));
+        PGB_CK(r, cudaMalloc(&r->mg32_r[l], n2 * sizeof(float)));
         tabs[l] = r->mg_u[l];
         tabs[PGB_MAX_LEVELS + l] = r->mg_f[l];
         tabs[2 * PGB_MAX_LEVELS + l] = r->mg_v[l];
         tabs[3 * PGB_MAX_LEVELS + l] = r->mg_r[l];
+        tabs32[l] = r->mg32_u[l];
+        tabs32[PGB_MAX_LEVELS + l] = r->mg32_f[l];
+        tabs32[2 * PGB_MAX_LEVELS + l] = r->mg32_v[l];
+        tabs32[3 * PGB_MAX_LEVELS + l] = r->mg32_r[l];
     }
     PGB_CK(r, cudaMalloc(&r->mg_tab, sizeof(tabs)));
     PGB_CK(r, cudaMemcpy(r->mg_tab, tabs, sizeof(tabs), cudaMemcpyHostToDevice));
-    int jsmall = 0;
-    while (jsmall + 1 < r->ng && r->mg_n[jsmall + 1] <= PGB_MG_SMALL) jsmall++;
-    size_t smem = small_smem_bytes(jsmall, sizeof(double));
-    PGB_CK(r, cudaFuncSetAttribute(k_mg_small<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PGB_CK(r, cudaMalloc(&r->mg32_tab, sizeof(tabs32)));
+    PGB_CK(r, cudaMemcpy(r->mg32_tab, tabs32, sizeof(tabs32), cudaMemcpyHostToDevice));
+    size_t G = (size_t)r->nx * r->ny;
+    PGB_CK(r, cudaMalloc(&r->dc_u, G * sizeof(double)));
+    int jsmall = small_top(r);
+    PGB_CK(r, cudaFuncSetAttribute(k_mg_small<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)small_smem_bytes(jsmall, sizeof(double))));
+    PGB_CK(r, cudaFuncSetAttribute(k_mg_small<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)small_smem_bytes(jsmall, sizeof(float))));
     return 0;
 }
 
-int pgb_poisson_solve(pgb_run* r, int64_t t) {
-    double phi_right = r->p.phi_right * cos(r->p.phi_period * (double)t);
-    if (fmg(r)) return PGB_ERR_CUDA;
-    PGB_CK(r, cudaMemcpyAsync(r->phi, r->mg_u[r->ng - 1], sizeof(double) * r->nx * r->ny, cudaMemcpyDeviceToDevice,
-                              r->stream));
-    k_walls<<<blocks_for((long long)r->nx * r->ny), 256, 0, r->stream>>>(r->phi, r->nx, r->ny, r->p.phi_left, phi_right,
-                                                                         r->p.phi_bottom, r->p.phi_top);
+void pgb_mg_free(pgb_run* r) {
+    for (int l = 0; l < r->ng; ++l) {
+        cudaFree(r->mg32_u[l]); cudaFree(r->mg32_f[l]); cudaFree(r->mg32_v[l]); cudaFree(r->mg32_r[l]);
+    }
+    cudaFree(r->mg32_tab);
+    cudaFree(r->dc_u);
+}
+
+/* fields::grid_potential after the right-hand side is in mg_f[ng-1]:
+ *   FMG_REF  FP64 full multigrid with the reference's schedule (bitwise)
+ *   FMG32    the same schedule in FP32
+ *   FP32_DC  FP32 full multigrid inside an FP64 defect-correction loop   */
+int pgb_poisson_solve(pgb_run* r) {
+    const int top = r->ng - 1, n = r->nx;
+    const int G = n * n;
+    const int gb = blocks_for(G);
+    if (r->p.poisson_mode == PGB_POISSON_FMG_REF) {
+        if (fmg<double>(r, levels64(r))) return PGB_ERR_CUDA;
+        PGB_CK(r, cudaMemcpyAsync(r->phi, r->mg_u[top], sizeof(double) * G, cudaMemcpyDeviceToDevice, r->stream));
+    } else if (r->p.poisson_mode == PGB_POISSON_FMG32) {
+        Levels<float> L = levels32(r);
+        k_to32<<<gb, 256, 0, r->stream>>>(L.f[top], r->mg_f[top], G);
+        r->launches++;
+        if (fmg<float>(r, L)) return PGB_ERR_CUDA;
+        k_to64<<<gb, 256, 0, r->stream>>>(r->phi, L.u[top], G);
+        r->launches++;
+    } else {
+        Levels<float> L = levels32(r);
+        double h = r->p.xlength / (n - 1), h2i = 1.0 / (h * h);
+        PGB_CK(r, cudaMemsetAsync(r->dc_u, 0, sizeof(double) * G, r->stream));
+        int iters = r->p.dc_max_iters > 0 ? r->p.dc_max_iters : 1;
+        for (int it = 0; it < iters; ++it) {
+            k_defect32<<<gb, 256, 0, r->stream>>>(r->dc_u, r->mg_f[top], L.f[top], n, h2i);
+            r->launches++;
+            if (fmg<float>(r, L)) return PGB_ERR_CUDA;
+            k_add32<<<gb, 256, 0, r->stream>>>(r->dc_u, L.u[top], G);
+            r->launches++;
+        }
+        PGB_CK(r, cudaMemcpyAsync(r->phi, r->dc_u, sizeof(double) * G, cudaMemcpyDeviceToDevice, r->stream));
+    }
+    k_walls<<<blocks_for((long long)r->nx * r->ny), 256, 0, r->stream>>>(r->phi, r->nx, r->ny, r->p.phi_left, r->phi_tab,
+                                                                         r->ds, r->p.phi_bottom, r->p.phi_top);
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
 
-int pgb_launch_efield(pgb_run* r) {
+int pgb_launch_efield(pgb_run* r, int advance) {
     int GE = (r->nx + 1) * (r->ny + 1);
-    k_efield<<<blocks_for(GE), 256, 0, r->stream>>>(r->phi, r->ex, r->ey, r->exy, r->nx, r->ny, 2.0 * r->dx);
+    k_efield<<<blocks_for(GE), 256, 0, r->stream>>>(r->phi, r->ex, r->ey, r->exy, r->nx, r->ny, 2.0 * r->dx, r->ds, advance);
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
 
-double pgb_phi_right(pgb_run* r, int64_t t) { return r->p.phi_right * cos(r->p.phi_period * (double)t); }
+

@@ -44,7 +44,8 @@ struct DevState {
     long long stats[ST_COUNT];
     int err;
     int pad1;
-    double cx_acc_dummy;
+    long long t;             /* the reference's time_step of the step being run */
+    long long t_base;        /* step of phi_tab[0]                              */
 };
 
 /* dense event lists (ordered by slot) */
@@ -95,6 +96,7 @@ struct pgb_run {
     int mg_n[PGB_MAX_LEVELS];
     double *mg_u[PGB_MAX_LEVELS], *mg_f[PGB_MAX_LEVELS], *mg_v[PGB_MAX_LEVELS], *mg_r[PGB_MAX_LEVELS];
     double** mg_tab = nullptr;                       /* device table of the level pointers */
+    float** mg32_tab = nullptr;
     double *dc_d = nullptr, *dc_u = nullptr;        /* FP32_DC defect correction (FP64) */
     float *mg32_u[PGB_MAX_LEVELS], *mg32_f[PGB_MAX_LEVELS], *mg32_v[PGB_MAX_LEVELS], *mg32_r[PGB_MAX_LEVELS];
     /* event lists */
@@ -109,6 +111,13 @@ struct pgb_run {
     float* neut[2] = {nullptr, nullptr};   /* [which]: 3 x N_neutral, FP32    */
     double* neut64[2] = {nullptr, nullptr};
     double* prob_cx = nullptr;             /* per-column CX accumulator       */
+    double* phi_tab = nullptr;             /* right-wall potential per step   */
+    long long phi_tab_cap = 0;
+    /* CUDA graphs of one step, keyed by (ion step, buffer orientation e, i) */
+    cudaGraphExec_t graph[8] = {};
+    int orient[2] = {0, 0};                /* which particle buffer is live   */
+    long long graph_launches[8] = {};      /* kernels in each graph           */
+    int use_graphs = 1;
     float* cx_p = nullptr;                 /* per-ion CX probability          */
     float* cx_tile_sum = nullptr;          /* [tile][column]                  */
     /* host staging */
@@ -137,7 +146,7 @@ int pgb_launch_push(pgb_run* r, int s, bool mcc, bool deposit, bool flag_ion);
 int pgb_launch_flag_outside(pgb_run* r, int s);
 int pgb_build_list(pgb_run* r, int which, int species_for_tiles);
 int pgb_launch_deposit(pgb_run* r, int s);
-int pgb_launch_finalize(pgb_run* r, int which_species_mask, bool make_rhs, double phi_right);
+int pgb_launch_finalize(pgb_run* r, int which_species_mask, bool make_rhs);
 int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e);
 int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i);
 int pgb_launch_mcc(pgb_run* r);
@@ -146,9 +155,10 @@ int pgb_launch_walls(pgb_run* r, int which);
 int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long n);
 int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap);
 int pgb_mg_setup(pgb_run* r);
+void pgb_mg_free(pgb_run* r);
 CollConsts pgb_coll_consts(pgb_run* r);
 int pgb_launch_compact(pgb_run* r, int s);
 int pgb_launch_reduce(pgb_run* r, int s);
-int pgb_poisson_solve(pgb_run* r, int64_t t);
-int pgb_launch_efield(pgb_run* r);
-int pgb_launch_rhs(pgb_run* r, double phi_right);
+int pgb_poisson_solve(pgb_run* r);
+int pgb_launch_efield(pgb_run* r, int advance);
+int pgb_launch_rhs(pgb_run* r);

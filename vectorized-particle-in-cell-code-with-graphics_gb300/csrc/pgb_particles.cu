@@ -39,7 +39,6 @@ struct PushArgs {
     int* tc_out;
     int* tl_ev;                 /* per-tile ionization-event list     */
     int* tc_ev;
-    unsigned int step;
 };
 
 /* gather (pic.cl:56-92) + push (pic.cl:95-149) of one particle in cell units */
@@ -185,7 +184,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_push(PushArgs a) {
             bool vchanged = false;
             if (MCC) {
                 unsigned int id = a.id[i];
-                f[1][k] = mcc_one(a.cc, a.neut64, id, a.step, pc.nx, pc.ny, p, vz, vchanged, st_loc);
+                f[1][k] = mcc_one(a.cc, a.neut64, id, (unsigned int)a.ds->t, pc.nx, pc.ny, p, vz, vchanged, st_loc);
             }
             bool moved;
             gather_push_one(pc, a.exy, p, vz, moved);
@@ -265,7 +264,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_mcc(PushArgs a) {
             if (is_dead(p.x)) continue;
             float vz = a.vz[i];
             bool vchanged = false;
-            f[0][k] = mcc_one(a.cc, a.neut64, a.id[i], a.step, a.pc.nx, a.pc.ny, p, vz, vchanged, st_loc);
+            f[0][k] = mcc_one(a.cc, a.neut64, a.id[i], (unsigned int)a.ds->t, a.pc.nx, a.pc.ny, p, vz, vchanged, st_loc);
             if (vchanged) { a.xv[i] = p; a.vz[i] = vz; }
         }
         int* const tla[1] = {a.tl_ev};
@@ -376,7 +375,6 @@ struct InjectArgs {
     int k;                       /* NUMBER_TO_INJECT */
     double dx, dy, xlength, ylength;
     uint64_t seed;
-    unsigned int step;
     PushConsts pce;
     const float2* exy;
     unsigned long long* qacc_e;
@@ -396,7 +394,7 @@ __global__ void k_inject(InjectArgs a) {
             unsigned int id = a.ds->next_id[s]++;
             a.ds->n[s] = slot + 1;
             pgb_stream st;
-            pgb_stream_init(&st, a.seed, id, a.step, PGB_STREAM_INJECT, (uint32_t)s);
+            pgb_stream_init(&st, a.seed, id, (unsigned int)a.ds->t, PGB_STREAM_INJECT, (uint32_t)s);
             double rx = pgb_u01d(pgb_stream_u32(&st));
             double ry = pgb_u01d(pgb_stream_u32(&st));
             double x = (a.dx + rx * (a.xlength - 2.0 * a.dx));
@@ -438,7 +436,6 @@ struct IonizeAppendArgs {
     CollConsts cc;
     const double* neut64;
     double dx, dy;
-    unsigned int step;
     int store_e, store_i;
 };
 __global__ void k_ionize_append(IonizeAppendArgs a) {
@@ -453,7 +450,7 @@ __global__ void k_ionize_append(IonizeAppendArgs a) {
          * parent's pre-event velocity is not needed because every product
          * is NaN (the excess energy is negative)                           */
         pgb_stream si;
-        pgb_stream_init(&si, a.cc.seed, pid, a.step, PGB_STREAM_IONIZE, 0);
+        pgb_stream_init(&si, a.cc.seed, pid, (unsigned int)a.ds->t, PGB_STREAM_IONIZE, 0);
         float4 pp = a.e.xv[slot];
         double xe = (double)pp.x * a.dx, ye = (double)pp.y * a.dy;
         IonizeOut o = ionize_fp64(&si, a.neut64, a.cc.n_neutral, a.cc, xe, ye, 0.0, 0.0, 0.0);
@@ -652,7 +649,6 @@ static PushArgs push_args(pgb_run* r, int s) {
     a.tc_out = r->tile_cnt[s == 0 ? LIST_OUT_E : LIST_OUT_I];
     a.tl_ev = r->tile_list[LIST_ION_EV];
     a.tc_ev = r->tile_cnt[LIST_ION_EV];
-    a.step = (unsigned int)r->time_step;
     return a;
 }
 
@@ -709,7 +705,7 @@ int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e) {
     InjectArgs a;
     a.e = r->sp[0]; a.i = r->sp[1]; a.ds = r->ds; a.k = r->p.number_to_inject;
     a.dx = r->dx; a.dy = r->dy; a.xlength = r->p.xlength; a.ylength = r->p.ylength;
-    a.seed = r->p.seed; a.step = (unsigned int)r->time_step;
+    a.seed = r->p.seed;
     a.pce = push_consts(r, 0); a.exy = r->exy; a.qacc_e = r->qacc[0];
     a.push_e = push_e; a.species_mask = species_mask;
     a.list_out_e = r->list[LIST_OUT_E]; a.list_cap = r->list_cap;
@@ -723,7 +719,7 @@ int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i) {
     IonizeAppendArgs a;
     a.e = r->sp[0]; a.i = r->sp[1]; a.ds = r->ds; a.ev = r->list[LIST_ION_EV];
     a.cc = pgb_coll_consts(r); a.neut64 = r->neut64[0];
-    a.dx = r->dx; a.dy = r->dy; a.step = (unsigned int)r->time_step;
+    a.dx = r->dx; a.dy = r->dy;
     a.store_e = store_e;
     a.store_i = store_i;
     k_ionize_append<<<r->sms * 2, 256, 0, r->stream>>>(a);

@@ -104,12 +104,15 @@ __device__ __forceinline__ float sig_ar_cx(float e) {
     if (e > 4.0f) return (2.0f + 5.5f / sqrtf(e)) * 10.0f;
     return (-2.95f * sqrtf(e) + 10.65f) * 10.0f;
 }
-/* ion_collisions.cpp:185-199: the energy is divided by 1000 and by AMU */
+/* ion_collisions.cpp:185-199: the energy is divided by 1000 and by AMU, so
+ * the scaled energy is ~1e22 and the fit's denominator overflows float to
+ * +inf for any physical energy; the FP64 value (~1e-72) gives the same zero
+ * probability once it enters 1-exp(-x) and the fixed-point accumulator.   */
 __device__ __forceinline__ float sig_h_cx(float e) {
-    double ee = (double)e / 1000.0 / PGB_AMU;
-    if (ee < 1.0e-4) return 0.0f;
-    return (float)((3.2345 * log((235.88 / ee) + 2.3713)) /
-                   (1.0 + 0.038371 * ee + 3.8068e-6 * pow(ee, 3.5) + 1.1832e-10 * pow(ee, 5.4)));
+    float ee = e / 1000.0f / 1.66054e-27f;
+    if (!(ee >= 1.0e-4f)) return 0.0f;
+    float den = 1.0f + 0.038371f * ee + 3.8068e-6f * __powf(ee, 3.5f) + 1.1832e-10f * __powf(ee, 5.4f);
+    return (3.2345f * logf((235.88f / ee) + 2.3713f)) / den;
 }
 
 struct CollConsts {

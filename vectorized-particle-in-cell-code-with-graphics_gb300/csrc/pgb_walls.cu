@@ -38,7 +38,6 @@ struct WallArgs {
     int e_see, refl, back, ion_see;
     double vte, vti, xlength, ylength;
     uint64_t seed;
-    unsigned int step;
 };
 
 __device__ __forceinline__ void store_particle(const Species& S, long long slot, double x, double y, double vx,
@@ -94,7 +93,7 @@ __global__ void k_iwall1(WallArgs a) {
         double energy = (0.5 / PGB_CHARGE) * a.mi * (vx * vx + vy * vy + vz * vz);
         double yield = ion_yield(a, energy);
         pgb_stream st;
-        pgb_stream_init(&st, a.seed, a.i.id[slot], a.step, PGB_STREAM_IWALL, 1);
+        pgb_stream_init(&st, a.seed, a.i.id[slot], (unsigned int)a.ds->t, PGB_STREAM_IWALL, 1);
         double R = pgb_u01d(pgb_stream_u32(&st));
         a.aux[k] = (R < yield) ? (int)floor(yield) + 1 : 0;
     }
@@ -118,7 +117,7 @@ __global__ void k_iwall2(WallArgs a) {
                 if (es >= a.e.cap) { atomicOr(&a.ds->err, ERR_CAP_E); break; }
                 unsigned int id = id0 + (unsigned int)(a.off[k] + j);
                 pgb_stream st;
-                pgb_stream_init(&st, a.seed, id, a.step, PGB_STREAM_SEE, 0);
+                pgb_stream_init(&st, a.seed, id, (unsigned int)a.ds->t, PGB_STREAM_SEE, 0);
                 double x = 0.0, y = 0.0, vx = 0.0, vy = 0.0, vz = 0.0, ww = 1.0;
                 if (jp < 0 || jp >= a.nx) {
                     double R = pgb_u01d(pgb_stream_u32(&st));
@@ -223,7 +222,7 @@ __global__ void k_ewall1(WallArgs a) {
         float4 p = a.e.xv[slot];
         double x = (double)p.x * a.dx, y = (double)p.y * a.dy, vx = p.z, vy = p.w, vz = a.e.vz[slot];
         pgb_stream st;
-        pgb_stream_init(&st, a.seed, a.e.id[slot], a.step, PGB_STREAM_EWALL, 0);
+        pgb_stream_init(&st, a.seed, a.e.id[slot], (unsigned int)a.ds->t, PGB_STREAM_EWALL, 0);
         int res = EW_RETRY, nsec = 0, kind = 0;
         const int jp = cellf(p.x), kp = cellf(p.y);
         for (int attempt = 0; attempt < 64 && res == EW_RETRY; ++attempt)
@@ -276,7 +275,7 @@ __global__ void k_ewall2(WallArgs a) {
             if (jpp < 0 || jpp >= a.nx) x = px;
             else y = py;
             pgb_stream st;
-            pgb_stream_init(&st, a.seed, id, a.step, PGB_STREAM_SEE, 0);
+            pgb_stream_init(&st, a.seed, id, (unsigned int)a.ds->t, PGB_STREAM_SEE, 0);
             double R = pgb_u01d(pgb_stream_u32(&st));
             double velocity = see_velocity(a, R);
             /* the new electron sits at the parent's x (left/right wall) or y */
@@ -375,7 +374,7 @@ __global__ void __launch_bounds__(1024) k_steady(WallArgs a, int* ion_by_rank) {
             if (cls == 2 && rhi + eb < cnt_hi) partner = ion_by_rank[mi_ - 1 - (rhi + eb)];
             if (partner >= 0) {
                 pgb_stream st;
-                pgb_stream_init(&st, a.seed, a.e.id[slot], a.step, PGB_STREAM_PLOP, 0);
+                pgb_stream_init(&st, a.seed, a.e.id[slot], (unsigned int)a.ds->t, PGB_STREAM_PLOP, 0);
                 double rx = pgb_u01d(pgb_stream_u32(&st)), ry = pgb_u01d(pgb_stream_u32(&st));
                 double x = (a.dx + rx * (a.xlength - 2.0 * a.dx));
                 double y = (a.dy + ry * (a.ylength - 2.0 * a.dy));
@@ -420,7 +419,6 @@ struct CxArgs {
     long long* col_acc;      /* per-column accumulator carried across steps (fixed point) */
     const double* neut64_i;  /* ion-neutral table */
     uint64_t seed;
-    unsigned int step;
 };
 
 __device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, float vz, int& col) {
@@ -502,7 +500,7 @@ __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
                     if (lane == l) {
                         /* charge_exchange_velocity (ion_collisions.cpp:209-221) */
                         pgb_stream st;
-                        pgb_stream_init(&st, a.seed, a.i.id[i], a.step, PGB_STREAM_CX, 1);
+                        pgb_stream_init(&st, a.seed, a.i.id[i], (unsigned int)a.ds->t, PGB_STREAM_CX, 1);
                         (void)pgb_stream_u32(&st);
                         int nn = a.cc.n_neutral;
                         int index = (int)(pgb_stream_u32(&st) % (uint32_t)(nn - 1));
@@ -539,7 +537,7 @@ static WallArgs wall_args(pgb_run* r) {
     a.e_see = r->p.e_impact_see; a.refl = r->p.reflection; a.back = r->p.backscatter;
     a.ion_see = (r->p.species == PGB_ARGON && r->p.ion_impact_see) ? 1 : 0;
     a.vte = r->p.vte; a.vti = r->p.vti; a.xlength = r->p.xlength; a.ylength = r->p.ylength;
-    a.seed = r->p.seed; a.step = (unsigned int)r->time_step;
+    a.seed = r->p.seed;
     return a;
 }
 
@@ -587,7 +585,7 @@ int pgb_launch_cx(pgb_run* r) {
     a.tile_sum = (long long*)r->cx_tile_sum;
     a.col_acc = (long long*)r->prob_cx;
     a.neut64_i = r->neut64[1];
-    a.seed = r->p.seed; a.step = (unsigned int)r->time_step;
+    a.seed = r->p.seed;
     k_cx_tiles<<<r->sms * 4, 256, sizeof(unsigned long long) * r->nx, r->stream>>>(a);
     r->launches++;
     int warps = 8;

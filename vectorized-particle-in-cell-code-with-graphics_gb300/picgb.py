@@ -33,7 +33,8 @@ PGB_ELECTRONS, PGB_IONS = 0, 1
 PGB_ARGON, PGB_HYDROGEN = 0, 1
 PGB_SIGMA_CONSTANT, PGB_SIGMA_ENERGY_DEPENDENT = 0, 1
 GRID = {"q_e": 0, "q_i": 1, "rho": 2, "phi": 3, "ex": 4, "ey": 5}
-PGB_POISSON_FMG_REF, PGB_POISSON_FP32_DC = 0, 1
+PGB_POISSON_FMG_REF, PGB_POISSON_FP32_DC, PGB_POISSON_FMG32 = 0, 1, 2
+POISSON_MODES = {"FMG_REF": 0, "FP32_DC": 1, "FMG32": 2}
 PGB_BOUNDARY_IONS, PGB_BOUNDARY_ELECTRONS = 0, 1
 
 
@@ -193,7 +194,7 @@ def make_params(**kw) -> PgbParams:
     p.size_to_check_i = stc
     p.size_to_check_e = int(g["SIZE_TO_CHECK_E"]) if g["SIZE_TO_CHECK_E"] is not None else stc
     p.seed = int(g["RAND_SEED"])
-    p.poisson_mode = PGB_POISSON_FMG_REF if g["POISSON"] == "FMG_REF" else PGB_POISSON_FP32_DC
+    p.poisson_mode = POISSON_MODES[str(g["POISSON"]).upper()]
     p.dc_max_iters = int(g["DC_MAX_ITERS"])
     p.dc_tolerance = float(g["DC_TOLERANCE"])
     p.sort_interval = int(g["SORT_INTERVAL"])
