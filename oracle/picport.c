@@ -1163,6 +1163,45 @@ void orc_contain_growth(orc_run* r, int spi) {
     if (spi == 0) r->c.reductions_e++; else r->c.reductions_i++;
 }
 
+/* Stable sort of a species by spatial bin, as the CUDA library orders its
+ * particle slots every sort_interval steps (bins of 32x32 cells inside the
+ * deposit region of pic.cl:35, then everything else).  Only the order
+ * changes; it matters for the order-dependent rules (charge-exchange
+ * accumulation, wall lists).                                              */
+static int64_t* g_sort_keys;
+static int key_cmp(const void* a, const void* b) {
+    int64_t x = *(const int64_t*)a, y = *(const int64_t*)b;
+    int64_t kx = g_sort_keys[x], ky = g_sort_keys[y];
+    if (kx != ky) return kx < ky ? -1 : 1;
+    return x < y ? -1 : (x > y);
+}
+static void orc_sort_bins(orc_run* r, int spi) {
+    orc_sp* S = &r->sp[spi];
+    const int nx = r->nx, ny = r->ny, BIN = 32;
+    const int nbx = (nx - 1 + BIN - 1) / BIN, nby = (ny - 1 + BIN - 1) / BIN, nbins = nbx * nby;
+    int64_t n = S->n;
+    if (n == 0) return;
+    int64_t* keys = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+    int64_t* idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        /* the library classifies in FP32 cell units */
+        float xs = (float)(S->p[i].x / r->dx), ys = (float)(S->p[i].y / r->dy);
+        int jp = (xs >= -2147483648.0f && xs < 2147483648.0f) ? (int)xs : INT_MIN;
+        int kp = (ys >= -2147483648.0f && ys < 2147483648.0f) ? (int)ys : INT_MIN;
+        keys[i] = (jp < nx - 1 && xs > 0.0f && kp < ny - 1 && ys > 0.0f) ? (kp / BIN) * nbx + jp / BIN : nbins;
+        idx[i] = i;
+    }
+    g_sort_keys = keys;
+    qsort(idx, (size_t)n, sizeof(int64_t), key_cmp);
+    orc_pv* p2 = (orc_pv*)malloc(sizeof(orc_pv) * (size_t)n);
+    uint32_t* id2 = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n);
+    for (int64_t k = 0; k < n; ++k) { p2[k] = S->p[idx[k]]; id2[k] = S->id[idx[k]]; }
+    memcpy(S->p, p2, sizeof(orc_pv) * (size_t)n);
+    memcpy(S->id, id2, sizeof(uint32_t) * (size_t)n);
+    free(keys); free(idx); free(p2); free(id2);
+    (void)nby;
+}
+
 /* ------------------------------------------------------------- driver */
 /* pic::pic_run, the two boundary calls ahead of the loop (pic.cpp:1049-1057) */
 void orc_initial_boundary(orc_run* r) {
@@ -1176,6 +1215,10 @@ void orc_step(orc_run* r, int nsteps) {
     for (int k = 0; k < nsteps; ++k) {
         int64_t t = r->time_step;
         r->rng_step = (uint32_t)t;
+        if (r->order_mode == ORC_ORDER_STABLE && r->prm.sort_interval > 0 && t % r->prm.sort_interval == 0) {
+            orc_sort_bins(r, PGB_ELECTRONS);
+            orc_sort_bins(r, PGB_IONS);
+        }
         if (r->prm.have_collisions) orc_collide_electrons(r);
         orc_inject(r);
         orc_gather_push(r, PGB_ELECTRONS);

@@ -311,3 +311,41 @@ def test_defect_correction_converges_to_exact_solution(n):
         e = rel_err(r.get_grid("phi"), o.get_grid("phi"))
     print(n, "dc err", e)
     assert e <= 1e-9
+
+
+# ------------------------------------------------------------- spatial sort
+@pytest.mark.parametrize("case", ["see33", "arcoll33", "steady33"])
+def test_binned_runs_match_oracle(case):
+    """With the spatial sort on, the oracle applies the same stable bin order,
+    so the comparison is the same as without it."""
+    g = load_golden(case)
+    g = dict(g)
+    kw = dict(g["kw"], SORT_INTERVAL=2)
+    g["p"] = picgb.make_params(**kw)
+    o, r = run_pair(g)
+    co, cr = o.counters(), r.counters()
+    for k in ("n_e", "n_i", "absorbed_e", "absorbed_i", "plopped", "see_events", "elastic", "ionization",
+              "charge_exchange"):
+        assert abs(cr[k] - co[k]) <= 0.01 * co[k] + 2, f"{case} {k}: gpu {cr[k]} oracle {co[k]}"
+    e = rel_err(r.get_grid("phi"), o.get_grid("phi"))
+    assert e <= 2e-2, e
+    r.close()
+
+
+def test_sort_leaves_deterministic_physics_unchanged():
+    """Sorting only permutes particles: without random events the fields are
+    bit-identical with and without it (the deposit is order-free)."""
+    g = load_golden("core65")
+    res = {}
+    for k in (0, 2):
+        p = picgb.make_params(**dict(g["kw"], SORT_INTERVAL=k))
+        with picgb.Run(p) as r:
+            r.load_particles(0, g["e_in"])
+            r.load_particles(1, g["i_in"])
+            r.initial_boundary()
+            r.step(int(g["nsteps"]))
+            e = r.get_particles(0)
+            res[k] = (r.get_grid("phi"), e[np.lexsort(e.T[::-1])], r.counters()["n_e"])
+    assert np.array_equal(res[0][0], res[2][0])
+    assert res[0][2] == res[2][2]
+    assert np.array_equal(res[0][1], res[2][1])

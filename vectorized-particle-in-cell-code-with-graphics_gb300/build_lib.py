@@ -27,6 +27,7 @@ UNITS = {
     "pgb_particles.cu": [],
     "pgb_walls.cu": [],
     "pgb_fields.cu": ["--fmad=false"],
+    "pgb_sort.cu": [],
 }
 
 

@@ -141,6 +141,13 @@ static void free_lists(pgb_run* r) {
         r->tile_list[l] = r->tile_cnt[l] = r->list[l] = nullptr;
     }
     cudaFree(r->aux_i); cudaFree(r->aux_j); cudaFree(r->cx_tile_sum);
+    for (int q = 0; q < 2; ++q) {
+        cudaFree(r->tile_bin[q]); cudaFree(r->pieces[q]);
+        r->tile_bin[q] = nullptr; r->pieces[q] = nullptr;
+    }
+    cudaFree(r->sort_counts); cudaFree(r->sort_offs); cudaFree(r->sort_key_total); cudaFree(r->sort_key_start);
+    r->sort_counts = r->sort_offs = r->sort_key_total = nullptr;
+    r->sort_key_start = nullptr;
     r->aux_i = r->aux_j = nullptr;
     r->cx_tile_sum = nullptr;
     r->list_cap = 0;
@@ -194,7 +201,26 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
             cudaGetLastError();
             return fail(r, PGB_ERR_NOMEM, "device allocation of scratch failed");
         }
+        int nbx, nby;
+        pgb_bins(r, &nbx, &nby);
+        long long nkeys = (long long)nbx * nby + 1;
+        r->sort_chunks_cap = (lc + 4096 - 1) / 4096 + 1;
+        for (int q = 0; q < 2; ++q) {
+            if (cudaMalloc(&r->tile_bin[q], sizeof(int) * nt) != cudaSuccess ||
+                cudaMalloc(&r->pieces[q], sizeof(int4) * (nt + nkeys + 1)) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(r, PGB_ERR_NOMEM, "device allocation of sort tables failed");
+            }
+        }
+        if (cudaMalloc(&r->sort_counts, sizeof(int) * nkeys * r->sort_chunks_cap) != cudaSuccess ||
+            cudaMalloc(&r->sort_offs, sizeof(int) * nkeys * r->sort_chunks_cap) != cudaSuccess ||
+            cudaMalloc(&r->sort_key_total, sizeof(int) * nkeys) != cudaSuccess ||
+            cudaMalloc(&r->sort_key_start, sizeof(long long) * (nkeys + 1)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(r, PGB_ERR_NOMEM, "device allocation of sort scratch failed");
+        }
         long long cxt = (lc + 4096 - 1) / 4096 + 1;
+        r->cx_tiles_cap = cxt;
         if (cudaMalloc(&r->cx_tile_sum, sizeof(long long) * cxt * r->nx) != cudaSuccess) {
             cudaGetLastError();
             return fail(r, PGB_ERR_NOMEM, "device allocation of CX scratch failed");
@@ -272,7 +298,7 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
         nn = nn / 2 + 1;
     }
     for (int w = 0; w < 2; ++w)
-        ok = ok && cudaMalloc(&r->neut64[w], sizeof(double) * 3 * p->init_no_neutrals) == cudaSuccess;
+        ok = ok && cudaMalloc(&r->neut[w], sizeof(float) * 3 * p->init_no_neutrals) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         fail(nullptr, PGB_ERR_NOMEM, "device allocation failed");
@@ -289,13 +315,17 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
     cudaMemset(r->exy, 0, sizeof(float2) * GE);
     cudaMemset(r->prob_cx, 0, sizeof(long long) * r->nx);
     /* ion table first, then electron table (pic.cpp:135-138) */
-    double* tab = (double*)malloc(sizeof(double) * 3 * p->init_no_neutrals);
-    for (int w = 1; w >= 0; --w) {
-        neutral_table(*p, w, tab);
-        cudaMemcpy(r->neut64[w], tab, sizeof(double) * 3 * p->init_no_neutrals, cudaMemcpyHostToDevice);
+    {
+        const int nn = 3 * p->init_no_neutrals;
+        std::vector<double> tab((size_t)nn);
+        std::vector<float> tab32((size_t)nn);
+        for (int w = 1; w >= 0; --w) {
+            neutral_table(*p, w, tab.data());
+            for (int k = 0; k < nn; ++k) tab32[k] = (float)tab[k];
+            cudaMemcpy(r->neut[w], tab32.data(), sizeof(float) * nn, cudaMemcpyHostToDevice);
+        }
     }
-    free(tab);
-    if (pgb_mg_setup(r)) { g_create_error = r->err; return bail(PGB_ERR_CUDA); }
+    if (pgb_mg_setup(r) || pgb_sort_setup(r)) { g_create_error = r->err; return bail(PGB_ERR_CUDA); }
     if (!pgb_cuda_ok(nullptr, cudaDeviceSynchronize(), "create")) return bail(PGB_ERR_CUDA);
     *out = r;
     return 0;
@@ -317,7 +347,7 @@ extern "C" int pgb_destroy(pgb_run* r) {
     for (int j = 0; j < r->ng; ++j) { cudaFree(r->mg_u[j]); cudaFree(r->mg_f[j]); cudaFree(r->mg_v[j]); cudaFree(r->mg_r[j]); }
     cudaFree(r->mg_tab);
     pgb_mg_free(r);
-    for (int w = 0; w < 2; ++w) cudaFree(r->neut64[w]);
+    for (int w = 0; w < 2; ++w) cudaFree(r->neut[w]);
     if (r->h_stage) cudaFreeHost(r->h_stage);
     cudaFree(r->d_stage);
     if (r->prof_ev_ok)
@@ -371,6 +401,8 @@ extern "C" int pgb_load_species(pgb_run* r, int s, const double* aos6, int64_t n
     PGB_CK(r, cudaMemcpyAsync(&r->ds->n[s], &r->hs->n[s], sizeof(long long), cudaMemcpyHostToDevice, r->stream));
     PGB_CK(r, cudaMemcpyAsync(&r->ds->dead[s], &r->hs->dead[s], sizeof(long long), cudaMemcpyHostToDevice, r->stream));
     PGB_CK(r, cudaMemcpyAsync(&r->ds->next_id[s], &r->hs->next_id[s], sizeof(unsigned), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaMemsetAsync(&r->ds->n_pieces[s], 0, sizeof(int), r->stream));
+    PGB_CK(r, cudaMemsetAsync(&r->ds->sorted_tiles[s], 0, sizeof(long long), r->stream));
     PGB_CK(r, cudaStreamSynchronize(r->stream));
     return 0;
 }
@@ -674,13 +706,22 @@ extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
         int chunk = std::min<int>(nsteps - done, (int)r->phi_tab_cap);
         if ((rc = set_device_step(r, r->time_step, chunk))) return rc;
         for (int k = 0; k < chunk; ++k) {
-            /* compact when tombstones exceed 1/8 of the slots (counts read lazily) */
-            for (int s = 0; s < 2; ++s)
-                if (r->hs->dead[s] * 8 > r->hs->n[s] && r->hs->dead[s] > 0) {
-                    if (pgb_launch_compact(r, s)) return PGB_ERR_CUDA;
-                    r->orient[s] ^= 1;
-                    r->hs->dead[s] = 0;
-                }
+            if (r->p.sort_interval > 0) {
+                /* spatial sort (drops tombstones too) every sort_interval steps */
+                if (r->time_step % r->p.sort_interval == 0)
+                    for (int s = 0; s < 2; ++s) {
+                        if (pgb_launch_sort(r, s)) return PGB_ERR_CUDA;
+                        r->orient[s] ^= 1;
+                    }
+            } else {
+                /* compact when tombstones exceed 1/8 of the slots (counts read lazily) */
+                for (int s = 0; s < 2; ++s)
+                    if (r->hs->dead[s] * 8 > r->hs->n[s] && r->hs->dead[s] > 0) {
+                        if (pgb_launch_compact(r, s)) return PGB_ERR_CUDA;
+                        r->orient[s] ^= 1;
+                        r->hs->dead[s] = 0;
+                    }
+            }
             if (r->prof_on) {
                 if ((rc = sync_state(r))) return rc;
                 r->prof.slots_e += r->hs->n[0];

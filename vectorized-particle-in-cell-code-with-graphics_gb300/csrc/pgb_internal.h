@@ -27,6 +27,10 @@
 #define PGB_FIX_SCALE 4294967296.0   /* deposit fixed point: 2^32 per unit weight */
 #define PGB_MG_SMALL 65        /* levels with n <= 65 are solved by one CTA  */
 #define PGB_MAX_LEVELS 16
+#define PGB_BIN 32             /* bin edge in cells (spatial sort)            */
+#define PGB_HALO 16            /* deposit window halo around a bin, cells     */
+#define PGB_WIN (PGB_BIN + 2 * PGB_HALO + 1)   /* window edge in nodes         */
+#define PGB_PIECE_TILES 16     /* tiles of one bin per work piece             */
 
 enum { ST_ABS_E = 0, ST_ABS_I, ST_PLOP, ST_REFL, ST_BACK, ST_SEE_EV, ST_SEE_EM, ST_ISEE_EM,
        ST_ELASTIC, ST_IONIZE, ST_CX, ST_INJ_E, ST_INJ_I, ST_RED_E, ST_RED_I, ST_COUNT };
@@ -45,6 +49,8 @@ struct DevState {
     int err;
     int pad1;
     long long t;             /* the reference's time_step of the step being run */
+    long long sorted_tiles[2];  /* tiles covered by bin pieces (0 = unsorted)   */
+    int n_pieces[2];
     long long t_base;        /* step of phi_tab[0]                              */
 };
 
@@ -119,7 +125,16 @@ struct pgb_run {
     long long graph_launches[8] = {};      /* kernels in each graph           */
     int use_graphs = 1;
     float* cx_p = nullptr;                 /* per-ion CX probability          */
-    float* cx_tile_sum = nullptr;          /* [tile][column]                  */
+    float* cx_tile_sum = nullptr;          /* [column][tile] (int64)          */
+    long long cx_tiles_cap = 0;
+    /* spatial sort */
+    int* tile_bin[2] = {nullptr, nullptr};
+    int4* pieces[2] = {nullptr, nullptr};
+    int* sort_counts = nullptr;
+    int* sort_offs = nullptr;
+    int* sort_key_total = nullptr;
+    long long* sort_key_start = nullptr;
+    long long sort_chunks_cap = 0;
     /* host staging */
     double* h_stage = nullptr;
     size_t h_stage_bytes = 0;
@@ -158,6 +173,9 @@ int pgb_mg_setup(pgb_run* r);
 void pgb_mg_free(pgb_run* r);
 CollConsts pgb_coll_consts(pgb_run* r);
 int pgb_launch_compact(pgb_run* r, int s);
+int pgb_launch_sort(pgb_run* r, int s);
+int pgb_sort_setup(pgb_run* r);
+void pgb_bins(pgb_run* r, int* nbx, int* nby);
 int pgb_launch_reduce(pgb_run* r, int s);
 int pgb_poisson_solve(pgb_run* r);
 int pgb_launch_efield(pgb_run* r, int advance);

@@ -34,7 +34,9 @@ struct PushArgs {
     int s;
     PushConsts pc;
     CollConsts cc;
-    const double* neut64;       /* electron-neutral table (FP64), 3 x N */
+    const float* neut;          /* electron-neutral table (FP32), 3 x N */
+    const int4* pieces;         /* bin pieces of the last sort              */
+    int nbx;                    /* bins per row                             */
     int* tl_out;                /* per-tile outside list              */
     int* tc_out;
     int* tl_ev;                 /* per-tile ionization-event list     */
@@ -76,7 +78,7 @@ __device__ __forceinline__ void gather_push_one(const PushConsts& pc, const floa
 
 /* electron-neutral collision test and event (e_collisions.cpp:504-562).
  * Returns true if the electron ionized (its velocity is then NaN).        */
-__device__ __forceinline__ bool mcc_one(const CollConsts& cc, const double* neut64, unsigned int id, unsigned int step,
+__device__ __forceinline__ bool mcc_one(const CollConsts& cc, const float* neut, unsigned int id, unsigned int step,
                                         int nx, int ny, float4& p, float& vz, bool& vchanged, int* stats) {
     int jp = cellf(p.x), kp = cellf(p.y);
     if (!(jp >= 0 && jp < nx && kp >= 0 && kp < ny)) return false;
@@ -90,10 +92,7 @@ __device__ __forceinline__ bool mcc_one(const CollConsts& cc, const double* neut
     float P = -expm1f(-(u * cc.e_pcoef * sel));
     bool ion = false;
     if (P > 2.0f * R) {
-        double vx = p.z, vy = p.w, vzz = vz;
-        double e64 = (0.5 / PGB_CHARGE) * cc.me * (vx * vx + vy * vy + vzz * vzz);
-        scatter_fp64(&st, neut64, cc.n_neutral, e64, cc.reduced_mass, vx, vy, vzz);
-        p.z = (float)vx; p.w = (float)vy; vz = (float)vzz;
+        scatter_f32(&st, neut, cc.n_neutral, energy, (float)cc.reduced_mass, p.z, p.w, vz);
         vchanged = true;
         stats[0] += 1;
     }
@@ -102,7 +101,7 @@ __device__ __forceinline__ bool mcc_one(const CollConsts& cc, const double* neut
         pgb_stream si;
         pgb_stream_init(&si, cc.seed, id, step, PGB_STREAM_IONIZE, 0);
         /* positions enter only the products; the parent keeps its position */
-        IonizeOut o = ionize_fp64(&si, neut64, cc.n_neutral, cc, 0.0, 0.0, (double)p.z, (double)p.w, (double)vz);
+        IonizeOut o = ionize_f32(&si, neut, cc.n_neutral, cc, 0.0, 0.0, p.z, p.w, vz);
         p.z = (float)o.evx; p.w = (float)o.evy; vz = (float)o.evz;
         vchanged = true;
         ion = true;
@@ -163,52 +162,105 @@ __device__ __forceinline__ void tile_lists(const bool (&f)[NL][PGB_ITEMS], long 
     __syncthreads();
 }
 
-template <bool MCC, bool DEP, bool FLAG>
+/* deposit into the CTA's shared window when the four nodes fall inside it,
+ * else into the global grid                                               */
+__device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned long long* win, int ox, int oy, int nx,
+                                            float xs, float ys, float w) {
+    int jp = cellf(xs), kp = cellf(ys);
+    int lx = jp - ox, ly = kp - oy;
+    if (win && lx >= 0 && ly >= 0 && lx < PGB_WIN - 1 && ly < PGB_WIN - 1) {
+        float wj = xs - (float)jp, wk = ys - (float)kp;
+        float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
+        float a2 = wk * (1.0f - wj), a1 = wj * wk;
+        const float S = 4294967296.0f;
+        unsigned long long* q = win + ly * PGB_WIN + lx;
+        atomicAdd(q, (unsigned long long)__float2ll_rn(a4 * w * S));
+        atomicAdd(q + 1, (unsigned long long)__float2ll_rn(a3 * w * S));
+        atomicAdd(q + PGB_WIN, (unsigned long long)__float2ll_rn(a2 * w * S));
+        atomicAdd(q + PGB_WIN + 1, (unsigned long long)__float2ll_rn(a1 * w * S));
+    } else {
+        deposit_cell(qacc, nx, xs, ys, w);
+    }
+}
+
+template <bool MCC, bool DEP>
+__device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& pc, int tile, long long n,
+                                          unsigned long long* win, int ox, int oy, unsigned step, int (&st_loc)[2]) {
+    const long long base = (long long)tile * PGB_TILE;
+    bool f[2][PGB_ITEMS];
+#pragma unroll
+    for (int k = 0; k < PGB_ITEMS; ++k) {
+        f[0][k] = false;
+        f[1][k] = false;
+        long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+        if (i >= n) continue;
+        float4 p = a.xv[i];
+        if (is_dead(p.x)) continue;
+        float vz = (MCC || pc.bfield) ? a.vz[i] : 0.0f;
+        bool vchanged = false;
+        if (MCC) f[1][k] = mcc_one(a.cc, a.neut, a.id[i], step, pc.nx, pc.ny, p, vz, vchanged, st_loc);
+        bool moved;
+        gather_push_one(pc, a.exy, p, vz, moved);
+        if (moved || vchanged) a.xv[i] = p;
+        if ((MCC && vchanged) || (pc.bfield && moved)) a.vz[i] = vz;
+        if (DEP && deposit_ok(p.x, p.y, pc.nx, pc.ny)) deposit_win(a.qacc, win, ox, oy, pc.nx, p.x, p.y, a.w[i]);
+        f[0][k] = pc.steady ? outside_steady(p.x, p.y, pc.nx, pc.ny) : outside_absorbing(p.x, p.y, pc.nx, pc.ny);
+    }
+    if (MCC) {
+        int* const tl[2] = {a.tl_out, a.tl_ev};
+        int* const tc[2] = {a.tc_out, a.tc_ev};
+        tile_lists<2>(f, base, tile, tl, tc);
+    } else {
+        bool g[1][PGB_ITEMS];
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k) g[0][k] = f[0][k];
+        int* const tl[1] = {a.tl_out};
+        int* const tc[1] = {a.tc_out};
+        tile_lists<1>(g, base, tile, tl, tc);
+    }
+}
+
+/* Work items: the bin pieces of the last sort (tiles of one bin, deposited
+ * through a shared window), then every tile after the sorted region.     */
+template <bool MCC, bool DEP>
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_push(PushArgs a) {
+    __shared__ unsigned long long s_win[PGB_WIN * PGB_WIN];
     const long long n = a.ds->n[a.s];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    const int npieces = a.ds->n_pieces[a.s];
+    const int tile0 = (int)a.ds->sorted_tiles[a.s];
+    const int nitems = npieces + (ntiles > tile0 ? ntiles - tile0 : 0);
+    const unsigned step = (unsigned)a.ds->t;
     const PushConsts pc = a.pc;
     int st_loc[2] = {0, 0};
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long long base = (long long)tile * PGB_TILE;
-        bool f[2][PGB_ITEMS];
-#pragma unroll
-        for (int k = 0; k < PGB_ITEMS; ++k) {
-            f[0][k] = false;
-            f[1][k] = false;
-            long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
-            if (i >= n) continue;
-            float4 p = a.xv[i];
-            if (is_dead(p.x)) continue;
-            float vz = (MCC || pc.bfield) ? a.vz[i] : 0.0f;
-            bool vchanged = false;
-            if (MCC) {
-                unsigned int id = a.id[i];
-                f[1][k] = mcc_one(a.cc, a.neut64, id, (unsigned int)a.ds->t, pc.nx, pc.ny, p, vz, vchanged, st_loc);
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        if (item < npieces) {
+            int4 pc4 = a.pieces[item];
+            unsigned long long* win = nullptr;
+            int ox = 0, oy = 0;
+            if (DEP && pc4.z >= 0) {
+                win = s_win;
+                ox = (pc4.z % a.nbx) * PGB_BIN - PGB_HALO;
+                oy = (pc4.z / a.nbx) * PGB_BIN - PGB_HALO;
+                for (int k = threadIdx.x; k < PGB_WIN * PGB_WIN; k += blockDim.x) s_win[k] = 0ull;
+                __syncthreads();
             }
-            bool moved;
-            gather_push_one(pc, a.exy, p, vz, moved);
-            if (moved || vchanged) a.xv[i] = p;
-            if ((MCC && vchanged) || (pc.bfield && moved)) a.vz[i] = vz;
-            if (DEP) {
-                if (deposit_ok(p.x, p.y, pc.nx, pc.ny)) deposit_cell(a.qacc, pc.nx, p.x, p.y, a.w[i]);
+            for (int t = pc4.x; t < pc4.x + pc4.y && t < ntiles; ++t)
+                push_tile<MCC, DEP>(a, pc, t, n, win, ox, oy, step, st_loc);
+            if (win) {
+                __syncthreads();
+                for (int k = threadIdx.x; k < PGB_WIN * PGB_WIN; k += blockDim.x) {
+                    unsigned long long v = s_win[k];
+                    if (v) {
+                        int gx = ox + k % PGB_WIN, gy = oy + k / PGB_WIN;
+                        if (gx >= 0 && gy >= 0 && gx < pc.nx && gy < pc.ny)
+                            atomicAdd(&a.qacc[(long long)gy * pc.nx + gx], v);
+                    }
+                }
+                __syncthreads();
             }
-            if (FLAG) f[0][k] = pc.steady ? outside_steady(p.x, p.y, pc.nx, pc.ny)
-                                          : outside_absorbing(p.x, p.y, pc.nx, pc.ny);
-        }
-        if (FLAG) {
-            if (MCC) {
-                int* const tl[2] = {a.tl_out, a.tl_ev};
-                int* const tc[2] = {a.tc_out, a.tc_ev};
-                tile_lists<2>(f, base, tile, tl, tc);
-            } else {
-                bool g[1][PGB_ITEMS];
-#pragma unroll
-                for (int k = 0; k < PGB_ITEMS; ++k) g[0][k] = f[0][k];
-                int* const tl[1] = {a.tl_out};
-                int* const tc[1] = {a.tc_out};
-                tile_lists<1>(g, base, tile, tl, tc);
-            }
+        } else {
+            push_tile<MCC, DEP>(a, pc, tile0 + (item - npieces), n, nullptr, 0, 0, step, st_loc);
         }
     }
     if (MCC) flush_stats(st_loc, a.ds->stats);
@@ -264,7 +316,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_mcc(PushArgs a) {
             if (is_dead(p.x)) continue;
             float vz = a.vz[i];
             bool vchanged = false;
-            f[0][k] = mcc_one(a.cc, a.neut64, a.id[i], (unsigned int)a.ds->t, a.pc.nx, a.pc.ny, p, vz, vchanged, st_loc);
+            f[0][k] = mcc_one(a.cc, a.neut, a.id[i], (unsigned int)a.ds->t, a.pc.nx, a.pc.ny, p, vz, vchanged, st_loc);
             if (vchanged) { a.xv[i] = p; a.vz[i] = vz; }
         }
         int* const tla[1] = {a.tl_ev};
@@ -434,7 +486,7 @@ struct IonizeAppendArgs {
     DevState* ds;
     const int* ev;               /* dense event list (electron slots)      */
     CollConsts cc;
-    const double* neut64;
+    const float* neut;
     double dx, dy;
     int store_e, store_i;
 };
@@ -453,7 +505,7 @@ __global__ void k_ionize_append(IonizeAppendArgs a) {
         pgb_stream_init(&si, a.cc.seed, pid, (unsigned int)a.ds->t, PGB_STREAM_IONIZE, 0);
         float4 pp = a.e.xv[slot];
         double xe = (double)pp.x * a.dx, ye = (double)pp.y * a.dy;
-        IonizeOut o = ionize_fp64(&si, a.neut64, a.cc.n_neutral, a.cc, xe, ye, 0.0, 0.0, 0.0);
+        IonizeOut o = ionize_f32(&si, a.neut, a.cc.n_neutral, a.cc, xe, ye, 0.0f, 0.0f, 0.0f);
         if (a.store_i) {
             long long s2 = ni0 + r;
             if (s2 < a.i.cap) {
@@ -546,6 +598,8 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_compact(Species S, DevStat
 __global__ void k_compact_commit(DevState* ds, int s, const long long* total) {
     ds->n[s] = *total;
     ds->dead[s] = 0;
+    ds->n_pieces[s] = 0;       /* slot order changed: the bin pieces are gone */
+    ds->sorted_tiles[s] = 0;
 }
 
 /* ------------------------------------------------------------ load / dump */
@@ -644,7 +698,12 @@ static PushArgs push_args(pgb_run* r, int s) {
     a.exy = r->exy; a.qacc = r->qacc[s]; a.ds = r->ds; a.s = s;
     a.pc = push_consts(r, s);
     a.cc = pgb_coll_consts(r);
-    a.neut64 = r->neut64[0];
+    a.neut = r->neut[0];
+    a.pieces = r->pieces[s];
+    {
+        int nby;
+        pgb_bins(r, &a.nbx, &nby);
+    }
     a.tl_out = r->tile_list[s == 0 ? LIST_OUT_E : LIST_OUT_I];
     a.tc_out = r->tile_cnt[s == 0 ? LIST_OUT_E : LIST_OUT_I];
     a.tl_ev = r->tile_list[LIST_ION_EV];
@@ -656,10 +715,10 @@ int pgb_launch_push(pgb_run* r, int s, bool mcc, bool deposit, bool flag_ion) {
     (void)flag_ion;
     PushArgs a = push_args(r, s);
     int g = grid_for(r, 8);
-    if (mcc && deposit) k_push<true, true, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
-    else if (mcc) k_push<true, false, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
-    else if (deposit) k_push<false, true, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
-    else k_push<false, false, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    if (mcc && deposit) k_push<true, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    else if (mcc) k_push<true, false><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    else if (deposit) k_push<false, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    else k_push<false, false><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -718,7 +777,7 @@ int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e) {
 int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i) {
     IonizeAppendArgs a;
     a.e = r->sp[0]; a.i = r->sp[1]; a.ds = r->ds; a.ev = r->list[LIST_ION_EV];
-    a.cc = pgb_coll_consts(r); a.neut64 = r->neut64[0];
+    a.cc = pgb_coll_consts(r); a.neut = r->neut[0];
     a.dx = r->dx; a.dy = r->dy;
     a.store_e = store_e;
     a.store_i = store_i;

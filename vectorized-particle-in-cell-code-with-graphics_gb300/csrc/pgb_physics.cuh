@@ -142,70 +142,81 @@ __device__ __forceinline__ float sigma_cx(const CollConsts& c, float e) {
 }
 
 /* ------------------------------------------------ electron collisions */
-/* collisions::scattered_velocity (collisions.cpp:107-171), FP64 */
-__device__ inline void scatter_fp64(pgb_stream* st, const double* neut, int nn, double energy, double cf,
-                                    double& vx, double& vy, double& vz) {
-    const double two_pi = 2.0 * PGB_PI;
-    double R = pgb_u01d(pgb_stream_u32(st)), cosChi;
-    if (energy < 1.0e-2) cosChi = sqrt(1.0 - R);
-    else cosChi = 2.0 * (1.0 - pow((1.0 + energy), R)) / energy + 1.0;
-    double sinChi = sqrt(1.0 - cosChi * cosChi);
-    double cosPhi = cos(two_pi * R), sinPhi = sin(two_pi * R);
+/* collisions::scattered_velocity (collisions.cpp:107-171) in FP32.  The
+ * scattering angle cosChi = 2(1-(1+E)^R)/E + 1 is evaluated as
+ * 1 - t with t = 2*expm1(R*log1p(E))/E, and sinChi = sqrt(t(2-t)): the same
+ * values without the cancellation of 1-(1+E)^R and of 1-cosChi^2 that FP32
+ * would otherwise suffer near forward scattering.  Events are rare (a few
+ * per cent of the particles per step), and FP64 here would run at 1/64 rate
+ * on a divergent warp.                                                    */
+__device__ __forceinline__ void scatter_f32(pgb_stream* st, const float* neut, int nn, float energy, float cf,
+                                            float& vx, float& vy, float& vz) {
+    const float two_pi = (float)(2.0 * PGB_PI);
+    float R = pgb_u01f(pgb_stream_u32(st));
+    float t;   /* 1 - cosChi */
+    if (energy < 1.0e-2f) t = 1.0f - sqrtf(1.0f - R);
+    else t = 2.0f * expm1f(R * log1pf(energy)) / energy;
+    float cosChi = 1.0f - t;
+    float sinChi = sqrtf(fmaxf(t * (2.0f - t), 0.0f));
+    float sinPhi, cosPhi;
+    sincosf(two_pi * R, &sinPhi, &cosPhi);
     int index = (int)(pgb_stream_u32(st) % (uint32_t)(nn - 1));
-    double nvx = neut[index], nvy = neut[nn + index], nvz = neut[2 * nn + index];
-    double ux = vx - nvx, uy = vy - nvy, uz = vz - nvz;
-    double uperp = sqrt(uy * uy + uz * uz);
-    double u = sqrt(ux * ux + uperp * uperp);
-    double uyp, uzp;
-    if (uperp < 1.0) { uyp = 1.0; uzp = 1.0; }
+    float nvx = neut[index], nvy = neut[nn + index], nvz = neut[2 * nn + index];
+    float ux = vx - nvx, uy = vy - nvy, uz = vz - nvz;
+    float uperp = sqrtf(uy * uy + uz * uz);
+    float u = sqrtf(ux * ux + uperp * uperp);
+    float uyp, uzp;
+    if (uperp < 1.0f) { uyp = 1.0f; uzp = 1.0f; }
     else { uyp = uy / uperp; uzp = uz / uperp; }
-    vz -= cf * (uz * (1.0 - cosChi) - (ux * uzp * cosPhi - u * uyp * sinPhi) * sinChi);
-    vy -= cf * (uy * (1.0 - cosChi) - (ux * uyp * cosPhi + u * uzp * sinPhi) * sinChi);
-    vx -= cf * (ux * (1.0 - cosChi) + uperp * cosPhi * sinChi);
+    (void)cosChi;
+    vz -= cf * (uz * t - (ux * uzp * cosPhi - u * uyp * sinPhi) * sinChi);
+    vy -= cf * (uy * t - (ux * uyp * cosPhi + u * uzp * sinPhi) * sinChi);
+    vx -= cf * (ux * t + uperp * cosPhi * sinChi);
 }
 
-/* e_collisions::ionization (e_collisions.cpp:319-443), FP64.  The excess
- * energy mixes J and eV (line 377) and is negative, so every output is NaN
- * as in the reference.  Returns the parent's new velocity and the new
- * electron/ion states (positions in metres).                              */
+/* e_collisions::ionization (e_collisions.cpp:319-443).  The excess energy
+ * mixes J and eV (line 377) and is negative, so every output is NaN as in
+ * the reference.  Returns the parent's new velocity and the new electron
+ * and ion states (positions in metres).                                   */
 struct IonizeOut {
-    double evx, evy, evz;             /* parent electron after               */
-    double nx_, ny_, nvx, nvy, nvz;   /* new electron                        */
-    double ix, iy, ivx, ivy, ivz;     /* new ion                             */
+    float evx, evy, evz;              /* parent electron after               */
+    double nx_, ny_;                  /* new electron position               */
+    float nvx, nvy, nvz;
+    double ix, iy;                    /* new ion position                    */
+    float ivx, ivy, ivz;
 };
-__device__ inline IonizeOut ionize_fp64(pgb_stream* st, const double* neut, int nn, const CollConsts& c,
-                                        double xe, double ye, double vxe, double vye, double vze) {
-    const double me = c.me, mi = c.mi;
-    double reduced_mass = c.reduced_mass * me;
-    double R = pgb_u01d(pgb_stream_u32(st));
-    double Rxe = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
-    double Rye = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
-    double Rze = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
-    double R2xe = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
-    double R2ye = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
-    double R2ze = 1.0 - 2.0 * pgb_u01d(pgb_stream_u32(st));
+__device__ inline IonizeOut ionize_f32(pgb_stream* st, const float* neut, int nn, const CollConsts& c,
+                                       double xe, double ye, float vxe, float vye, float vze) {
+    const float me = (float)c.me, mi = (float)c.mi;
+    float reduced_mass = (float)(c.reduced_mass * c.me);
+    float R = pgb_u01f(pgb_stream_u32(st));
+    float Rxe = 1.0f - 2.0f * pgb_u01f(pgb_stream_u32(st));
+    float Rye = 1.0f - 2.0f * pgb_u01f(pgb_stream_u32(st));
+    float Rze = 1.0f - 2.0f * pgb_u01f(pgb_stream_u32(st));
+    float R2xe = 1.0f - 2.0f * pgb_u01f(pgb_stream_u32(st));
+    float R2ye = 1.0f - 2.0f * pgb_u01f(pgb_stream_u32(st));
+    float R2ze = 1.0f - 2.0f * pgb_u01f(pgb_stream_u32(st));
     int index = (int)(pgb_stream_u32(st) % (uint32_t)(nn - 1));
-    double nvx = neut[index], nvy = neut[nn + index], nvz = neut[2 * nn + index];
-    double Wx = (mi * nvx + me * vxe) / (mi + me);
-    double Wy = (mi * nvy + me * vye) / (mi + me);
-    double Wz = (mi * nvz + me * vze) / (mi + me);
-    double ve = sqrt(vxe * vxe + vye * vye + vze * vze);
-    double vn = sqrt(nvx * nvx + nvy * nvy + nvz * nvz);
-    double excess = (reduced_mass / 2.0) * (ve - vn) * (ve - vn) - c.threshold;
-    double ve_after = sqrt(2.0 * R * excess / me);
-    double v2e_after = sqrt(2.0 * (1.0 - R) * excess / me);
-    double a0 = ve_after * Rxe, a1 = ve_after * Rye, a2 = ve_after * Rze;
-    double b0 = v2e_after * R2xe, b1 = v2e_after * R2ye, b2 = v2e_after * R2ze;
+    float nvx = neut[index], nvy = neut[nn + index], nvz = neut[2 * nn + index];
+    float mr = me / (mi + me), nr = mi / (mi + me);
+    float Wx = nr * nvx + mr * vxe, Wy = nr * nvy + mr * vye, Wz = nr * nvz + mr * vze;
+    float ve = sqrtf(vxe * vxe + vye * vye + vze * vze);
+    float vn = sqrtf(nvx * nvx + nvy * nvy + nvz * nvz);
+    float excess = (reduced_mass / 2.0f) * (ve - vn) * (ve - vn) - (float)c.threshold;
+    float ve_after = sqrtf(2.0f * R * excess / me);
+    float v2e_after = sqrtf(2.0f * (1.0f - R) * excess / me);
+    float a0 = ve_after * Rxe, a1 = ve_after * Rye, a2 = ve_after * Rze;
+    float b0 = v2e_after * R2xe, b1 = v2e_after * R2ye, b2 = v2e_after * R2ze;
     IonizeOut o;
     o.ivx = Wx - (me / mi) * (a0 + b0);
     o.ivy = Wy - (me / mi) * (a1 + b1);
     o.ivz = Wz - (me / mi) * (a2 + b2);
-    o.ix = xe + o.ivx * c.dti;
-    o.iy = ye + o.ivy * c.dti;
+    o.ix = xe + (double)o.ivx * c.dti;
+    o.iy = ye + (double)o.ivy * c.dti;
     o.evx = a0 + Wx; o.evy = a1 + Wy; o.evz = a2 + Wz;
     o.nvx = b0 + Wx; o.nvy = b1 + Wy; o.nvz = b2 + Wz;
-    o.nx_ = xe + o.nvx * c.dt;
-    o.ny_ = ye + o.nvy * c.dt;
+    o.nx_ = xe + (double)o.nvx * c.dt;
+    o.ny_ = ye + (double)o.nvy * c.dt;
     return o;
 }
 

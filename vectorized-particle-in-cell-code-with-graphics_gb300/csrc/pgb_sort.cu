@@ -1,0 +1,240 @@
+/*
+ * Spatial binning of the particles (stable counting sort by bin).
+ *
+ * The deposit (particle::collect_charge, pic.cl:22-52) scatters four adds
+ * per particle; on particles in arbitrary order they land on random grid
+ * nodes and the adds go to L2 as global atomics.  Every sort_interval steps
+ * the particles of a species are re-ordered by bin (BIN x BIN cells), each
+ * bin starting on a 1024-slot tile boundary, so the push kernel can give a
+ * CTA a run of tiles of one bin and accumulate its deposit in a shared-
+ * memory window of the bin's nodes plus a halo.
+ *
+ * The sort is stable (particles keep their relative order within a bin),
+ * so the resulting order -- and every order-dependent rule that follows it
+ * (charge-exchange accumulation, wall-list order) -- is deterministic.  It
+ * also drops removed particles (tombstones).  Passes:
+ *   count    per chunk of 4096 slots, a shared histogram of bin keys
+ *   scan     per bin over chunks, then over bins with tile padding
+ *   scatter  one warp per chunk walks its slots in order and writes each
+ *            particle to its bin at a running per-bin cursor
+ *   pieces   tile -> bin map and work pieces (runs of tiles of one bin)
+ */
+#include <cuda_runtime.h>
+#include "pgb_internal.h"
+#include "pgb_physics.cuh"
+
+#define SORT_CHUNK 4096
+
+struct SortArgs {
+    Species S;
+    DevState* ds;
+    int s;
+    int nx, ny;              /* nodes */
+    int nbx, nby, nbins;     /* bins; key nbins = not in the deposit region */
+    long long nchunks_cap;
+    int* counts;             /* [key][chunk] */
+    int* offs;               /* [key][chunk] exclusive within the key */
+    int* key_total;          /* [key] */
+    long long* key_start;    /* [key+1] padded starts */
+    int* tile_bin;           /* [tile] */
+    int4* pieces;            /* {first tile, tiles, bin, 0} */
+    int piece_tiles;
+};
+
+__device__ __forceinline__ int bin_key(float4 p, int nx, int ny, int nbx, int nbins) {
+    if (is_dead(p.x)) return -1;
+    int jp = cellf(p.x), kp = cellf(p.y);
+    /* the deposit region of collectCharge (pic.cl:35) */
+    if (!(jp < nx - 1 && p.x > 0.0f && kp < ny - 1 && p.y > 0.0f)) return nbins;
+    return (kp / PGB_BIN) * nbx + (jp / PGB_BIN);
+}
+
+__global__ void __launch_bounds__(256) k_sort_count(SortArgs a) {
+    extern __shared__ int s_hist[];
+    const long long n = a.ds->n[a.s];
+    const int nch = (int)((n + SORT_CHUNK - 1) / SORT_CHUNK);
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        for (int k = threadIdx.x; k <= a.nbins; k += blockDim.x) s_hist[k] = 0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < SORT_CHUNK; k += blockDim.x) {
+            long long i = (long long)c * SORT_CHUNK + k;
+            if (i >= n) break;
+            int key = bin_key(a.S.xv[i], a.nx, a.ny, a.nbx, a.nbins);
+            if (key >= 0) atomicAdd(&s_hist[key], 1);
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k <= a.nbins; k += blockDim.x) a.counts[(long long)k * a.nchunks_cap + c] = s_hist[k];
+        __syncthreads();
+    }
+}
+
+/* per key: exclusive scan over the live chunks */
+__global__ void __launch_bounds__(256) k_sort_scan_keys(SortArgs a) {
+    const long long n = a.ds->n[a.s];
+    const int nch = (int)((n + SORT_CHUNK - 1) / SORT_CHUNK);
+    __shared__ int s_w[8];
+    __shared__ int s_carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int key = blockIdx.x; key <= a.nbins; key += gridDim.x) {
+        const int* row = a.counts + (long long)key * a.nchunks_cap;
+        int* out = a.offs + (long long)key * a.nchunks_cap;
+        if (threadIdx.x == 0) s_carry = 0;
+        __syncthreads();
+        for (int b = 0; b < nch; b += 256) {
+            int c = b + threadIdx.x;
+            int v = c < nch ? row[c] : 0;
+            int x = v;
+            for (int d = 1; d < 32; d <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= d) x += y;
+            }
+            if (lane == 31) s_w[warp] = x;
+            __syncthreads();
+            int wo = 0;
+            for (int w = 0; w < warp; ++w) wo += s_w[w];
+            if (c < nch) out[c] = s_carry + wo + x - v;
+            __syncthreads();
+            if (threadIdx.x == 0) for (int w = 0; w < 8; ++w) s_carry += s_w[w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) a.key_total[key] = s_carry;
+        __syncthreads();
+    }
+}
+
+/* over keys: padded starts (each key begins on a tile boundary), pieces */
+__global__ void __launch_bounds__(1024) k_sort_scan_bins(SortArgs a) {
+    __shared__ long long s_tot;
+    __shared__ int s_np;
+    if (threadIdx.x == 0) {
+        long long acc = 0;
+        int np = 0;
+        for (int key = 0; key <= a.nbins; ++key) {
+            a.key_start[key] = acc;
+            long long c = a.key_total[key];
+            long long tiles = (c + PGB_TILE - 1) / PGB_TILE;
+            int bin = key < a.nbins ? key : -1;
+            for (long long t = 0; t < tiles; t += a.piece_tiles) {
+                int len = (int)((tiles - t) < a.piece_tiles ? (tiles - t) : a.piece_tiles);
+                a.pieces[np++] = make_int4((int)(acc / PGB_TILE + t), len, bin, 0);
+            }
+            acc += tiles * PGB_TILE;
+        }
+        a.key_start[a.nbins + 1] = acc;
+        s_tot = acc;
+        s_np = np;
+    }
+    __syncthreads();
+    /* tile -> bin map */
+    for (int key = 0; key <= a.nbins; ++key) {
+        long long t0 = a.key_start[key] / PGB_TILE, t1 = a.key_start[key + 1] / PGB_TILE;
+        for (long long t = t0 + threadIdx.x; t < t1; t += blockDim.x) a.tile_bin[t] = key < a.nbins ? key : -1;
+    }
+    if (threadIdx.x == 0) {
+        a.ds->n_pieces[a.s] = s_np;
+        a.ds->sorted_tiles[a.s] = s_tot / PGB_TILE;
+    }
+}
+
+/* one warp per chunk: stable placement at per-key cursors */
+__global__ void __launch_bounds__(256) k_sort_scatter(SortArgs a) {
+    extern __shared__ long long s_cur[];   /* [warp][key] */
+    const long long n = a.ds->n[a.s];
+    const int nch = (int)((n + SORT_CHUNK - 1) / SORT_CHUNK);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    long long* cur = s_cur + (long long)warp * (a.nbins + 1);
+    const unsigned lt = (1u << lane) - 1u;
+    for (int c = blockIdx.x * nw + warp; c < nch; c += gridDim.x * nw) {
+        for (int k = lane; k <= a.nbins; k += 32) cur[k] = a.key_start[k] + a.offs[(long long)k * a.nchunks_cap + c];
+        __syncwarp();
+        for (int b = 0; b < SORT_CHUNK; b += 32) {
+            long long i = (long long)c * SORT_CHUNK + b + lane;
+            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+            int key = -1;
+            if (i < n) {
+                p = a.S.xv[i];
+                key = bin_key(p, a.nx, a.ny, a.nbx, a.nbins);
+            }
+            unsigned peers = __match_any_sync(0xffffffffu, key);
+            long long pos = -1;
+            if (key >= 0) pos = cur[key] + __popc(peers & lt);
+            __syncwarp();
+            if (key >= 0 && (peers & lt) == 0) cur[key] += __popc(peers);
+            __syncwarp();
+            if (key >= 0) {
+                a.S.xv2[pos] = p;
+                a.S.vz2[pos] = a.S.vz[i];
+                a.S.w2[pos] = a.S.w[i];
+                a.S.id2[pos] = a.S.id[i];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+/* tombstones in the padding after each key's particles; new counts */
+__global__ void k_sort_pad(SortArgs a) {
+    for (int key = blockIdx.x; key <= a.nbins; key += gridDim.x) {
+        long long s0 = a.key_start[key] + a.key_total[key], s1 = a.key_start[key + 1];
+        for (long long i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+            a.S.xv2[i] = make_float4(-INFINITY, 0.f, 0.f, 0.f);
+            a.S.vz2[i] = 0.f;
+            a.S.w2[i] = 0.f;
+            a.S.id2[i] = 0u;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        long long live = 0;
+        for (int key = 0; key <= a.nbins; ++key) live += a.key_total[key];
+        long long tot = a.key_start[a.nbins + 1];
+        a.ds->n[a.s] = tot;
+        a.ds->dead[a.s] = tot - live;
+    }
+}
+
+/* ============================================================ host side */
+void pgb_bins(pgb_run* r, int* nbx, int* nby) {
+    *nbx = (r->nx - 1 + PGB_BIN - 1) / PGB_BIN;
+    *nby = (r->ny - 1 + PGB_BIN - 1) / PGB_BIN;
+}
+
+int pgb_launch_sort(pgb_run* r, int s) {
+    SortArgs a;
+    a.S = r->sp[s]; a.ds = r->ds; a.s = s; a.nx = r->nx; a.ny = r->ny;
+    pgb_bins(r, &a.nbx, &a.nby);
+    a.nbins = a.nbx * a.nby;
+    a.nchunks_cap = r->sort_chunks_cap;
+    a.counts = r->sort_counts; a.offs = r->sort_offs; a.key_total = r->sort_key_total;
+    a.key_start = r->sort_key_start; a.tile_bin = r->tile_bin[s]; a.pieces = r->pieces[s];
+    a.piece_tiles = PGB_PIECE_TILES;
+    size_t hist = sizeof(int) * (a.nbins + 1);
+    k_sort_count<<<r->sms * 4, 256, hist, r->stream>>>(a);
+    r->launches++;
+    k_sort_scan_keys<<<r->sms * 2, 256, 0, r->stream>>>(a);
+    r->launches++;
+    k_sort_scan_bins<<<1, 1024, 0, r->stream>>>(a);
+    r->launches++;
+    size_t cur = sizeof(long long) * (a.nbins + 1) * 8;
+    k_sort_scatter<<<r->sms * 4, 256, cur, r->stream>>>(a);
+    r->launches++;
+    k_sort_pad<<<r->sms, 256, 0, r->stream>>>(a);
+    r->launches++;
+    PGB_CK(r, cudaGetLastError());
+    Species& S = r->sp[s];
+    std::swap(S.xv, S.xv2);
+    std::swap(S.vz, S.vz2);
+    std::swap(S.w, S.w2);
+    std::swap(S.id, S.id2);
+    return 0;
+}
+
+int pgb_sort_setup(pgb_run* r) {
+    int nbx, nby;
+    pgb_bins(r, &nbx, &nby);
+    int nbins = nbx * nby;
+    size_t cur = sizeof(long long) * (nbins + 1) * 8;
+    if (cur > 48 * 1024) PGB_CK(r, cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cur));
+    size_t hist = sizeof(int) * (nbins + 1);
+    if (hist > 48 * 1024) PGB_CK(r, cudaFuncSetAttribute(k_sort_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist));
+    return 0;
+}

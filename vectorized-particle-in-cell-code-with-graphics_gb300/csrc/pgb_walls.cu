@@ -415,9 +415,10 @@ struct CxArgs {
     int nx, ny;
     float pcoef, ecoef;      /* DTI*1e-20*n_g, (0.5/CHARGE)*MI */
     CollConsts cc;
-    long long* tile_sum;     /* [tile][column] fixed point */
+    long long* tile_sum;     /* [column][tile] fixed point */
+    long long ntl;           /* tiles capacity (row length of tile_sum) */
     long long* col_acc;      /* per-column accumulator carried across steps (fixed point) */
-    const double* neut64_i;  /* ion-neutral table */
+    const float* neut_i;     /* ion-neutral table (FP32) */
     uint64_t seed;
 };
 
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
             if (col >= 0 && pf) atomicAdd(&s_sum[col], (unsigned long long)pf);
         }
         __syncthreads();
-        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) a.tile_sum[(long long)t * a.nx + c] = (long long)s_sum[c];
+        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) a.tile_sum[(long long)c * a.ntl + t] = (long long)s_sum[c];
         __syncthreads();
     }
 }
@@ -464,9 +465,18 @@ __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
     const int ntiles = (int)((n + CX_TILE - 1) / CX_TILE);
     long long acc = a.col_acc[col];
     int fired = 0;
+    const long long* row = a.tile_sum + (long long)col * a.ntl;
+    /* most columns do not reach 1 in a step: test the column total first */
+    long long tot = 0;
+    for (int t = lane; t < ntiles; t += 32) tot += row[t];
+    for (int d = 16; d; d >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, d);
+    if (acc + tot <= CX_ONE) {
+        if (lane == 0) a.col_acc[col] = acc + tot;
+        return;
+    }
     for (int t0 = 0; t0 < ntiles; t0 += 32) {
         int t = t0 + lane;
-        long long s = (t < ntiles) ? a.tile_sum[(long long)t * a.nx + col] : 0;
+        long long s = (t < ntiles) ? row[t] : 0;
         /* inclusive prefix over the 32 tiles */
         long long ps = s;
         for (int d = 1; d < 32; d <<= 1) {
@@ -505,10 +515,10 @@ __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
                         int nn = a.cc.n_neutral;
                         int index = (int)(pgb_stream_u32(&st) % (uint32_t)(nn - 1));
                         float4 p = a.i.xv[i];
-                        p.z = (float)a.neut64_i[index];
-                        p.w = (float)a.neut64_i[nn + index];
+                        p.z = a.neut_i[index];
+                        p.w = a.neut_i[nn + index];
                         a.i.xv[i] = p;
-                        a.i.vz[i] = (float)a.neut64_i[2 * nn + index];
+                        a.i.vz[i] = a.neut_i[2 * nn + index];
                     }
                     fired++;
                 }
@@ -583,8 +593,9 @@ int pgb_launch_cx(pgb_run* r) {
     a.cc = pgb_coll_consts(r);
     a.pcoef = a.cc.i_pcoef; a.ecoef = a.cc.i_energy_coef;
     a.tile_sum = (long long*)r->cx_tile_sum;
+    a.ntl = r->cx_tiles_cap;
     a.col_acc = (long long*)r->prob_cx;
-    a.neut64_i = r->neut64[1];
+    a.neut_i = r->neut[1];
     a.seed = r->p.seed;
     k_cx_tiles<<<r->sms * 4, 256, sizeof(unsigned long long) * r->nx, r->stream>>>(a);
     r->launches++;
