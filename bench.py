@@ -46,7 +46,7 @@ ALG_BYTES = 48          # per particle-step: read x,y,vx,vy,vz,w,id (28 B) + wri
 METRIC = "particle-steps/s"
 
 
-def workload_params(picgb, seed=1003, n_per_species=N_PER_SPECIES, poisson="FMG32"):
+def workload_params(picgb, seed=1003, n_per_species=N_PER_SPECIES, poisson="FMG32", sort_interval=0):
     """H preset ("H with coll-boundary") at 513^2 nodes and Te = 3 eV.  The
     macro-particle size is set so that the mean density equals the design
     density ELECTRON_PARTICLE_DENSITY = 1e15 m^-3 (parameters.h:71) for
@@ -55,7 +55,7 @@ def workload_params(picgb, seed=1003, n_per_species=N_PER_SPECIES, poisson="FMG3
               HAVE_COLLISIONS=True, SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT",
               SIGMA_IONIZATION="ENERGY_DEPENDENT", E_IMPACT_SEE="YES", ION_IMPACT_SEE="NO", REFLECTION="YES",
               BACKSCATTER="YES", STEADYSTATE="NO", NUMBER_TO_INJECT=10, SIZE_TO_CHECK=2**31 - 1, RAND_SEED=seed,
-              POISSON=poisson)
+              POISSON=poisson, SORT_INTERVAL=sort_interval)
     L = picgb.make_params(**kw).xlength
     size = 1.0e15 * L * L / n_per_species
     return picgb.make_params(E_MACROPARTICLE_SIZE=size, ION_MACROPARTICLE_SIZE=size, **kw)
@@ -179,7 +179,7 @@ def run_gpu(args, rank, world):
     build_lib.build()
     torch.cuda.set_device(rank % max(torch.cuda.device_count(), 1))
     n = int(N_PER_SPECIES * args.scale)
-    p = workload_params(picgb, seed=1003 + rank, n_per_species=n, poisson=args.poisson)
+    p = workload_params(picgb, seed=1003 + rank, n_per_species=n, poisson=args.poisson, sort_interval=args.sort)
     e, i = gaussian_state(p, n, 3.0, 0.026, 1003 + rank, p.ion_mass)
     run = picgb.Run(p)
     run.load_particles(0, e)
@@ -250,6 +250,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--poisson", default="FMG32", choices=["FMG32", "FMG_REF", "FP32_DC"])
+    ap.add_argument("--sort", type=int, default=8, help="spatial sort every k steps (0 = off)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -262,7 +263,7 @@ def main():
               "poisson": {"FMG32": "full multigrid, reference schedule, FP32",
                           "FMG_REF": "full multigrid, reference schedule, FP64 (bit-identical)",
                           "FP32_DC": "FP32 full multigrid + FP64 defect correction"}[args.poisson],
-              "macro_particle_size": "mean density 1e15 m^-3",
+              "macro_particle_size": "mean density 1e15 m^-3", "sort_interval": args.sort,
               "parallelism": "replicas" if world > 1 else "single"}
     threads = os.cpu_count() or 1
     if args.impl == "reference":

@@ -449,9 +449,10 @@ static int set_device_step(pgb_run* r, int64_t t0, int n) {
     if (n > r->phi_tab_cap) return fail(r, PGB_ERR_ARG, "step table too small");
     std::vector<double> tab((size_t)n);
     for (int k = 0; k < n; ++k) tab[k] = r->p.phi_right * cos(r->p.phi_period * (double)(t0 + k));
-    long long tt[2] = {(long long)t0, (long long)t0};
+    long long tt = (long long)t0;
     PGB_CK(r, cudaMemcpyAsync(r->phi_tab, tab.data(), sizeof(double) * n, cudaMemcpyHostToDevice, r->stream));
-    PGB_CK(r, cudaMemcpyAsync(&r->ds->t, tt, sizeof(tt), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaMemcpyAsync(&r->ds->t, &tt, sizeof(tt), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaMemcpyAsync(&r->ds->t_base, &tt, sizeof(tt), cudaMemcpyHostToDevice, r->stream));
     PGB_CK(r, cudaStreamSynchronize(r->stream));
     return 0;
 }
