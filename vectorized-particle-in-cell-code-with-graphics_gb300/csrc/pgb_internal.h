@@ -30,7 +30,7 @@
 #define PGB_BIN 32             /* bin edge in cells (spatial sort)            */
 #define PGB_HALO 16            /* deposit window halo around a bin, cells     */
 #define PGB_WIN (PGB_BIN + 2 * PGB_HALO + 1)   /* window edge in nodes         */
-#define PGB_PIECE_TILES 16     /* tiles of one bin per work piece             */
+#define PGB_PIECE_TILES 64     /* tiles of one bin per work piece             */
 
 enum { ST_ABS_E = 0, ST_ABS_I, ST_PLOP, ST_REFL, ST_BACK, ST_SEE_EV, ST_SEE_EM, ST_ISEE_EM,
        ST_ELASTIC, ST_IONIZE, ST_CX, ST_INJ_E, ST_INJ_I, ST_RED_E, ST_RED_I, ST_COUNT };
