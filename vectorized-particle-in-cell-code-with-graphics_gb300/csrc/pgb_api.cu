@@ -285,6 +285,7 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
     ok = ok && cudaMalloc(&r->exy, sizeof(float2) * GE) == cudaSuccess;
     ok = ok && cudaMalloc(&r->prob_cx, sizeof(long long) * r->nx) == cudaSuccess;
     r->phi_tab_cap = 4096;
+    ok = ok && cudaMalloc(&r->inject_flag, sizeof(int) * (p->number_to_inject + 1)) == cudaSuccess;
     ok = ok && cudaMalloc(&r->phi_tab, sizeof(double) * r->phi_tab_cap) == cudaSuccess;
     int ng = 0, nn = r->nx;
     while (nn >>= 1) ng++;
@@ -314,6 +315,7 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
     cudaMemset(r->ey, 0, sizeof(double) * GE);
     cudaMemset(r->exy, 0, sizeof(float2) * GE);
     cudaMemset(r->prob_cx, 0, sizeof(long long) * r->nx);
+    cudaMemset(r->inject_flag, 0, sizeof(int) * (p->number_to_inject + 1));
     /* ion table first, then electron table (pic.cpp:135-138) */
     {
         const int nn = 3 * p->init_no_neutrals;
@@ -336,6 +338,7 @@ extern "C" int pgb_destroy(pgb_run* r) {
     if (r->stream) cudaStreamSynchronize(r->stream);
     drop_graphs(r);
     cudaFree(r->phi_tab);
+    cudaFree(r->inject_flag);
     free_species(r->sp[0]);
     free_species(r->sp[1]);
     free_lists(r);

@@ -28,9 +28,9 @@
 #define PGB_MG_SMALL 65        /* levels with n <= 65 are solved by one CTA  */
 #define PGB_MAX_LEVELS 16
 #define PGB_BIN 32             /* bin edge in cells (spatial sort)            */
-#define PGB_HALO 16            /* deposit window halo around a bin, cells     */
+#define PGB_HALO 8             /* deposit window halo around a bin, cells     */
 #define PGB_WIN (PGB_BIN + 2 * PGB_HALO + 1)   /* window edge in nodes         */
-#define PGB_PIECE_TILES 64     /* tiles of one bin per work piece             */
+#define PGB_PIECE_TILES 4      /* tiles of one bin per work piece             */
 
 enum { ST_ABS_E = 0, ST_ABS_I, ST_PLOP, ST_REFL, ST_BACK, ST_SEE_EV, ST_SEE_EM, ST_ISEE_EM,
        ST_ELASTIC, ST_IONIZE, ST_CX, ST_INJ_E, ST_INJ_I, ST_RED_E, ST_RED_I, ST_COUNT };
@@ -112,6 +112,7 @@ struct pgb_run {
     long long list_cap = 0;   /* = max particle capacity                       */
     long long ntiles_cap = 0;
     int* aux_i = nullptr;     /* scratch ints (wall passes), list_cap entries  */
+    int* inject_flag = nullptr;   /* NUMBER_TO_INJECT flags                     */
     int* aux_j = nullptr;
     /* collisions */
     float* neut[2] = {nullptr, nullptr};   /* [which]: 3 x N_neutral, FP32    */

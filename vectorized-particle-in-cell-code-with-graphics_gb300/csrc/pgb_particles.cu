@@ -329,19 +329,20 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_mcc(PushArgs a) {
 /* ------------------------------------------------------------ scans */
 /* exclusive scan of cnt[0..m) (m read from *m_ptr or given) into off[];
  * total written to *total.  Single block; m up to a few 1e5.             */
-__global__ void __launch_bounds__(1024) k_scan_small(const int* cnt, int* off, const long long* n_ptr, long long m_const,
-                                                     long long* total) {
+__device__ __forceinline__ long long block_excl_scan8(const int* cnt, int* off, long long m, long long carry0) {
+    /* exclusive scan of cnt[0..m) with 8 consecutive items per thread; returns the total */
     __shared__ long long s_warp[32];
     __shared__ long long s_carry;
-    /* n_ptr: particle count whose tiles are scanned; else m_const entries */
-    const long long m = n_ptr ? (*n_ptr + PGB_TILE - 1) / PGB_TILE : m_const;
-    if (threadIdx.x == 0) s_carry = 0;
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (long long b = 0; b < m; b += 1024) {
-        long long i = b + threadIdx.x;
-        long long v = (i < m) ? cnt[i] : 0;
-        long long x = v;
+    if (threadIdx.x == 0) s_carry = carry0;
+    __syncthreads();
+    for (long long b = 0; b < m; b += 8 * 1024) {
+        long long i0 = b + 8 * (long long)threadIdx.x;
+        int v[8];
+        long long sum = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { v[q] = (i0 + q < m) ? cnt[i0 + q] : 0; sum += v[q]; }
+        long long x = sum;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             long long y = __shfl_up_sync(0xffffffffu, x, d);
@@ -359,51 +360,31 @@ __global__ void __launch_bounds__(1024) k_scan_small(const int* cnt, int* off, c
             s_warp[lane] = t;
         }
         __syncthreads();
-        long long excl = s_carry + (warp ? s_warp[warp - 1] : 0) + x - v;
-        if (i < m) off[i] = (int)excl;
+        long long excl = s_carry + (warp ? s_warp[warp - 1] : 0) + x - sum;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            if (i0 + q < m) off[i0 + q] = (int)excl;
+            excl += v[q];
+        }
         __syncthreads();
         if (threadIdx.x == 0) s_carry += s_warp[31];
         __syncthreads();
     }
-    if (threadIdx.x == 0) *total = s_carry;
+    return s_carry;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_small(const int* cnt, int* off, const long long* n_ptr, long long m_const,
+                                                     long long* total) {
+    /* n_ptr: particle count whose tiles are scanned; else m_const entries */
+    const long long m = n_ptr ? (*n_ptr + PGB_TILE - 1) / PGB_TILE : m_const;
+    long long t = block_excl_scan8(cnt, off, m, 0);
+    if (threadIdx.x == 0) *total = t;
 }
 
 /* exclusive scan of a list-length array (length read from device memory) */
 __global__ void __launch_bounds__(1024) k_scan_list(const int* cnt, int* off, const long long* m_ptr, long long* total) {
-    __shared__ long long s_warp[32];
-    __shared__ long long s_carry;
-    const long long m = *m_ptr;
-    if (threadIdx.x == 0) s_carry = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (long long b = 0; b < m; b += 1024) {
-        long long i = b + threadIdx.x;
-        long long v = (i < m) ? cnt[i] : 0;
-        long long x = v;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            long long y = __shfl_up_sync(0xffffffffu, x, d);
-            if (lane >= d) x += y;
-        }
-        if (lane == 31) s_warp[warp] = x;
-        __syncthreads();
-        if (warp == 0) {
-            long long t = s_warp[lane];
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                long long y = __shfl_up_sync(0xffffffffu, t, d);
-                if (lane >= d) t += y;
-            }
-            s_warp[lane] = t;
-        }
-        __syncthreads();
-        long long excl = s_carry + (warp ? s_warp[warp - 1] : 0) + x - v;
-        if (i < m) off[i] = (int)excl;
-        __syncthreads();
-        if (threadIdx.x == 0) s_carry += s_warp[31];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *total = s_carry;
+    long long t = block_excl_scan8(cnt, off, *m_ptr, 0);
+    if (threadIdx.x == 0) *total = t;
 }
 
 /* gather per-tile lists into one dense list in slot order */
@@ -434,44 +415,66 @@ struct InjectArgs {
     int species_mask;            /* 1 = electrons, 2 = ions                  */
     int* list_out_e;             /* append outside electrons (ordered)       */
     long long list_cap;
+    int* flag;                   /* per new electron: outside after its push */
 };
 __global__ void k_inject(InjectArgs a) {
+    /* one thread per new particle; electrons first, then ions, in id order */
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int total = a.k * ((a.species_mask & 1) + ((a.species_mask >> 1) & 1));
+    if (j >= total) return;
+    const int s = ((a.species_mask & 1) && j < a.k) ? 0 : 1;
+    const int jj = (s == 0 || !(a.species_mask & 1)) ? j : j - a.k;
+    const Species& S = s == 0 ? a.e : a.i;
+    const long long n0 = a.ds->n[s];
+    const long long slot = n0 + jj;
+    if (slot >= S.cap) { atomicOr(&a.ds->err, s == 0 ? ERR_CAP_E : ERR_CAP_I); return; }
+    const unsigned int id = a.ds->next_id[s] + (unsigned int)jj;
+    pgb_stream st;
+    pgb_stream_init(&st, a.seed, id, (unsigned int)a.ds->t, PGB_STREAM_INJECT, (uint32_t)s);
+    double rx = pgb_u01d(pgb_stream_u32(&st));
+    double ry = pgb_u01d(pgb_stream_u32(&st));
+    double x = (a.dx + rx * (a.xlength - 2.0 * a.dx));
+    double y = (a.dy + ry * (a.ylength - 2.0 * a.dy));
+    float vt = (float)S.vt;
+    float vx = maxwell_f32(&st, vt), vy = maxwell_f32(&st, vt), vz = maxwell_f32(&st, vt);
+    float4 p = make_float4((float)(x / a.dx), (float)(y / a.dy), vx, vy);
+    bool out = false;
+    if (s == 0 && a.push_e) {
+        bool moved;
+        gather_push_one(a.pce, a.exy, p, vz, moved);
+        /* weight 0: the deposit adds nothing (particle.cpp:497) */
+        out = a.pce.steady ? outside_steady(p.x, p.y, a.pce.nx, a.pce.ny)
+                           : outside_absorbing(p.x, p.y, a.pce.nx, a.pce.ny);
+    }
+    S.xv[slot] = p;
+    S.vz[slot] = vz;
+    S.w[slot] = 0.0f;
+    S.id[slot] = id;
+    /* outside electrons join the end of the wall list in slot order */
+    if (out) a.flag[jj] = 1;
+}
+
+/* after k_inject: counts, ids, and the wall list entries of new electrons */
+__global__ void k_inject_commit(InjectArgs a) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     for (int s = 0; s < 2; ++s) {
         if (!(a.species_mask & (1 << s))) continue;
         const Species& S = s == 0 ? a.e : a.i;
-        for (int j = 0; j < a.k; ++j) {
-            long long slot = a.ds->n[s];
-            if (slot >= S.cap) { a.ds->err |= (s == 0 ? ERR_CAP_E : ERR_CAP_I); break; }
-            unsigned int id = a.ds->next_id[s]++;
-            a.ds->n[s] = slot + 1;
-            pgb_stream st;
-            pgb_stream_init(&st, a.seed, id, (unsigned int)a.ds->t, PGB_STREAM_INJECT, (uint32_t)s);
-            double rx = pgb_u01d(pgb_stream_u32(&st));
-            double ry = pgb_u01d(pgb_stream_u32(&st));
-            double x = (a.dx + rx * (a.xlength - 2.0 * a.dx));
-            double y = (a.dy + ry * (a.ylength - 2.0 * a.dy));
-            double vx = maxwell_fp64(&st, S.vt), vy = maxwell_fp64(&st, S.vt), vz = maxwell_fp64(&st, S.vt);
-            float4 p = make_float4((float)(x / a.dx), (float)(y / a.dy), (float)vx, (float)vy);
-            float vzf = (float)vz;
-            if (s == 0 && a.push_e) {
-                bool moved;
-                gather_push_one(a.pce, a.exy, p, vzf, moved);
-                if (deposit_ok(p.x, p.y, a.pce.nx, a.pce.ny)) deposit_cell(a.qacc_e, a.pce.nx, p.x, p.y, 0.0f);
-                bool out = a.pce.steady ? outside_steady(p.x, p.y, a.pce.nx, a.pce.ny)
-                                        : outside_absorbing(p.x, p.y, a.pce.nx, a.pce.ny);
-                if (out) {
+        long long n0 = a.ds->n[s];
+        int k = a.k;
+        if (n0 + k > S.cap) k = (int)(S.cap - n0 > 0 ? S.cap - n0 : 0);
+        if (s == 0 && a.push_e) {
+            for (int j = 0; j < k; ++j)
+                if (a.flag[j]) {
                     long long pos = a.ds->list_n[LIST_OUT_E];
-                    if (pos < a.list_cap) { a.list_out_e[pos] = (int)slot; a.ds->list_n[LIST_OUT_E] = pos + 1; }
+                    if (pos < a.list_cap) { a.list_out_e[pos] = (int)(n0 + j); a.ds->list_n[LIST_OUT_E] = pos + 1; }
                     else a.ds->err |= ERR_LIST;
+                    a.flag[j] = 0;
                 }
-            }
-            S.xv[slot] = p;
-            S.vz[slot] = vzf;
-            S.w[slot] = 0.0f;
-            S.id[slot] = id;
-            atomicAdd((unsigned long long*)&a.ds->stats[s == 0 ? ST_INJ_E : ST_INJ_I], 1ull);
         }
+        a.ds->n[s] = n0 + k;
+        a.ds->next_id[s] += (unsigned int)k;
+        a.ds->stats[s == 0 ? ST_INJ_E : ST_INJ_I] += k;
     }
 }
 
@@ -768,8 +771,11 @@ int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e) {
     a.pce = push_consts(r, 0); a.exy = r->exy; a.qacc_e = r->qacc[0];
     a.push_e = push_e; a.species_mask = species_mask;
     a.list_out_e = r->list[LIST_OUT_E]; a.list_cap = r->list_cap;
-    k_inject<<<1, 32, 0, r->stream>>>(a);
-    r->launches++;
+    a.flag = r->inject_flag;
+    int tot = 2 * a.k;
+    k_inject<<<(tot + 127) / 128, 128, 0, r->stream>>>(a);
+    k_inject_commit<<<1, 32, 0, r->stream>>>(a);
+    r->launches += 2;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }

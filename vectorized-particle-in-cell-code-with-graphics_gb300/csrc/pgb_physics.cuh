@@ -220,6 +220,18 @@ __device__ inline IonizeOut ionize_f32(pgb_stream* st, const float* neut, int nn
     return o;
 }
 
+/* particle::get_particle_velocity (particle.cpp:452-464) in FP32 */
+__device__ inline float maxwell_f32(pgb_stream* st, float vt) {
+    float v = 0.0f;
+    for (int k = 0; k < 64; ++k) {
+        float R1 = pgb_u01f(pgb_stream_u32(st));
+        float R2 = pgb_u01f(pgb_stream_u32(st));
+        v = vt * cosf((float)(2.0 * PGB_PI) * R2) * sqrtf(fabsf(logf(R1)));
+        if (!(fabsf(v) > vt * 10000.0f)) break;
+    }
+    return v;
+}
+
 /* particle::get_particle_velocity / boundary::get_particle_velocity
  * (particle.cpp:452-464, boundary.cpp:833-845), FP64                     */
 __device__ inline double maxwell_fp64(pgb_stream* st, double vt) {

@@ -444,12 +444,14 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         for (int c = threadIdx.x; c < a.nx; c += blockDim.x) s_sum[c] = 0ull;
         __syncthreads();
+#pragma unroll 4
         for (int k = threadIdx.x; k < CX_TILE; k += blockDim.x) {
             long long i = (long long)t * CX_TILE + k;
-            if (i >= n) break;
-            int col;
-            long long pf = cx_prob_fixed(a, a.i.xv[i], a.i.vz[i], col);
-            if (col >= 0 && pf) atomicAdd(&s_sum[col], (unsigned long long)pf);
+            if (i < n) {
+                int col;
+                long long pf = cx_prob_fixed(a, a.i.xv[i], a.i.vz[i], col);
+                if (col >= 0 && pf) atomicAdd(&s_sum[col], (unsigned long long)pf);
+            }
         }
         __syncthreads();
         for (int c = threadIdx.x; c < a.nx; c += blockDim.x) a.tile_sum[(long long)c * a.ntl + t] = (long long)s_sum[c];
