@@ -142,14 +142,85 @@ __global__ void k_relax_rows(T* u, const T* f, int n, T h2, int color) {
         u[i * n + j] = gs_point(u, f, n, i, j, h2);
     }
 }
+/* One red-black Gauss-Seidel relaxation (both colours, mglin.cpp:116-127)
+ * on a RT x RTX tile of interior points.  The tile and a two-point halo
+ * of u are staged in shared memory; red points of the tile and of a
+ * one-point ring are updated (the ring values are recomputed by the
+ * neighbouring tiles too, from the same inputs, so they agree), then the
+ * black points of the tile, which read only updated red values.  The
+ * result equals the two separate colour sweeps bit for bit.
+ * mode 0: relax u in place
+ * mode 1: u += prolong(vc) first (addint, mglin.cpp:90-97), then relax
+ * mode 2: u  = prolong(vc) first (FMG interpolation, mglin.cpp:49), then relax */
+#define RT 8
+#define RTX 32
+template <class T, int MODE>
+__global__ void __launch_bounds__(RT * RTX) k_relax_tile(T* u, const T* f, int n, T h2, const T* vc) {
+    __shared__ T su[RT + 4][RTX + 4];
+    __shared__ T sf[RT + 2][RTX + 2];
+    const int nc = n / 2 + 1;
+    const int i0 = 1 + blockIdx.y * RT, j0 = 1 + blockIdx.x * RTX;   /* first interior point of the tile */
+    const int tid = threadIdx.y * RTX + threadIdx.x;
+    for (int k = tid; k < (RT + 4) * (RTX + 4); k += RT * RTX) {
+        int li = k / (RTX + 4), lj = k - li * (RTX + 4);
+        int i = i0 - 2 + li, j = j0 - 2 + lj;
+        T v = (T)0;
+        if (i >= 0 && j >= 0 && i < n && j < n) {
+            if (MODE == 2) v = prolong_point(vc, nc, i, j);
+            else {
+                v = u[i * n + j];
+                if (MODE == 1) v = v + prolong_point(vc, nc, i, j);
+            }
+        }
+        su[li][lj] = v;
+    }
+    for (int k = tid; k < (RT + 2) * (RTX + 2); k += RT * RTX) {
+        int li = k / (RTX + 2), lj = k - li * (RTX + 2);
+        int i = i0 - 1 + li, j = j0 - 1 + lj;
+        sf[li][lj] = (i >= 0 && j >= 0 && i < n && j < n) ? f[i * n + j] : (T)0;
+    }
+    __syncthreads();
+    /* red: (i+j) even, on the tile and its one-point ring */
+    for (int k = tid; k < (RT + 2) * (RTX + 2); k += RT * RTX) {
+        int li = k / (RTX + 2), lj = k - li * (RTX + 2);
+        int i = i0 - 1 + li, j = j0 - 1 + lj;
+        if (i >= 1 && j >= 1 && i < n - 1 && j < n - 1 && ((i + j) & 1) == 0) {
+            int a = li + 1, b = lj + 1;
+            su[a][b] = (T)0.25 * (su[a + 1][b] + su[a - 1][b] + su[a][b + 1] + su[a][b - 1] - h2 * sf[li][lj]);
+        }
+    }
+    __syncthreads();
+    /* black: (i+j) odd, on the tile */
+    {
+        int li = threadIdx.y, lj = threadIdx.x;
+        int i = i0 + li, j = j0 + lj;
+        if (i < n - 1 && j < n - 1 && ((i + j) & 1) == 1) {
+            int a = li + 2, b = lj + 2;
+            su[a][b] = (T)0.25 * (su[a + 1][b] + su[a - 1][b] + su[a][b + 1] + su[a][b - 1] - h2 * sf[li + 1][lj + 1]);
+        }
+    }
+    __syncthreads();
+    /* write back the tile; the walls of every level stay 0 (mglin.cpp:103-110,
+     * 143: the coarse solve, the residual and so every correction vanish
+     * there), so they are never rewritten                                 */
+    {
+        int li = threadIdx.y, lj = threadIdx.x;
+        int i = i0 + li, j = j0 + lj;
+        if (i < n - 1 && j < n - 1) u[i * n + j] = su[li + 2][lj + 2];
+    }
+}
+
+/* minus the residual, half-weighted onto the coarse grid (mglin.cpp:133-169);
+ * also zeroes the coarse correction vc that the next level starts from    */
 template <class T>
-__global__ void k_resid_restrict(T* rc, const T* u, const T* f, int nf, T h2i) {
+__global__ void k_resid_restrict(T* rc, T* vc, const T* u, const T* f, int nf, T h2i) {
     const int nc = (nf + 1) / 2;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc * nc; k += gridDim.x * blockDim.x) {
         int ic = k / nc, jc = k - ic * nc;
         T v = (T)0;
         if (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) v = restrict_resid_point(u, f, nf, ic, jc, h2i);
         rc[k] = v;
+        vc[k] = (T)0;
     }
 }
 template <class T>
@@ -414,26 +485,31 @@ struct Levels {
 static Levels<double> levels64(pgb_run* r) { return {r->mg_u, r->mg_f, r->mg_v, r->mg_r, r->mg_tab}; }
 static Levels<float> levels32(pgb_run* r) { return {r->mg32_u, r->mg32_f, r->mg32_v, r->mg32_r, r->mg32_tab}; }
 
-/* V-cycle at level j > small on (u, f) (mglin.cpp:176-196) */
+template <class T, int MODE>
+static void relax_launch(pgb_run* r, T* u, const T* f, int n, T h2, const T* vc) {
+    dim3 grid((n - 2 + RTX - 1) / RTX, (n - 2 + RT - 1) / RT), block(RTX, RT);
+    k_relax_tile<T, MODE><<<grid, block, 0, r->stream>>>(u, f, n, h2, vc);
+    r->launches++;
+}
+
+/* V-cycle at level j > small on (u, f) (mglin.cpp:176-196).  first_mode 2
+ * replaces u by the prolongation of the coarser level before the
+ * pre-smoothing (the FMG interpolation of mglin.cpp:49).                */
 template <class T>
-static int vcycle(pgb_run* r, const Levels<T>& L, int j, int jsmall, T* u, const T* f) {
+static int vcycle(pgb_run* r, const Levels<T>& L, int j, int jsmall, T* u, const T* f, int first_mode,
+                  const T* coarse_u) {
     int nf = r->mg_n[j], nc = r->mg_n[j - 1];
     T h = (T)r->p.xlength / (T)(nf - 1), h2 = h * h, h2i = (T)1.0 / (h * h);
-    long long rw = (long long)(nf - 2) * ((nf - 1) / 2);
-    k_relax_rows<T><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
-    k_relax_rows<T><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
-    k_resid_restrict<T><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(L.rr[j - 1], u, f, nf, h2i);
-    r->launches += 3;
-    PGB_CK(r, cudaMemsetAsync(L.v[j - 1], 0, sizeof(T) * nc * nc, r->stream));
+    if (first_mode == 2) relax_launch<T, 2>(r, u, f, nf, h2, coarse_u);
+    else relax_launch<T, 0>(r, u, f, nf, h2, nullptr);
+    k_resid_restrict<T><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(L.rr[j - 1], L.v[j - 1], u, f, nf, h2i);
+    r->launches++;
     if (j - 1 <= jsmall) {
         if (small_launch<T>(r, L.tab, j - 1, 1)) return PGB_ERR_CUDA;
     } else {
-        if (vcycle<T>(r, L, j - 1, jsmall, L.v[j - 1], L.rr[j - 1])) return PGB_ERR_CUDA;
+        if (vcycle<T>(r, L, j - 1, jsmall, L.v[j - 1], L.rr[j - 1], 0, nullptr)) return PGB_ERR_CUDA;
     }
-    k_prolong<T><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(u, L.v[j - 1], nf, 1);
-    k_relax_rows<T><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 0);
-    k_relax_rows<T><<<blocks_for(rw), 256, 0, r->stream>>>(u, f, nf, h2, 1);
-    r->launches += 3;
+    relax_launch<T, 1>(r, u, f, nf, h2, L.v[j - 1]);
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -455,13 +531,9 @@ static int fmg(pgb_run* r, const Levels<T>& L) {
     }
     int jsmall = small_top(r);
     if (small_launch<T>(r, L.tab, jsmall, 0)) return PGB_ERR_CUDA;
-    for (int j = jsmall + 1; j < ng; ++j) {
-        int nf = r->mg_n[j];
-        k_prolong<T><<<blocks_for((long long)nf * nf), 256, 0, r->stream>>>(L.u[j], L.u[j - 1], nf, 0);
-        r->launches++;
+    for (int j = jsmall + 1; j < ng; ++j)
         for (int c = 0; c < 2; ++c)
-            if (vcycle<T>(r, L, j, jsmall, L.u[j], L.f[j])) return PGB_ERR_CUDA;
-    }
+            if (vcycle<T>(r, L, j, jsmall, L.u[j], L.f[j], c == 0 ? 2 : 0, L.u[j - 1])) return PGB_ERR_CUDA;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -503,6 +575,13 @@ int pgb_mg_setup(pgb_run* r) {
         tabs32[PGB_MAX_LEVELS + l] = r->mg32_f[l];
         tabs32[2 * PGB_MAX_LEVELS + l] = r->mg32_v[l];
         tabs32[3 * PGB_MAX_LEVELS + l] = r->mg32_r[l];
+    }
+    for (int l = 0; l < r->ng; ++l) {
+        size_t n2 = (size_t)r->mg_n[l] * r->mg_n[l];
+        PGB_CK(r, cudaMemset(r->mg_u[l], 0, n2 * sizeof(double)));
+        PGB_CK(r, cudaMemset(r->mg_v[l], 0, n2 * sizeof(double)));
+        PGB_CK(r, cudaMemset(r->mg32_u[l], 0, n2 * sizeof(float)));
+        PGB_CK(r, cudaMemset(r->mg32_v[l], 0, n2 * sizeof(float)));
     }
     PGB_CK(r, cudaMalloc(&r->mg_tab, sizeof(tabs)));
     PGB_CK(r, cudaMemcpy(r->mg_tab, tabs, sizeof(tabs), cudaMemcpyHostToDevice));

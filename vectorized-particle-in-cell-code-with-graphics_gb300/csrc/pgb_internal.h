@@ -25,7 +25,7 @@
 #define PGB_PUSH_THREADS 256
 #define PGB_ITEMS (PGB_TILE / PGB_PUSH_THREADS)
 #define PGB_FIX_SCALE 4294967296.0   /* deposit fixed point: 2^32 per unit weight */
-#define PGB_MG_SMALL 65        /* levels with n <= 65 are solved by one CTA  */
+#define PGB_MG_SMALL 33        /* levels with n <= 33 are solved by one CTA  */
 #define PGB_MAX_LEVELS 16
 #define PGB_BIN 32             /* bin edge in cells (spatial sort)            */
 #define PGB_HALO 8             /* deposit window halo around a bin, cells     */

@@ -773,6 +773,7 @@ int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e) {
     a.list_out_e = r->list[LIST_OUT_E]; a.list_cap = r->list_cap;
     a.flag = r->inject_flag;
     int tot = 2 * a.k;
+    if (tot <= 0) return 0;
     k_inject<<<(tot + 127) / 128, 128, 0, r->stream>>>(a);
     k_inject_commit<<<1, 32, 0, r->stream>>>(a);
     r->launches += 2;

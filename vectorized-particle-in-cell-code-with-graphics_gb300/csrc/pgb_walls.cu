@@ -434,7 +434,7 @@ __device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, fl
     float s = sigma_cx(a.cc, energy);
     /* no contraction: both CX passes must compute the same bits */
     float P = -expm1f(-__fmul_rn(__fmul_rn(u, a.pcoef), s));
-    return __double2ll_rn((double)P * (double)CX_ONE);
+    return __float2ll_rn(P * 1099511627776.0f);   /* P * 2^40, exact scaling */
 }
 
 __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
