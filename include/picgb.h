@@ -144,6 +144,13 @@ typedef struct pgb_run pgb_run;
  * steady state, no collisions) and this library's run controls.           */
 PGB_API int pgb_params_default(pgb_params* p);
 
+/* Read the run parameters from a parameters.h file at run time: its macro
+ * expressions are evaluated as the compiler would (C arithmetic, the
+ * constants of constants.h), so derived quantities (DX, DT, VTE, ...) come
+ * from the file itself (parameters.h:41-366).  RAND_SEED is replaced by
+ * seed.  Returns PGB_ERR_IO when the file cannot be read or parsed.       */
+PGB_API int pgb_params_from_header(const char* path, uint64_t seed, pgb_params* out);
+
 /* pic::pic (pic.cpp:55-221) minus particle loading: allocate the device
  * state, build the neutral velocity tables (collisions.cpp:66-89).          */
 PGB_API int pgb_create(const pgb_params* p, pgb_run** out);

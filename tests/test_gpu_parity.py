@@ -351,3 +351,29 @@ def test_sort_leaves_deterministic_physics_unchanged():
     assert np.array_equal(res[0][0], res[2][0])
     assert res[0][2] == res[2][2]
     assert np.array_equal(res[0][1], res[2][1])
+
+
+# ------------------------------------------------------------- host driver
+def test_batch_driver_runs_and_writes_reference_files(tmp_path):
+    """picgb_run (the main.cpp batch counterpart) reads a parameters.h, loads
+    the dataDump files, runs, and writes dataDump_*.txt and timeData.txt in
+    the reference's text formats."""
+    import os
+    import subprocess
+    from test_host_driver import PARAMS_TEXT
+    g = load_golden("core65")
+    text = PARAMS_TEXT.replace("#define X_NO_OF_CELLS 129", "#define X_NO_OF_CELLS 65") \
+                      .replace("#define Y_NO_OF_CELLS 129", "#define Y_NO_OF_CELLS 65")
+    (tmp_path / "parameters.h").write_text(text)
+    picgb.write_datadump(str(tmp_path / "dataDump_e.txt"), g["e_in"])
+    picgb.write_datadump(str(tmp_path / "dataDump_i1.txt"), g["i_in"])
+    exe = os.path.join(os.path.dirname(picgb.library_path()), "picgb_run")
+    out = subprocess.run([exe, str(tmp_path / "parameters.h"), str(tmp_path), "--steps", "150", "--seed", "3"],
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    e = picgb.read_datadump(str(tmp_path / "dataDump_e.txt"))
+    i = picgb.read_datadump(str(tmp_path / "dataDump_i1.txt"))
+    assert e.shape[1] == 6 and i.shape[0] > 0
+    rows = [l.split() for l in open(tmp_path / "timeData.txt")]
+    assert [int(r[0]) for r in rows] == [0, 100]
+    assert all(len(r) == 8 for r in rows)

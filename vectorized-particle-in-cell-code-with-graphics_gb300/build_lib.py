@@ -18,6 +18,8 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 OUT = os.path.join(HERE, "libpicgb.so")
+EXE = os.path.join(HERE, "picgb_run")
+HOST = os.path.join(HERE, "host")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
@@ -68,7 +70,18 @@ def build(verbose: bool = False, force: bool = False) -> str:
         return unit
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         list(ex.map(run, jobs))
-    objs = [os.path.join(BUILD, u.replace(".cu", ".o")) for u in UNITS]
+    host_obj = os.path.join(BUILD, "pic_host.o")
+    host_src = os.path.join(HOST, "pic_host.cpp")
+    if force or _stale(host_obj, [host_src, os.path.join(HOST, "pic_host.h")] + headers):
+        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", f"-I{os.path.join(REPO, 'include')}",
+               f"-I{CSRC}", f"-I{HOST}", "-c", host_src, "-o", host_obj]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"g++ failed on pic_host.cpp:\n{p.stdout}\n{p.stderr}")
+        jobs.append(("pic_host.cpp", None))
+    objs = [os.path.join(BUILD, u.replace(".cu", ".o")) for u in UNITS] + [host_obj]
     if force or jobs or _stale(OUT, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", OUT] + objs + ["-lcudart"]
         if verbose:
@@ -76,6 +89,13 @@ def build(verbose: bool = False, force: bool = False) -> str:
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError(f"link failed:\n{p.stdout}\n{p.stderr}")
+    main_src = os.path.join(HOST, "picgb_main.cpp")
+    if force or _stale(EXE, [main_src, host_src, OUT, os.path.join(HOST, "pic_host.h")]):
+        cmd = ["g++", "-std=c++17", "-O2", "-DPGB_HOST_IN_EXE", f"-I{os.path.join(REPO, 'include')}", f"-I{HOST}",
+               f"-I{CSRC}", main_src, host_src, "-o", EXE, f"-L{HERE}", "-lpicgb", "-Wl,-rpath,$ORIGIN"]
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"g++ failed on picgb_main.cpp:\n{p.stdout}\n{p.stderr}")
     return OUT
 
 

@@ -360,16 +360,6 @@ extern "C" int pgb_destroy(pgb_run* r) {
     return 0;
 }
 
-static int stage(pgb_run* r, size_t bytes) {
-    if (bytes <= r->h_stage_bytes) return 0;
-    if (r->h_stage) cudaFreeHost(r->h_stage);
-    r->h_stage = nullptr;
-    r->h_stage_bytes = 0;
-    PGB_CK(r, cudaMallocHost(&r->h_stage, bytes));
-    r->h_stage_bytes = bytes;
-    return 0;
-}
-
 /* device staging buffer for AoS transfers, kept between calls */
 static int dstage(pgb_run* r, size_t bytes) {
     if (bytes <= r->d_stage_bytes) return 0;

@@ -156,7 +156,6 @@ __device__ __forceinline__ void scatter_f32(pgb_stream* st, const float* neut, i
     float t;   /* 1 - cosChi */
     if (energy < 1.0e-2f) t = 1.0f - sqrtf(1.0f - R);
     else t = 2.0f * expm1f(R * log1pf(energy)) / energy;
-    float cosChi = 1.0f - t;
     float sinChi = sqrtf(fmaxf(t * (2.0f - t), 0.0f));
     float sinPhi, cosPhi;
     sincosf(two_pi * R, &sinPhi, &cosPhi);
@@ -168,7 +167,6 @@ __device__ __forceinline__ void scatter_f32(pgb_stream* st, const float* neut, i
     float uyp, uzp;
     if (uperp < 1.0f) { uyp = 1.0f; uzp = 1.0f; }
     else { uyp = uy / uperp; uzp = uz / uperp; }
-    (void)cosChi;
     vz -= cf * (uz * t - (ux * uzp * cosPhi - u * uyp * sinPhi) * sinChi);
     vy -= cf * (uy * t - (ux * uyp * cosPhi + u * uzp * sinPhi) * sinChi);
     vx -= cf * (ux * t + uperp * cosPhi * sinChi);

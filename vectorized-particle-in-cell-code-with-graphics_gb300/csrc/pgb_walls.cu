@@ -110,7 +110,7 @@ __global__ void k_iwall2(WallArgs a) {
         float4 p = a.i.xv[slot];
         int c = a.aux[k];
         if (c > 0) {
-            double ix = (double)p.x * a.dx, iy = (double)p.y * a.dy, w = a.i.w[slot];
+            double w = a.i.w[slot];
             int jp = cellf(p.x), kp = cellf(p.y);
             for (int j = 0; j < c; ++j) {
                 long long es = ne0 + a.off[k] + j;
@@ -143,7 +143,6 @@ __global__ void k_iwall2(WallArgs a) {
                     y = R * a.dt * fabs(vy);
                     if (kp >= a.ny) { y = lengthY - y; vy = -fabs(velocity * cos(chi)); }
                 }
-                (void)ix; (void)iy;
                 store_particle(a.e, es, x, y, vx, vy, vz, a.dx, a.dy);
                 a.e.w[es] = (float)ww;
                 a.e.id[es] = id;
