@@ -207,6 +207,45 @@ PGB_API int pgb_get_profile(pgb_run* run, pgb_profile* out);
 /* Wait for all work queued on the handle's stream. */
 PGB_API int pgb_sync(pgb_run* run);
 
+/*
+ * Charge grid of one species from particle records already on the device,
+ * with no run handle and no allocation.  It has no counterpart in the
+ * reference: it is the deposit of pgb_deposit (particle::collect_charge,
+ * particle.cpp:663-858) for callers that can't allocate device memory.
+ * Two kinds of caller need it:
+ *   - a diagnostic or viewer hook that runs between steps on the
+ *     simulation's stream.  cudaMalloc and cudaFree would synchronise the
+ *     device and drain the queued steps;
+ *   - a host that has reserved the device memory for particle capacity.
+ *
+ * Arguments:
+ *   d_aos6  device pointer to n particleVec records {x, y, vx, vy, vz, w}.
+ *   d_q     device pointer that receives nx*ny doubles, equal to
+ *           pgb_get_grid(PGB_GRID_Q_E or Q_I) after pgb_deposit on the same
+ *           records.  Its layout is [ny][nx].
+ *   dx, dy  cell sizes; qc is the macro-particle charge.
+ *   stream  a cudaStream_t of the current device, or NULL for the default
+ *           stream.  The work is queued on it and the call returns without
+ *           waiting.
+ *
+ * Scratch: the per-node accumulator is a fixed device array of
+ * PGB_STATIC_DEPOSIT_MAX_NODES entries (513 x 513 nodes, 2.1 MB).
+ *   - A grid with more nodes returns PGB_ERR_CAPACITY, and
+ *     pgb_last_error(NULL) names the limit.
+ *   - Every call shares the array and clears the part it uses first.  Calls
+ *     whose work overlaps on the GPU, such as calls on two streams without
+ *     an event between them, race.
+ *   - The first call on a device looks up the array with
+ *     cudaGetSymbolAddress.  Make that first call with the device current,
+ *     before any stream capture begins.
+ *
+ * Errors: other failures return PGB_ERR_ARG or PGB_ERR_CUDA, with the
+ * message in pgb_last_error(NULL).
+ */
+#define PGB_STATIC_DEPOSIT_MAX_NODES 263169
+PGB_API int pgb_deposit_static(const double* d_aos6, int64_t n, int32_t nx, int32_t ny, double dx, double dy,
+                               double qc, double* d_q, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

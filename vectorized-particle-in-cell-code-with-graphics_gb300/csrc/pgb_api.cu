@@ -41,6 +41,8 @@ static int fail(pgb_run* r, int code, const std::string& msg) {
     return code;
 }
 
+void pgb_set_unbound_error(const std::string& msg) { g_create_error = msg; }
+
 extern "C" const char* pgb_last_error(const pgb_run* r) {
     return r ? r->err.c_str() : g_create_error.c_str();
 }

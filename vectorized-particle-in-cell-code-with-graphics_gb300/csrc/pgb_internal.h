@@ -151,6 +151,8 @@ struct pgb_run {
 
 /* ------------------------------------------------------------ helpers */
 bool pgb_cuda_ok(pgb_run* r, cudaError_t e, const char* what);
+/* message for pgb_last_error(NULL), from entry points without a handle */
+void pgb_set_unbound_error(const std::string& msg);
 #define PGB_CK(r, call)                                  \
     do {                                                 \
         if (!pgb_cuda_ok((r), (call), #call)) return PGB_ERR_CUDA; \

@@ -257,6 +257,8 @@ def load_library():
         "pgb_get_stream": (C.c_int, [R, C.POINTER(C.c_void_p)]),
         "pgb_set_profiling": (C.c_int, [R, C.c_int]),
         "pgb_get_profile": (C.c_int, [R, C.POINTER(PgbProfile)]),
+        "pgb_deposit_static": (C.c_int, [C.c_void_p, i64, i32, i32, C.c_double, C.c_double, C.c_double,
+                                         C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
