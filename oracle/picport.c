@@ -210,7 +210,9 @@ void orc_destroy(orc_run* r) {
 }
 
 void orc_set_threads(orc_run* r, int threads) { r->threads = threads > 0 ? threads : 1; }
-void orc_set_time_step(orc_run* r, int64_t t) { r->time_step = t; r->c.step = t; }
+/* the phase entry points draw from the streams of step t, as pic_run's
+ * loop body for time_step = t does                                     */
+void orc_set_time_step(orc_run* r, int64_t t) { r->time_step = t; r->c.step = t; r->rng_step = (uint32_t)t; }
 
 int orc_load_species(orc_run* r, int sp, const double* aos6, int64_t n) {
     if (sp < 0 || sp > 1 || n < 0) return PGB_ERR_ARG;

@@ -198,10 +198,22 @@ using namespace std;
 #define ION_TYPE (char *)"i1"
 #define ELECTRON_TYPE (char *)"e"
 #define NO_GROUPS (int)3
-#define UPPER_GROUP_LIMIT (int)400000
-#define UPPER_GROUP_LIMIT2 (int)100000
-#define NEW_GROUP_SIZE (int)200000
-#define NEW_GROUP_SIZE2 (int)50000
+#ifndef ORC_GROUP_LIMIT
+#define ORC_GROUP_LIMIT 400000
+#endif
+#ifndef ORC_GROUP_LIMIT2
+#define ORC_GROUP_LIMIT2 100000
+#endif
+#ifndef ORC_NEW_GROUP
+#define ORC_NEW_GROUP 200000
+#endif
+#ifndef ORC_NEW_GROUP2
+#define ORC_NEW_GROUP2 50000
+#endif
+#define UPPER_GROUP_LIMIT (int)ORC_GROUP_LIMIT
+#define UPPER_GROUP_LIMIT2 (int)ORC_GROUP_LIMIT2
+#define NEW_GROUP_SIZE (int)ORC_NEW_GROUP
+#define NEW_GROUP_SIZE2 (int)ORC_NEW_GROUP2
 #define UPPER_V_LIMIT ((double)1000.0*VTE)
 #define UPPER_V_LIMIT_I ((double)1000.0*VTI)
 #define VI1 (double)2.0*VTI

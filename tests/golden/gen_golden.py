@@ -59,6 +59,9 @@ CASES = {
     "see33": ("see33", dict(X_NO_OF_CELLS=33, E_IMPACT_SEE="YES", ION_IMPACT_SEE="YES", REFLECTION="YES",
                             BACKSCATTER="YES"),
               dict(n=1000, te=200.0, ti=3000.0, seed=18, outside=0.2), 8),
+    "reduce33": ("reduce33", dict(X_NO_OF_CELLS=33, NUMBER_TO_INJECT=20, SIZE_TO_CHECK=900, UPPER_GROUP_LIMIT=550,
+                                  NEW_GROUP_SIZE=520, UPPER_GROUP_LIMIT2=200, NEW_GROUP_SIZE2=180),
+                 dict(n=1000, te=3.0, ti=3.0, seed=19), 10),
     "fields65": ("core65", dict(X_NO_OF_CELLS=65), dict(mode="fields", seed=21), 0),
     "fields129": ("core129", dict(X_NO_OF_CELLS=129), dict(mode="fields", seed=22), 0),
 }

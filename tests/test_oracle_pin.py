@@ -69,7 +69,8 @@ def test_golden_cases_exercise_the_paths():
         for k, v in o.counters().items():
             seen[k] = seen.get(k, 0) + v
     for k in ("absorbed_e", "absorbed_i", "plopped", "reflected", "backscattered", "see_events",
-              "ion_see_emitted", "elastic", "ionization", "charge_exchange", "injected_e"):
+              "ion_see_emitted", "elastic", "ionization", "charge_exchange", "injected_e", "reductions_e",
+              "reductions_i"):
         assert seen[k] > 0, f"no golden case exercises {k}"
 
 

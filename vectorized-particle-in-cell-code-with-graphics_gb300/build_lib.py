@@ -30,6 +30,7 @@ UNITS = {
     "pgb_walls.cu": [],
     "pgb_fields.cu": ["--fmad=false"],
     "pgb_sort.cu": [],
+    "pgb_reduce.cu": [],
     "pgb_static.cu": [],
 }
 

@@ -355,6 +355,7 @@ extern "C" int pgb_destroy(pgb_run* r) {
     for (int w = 0; w < 2; ++w) cudaFree(r->neut[w]);
     if (r->h_stage) cudaFreeHost(r->h_stage);
     cudaFree(r->d_stage);
+    cudaFree(r->kh);
     if (r->prof_ev_ok)
         for (int k = 0; k < 12; ++k) cudaEventDestroy(r->prof_ev[k]);
     if (r->stream) cudaStreamDestroy(r->stream);
@@ -531,8 +532,10 @@ extern "C" int pgb_contain_growth(pgb_run* r, int s) {
     if (rc) return rc;
     long long live = r->hs->n[s] - r->hs->dead[s];
     long long lim = s == 0 ? r->p.size_to_check_e : r->p.size_to_check_i;
-    if (live > lim) return pgb_launch_reduce(r, s) ? PGB_ERR_CUDA : sync_state(r);
-    return 0;
+    if (!(live > lim)) return 0;
+    if ((rc = set_device_step(r, r->time_step, 1))) return rc;
+    if ((rc = pgb_launch_reduce(r, s))) return rc;
+    return sync_state(r);
 }
 
 extern "C" int pgb_deposit(pgb_run* r, int s) {
@@ -616,7 +619,7 @@ static int step_once(pgb_run* r, bool ion_step) {
                 int rc = sync_state(r);
                 if (rc) return rc;
                 if (r->hs->n[s] - r->hs->dead[s] > lim) {
-                    if (pgb_launch_reduce(r, s)) return PGB_ERR_CUDA;
+                    if ((rc = pgb_launch_reduce(r, s))) return rc;
                     /* the reduction changes weights: rebuild both charges */
                     PGB_CK(r, cudaMemsetAsync(r->qacc[0], 0, sizeof(unsigned long long) * G, r->stream));
                     PGB_CK(r, cudaMemsetAsync(r->qacc[1], 0, sizeof(unsigned long long) * G, r->stream));
@@ -822,9 +825,3 @@ extern "C" int pgb_sync(pgb_run* r) {
     return sync_state(r);
 }
 
-/* Kunhardt reduction: not yet on the device; report instead of guessing */
-int pgb_launch_reduce(pgb_run* r, int s) {
-    (void)s;
-    fail(r, PGB_ERR_STATE, "population reduction (SIZE_TO_CHECK exceeded) is not implemented on the device yet");
-    return PGB_ERR_STATE;
-}

@@ -136,6 +136,8 @@ struct pgb_run {
     int* sort_key_total = nullptr;
     long long* sort_key_start = nullptr;
     long long sort_chunks_cap = 0;
+    /* population control (Kunhardt): group counts and digit histograms */
+    void* kh = nullptr;
     /* host staging */
     double* h_stage = nullptr;
     size_t h_stage_bytes = 0;

@@ -123,7 +123,8 @@ def make_params(**kw) -> PgbParams:
         ELECTRON_PARTICLE_DENSITY=1.0e15, DT_SCALE=0.1, DTI_RATIO=1.0, MAGNETIC_FIELD=0.0,
         ANGLE_DEG=30.0, PHI_LEFT=0.0, PHI_RIGHT=0.0, PHI_PERIOD=0.0, PHI_TOP=0.0,
         PHI_BOTTOM=0.0, E_MACROPARTICLE_SIZE=1.0e6, ION_MACROPARTICLE_SIZE=1.0e6,
-        SIZE_TO_CHECK=1000001, SIZE_TO_CHECK_E=None, RAND_SEED=1, POISSON="FMG_REF",
+        SIZE_TO_CHECK=1000001, SIZE_TO_CHECK_E=None, UPPER_GROUP_LIMIT=400000, UPPER_GROUP_LIMIT2=100000,
+        NEW_GROUP_SIZE=200000, NEW_GROUP_SIZE2=50000, RAND_SEED=1, POISSON="FMG_REF",
         DC_MAX_ITERS=8, DC_TOLERANCE=1e-10, SORT_INTERVAL=0, CAPACITY_E=0, CAPACITY_I=0,
     )
     for k, v in kw.items():
@@ -185,11 +186,13 @@ def make_params(**kw) -> PgbParams:
         p.v_limit_e[k] = v
     for k, v in enumerate((2.0 * vti, 3.0 * vti, 1000.0 * vti)):
         p.v_limit_i[k] = v
+    gl, gl2 = int(g["UPPER_GROUP_LIMIT"]), int(g["UPPER_GROUP_LIMIT2"])
+    ng, ng2 = int(g["NEW_GROUP_SIZE"]), int(g["NEW_GROUP_SIZE2"])
     for k in range(3):
-        p.group_limit_e[k] = 400000
-        p.new_group_size_e[k] = 200000
-    p.group_limit_i[0], p.group_limit_i[1], p.group_limit_i[2] = 400000, 100000, 100000
-    p.new_group_size_i[0], p.new_group_size_i[1], p.new_group_size_i[2] = 200000, 50000, 50000
+        p.group_limit_e[k] = gl
+        p.new_group_size_e[k] = ng
+    p.group_limit_i[0], p.group_limit_i[1], p.group_limit_i[2] = gl, gl2, gl2
+    p.new_group_size_i[0], p.new_group_size_i[1], p.new_group_size_i[2] = ng, ng2, ng2
     stc = int(g["SIZE_TO_CHECK"])
     p.size_to_check_i = stc
     p.size_to_check_e = int(g["SIZE_TO_CHECK_E"]) if g["SIZE_TO_CHECK_E"] is not None else stc
