@@ -136,6 +136,7 @@ typedef struct pgb_profile {
     int64_t steps;                 /* steps profiled                               */
     int64_t slots_e, slots_i;      /* particle slots swept by the push kernels     */
     int64_t launches;              /* kernel launches issued since pgb_create      */
+    double ms_push_e_kernel;       /* the electron push kernel alone (in ms_push_e) */
 } pgb_profile;
 
 typedef struct pgb_run pgb_run;

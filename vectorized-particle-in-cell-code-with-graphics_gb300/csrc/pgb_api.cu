@@ -206,7 +206,7 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
         int nbx, nby;
         pgb_bins(r, &nbx, &nby);
         long long nkeys = (long long)nbx * nby + 1;
-        r->sort_chunks_cap = (lc + 4096 - 1) / 4096 + 1;
+        r->sort_chunks_cap = (lc + PGB_SORT_CHUNK - 1) / PGB_SORT_CHUNK + 1;
         for (int q = 0; q < 2; ++q) {
             if (cudaMalloc(&r->tile_bin[q], sizeof(int) * nt) != cudaSuccess ||
                 cudaMalloc(&r->pieces[q], sizeof(int4) * (nt + nkeys + 1)) != cudaSuccess) {
@@ -326,6 +326,12 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
         for (int w = 1; w >= 0; --w) {
             neutral_table(*p, w, tab.data());
             for (int k = 0; k < nn; ++k) tab32[k] = (float)tab[k];
+            double vmax = 0.0;
+            for (int k = 0; k < p->init_no_neutrals; ++k) {
+                double a = tab32[k], b = tab32[p->init_no_neutrals + k], c = tab32[2 * p->init_no_neutrals + k];
+                vmax = std::max(vmax, std::sqrt(a * a + b * b + c * c));
+            }
+            r->vn_max[w] = (float)vmax;
             cudaMemcpy(r->neut[w], tab32.data(), sizeof(float) * nn, cudaMemcpyHostToDevice);
         }
     }
@@ -585,6 +591,7 @@ static int step_once(pgb_run* r, bool ion_step) {
     /* e_collisions::collision + get_particle_electric_field + move_particles */
     PROF_MARK(r, 0);
     if (pgb_launch_push(r, 0, coll, true, coll)) return PGB_ERR_CUDA;
+    PROF_MARK(r, 7);
     if (pgb_build_list(r, LIST_OUT_E, 0)) return PGB_ERR_CUDA;
     PROF_MARK(r, 1);
     if (coll) {
@@ -643,6 +650,9 @@ static int profile_collect(pgb_run* r) {
     float ms[6];
     for (int k = 0; k < 6; ++k) PGB_CK(r, cudaEventElapsedTime(&ms[k], r->prof_ev[k], r->prof_ev[k + 1]));
     r->prof.ms_push_e += ms[0];
+    float mk;
+    PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[0], r->prof_ev[7]));
+    r->prof.ms_push_e_kernel += mk;
     r->prof.ms_walls += ms[1] + ms[4];
     r->prof.ms_collide_ions += ms[2];
     r->prof.ms_push_i += ms[3];

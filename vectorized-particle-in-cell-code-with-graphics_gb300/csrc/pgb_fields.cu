@@ -16,9 +16,9 @@
  *
  * Schedule (one call): restrict the right-hand side to every level, solve
  * the 3x3 grid, then for each finer level prolong and run two V(1,1)
- * cycles.  Levels with n <= PGB_MG_SMALL (65) run inside one CTA with all
- * their arrays in shared memory (one launch per coarse sub-solve); finer
- * levels use one launch per grid operation.
+ * cycles.  Levels with n <= PGB_MG_SMALL (65; PGB_MG_SMALL64 = 33 in FP64)
+ * run inside one CTA with all their arrays in shared memory (one launch per
+ * coarse sub-solve); finer levels use one launch per grid operation.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -258,13 +258,21 @@ struct SmallMG {
     T length;
 };
 
+/* Loops of the one-CTA solver run over flat point indices so that every
+ * lane has work (FP64 issue slots are scarce).  Rows are found without an
+ * integer division: a relaxation colour has (n-1)/2 points per row, a
+ * power of two; other grids use row = (int)((k + 0.5) / n) in FP32, exact
+ * for k < 2^16 since k + 0.5 is never within FP32 rounding of a multiple
+ * of n.                                                                  */
+__device__ __forceinline__ int sm_row(int k, float inv_n) { return (int)(((float)k + 0.5f) * inv_n); }
+
 template <class T>
 __device__ void sm_relax(T* u, const T* f, int n, T length) {
     T h = length / (T)(n - 1), h2 = h * h;
-    const int m = n - 2, per_row = (m + 1) / 2;
+    const int m = n - 2, per_row = (n - 1) >> 1, sh = __ffs(per_row) - 1;
     for (int color = 0; color < 2; ++color) {
         for (int t = threadIdx.x; t < m * per_row; t += blockDim.x) {
-            int r = t / per_row, c = t - r * per_row;
+            int r = t >> sh, c = t & (per_row - 1);
             int i = r + 1, j = 1 + ((i + 1 + color) & 1) + 2 * c;
             if (j <= n - 2) u[i * n + j] = gs_point(u, f, n, i, j, h2);
         }
@@ -290,8 +298,9 @@ __device__ void sm_vcycle(SmallMG<T>& s, int j, T* u, const T* f) {
         int nf = s.n[l], nc = s.n[l - 1];
         T h = s.length / (T)(nf - 1), h2i = (T)1.0 / (h * h);
         sm_relax(ul, fl, nf, s.length);
+        const float inv = 1.0f / (float)nc;
         for (int k = threadIdx.x; k < nc * nc; k += blockDim.x) {
-            int ic = k / nc, jc = k - ic * nc;
+            int ic = sm_row(k, inv), jc = k - ic * nc;
             T v = (T)0;
             if (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) v = restrict_resid_point(ul, fl, nf, ic, jc, h2i);
             s.R[l - 1][k] = v;
@@ -304,8 +313,9 @@ __device__ void sm_vcycle(SmallMG<T>& s, int j, T* u, const T* f) {
         T* ul = (l == j) ? u : s.V[l];
         const T* fl = (l == j) ? f : s.R[l];
         int nf = s.n[l], nc = s.n[l - 1];
+        const float inv = 1.0f / (float)nf;
         for (int k = threadIdx.x; k < nf * nf; k += blockDim.x) {
-            int i = k / nf, jj = k - i * nf;
+            int i = sm_row(k, inv), jj = k - i * nf;
             ul[k] = ul[k] + prolong_point(s.V[l - 1], nc, i, jj);
         }
         __syncthreads();
@@ -313,11 +323,11 @@ __device__ void sm_vcycle(SmallMG<T>& s, int j, T* u, const T* f) {
     }
 }
 
-/* mode 0: full multigrid from level 0 to J with rhs levels in g_f[0..J];
- *         writes u_J to g_u[J].
+/* mode 0: full multigrid from level 0 to J on the rhs g_f[J] (the coarser
+ *         right-hand sides are restricted here); writes u_J to g_u[J].
  * mode 1: one V-cycle at level J on (g_v[J], g_r[J]) in place.          */
 template <class T>
-__global__ void k_mg_small(int J, int mode, T length, T** g_u, T** g_f, T** g_v, T** g_r) {
+__global__ void __launch_bounds__(1024, 1) k_mg_small(int J, int mode, T length, T** g_u, T** g_f, T** g_v, T** g_r) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmallMG<T> s;
     s.length = length;
@@ -331,14 +341,25 @@ __global__ void k_mg_small(int J, int mode, T length, T** g_u, T** g_f, T** g_v,
         s.R[l] = p; p += n * n;
     }
     if (mode == 0) {
-        for (int l = 0; l <= J; ++l)
-            for (int k = threadIdx.x; k < s.n[l] * s.n[l]; k += blockDim.x) s.F[l][k] = g_f[l][k];
+        for (int k = threadIdx.x; k < s.n[J] * s.n[J]; k += blockDim.x) s.F[J][k] = g_f[J][k];
         __syncthreads();
+        /* right-hand sides of the coarser levels, as k_restrict computes them */
+        for (int l = J - 1; l >= 0; --l) {
+            const int nc = s.n[l], nf = s.n[l + 1];
+            const float inv = 1.0f / (float)nc;
+            for (int k = threadIdx.x; k < nc * nc; k += blockDim.x) {
+                int ic = sm_row(k, inv), jc = k - ic * nc;
+                s.F[l][k] = (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) ? restrict_point(s.F[l + 1], nf, ic, jc)
+                                                                             : s.F[l + 1][(2 * ic) * nf + 2 * jc];
+            }
+            __syncthreads();
+        }
         sm_coarsest(s.U[0], s.F[0], length);
         for (int l = 1; l <= J; ++l) {
             int nf = s.n[l], nc = s.n[l - 1];
+            const float inv = 1.0f / (float)nf;
             for (int k = threadIdx.x; k < nf * nf; k += blockDim.x) {
-                int i = k / nf, jj = k - i * nf;
+                int i = sm_row(k, inv), jj = k - i * nf;
                 s.U[l][k] = prolong_point(s.U[l - 1], nc, i, jj);
             }
             __syncthreads();
@@ -514,9 +535,13 @@ static int vcycle(pgb_run* r, const Levels<T>& L, int j, int jsmall, T* u, const
     return 0;
 }
 
-static int small_top(pgb_run* r) {
+/* top level of the one-CTA solver.  FP32 levels up to 65 nodes are faster
+ * in one CTA than as separate launches; FP64 runs at a small fraction of
+ * the FP32 rate, and one SM is too slow for more than 33 nodes.          */
+static int small_top(pgb_run* r, size_t elem) {
+    const int lim = elem == sizeof(float) ? PGB_MG_SMALL : PGB_MG_SMALL64;
     int jsmall = 0;
-    while (jsmall + 1 < r->ng && r->mg_n[jsmall + 1] <= PGB_MG_SMALL) jsmall++;
+    while (jsmall + 1 < r->ng && r->mg_n[jsmall + 1] <= lim) jsmall++;
     return jsmall;
 }
 
@@ -524,12 +549,13 @@ static int small_top(pgb_run* r) {
 template <class T>
 static int fmg(pgb_run* r, const Levels<T>& L) {
     const int ng = r->ng;
-    for (int j = ng - 2; j >= 0; --j) {
+    int jsmall = small_top(r, sizeof(T));
+    /* the one-CTA solver restricts the levels below jsmall itself */
+    for (int j = ng - 2; j >= jsmall; --j) {
         int nc = r->mg_n[j];
         k_restrict<T><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(L.f[j], L.f[j + 1], nc);
         r->launches++;
     }
-    int jsmall = small_top(r);
     if (small_launch<T>(r, L.tab, jsmall, 0)) return PGB_ERR_CUDA;
     for (int j = jsmall + 1; j < ng; ++j)
         for (int c = 0; c < 2; ++c)
@@ -589,11 +615,10 @@ int pgb_mg_setup(pgb_run* r) {
     PGB_CK(r, cudaMemcpy(r->mg32_tab, tabs32, sizeof(tabs32), cudaMemcpyHostToDevice));
     size_t G = (size_t)r->nx * r->ny;
     PGB_CK(r, cudaMalloc(&r->dc_u, G * sizeof(double)));
-    int jsmall = small_top(r);
     PGB_CK(r, cudaFuncSetAttribute(k_mg_small<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)small_smem_bytes(jsmall, sizeof(double))));
+                                   (int)small_smem_bytes(small_top(r, sizeof(double)), sizeof(double))));
     PGB_CK(r, cudaFuncSetAttribute(k_mg_small<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)small_smem_bytes(jsmall, sizeof(float))));
+                                   (int)small_smem_bytes(small_top(r, sizeof(float)), sizeof(float))));
     return 0;
 }
 

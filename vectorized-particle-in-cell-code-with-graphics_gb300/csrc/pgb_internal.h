@@ -25,12 +25,14 @@
 #define PGB_PUSH_THREADS 256
 #define PGB_ITEMS (PGB_TILE / PGB_PUSH_THREADS)
 #define PGB_FIX_SCALE 4294967296.0   /* deposit fixed point: 2^32 per unit weight */
-#define PGB_MG_SMALL 33        /* levels with n <= 33 are solved by one CTA  */
+#define PGB_MG_SMALL 65        /* levels with n <= 65 are solved by one CTA  */
+#define PGB_MG_SMALL64 33      /* the same for the FP64 multigrid            */
 #define PGB_MAX_LEVELS 16
 #define PGB_BIN 32             /* bin edge in cells (spatial sort)            */
 #define PGB_HALO 8             /* deposit window halo around a bin, cells     */
 #define PGB_WIN (PGB_BIN + 2 * PGB_HALO + 1)   /* window edge in nodes         */
 #define PGB_PIECE_TILES 4      /* tiles of one bin per work piece             */
+#define PGB_SORT_CHUNK 2048    /* slots per chunk of the bin sort passes      */
 
 enum { ST_ABS_E = 0, ST_ABS_I, ST_PLOP, ST_REFL, ST_BACK, ST_SEE_EV, ST_SEE_EM, ST_ISEE_EM,
        ST_ELASTIC, ST_IONIZE, ST_CX, ST_INJ_E, ST_INJ_I, ST_RED_E, ST_RED_I, ST_COUNT };
@@ -116,6 +118,7 @@ struct pgb_run {
     int* aux_j = nullptr;
     /* collisions */
     float* neut[2] = {nullptr, nullptr};   /* [which]: 3 x N_neutral, FP32    */
+    float vn_max[2] = {0.0f, 0.0f};        /* largest neutral speed per table */
     double* neut64[2] = {nullptr, nullptr};
     double* prob_cx = nullptr;             /* per-column CX accumulator       */
     double* phi_tab = nullptr;             /* right-wall potential per step   */

@@ -76,38 +76,76 @@ __device__ __forceinline__ void gather_push_one(const PushConsts& pc, const floa
     }
 }
 
-/* electron-neutral collision test and event (e_collisions.cpp:504-562).
- * Returns true if the electron ionized (its velocity is then NaN).        */
-__device__ __forceinline__ bool mcc_one(const CollConsts& cc, const float* neut, unsigned int id, unsigned int step,
-                                        int nx, int ny, float4& p, float& vz, bool& vchanged, int* stats) {
+/* electron-neutral collision test (e_collisions.cpp:504-551): both
+ * probabilities come from the energy before any event.  Returns a bit set
+ * MCC_SCATTER | MCC_IONIZE; *energy is the electron's energy (eV) and *st
+ * the EMCC stream after its first draw, as the scattering continues it.  */
+#define MCC_SCATTER 1
+#define MCC_IONIZE 2
+__device__ __forceinline__ int mcc_test(const CollConsts& cc, unsigned int id, unsigned int step, int nx, int ny,
+                                        const float4& p, float vz, float* energy_out, pgb_stream* st) {
     int jp = cellf(p.x), kp = cellf(p.y);
-    if (!(jp >= 0 && jp < nx && kp >= 0 && kp < ny)) return false;
+    if (!(jp >= 0 && jp < nx && kp >= 0 && kp < ny)) return 0;
     float u2 = p.z * p.z + p.w * p.w + vz * vz;
     float energy = cc.e_energy_coef * u2;
     float u = sqrtf(u2);
     float sel = sigma_el(cc, energy), sio = sigma_ion(cc, energy);
-    pgb_stream st;
-    pgb_stream_init(&st, cc.seed, id, step, PGB_STREAM_EMCC, 0);
-    float R = pgb_u01f(pgb_stream_u32(&st));
+    pgb_stream_init(st, cc.seed, id, step, PGB_STREAM_EMCC, 0);
+    float R = pgb_u01f(pgb_stream_u32(st));
     float P = -expm1f(-(u * cc.e_pcoef * sel));
-    bool ion = false;
-    if (P > 2.0f * R) {
+    int ev = 0;
+    if (P > 2.0f * R) ev |= MCC_SCATTER;
+    /* the ionization test is P = 1 - exp(-x) > 0 (e_collisions.cpp:546-551),
+     * which holds exactly when x > 0 (for NaN x neither holds)          */
+    if (u * cc.e_pcoef * sio > 0.0f) ev |= MCC_IONIZE;
+    *energy_out = energy;
+    return ev;
+}
+
+/* the full ionization of a parent electron (never reached while the
+ * reference's energy units make the excess negative): kept out of line so
+ * that it does not weigh on the push kernels' registers                  */
+__device__ __noinline__ void mcc_ionize_full(const CollConsts& cc, const float* neut, unsigned int id, unsigned int step,
+                                             float4& p, float& vz) {
+    pgb_stream si;
+    pgb_stream_init(&si, cc.seed, id, step, PGB_STREAM_IONIZE, 0);
+    /* positions enter only the products; the parent keeps its position */
+    IonizeOut o = ionize_f32(&si, neut, cc.n_neutral, cc, 0.0, 0.0, p.z, p.w, vz);
+    p.z = (float)o.evx; p.w = (float)o.evy; vz = (float)o.evz;
+}
+
+/* e_collisions::ionization's effect on the parent electron, from its
+ * velocity after any scattering (e_collisions.cpp:319-443)              */
+__device__ __forceinline__ void mcc_ionize(const CollConsts& cc, const float* neut, unsigned int id, unsigned int step,
+                                           float4& p, float& vz) {
+    if (p.z * p.z + p.w * p.w + vz * vz < cc.ion_vcap * cc.ion_vcap) {
+        /* (rm/2)(ve-vn)^2 - THRESHOLD < 0 at this speed for every neutral
+         * of the table, so ionize_f32 would return NaN velocities from
+         * sqrt of a negative number whatever it draws                   */
+        p.z = p.w = vz = __int_as_float(0x7fffffff);
+    } else {
+        mcc_ionize_full(cc, neut, id, step, p, vz);
+    }
+}
+
+/* test and events of one electron in place (e_collisions.cpp:504-562).
+ * Returns true if the electron ionized (its velocity is then NaN).        */
+__device__ __forceinline__ bool mcc_one(const CollConsts& cc, const float* neut, unsigned int id, unsigned int step,
+                                        int nx, int ny, float4& p, float& vz, bool& vchanged, int* stats) {
+    float energy;
+    pgb_stream st;
+    int ev = mcc_test(cc, id, step, nx, ny, p, vz, &energy, &st);
+    if (ev & MCC_SCATTER) {
         scatter_f32(&st, neut, cc.n_neutral, energy, (float)cc.reduced_mass, p.z, p.w, vz);
         vchanged = true;
         stats[0] += 1;
     }
-    float Pi = -expm1f(-(u * cc.e_pcoef * sio));
-    if (Pi > 0.0f) {
-        pgb_stream si;
-        pgb_stream_init(&si, cc.seed, id, step, PGB_STREAM_IONIZE, 0);
-        /* positions enter only the products; the parent keeps its position */
-        IonizeOut o = ionize_f32(&si, neut, cc.n_neutral, cc, 0.0, 0.0, p.z, p.w, vz);
-        p.z = (float)o.evx; p.w = (float)o.evy; vz = (float)o.evz;
+    if (ev & MCC_IONIZE) {
+        mcc_ionize(cc, neut, id, step, p, vz);
         vchanged = true;
-        ion = true;
         stats[1] += 1;
     }
-    return ion;
+    return (ev & MCC_IONIZE) != 0;
 }
 
 /* add per-thread event counts (elastic, ionization) with one atomic per warp */
@@ -183,41 +221,123 @@ __device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned l
     }
 }
 
-template <bool MCC, bool DEP>
-__device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& pc, int tile, long long n,
-                                          unsigned long long* win, int ox, int oy, unsigned step, int (&st_loc)[2]) {
+/* Elastic-scattering events of one tile, queued so that full warps run
+ * them: about one electron in twenty scatters per step, and inline the
+ * event would hold a whole warp for one or two active lanes.  The queue
+ * holds a whole tile, so it never overflows.                            */
+#define SCATTER_QCAP PGB_TILE
+struct ScatterQueue {
+    float4 v[SCATTER_QCAP];        /* vx, vy, vz; energy (eV) */
+    unsigned int id[SCATTER_QCAP];
+    int n;
+};
+
+template <bool DEP>
+__device__ __forceinline__ void push_tile_mcc(const PushArgs& a, const PushConsts& pc, int tile, long long n,
+                                              unsigned long long* win, int ox, int oy, unsigned step,
+                                              int (&st_loc)[2], ScatterQueue& q) {
     const long long base = (long long)tile * PGB_TILE;
+    int code[PGB_ITEMS];   /* -1 absent; else MCC bits | (queue slot + 1) << 2 */
+    /* 1: collision tests; scattering events go to the queue.  Only the
+     * codes live across the barriers; step 3 reads the particle again
+     * (from L1/L2)                                                     */
+#pragma unroll
+    for (int k = 0; k < PGB_ITEMS; ++k) {
+        code[k] = -1;
+        long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+        if (i >= n) continue;
+        float4 p = a.xv[i];
+        if (is_dead(p.x)) continue;
+        float vz = a.vz[i];
+        unsigned int id = a.id[i];
+        float energy;
+        pgb_stream st;
+        int ev = mcc_test(a.cc, id, step, pc.nx, pc.ny, p, vz, &energy, &st);
+        if (ev & MCC_SCATTER) {
+            st_loc[0] += 1;
+            int slot = atomicAdd(&q.n, 1);   /* < PGB_TILE: one entry per slot at most */
+            q.v[slot] = make_float4(p.z, p.w, vz, energy);
+            q.id[slot] = id;
+            ev |= (slot + 1) << 2;
+        }
+        code[k] = ev;
+    }
+    __syncthreads();
+    /* 2: the queued scatterings, one per thread */
+    const int qn = q.n;
+    for (int e = threadIdx.x; e < qn; e += blockDim.x) {
+        float4 v = q.v[e];
+        pgb_stream st;
+        pgb_stream_init(&st, a.cc.seed, q.id[e], step, PGB_STREAM_EMCC, 0);
+        (void)pgb_stream_u32(&st);   /* the collision test's draw */
+        scatter_f32(&st, a.neut, a.cc.n_neutral, v.w, (float)a.cc.reduced_mass, v.x, v.y, v.z);
+        q.v[e] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) q.n = 0;   /* read again only after the list barriers */
+    /* 3: ionization, gather, push, deposit, wall and event flags */
     bool f[2][PGB_ITEMS];
 #pragma unroll
     for (int k = 0; k < PGB_ITEMS; ++k) {
         f[0][k] = false;
         f[1][k] = false;
+        if (code[k] < 0) continue;
+        long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+        float4 p = a.xv[i];
+        float vz = a.vz[i];
+        bool vchanged = false;
+        int slot = (code[k] >> 2) - 1;
+        if (slot >= 0) {
+            float4 v = q.v[slot];
+            p.z = v.x; p.w = v.y; vz = v.z;
+            vchanged = true;
+        }
+        if (code[k] & MCC_IONIZE) {
+            mcc_ionize(a.cc, a.neut, a.id[i], step, p, vz);
+            vchanged = true;
+            st_loc[1] += 1;
+            f[1][k] = true;
+        }
+        bool moved;
+        gather_push_one(pc, a.exy, p, vz, moved);
+        if (moved || vchanged) a.xv[i] = p;
+        if (vchanged || (pc.bfield && moved)) a.vz[i] = vz;
+        if (DEP && deposit_ok(p.x, p.y, pc.nx, pc.ny)) deposit_win(a.qacc, win, ox, oy, pc.nx, p.x, p.y, a.w[i]);
+        f[0][k] = pc.steady ? outside_steady(p.x, p.y, pc.nx, pc.ny) : outside_absorbing(p.x, p.y, pc.nx, pc.ny);
+    }
+    int* const tl[2] = {a.tl_out, a.tl_ev};
+    int* const tc[2] = {a.tc_out, a.tc_ev};
+    tile_lists<2>(f, base, tile, tl, tc);
+}
+
+template <bool MCC, bool DEP>
+__device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& pc, int tile, long long n,
+                                          unsigned long long* win, int ox, int oy, unsigned step, int (&st_loc)[2],
+                                          ScatterQueue& q) {
+    if (MCC) {
+        push_tile_mcc<DEP>(a, pc, tile, n, win, ox, oy, step, st_loc, q);
+        return;
+    }
+    const long long base = (long long)tile * PGB_TILE;
+    bool f[1][PGB_ITEMS];
+#pragma unroll
+    for (int k = 0; k < PGB_ITEMS; ++k) {
+        f[0][k] = false;
         long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
         if (i >= n) continue;
         float4 p = a.xv[i];
         if (is_dead(p.x)) continue;
-        float vz = (MCC || pc.bfield) ? a.vz[i] : 0.0f;
-        bool vchanged = false;
-        if (MCC) f[1][k] = mcc_one(a.cc, a.neut, a.id[i], step, pc.nx, pc.ny, p, vz, vchanged, st_loc);
+        float vz = pc.bfield ? a.vz[i] : 0.0f;
         bool moved;
         gather_push_one(pc, a.exy, p, vz, moved);
-        if (moved || vchanged) a.xv[i] = p;
-        if ((MCC && vchanged) || (pc.bfield && moved)) a.vz[i] = vz;
+        if (moved) a.xv[i] = p;
+        if (pc.bfield && moved) a.vz[i] = vz;
         if (DEP && deposit_ok(p.x, p.y, pc.nx, pc.ny)) deposit_win(a.qacc, win, ox, oy, pc.nx, p.x, p.y, a.w[i]);
         f[0][k] = pc.steady ? outside_steady(p.x, p.y, pc.nx, pc.ny) : outside_absorbing(p.x, p.y, pc.nx, pc.ny);
     }
-    if (MCC) {
-        int* const tl[2] = {a.tl_out, a.tl_ev};
-        int* const tc[2] = {a.tc_out, a.tc_ev};
-        tile_lists<2>(f, base, tile, tl, tc);
-    } else {
-        bool g[1][PGB_ITEMS];
-#pragma unroll
-        for (int k = 0; k < PGB_ITEMS; ++k) g[0][k] = f[0][k];
-        int* const tl[1] = {a.tl_out};
-        int* const tc[1] = {a.tc_out};
-        tile_lists<1>(g, base, tile, tl, tc);
-    }
+    int* const tl[1] = {a.tl_out};
+    int* const tc[1] = {a.tc_out};
+    tile_lists<1>(f, base, tile, tl, tc);
 }
 
 /* Work items: the bin pieces of the last sort (tiles of one bin, deposited
@@ -225,6 +345,9 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
 template <bool MCC, bool DEP>
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_push(PushArgs a) {
     __shared__ unsigned long long s_win[PGB_WIN * PGB_WIN];
+    __shared__ ScatterQueue s_q;
+    if (MCC && threadIdx.x == 0) s_q.n = 0;
+    __syncthreads();
     const long long n = a.ds->n[a.s];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     const int npieces = a.ds->n_pieces[a.s];
@@ -246,7 +369,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_push(PushArgs a) {
                 __syncthreads();
             }
             for (int t = pc4.x; t < pc4.x + pc4.y && t < ntiles; ++t)
-                push_tile<MCC, DEP>(a, pc, t, n, win, ox, oy, step, st_loc);
+                push_tile<MCC, DEP>(a, pc, t, n, win, ox, oy, step, st_loc, s_q);
             if (win) {
                 __syncthreads();
                 for (int k = threadIdx.x; k < PGB_WIN * PGB_WIN; k += blockDim.x) {
@@ -260,7 +383,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_push(PushArgs a) {
                 __syncthreads();
             }
         } else {
-            push_tile<MCC, DEP>(a, pc, tile0 + (item - npieces), n, nullptr, 0, 0, step, st_loc);
+            push_tile<MCC, DEP>(a, pc, tile0 + (item - npieces), n, nullptr, 0, 0, step, st_loc, s_q);
         }
     }
     if (MCC) flush_stats(st_loc, a.ds->stats);
@@ -691,6 +814,13 @@ CollConsts pgb_coll_consts(pgb_run* r) {
     c.reduced_mass = p.ion_mass / (p.electron_mass + p.ion_mass);
     c.n_neutral = p.init_no_neutrals;
     c.seed = p.seed;
+    /* (ve + vn) < sqrt(THRESHOLD/rm)/2 makes (rm/2)(ve-vn)^2 at most
+     * THRESHOLD/8, far from THRESHOLD whatever the FP32 rounding         */
+    {
+        double rm = (double)(float)(c.reduced_mass * c.me);
+        double cap = 0.5 * sqrt((double)(float)p.threshold / rm) - 1.001 * (double)r->vn_max[0];
+        c.ion_vcap = cap > 0.0 ? (float)cap : 0.0f;
+    }
     return c;
 }
 

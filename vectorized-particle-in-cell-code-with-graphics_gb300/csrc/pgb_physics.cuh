@@ -111,6 +111,9 @@ __device__ __forceinline__ float sig_ar_cx(float e) {
 __device__ __forceinline__ float sig_h_cx(float e) {
     float ee = e / 1000.0f / 1.66054e-27f;
     if (!(ee >= 1.0e-4f)) return 0.0f;
+    /* from ee = 1e10 on, ee^5.4 overflows FP32: den is +inf and the result
+     * is exactly 0, so the powers and the logarithm are skipped           */
+    if (ee >= 1.0e10f) return 0.0f;
     float den = 1.0f + 0.038371f * ee + 3.8068e-6f * __powf(ee, 3.5f) + 1.1832e-10f * __powf(ee, 5.4f);
     return (3.2345f * logf((235.88f / ee) + 2.3713f)) / den;
 }
@@ -124,6 +127,9 @@ struct CollConsts {
     float e_pcoef;            /* DT*1e-20*NEUTRAL_DENSITY  */
     float i_pcoef;            /* DTI*1e-20*NEUTRAL_DENSITY */
     double me, mi, dt, dti, threshold, reduced_mass;
+    /* electron speed below which e_collisions::ionization certainly gives
+     * a negative excess energy, hence NaN velocities (see mcc_one)      */
+    float ion_vcap;
     int n_neutral;
     uint64_t seed;
 };

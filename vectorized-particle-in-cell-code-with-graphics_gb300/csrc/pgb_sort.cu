@@ -13,7 +13,7 @@
  * so the resulting order -- and every order-dependent rule that follows it
  * (charge-exchange accumulation, wall-list order) -- is deterministic.  It
  * also drops removed particles (tombstones).  Passes:
- *   count    per chunk of 4096 slots, a shared histogram of bin keys
+ *   count    per chunk of SORT_CHUNK slots, a shared histogram of bin keys
  *   scan     per bin over chunks, then over bins with tile padding
  *   scatter  one warp per chunk walks its slots in order and writes each
  *            particle to its bin at a running per-bin cursor
@@ -23,7 +23,7 @@
 #include "pgb_internal.h"
 #include "pgb_physics.cuh"
 
-#define SORT_CHUNK 4096
+#define SORT_CHUNK PGB_SORT_CHUNK
 
 struct SortArgs {
     Species S;
@@ -68,75 +68,105 @@ __global__ void __launch_bounds__(256) k_sort_count(SortArgs a) {
     }
 }
 
-/* per key: exclusive scan over the live chunks */
-__global__ void __launch_bounds__(256) k_sort_scan_keys(SortArgs a) {
+/* exclusive scan of one value per thread over the CTA; *total = the sum.
+ * Every thread of the CTA must call it.                                  */
+__device__ __forceinline__ long long block_excl_scan_ll(long long v, long long* s_w, long long& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    long long x = v;
+    for (int d = 1; d < 32; d <<= 1) {
+        long long y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        long long w = lane < nw ? s_w[lane] : 0;
+        for (int d = 1; d < 32; d <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, w, d);
+            if (lane >= d) w += y;
+        }
+        if (lane < nw) s_w[lane] = w;   /* inclusive over warps */
+    }
+    __syncthreads();
+    long long before = warp ? s_w[warp - 1] : 0;
+    total = s_w[nw - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+/* per key: exclusive scan over the live chunks (one CTA per key) */
+__global__ void __launch_bounds__(1024) k_sort_scan_keys(SortArgs a) {
     const long long n = a.ds->n[a.s];
     const int nch = (int)((n + SORT_CHUNK - 1) / SORT_CHUNK);
-    __shared__ int s_w[8];
-    __shared__ int s_carry;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ long long s_w[32];
     for (int key = blockIdx.x; key <= a.nbins; key += gridDim.x) {
         const int* row = a.counts + (long long)key * a.nchunks_cap;
         int* out = a.offs + (long long)key * a.nchunks_cap;
-        if (threadIdx.x == 0) s_carry = 0;
-        __syncthreads();
-        for (int b = 0; b < nch; b += 256) {
+        long long carry = 0;
+        for (int b = 0; b < nch; b += blockDim.x) {
             int c = b + threadIdx.x;
-            int v = c < nch ? row[c] : 0;
-            int x = v;
-            for (int d = 1; d < 32; d <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, x, d);
-                if (lane >= d) x += y;
-            }
-            if (lane == 31) s_w[warp] = x;
-            __syncthreads();
-            int wo = 0;
-            for (int w = 0; w < warp; ++w) wo += s_w[w];
-            if (c < nch) out[c] = s_carry + wo + x - v;
-            __syncthreads();
-            if (threadIdx.x == 0) for (int w = 0; w < 8; ++w) s_carry += s_w[w];
-            __syncthreads();
+            long long v = c < nch ? row[c] : 0, tot;
+            long long ex = block_excl_scan_ll(v, s_w, tot);
+            if (c < nch) out[c] = (int)(carry + ex);
+            carry += tot;
         }
-        if (threadIdx.x == 0) a.key_total[key] = s_carry;
-        __syncthreads();
+        if (threadIdx.x == 0) a.key_total[key] = (int)carry;
     }
 }
 
-/* over keys: padded starts (each key begins on a tile boundary), pieces */
+/* over keys: padded starts (each key begins on a tile boundary), pieces.
+ * One CTA scans the keys 1024 at a time (tiles and pieces per key), each
+ * key's thread writes its pieces, then every tile finds its key by binary
+ * search over the starts.                                               */
 __global__ void __launch_bounds__(1024) k_sort_scan_bins(SortArgs a) {
-    __shared__ long long s_tot;
-    __shared__ int s_np;
-    if (threadIdx.x == 0) {
-        long long acc = 0;
-        int np = 0;
-        for (int key = 0; key <= a.nbins; ++key) {
-            a.key_start[key] = acc;
+    __shared__ long long s_w[32];
+    long long carry_t = 0, carry_p = 0;
+    for (int base = 0; base <= a.nbins; base += blockDim.x) {
+        const int key = base + threadIdx.x;
+        long long tiles = 0, np = 0;
+        if (key <= a.nbins) {
             long long c = a.key_total[key];
-            long long tiles = (c + PGB_TILE - 1) / PGB_TILE;
-            int bin = key < a.nbins ? key : -1;
-            for (long long t = 0; t < tiles; t += a.piece_tiles) {
-                int len = (int)((tiles - t) < a.piece_tiles ? (tiles - t) : a.piece_tiles);
-                a.pieces[np++] = make_int4((int)(acc / PGB_TILE + t), len, bin, 0);
-            }
-            acc += tiles * PGB_TILE;
+            tiles = (c + PGB_TILE - 1) / PGB_TILE;
+            np = (tiles + a.piece_tiles - 1) / a.piece_tiles;
         }
-        a.key_start[a.nbins + 1] = acc;
-        s_tot = acc;
-        s_np = np;
+        long long tot_t, tot_p;
+        long long t0 = carry_t + block_excl_scan_ll(tiles, s_w, tot_t);
+        long long p0 = carry_p + block_excl_scan_ll(np, s_w, tot_p);
+        if (key <= a.nbins) {
+            a.key_start[key] = t0 * PGB_TILE;
+            const int bin = key < a.nbins ? key : -1;
+            for (long long q = 0; q < np; ++q) {
+                long long t = q * a.piece_tiles;
+                int len = (int)((tiles - t) < a.piece_tiles ? (tiles - t) : a.piece_tiles);
+                a.pieces[p0 + q] = make_int4((int)(t0 + t), len, bin, 0);
+            }
+        }
+        carry_t += tot_t;
+        carry_p += tot_p;
+    }
+    if (threadIdx.x == 0) {
+        a.key_start[a.nbins + 1] = carry_t * PGB_TILE;
+        a.ds->n_pieces[a.s] = (int)carry_p;
+        a.ds->sorted_tiles[a.s] = carry_t;
     }
     __syncthreads();
-    /* tile -> bin map */
-    for (int key = 0; key <= a.nbins; ++key) {
-        long long t0 = a.key_start[key] / PGB_TILE, t1 = a.key_start[key + 1] / PGB_TILE;
-        for (long long t = t0 + threadIdx.x; t < t1; t += blockDim.x) a.tile_bin[t] = key < a.nbins ? key : -1;
-    }
-    if (threadIdx.x == 0) {
-        a.ds->n_pieces[a.s] = s_np;
-        a.ds->sorted_tiles[a.s] = s_tot / PGB_TILE;
+    /* tile -> bin map: the key whose [start, next start) holds the tile */
+    for (long long t = threadIdx.x; t < carry_t; t += blockDim.x) {
+        const long long slot = t * PGB_TILE;
+        int lo = 0, hi = a.nbins;   /* largest key with key_start <= slot */
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (a.key_start[mid] <= slot) lo = mid;
+            else hi = mid - 1;
+        }
+        a.tile_bin[t] = lo < a.nbins ? lo : -1;
     }
 }
 
-/* one warp per chunk: stable placement at per-key cursors */
+/* one warp per chunk: stable placement at per-key cursors.  Four batches of
+ * 32 slots are loaded at once (memory-level parallelism), then placed in
+ * slot order.                                                           */
+#define SCATTER_BATCHES 4
 __global__ void __launch_bounds__(256) k_sort_scatter(SortArgs a) {
     extern __shared__ long long s_cur[];   /* [warp][key] */
     const long long n = a.ds->n[a.s];
@@ -147,25 +177,37 @@ __global__ void __launch_bounds__(256) k_sort_scatter(SortArgs a) {
     for (int c = blockIdx.x * nw + warp; c < nch; c += gridDim.x * nw) {
         for (int k = lane; k <= a.nbins; k += 32) cur[k] = a.key_start[k] + a.offs[(long long)k * a.nchunks_cap + c];
         __syncwarp();
-        for (int b = 0; b < SORT_CHUNK; b += 32) {
-            long long i = (long long)c * SORT_CHUNK + b + lane;
-            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-            int key = -1;
-            if (i < n) {
-                p = a.S.xv[i];
-                key = bin_key(p, a.nx, a.ny, a.nbx, a.nbins);
+        for (int b = 0; b < SORT_CHUNK; b += 32 * SCATTER_BATCHES) {
+            float4 p[SCATTER_BATCHES];
+            float vz[SCATTER_BATCHES], w[SCATTER_BATCHES];
+            unsigned int id[SCATTER_BATCHES];
+            int key[SCATTER_BATCHES];
+#pragma unroll
+            for (int u = 0; u < SCATTER_BATCHES; ++u) {
+                long long i = (long long)c * SORT_CHUNK + b + u * 32 + lane;
+                key[u] = -1;
+                if (i < n) {
+                    p[u] = a.S.xv[i];
+                    vz[u] = a.S.vz[i];
+                    w[u] = a.S.w[i];
+                    id[u] = a.S.id[i];
+                    key[u] = bin_key(p[u], a.nx, a.ny, a.nbx, a.nbins);
+                }
             }
-            unsigned peers = __match_any_sync(0xffffffffu, key);
-            long long pos = -1;
-            if (key >= 0) pos = cur[key] + __popc(peers & lt);
-            __syncwarp();
-            if (key >= 0 && (peers & lt) == 0) cur[key] += __popc(peers);
-            __syncwarp();
-            if (key >= 0) {
-                a.S.xv2[pos] = p;
-                a.S.vz2[pos] = a.S.vz[i];
-                a.S.w2[pos] = a.S.w[i];
-                a.S.id2[pos] = a.S.id[i];
+#pragma unroll
+            for (int u = 0; u < SCATTER_BATCHES; ++u) {
+                unsigned peers = __match_any_sync(0xffffffffu, key[u]);
+                long long pos = -1;
+                if (key[u] >= 0) pos = cur[key[u]] + __popc(peers & lt);
+                __syncwarp();
+                if (key[u] >= 0 && (peers & lt) == 0) cur[key[u]] += __popc(peers);
+                __syncwarp();
+                if (key[u] >= 0) {
+                    a.S.xv2[pos] = p[u];
+                    a.S.vz2[pos] = vz[u];
+                    a.S.w2[pos] = w[u];
+                    a.S.id2[pos] = id[u];
+                }
             }
         }
         __syncwarp();
@@ -210,7 +252,7 @@ int pgb_launch_sort(pgb_run* r, int s) {
     size_t hist = sizeof(int) * (a.nbins + 1);
     k_sort_count<<<r->sms * 4, 256, hist, r->stream>>>(a);
     r->launches++;
-    k_sort_scan_keys<<<r->sms * 2, 256, 0, r->stream>>>(a);
+    k_sort_scan_keys<<<r->sms * 2, 1024, 0, r->stream>>>(a);
     r->launches++;
     k_sort_scan_bins<<<1, 1024, 0, r->stream>>>(a);
     r->launches++;
