@@ -241,15 +241,28 @@ __device__ __forceinline__ void push_tile_mcc(const PushArgs& a, const PushConst
     /* 1: collision tests; scattering events go to the queue.  Only the
      * codes live across the barriers; step 3 reads the particle again
      * (from L1/L2)                                                     */
+    float4 pa[PGB_ITEMS];
+    float vza[PGB_ITEMS];
+    unsigned int ida[PGB_ITEMS];
+#pragma unroll
+    for (int k = 0; k < PGB_ITEMS; ++k) {
+        long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+        pa[k] = make_float4(-INFINITY, 0.0f, 0.0f, 0.0f);
+        vza[k] = 0.0f;
+        ida[k] = 0u;
+        if (i < n) {
+            pa[k] = a.xv[i];
+            vza[k] = a.vz[i];
+            ida[k] = a.id[i];
+        }
+    }
 #pragma unroll
     for (int k = 0; k < PGB_ITEMS; ++k) {
         code[k] = -1;
-        long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
-        if (i >= n) continue;
-        float4 p = a.xv[i];
+        const float4 p = pa[k];
         if (is_dead(p.x)) continue;
-        float vz = a.vz[i];
-        unsigned int id = a.id[i];
+        const float vz = vza[k];
+        const unsigned int id = ida[k];
         float energy;
         pgb_stream st;
         int ev = mcc_test(a.cc, id, step, pc.nx, pc.ny, p, vz, &energy, &st);
@@ -320,20 +333,33 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
     }
     const long long base = (long long)tile * PGB_TILE;
     bool f[1][PGB_ITEMS];
+    /* all loads of the thread's items first, so that they are in flight
+     * together, then the pushes                                          */
+    float4 p[PGB_ITEMS];
+    float vz[PGB_ITEMS], w[PGB_ITEMS];
+#pragma unroll
+    for (int k = 0; k < PGB_ITEMS; ++k) {
+        long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+        p[k] = make_float4(-INFINITY, 0.0f, 0.0f, 0.0f);
+        vz[k] = 0.0f;
+        w[k] = 0.0f;
+        if (i < n) {
+            p[k] = a.xv[i];
+            if (pc.bfield) vz[k] = a.vz[i];
+            if (DEP) w[k] = a.w[i];
+        }
+    }
 #pragma unroll
     for (int k = 0; k < PGB_ITEMS; ++k) {
         f[0][k] = false;
         long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
-        if (i >= n) continue;
-        float4 p = a.xv[i];
-        if (is_dead(p.x)) continue;
-        float vz = pc.bfield ? a.vz[i] : 0.0f;
+        if (is_dead(p[k].x)) continue;
         bool moved;
-        gather_push_one(pc, a.exy, p, vz, moved);
-        if (moved) a.xv[i] = p;
-        if (pc.bfield && moved) a.vz[i] = vz;
-        if (DEP && deposit_ok(p.x, p.y, pc.nx, pc.ny)) deposit_win(a.qacc, win, ox, oy, pc.nx, p.x, p.y, a.w[i]);
-        f[0][k] = pc.steady ? outside_steady(p.x, p.y, pc.nx, pc.ny) : outside_absorbing(p.x, p.y, pc.nx, pc.ny);
+        gather_push_one(pc, a.exy, p[k], vz[k], moved);
+        if (moved) a.xv[i] = p[k];
+        if (pc.bfield && moved) a.vz[i] = vz[k];
+        if (DEP && deposit_ok(p[k].x, p[k].y, pc.nx, pc.ny)) deposit_win(a.qacc, win, ox, oy, pc.nx, p[k].x, p[k].y, w[k]);
+        f[0][k] = pc.steady ? outside_steady(p[k].x, p[k].y, pc.nx, pc.ny) : outside_absorbing(p[k].x, p[k].y, pc.nx, pc.ny);
     }
     int* const tl[1] = {a.tl_out};
     int* const tc[1] = {a.tc_out};
@@ -343,7 +369,7 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
 /* Work items: the bin pieces of the last sort (tiles of one bin, deposited
  * through a shared window), then every tile after the sorted region.     */
 template <bool MCC, bool DEP>
-__global__ void __launch_bounds__(PGB_PUSH_THREADS) k_push(PushArgs a) {
+__global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
     __shared__ unsigned long long s_win[PGB_WIN * PGB_WIN];
     __shared__ ScatterQueue s_q;
     if (MCC && threadIdx.x == 0) s_q.n = 0;
