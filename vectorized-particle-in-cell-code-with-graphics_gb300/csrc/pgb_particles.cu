@@ -89,14 +89,19 @@ __device__ __forceinline__ int mcc_test(const CollConsts& cc, unsigned int id, u
     float u2 = p.z * p.z + p.w * p.w + vz * vz;
     float energy = cc.e_energy_coef * u2;
     float u = sqrtf(u2);
-    float sel = sigma_el(cc, energy), sio = sigma_ion(cc, energy);
     pgb_stream_init(st, cc.seed, id, step, PGB_STREAM_EMCC, 0);
     float R = pgb_u01f(pgb_stream_u32(st));
-    float P = -expm1f(-(u * cc.e_pcoef * sel));
     int ev = 0;
-    if (P > 2.0f * R) ev |= MCC_SCATTER;
+    /* P = 1 - exp(-x) is at most 1, so P > 2R cannot hold for R >= 1/2:
+     * the cross-section and the exponential are needed only below      */
+    if (R < 0.5f) {
+        float sel = sigma_el(cc, energy);
+        float P = -expm1f(-(u * cc.e_pcoef * sel));
+        if (P > 2.0f * R) ev |= MCC_SCATTER;
+    }
     /* the ionization test is P = 1 - exp(-x) > 0 (e_collisions.cpp:546-551),
      * which holds exactly when x > 0 (for NaN x neither holds)          */
+    float sio = sigma_ion(cc, energy);
     if (u * cc.e_pcoef * sio > 0.0f) ev |= MCC_IONIZE;
     *energy_out = energy;
     return ev;

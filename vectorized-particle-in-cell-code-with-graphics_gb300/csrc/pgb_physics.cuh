@@ -109,10 +109,12 @@ __device__ __forceinline__ float sig_ar_cx(float e) {
  * +inf for any physical energy; the FP64 value (~1e-72) gives the same zero
  * probability once it enters 1-exp(-x) and the fixed-point accumulator.   */
 __device__ __forceinline__ float sig_h_cx(float e) {
+    /* from ee = 1e10 on, ee^5.4 overflows FP32: den is +inf and the result
+     * is exactly 0, so the powers and the logarithm are skipped.  A product
+     * within 1e-6 of ee decides the common case without the two divisions */
+    if (e * (1.0f / (1000.0f * 1.66054e-27f)) >= 2.0e10f) return 0.0f;
     float ee = e / 1000.0f / 1.66054e-27f;
     if (!(ee >= 1.0e-4f)) return 0.0f;
-    /* from ee = 1e10 on, ee^5.4 overflows FP32: den is +inf and the result
-     * is exactly 0, so the powers and the logarithm are skipped           */
     if (ee >= 1.0e10f) return 0.0f;
     float den = 1.0f + 0.038371f * ee + 3.8068e-6f * __powf(ee, 3.5f) + 1.1832e-10f * __powf(ee, 5.4f);
     return (3.2345f * logf((235.88f / ee) + 2.3713f)) / den;

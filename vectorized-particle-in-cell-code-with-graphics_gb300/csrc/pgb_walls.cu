@@ -429,8 +429,9 @@ __device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, fl
     col = jp;
     float u2 = __fadd_rn(__fadd_rn(__fmul_rn(p.z, p.z), __fmul_rn(p.w, p.w)), __fmul_rn(vz, vz));
     float energy = __fmul_rn(a.ecoef, u2);
-    float u = sqrtf(u2);
     float s = sigma_cx(a.cc, energy);
+    if (s == 0.0f) return 0;   /* P = -expm1f(-0) = 0 */
+    float u = sqrtf(u2);
     /* no contraction: both CX passes must compute the same bits */
     float P = -expm1f(-__fmul_rn(__fmul_rn(u, a.pcoef), s));
     return __float2ll_rn(P * 1099511627776.0f);   /* P * 2^40, exact scaling */
@@ -443,12 +444,24 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         for (int c = threadIdx.x; c < a.nx; c += blockDim.x) s_sum[c] = 0ull;
         __syncthreads();
-#pragma unroll 4
-        for (int k = threadIdx.x; k < CX_TILE; k += blockDim.x) {
-            long long i = (long long)t * CX_TILE + k;
-            if (i < n) {
+        /* four ions per thread in flight at a time */
+        for (int k0 = threadIdx.x; k0 < CX_TILE; k0 += 4 * blockDim.x) {
+            float4 p[4];
+            float vz[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                long long i = (long long)t * CX_TILE + k0 + q * blockDim.x;
+                p[q] = make_float4(-INFINITY, 0.f, 0.f, 0.f);
+                vz[q] = 0.f;
+                if (k0 + q * blockDim.x < CX_TILE && i < n) {
+                    p[q] = a.i.xv[i];
+                    vz[q] = a.i.vz[i];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
                 int col;
-                long long pf = cx_prob_fixed(a, a.i.xv[i], a.i.vz[i], col);
+                long long pf = cx_prob_fixed(a, p[q], vz[q], col);
                 if (col >= 0 && pf) atomicAdd(&s_sum[col], (unsigned long long)pf);
             }
         }
