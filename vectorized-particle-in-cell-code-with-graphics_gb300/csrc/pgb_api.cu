@@ -270,8 +270,15 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
     if (!pgb_cuda_ok(nullptr, cudaGetDevice(&r->dev), "cudaGetDevice")) return bail(PGB_ERR_CUDA);
     if (!pgb_cuda_ok(nullptr, cudaDeviceGetAttribute(&r->sms, cudaDevAttrMultiProcessorCount, r->dev), "sm count"))
         return bail(PGB_ERR_CUDA);
-    if (!pgb_cuda_ok(nullptr, cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "cudaStreamCreate"))
+    if (!pgb_cuda_ok(nullptr, cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !pgb_cuda_ok(nullptr, cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate"))
         return bail(PGB_ERR_CUDA);
+    for (int k = 0; k < PGB_COPY_EVENTS; ++k)
+        if (!pgb_cuda_ok(nullptr, cudaEventCreateWithFlags(&r->copy_ev[k], cudaEventDisableTiming), "cudaEventCreate")) {
+            for (int j = 0; j < k; ++j) cudaEventDestroy(r->copy_ev[j]);
+            return bail(PGB_ERR_CUDA);
+        }
+    r->copy_ev_ok = true;
     const size_t G = (size_t)r->nx * r->ny, GE = (size_t)(r->nx + 1) * (r->ny + 1);
     bool ok = true;
     ok = ok && cudaMalloc(&r->ds, sizeof(DevState)) == cudaSuccess;
@@ -364,6 +371,9 @@ extern "C" int pgb_destroy(pgb_run* r) {
     cudaFree(r->kh);
     if (r->prof_ev_ok)
         for (int k = 0; k < 12; ++k) cudaEventDestroy(r->prof_ev[k]);
+    if (r->copy_ev_ok)
+        for (int k = 0; k < PGB_COPY_EVENTS; ++k) cudaEventDestroy(r->copy_ev[k]);
+    if (r->copy_stream) cudaStreamDestroy(r->copy_stream);
     if (r->stream) cudaStreamDestroy(r->stream);
     delete r;
     return 0;
@@ -393,8 +403,19 @@ extern "C" int pgb_load_species(pgb_run* r, int s, const double* aos6, int64_t n
     if ((rc = ensure_capacity(r, 1 - s, std::max<long long>(r->sp[1 - s].cap, 1024)))) return rc;
     if (n > 0) {
         if ((rc = dstage(r, sizeof(double) * 6 * n))) return rc;
-        if (cudaMemcpyAsync(r->d_stage, aos6, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, r->stream) != cudaSuccess ||
-            pgb_launch_load(r, s, r->d_stage, n) || cudaStreamSynchronize(r->stream) != cudaSuccess)
+        /* chunks: the copy of chunk c+1 (copy stream) overlaps the
+         * conversion of chunk c (run stream)                              */
+        bool ok = cudaEventRecord(r->copy_ev[0], r->stream) == cudaSuccess &&
+                  cudaStreamWaitEvent(r->copy_stream, r->copy_ev[0], 0) == cudaSuccess;
+        for (long long c = 0, k = 1; ok && c < n; c += PGB_COPY_CHUNK, ++k) {
+            const long long e = std::min<long long>(n, c + PGB_COPY_CHUNK);
+            cudaEvent_t ev = r->copy_ev[k % PGB_COPY_EVENTS];
+            ok = cudaMemcpyAsync(r->d_stage + 6 * c, aos6 + 6 * c, sizeof(double) * 6 * (e - c), cudaMemcpyHostToDevice,
+                                 r->copy_stream) == cudaSuccess &&
+                 cudaEventRecord(ev, r->copy_stream) == cudaSuccess &&
+                 cudaStreamWaitEvent(r->stream, ev, 0) == cudaSuccess && pgb_launch_load(r, s, r->d_stage, c, e) == 0;
+        }
+        if (!ok || cudaStreamSynchronize(r->stream) != cudaSuccess)
             return fail(r, PGB_ERR_CUDA, "pgb_load_species: upload failed");
     }
     r->hs->n[s] = n;
@@ -426,9 +447,27 @@ extern "C" int pgb_dump_species(pgb_run* r, int s, double* aos6, int64_t cap, in
     long long m = std::min<long long>(live, cap);
     if (m <= 0 || r->sp[s].cap == 0) return 0;
     if ((rc = dstage(r, sizeof(double) * 6 * live))) return rc;
-    if (pgb_launch_dump(r, s, r->d_stage, live) ||
-        cudaMemcpyAsync(aos6, r->d_stage, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost, r->stream) != cudaSuccess ||
+    /* live-slot offsets of every tile, then chunks of tiles: the copy of
+     * chunk c (copy stream) overlaps the packing of chunk c+1 (run stream) */
+    const long long n = r->hs->n[s];
+    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    std::vector<int> toff((size_t)ntiles);
+    if (pgb_launch_dump_offsets(r, s) ||
+        cudaMemcpyAsync(toff.data(), r->aux_j, sizeof(int) * (size_t)ntiles, cudaMemcpyDeviceToHost, r->stream) != cudaSuccess ||
         cudaStreamSynchronize(r->stream) != cudaSuccess)
+        return fail(r, PGB_ERR_CUDA, "pgb_dump_species: offsets failed");
+    const int per = PGB_COPY_CHUNK / PGB_TILE;
+    bool ok = true;
+    for (int t0 = 0, k = 0; ok && t0 < ntiles; t0 += per, ++k) {
+        const int t1 = std::min(ntiles, t0 + per);
+        const long long a = std::min<long long>(toff[t0], m), b = std::min<long long>(t1 < ntiles ? toff[t1] : live, m);
+        cudaEvent_t ev = r->copy_ev[k % PGB_COPY_EVENTS];
+        ok = pgb_launch_dump(r, s, r->d_stage, live, t0, t1) == 0 && cudaEventRecord(ev, r->stream) == cudaSuccess &&
+             cudaStreamWaitEvent(r->copy_stream, ev, 0) == cudaSuccess &&
+             (b <= a || cudaMemcpyAsync(aos6 + 6 * a, r->d_stage + 6 * a, sizeof(double) * 6 * (b - a),
+                                        cudaMemcpyDeviceToHost, r->copy_stream) == cudaSuccess);
+    }
+    if (!ok || cudaStreamSynchronize(r->copy_stream) != cudaSuccess || cudaStreamSynchronize(r->stream) != cudaSuccess)
         return fail(r, PGB_ERR_CUDA, "pgb_dump_species: download failed");
     return 0;
 }

@@ -33,6 +33,8 @@
 #define PGB_WIN (PGB_BIN + 2 * PGB_HALO + 1)   /* window edge in nodes         */
 #define PGB_PIECE_TILES 4      /* tiles of one bin per work piece             */
 #define PGB_SORT_CHUNK 2048    /* slots per chunk of the bin sort passes      */
+#define PGB_COPY_CHUNK (1 << 20)   /* particles per host-copy chunk of load/dump */
+#define PGB_COPY_EVENTS 32
 
 enum { ST_ABS_E = 0, ST_ABS_I, ST_PLOP, ST_REFL, ST_BACK, ST_SEE_EV, ST_SEE_EM, ST_ISEE_EM,
        ST_ELASTIC, ST_IONIZE, ST_CX, ST_INJ_E, ST_INJ_I, ST_RED_E, ST_RED_I, ST_COUNT };
@@ -146,6 +148,9 @@ struct pgb_run {
     size_t h_stage_bytes = 0;
     double* d_stage = nullptr;     /* device staging for load/dump (AoS doubles) */
     size_t d_stage_bytes = 0;
+    cudaStream_t copy_stream = nullptr;   /* host copies of load/dump, overlapped with their kernels */
+    cudaEvent_t copy_ev[PGB_COPY_EVENTS];
+    bool copy_ev_ok = false;
     /* instrumentation */
     long long launches = 0;        /* kernel launches issued                     */
     int prof_on = 0;
@@ -175,8 +180,9 @@ int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i);
 int pgb_launch_mcc(pgb_run* r);
 int pgb_launch_cx(pgb_run* r);
 int pgb_launch_walls(pgb_run* r, int which);
-int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long n);
-int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap);
+int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long i0, long long i1);
+int pgb_launch_dump_offsets(pgb_run* r, int s);
+int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap, int t0, int t1);
 int pgb_mg_setup(pgb_run* r);
 void pgb_mg_free(pgb_run* r);
 CollConsts pgb_coll_consts(pgb_run* r);

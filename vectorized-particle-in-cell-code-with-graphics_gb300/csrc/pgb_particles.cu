@@ -760,8 +760,9 @@ __global__ void k_compact_commit(DevState* ds, int s, const long long* total) {
 }
 
 /* ------------------------------------------------------------ load / dump */
-__global__ void k_load(Species S, const double* aos, long long n, double dx, double dy) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+/* slots [i0, i1) from records aos[6 i ..] */
+__global__ void k_load(Species S, const double* aos, long long i0, long long i1, double dx, double dy) {
+    for (long long i = i0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < i1; i += (long long)gridDim.x * blockDim.x) {
         const double* r = aos + 6 * i;
         S.xv[i] = make_float4((float)(r[0] / dx), (float)(r[1] / dy), (float)r[2], (float)r[3]);
         S.vz[i] = (float)r[4];
@@ -771,13 +772,14 @@ __global__ void k_load(Species S, const double* aos, long long n, double dx, dou
 }
 /* dump live slots in order: out[j] for the j-th live slot; pos[] = exclusive
  * scan of the per-tile live counts                                        */
+/* tiles [t0, t1) of the live-slot order */
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_dump(Species S, DevState* ds, int s, const int* toff, double dx,
-                                                           double dy, double* out, long long cap) {
+                                                           double dy, double* out, long long cap, int t0, int t1) {
     const long long n = ds->n[s];
-    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    const int ntiles = min(t1, (int)((n + PGB_TILE - 1) / PGB_TILE));
     __shared__ int s_off[PGB_ITEMS][PGB_PUSH_THREADS / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int tile = t0 + blockIdx.x; tile < ntiles; tile += gridDim.x) {
         bool f[PGB_ITEMS];
         unsigned m[PGB_ITEMS];
         for (int k = 0; k < PGB_ITEMS; ++k) {
@@ -979,22 +981,28 @@ int pgb_launch_compact(pgb_run* r, int s) {
     return 0;
 }
 
-int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long n) {
-    k_load<<<grid_for(r, 4), 256, 0, r->stream>>>(r->sp[s], d_aos, n, r->dx, r->dy);
+int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long i0, long long i1) {
+    k_load<<<grid_for(r, 4), 256, 0, r->stream>>>(r->sp[s], d_aos, i0, i1, r->dx, r->dy);
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
 
-int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap) {
+/* live-slot offsets per tile (into r->aux_j) for pgb_launch_dump */
+int pgb_launch_dump_offsets(pgb_run* r, int s) {
     int* tc = r->tile_cnt[LIST_SPARE];
-    int* toff = r->aux_j;
     PGB_CK(r, cudaMemsetAsync(tc, 0, sizeof(int) * r->ntiles_cap, r->stream));
     k_alive_count<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s].xv, r->ds, s, tc);
     r->launches++;
-    k_scan_small<<<1, 1024, 0, r->stream>>>(tc, toff, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]);
+    k_scan_small<<<1, 1024, 0, r->stream>>>(tc, r->aux_j, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]);
     r->launches++;
-    k_dump<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s], r->ds, s, toff, r->dx, r->dy, d_out, cap);
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap, int t0, int t1) {
+    k_dump<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s], r->ds, s, r->aux_j, r->dx, r->dy, d_out, cap,
+                                                               t0, t1);
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
