@@ -205,9 +205,28 @@ __device__ __forceinline__ void tile_lists(const bool (&f)[NL][PGB_ITEMS], long 
     __syncthreads();
 }
 
+/* The shared deposit window holds each node's int64 sum as two 32-bit
+ * words, low words first (PGB_WIN^2 of them), then high words: 32-bit
+ * shared atomics are native, 64-bit ones are not.  A contribution adds its
+ * low word; the carry out of it (seen in the returned old value) and the
+ * contribution's high word go to the high word.  The pair then holds the
+ * exact 64-bit sum modulo 2^64, in any order of the adds.               */
+#define WIN_NODES (PGB_WIN * PGB_WIN)
+__device__ __forceinline__ void win_add(unsigned int* win, int k, long long c) {
+    const unsigned long long u = (unsigned long long)c;
+    const unsigned int l = (unsigned int)u;
+    unsigned int h = (unsigned int)(u >> 32);
+    const unsigned int old = atomicAdd(&win[k], l);
+    h += (old + l < old) ? 1u : 0u;
+    if (h) atomicAdd(&win[WIN_NODES + k], h);
+}
+__device__ __forceinline__ unsigned long long win_get(const unsigned int* win, int k) {
+    return ((unsigned long long)win[WIN_NODES + k] << 32) | win[k];
+}
+
 /* deposit into the CTA's shared window when the four nodes fall inside it,
  * else into the global grid                                               */
-__device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned long long* win, int ox, int oy, int nx,
+__device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned int* win, int ox, int oy, int nx,
                                             float xs, float ys, float w) {
     int jp = cellf(xs), kp = cellf(ys);
     int lx = jp - ox, ly = kp - oy;
@@ -216,11 +235,11 @@ __device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned l
         float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
         float a2 = wk * (1.0f - wj), a1 = wj * wk;
         const float S = 4294967296.0f;
-        unsigned long long* q = win + ly * PGB_WIN + lx;
-        atomicAdd(q, (unsigned long long)__float2ll_rn(a4 * w * S));
-        atomicAdd(q + 1, (unsigned long long)__float2ll_rn(a3 * w * S));
-        atomicAdd(q + PGB_WIN, (unsigned long long)__float2ll_rn(a2 * w * S));
-        atomicAdd(q + PGB_WIN + 1, (unsigned long long)__float2ll_rn(a1 * w * S));
+        const int k = ly * PGB_WIN + lx;
+        win_add(win, k, __float2ll_rn(a4 * w * S));
+        win_add(win, k + 1, __float2ll_rn(a3 * w * S));
+        win_add(win, k + PGB_WIN, __float2ll_rn(a2 * w * S));
+        win_add(win, k + PGB_WIN + 1, __float2ll_rn(a1 * w * S));
     } else {
         deposit_cell(qacc, nx, xs, ys, w);
     }
@@ -239,7 +258,7 @@ struct ScatterQueue {
 
 template <bool DEP>
 __device__ __forceinline__ void push_tile_mcc(const PushArgs& a, const PushConsts& pc, int tile, long long n,
-                                              unsigned long long* win, int ox, int oy, unsigned step,
+                                              unsigned int* win, int ox, int oy, unsigned step,
                                               int (&st_loc)[2], ScatterQueue& q) {
     const long long base = (long long)tile * PGB_TILE;
     int code[PGB_ITEMS];   /* -1 absent; else MCC bits | (queue slot + 1) << 2 */
@@ -330,7 +349,7 @@ __device__ __forceinline__ void push_tile_mcc(const PushArgs& a, const PushConst
 
 template <bool MCC, bool DEP>
 __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& pc, int tile, long long n,
-                                          unsigned long long* win, int ox, int oy, unsigned step, int (&st_loc)[2],
+                                          unsigned int* win, int ox, int oy, unsigned step, int (&st_loc)[2],
                                           ScatterQueue& q) {
     if (MCC) {
         push_tile_mcc<DEP>(a, pc, tile, n, win, ox, oy, step, st_loc, q);
@@ -375,7 +394,7 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
  * through a shared window), then every tile after the sorted region.     */
 template <bool MCC, bool DEP>
 __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
-    __shared__ unsigned long long s_win[PGB_WIN * PGB_WIN];
+    __shared__ unsigned int s_win[2 * WIN_NODES];
     __shared__ ScatterQueue s_q;
     if (MCC && threadIdx.x == 0) s_q.n = 0;
     __syncthreads();
@@ -390,21 +409,21 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         if (item < npieces) {
             int4 pc4 = a.pieces[item];
-            unsigned long long* win = nullptr;
+            unsigned int* win = nullptr;
             int ox = 0, oy = 0;
             if (DEP && pc4.z >= 0) {
                 win = s_win;
                 ox = (pc4.z % a.nbx) * PGB_BIN - PGB_HALO;
                 oy = (pc4.z / a.nbx) * PGB_BIN - PGB_HALO;
-                for (int k = threadIdx.x; k < PGB_WIN * PGB_WIN; k += blockDim.x) s_win[k] = 0ull;
+                for (int k = threadIdx.x; k < 2 * WIN_NODES; k += blockDim.x) s_win[k] = 0u;
                 __syncthreads();
             }
             for (int t = pc4.x; t < pc4.x + pc4.y && t < ntiles; ++t)
                 push_tile<MCC, DEP>(a, pc, t, n, win, ox, oy, step, st_loc, s_q);
             if (win) {
                 __syncthreads();
-                for (int k = threadIdx.x; k < PGB_WIN * PGB_WIN; k += blockDim.x) {
-                    unsigned long long v = s_win[k];
+                for (int k = threadIdx.x; k < WIN_NODES; k += blockDim.x) {
+                    unsigned long long v = win_get(s_win, k);
                     if (v) {
                         int gx = ox + k % PGB_WIN, gy = oy + k / PGB_WIN;
                         if (gx >= 0 && gy >= 0 && gx < pc.nx && gy < pc.ny)
