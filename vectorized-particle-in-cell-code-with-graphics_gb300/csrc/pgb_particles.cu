@@ -206,22 +206,21 @@ __device__ __forceinline__ void tile_lists(const bool (&f)[NL][PGB_ITEMS], long 
 }
 
 /* The shared deposit window holds each node's int64 sum as two 32-bit
- * words, low words first (PGB_WIN^2 of them), then high words: 32-bit
- * shared atomics are native, 64-bit ones are not.  A contribution adds its
- * low word; the carry out of it (seen in the returned old value) and the
- * contribution's high word go to the high word.  The pair then holds the
- * exact 64-bit sum modulo 2^64, in any order of the adds.               */
+ * sums (32-bit shared atomics are native, 64-bit ones are not): L, the sum
+ * of the contributions' low 16 bits, then H, the sum of the rest (units of
+ * 2^16).  The node's value is L + H 2^16.  A piece holds at most
+ * PGB_PIECE_TILES * PGB_TILE = 4096 particles, so L < 2^28 and, for
+ * weights in [0, 8), H < 2^31: neither wraps.  Other weights deposit
+ * straight into the global int64 grid.                                   */
 #define WIN_NODES (PGB_WIN * PGB_WIN)
+#define WIN_MAX_WEIGHT 8.0f
+static_assert(PGB_PIECE_TILES * PGB_TILE <= 4096, "window sums are sized for 4096 particles per piece");
 __device__ __forceinline__ void win_add(unsigned int* win, int k, long long c) {
-    const unsigned long long u = (unsigned long long)c;
-    const unsigned int l = (unsigned int)u;
-    unsigned int h = (unsigned int)(u >> 32);
-    const unsigned int old = atomicAdd(&win[k], l);
-    h += (old + l < old) ? 1u : 0u;
-    if (h) atomicAdd(&win[WIN_NODES + k], h);
+    atomicAdd(&win[k], (unsigned int)c & 0xFFFFu);
+    atomicAdd(&win[WIN_NODES + k], (unsigned int)((unsigned long long)c >> 16));
 }
 __device__ __forceinline__ unsigned long long win_get(const unsigned int* win, int k) {
-    return ((unsigned long long)win[WIN_NODES + k] << 32) | win[k];
+    return ((unsigned long long)win[WIN_NODES + k] << 16) + win[k];
 }
 
 /* deposit into the CTA's shared window when the four nodes fall inside it,
@@ -230,7 +229,7 @@ __device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned i
                                             float xs, float ys, float w) {
     int jp = cellf(xs), kp = cellf(ys);
     int lx = jp - ox, ly = kp - oy;
-    if (win && lx >= 0 && ly >= 0 && lx < PGB_WIN - 1 && ly < PGB_WIN - 1) {
+    if (win && lx >= 0 && ly >= 0 && lx < PGB_WIN - 1 && ly < PGB_WIN - 1 && w >= 0.0f && w < WIN_MAX_WEIGHT) {
         float wj = xs - (float)jp, wk = ys - (float)kp;
         float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
         float a2 = wk * (1.0f - wj), a1 = wj * wk;
