@@ -24,7 +24,8 @@
 #define PGB_TILE 1024          /* particles per tile of the push kernels   */
 #define PGB_PUSH_THREADS 256
 #define PGB_ITEMS (PGB_TILE / PGB_PUSH_THREADS)
-#define PGB_FIX_SCALE 4294967296.0   /* deposit fixed point: 2^32 per unit weight */
+#define PGB_FIX_SCALE 524288.0      /* deposit fixed point: 2^19 per unit weight */
+#define PGB_FIX_SCALE_F 524288.0f
 #define PGB_MG_SMALL 65        /* levels with n <= 65 are solved by one CTA  */
 #define PGB_MG_SMALL64 33      /* the same for the FP64 multigrid            */
 #define PGB_MAX_LEVELS 16

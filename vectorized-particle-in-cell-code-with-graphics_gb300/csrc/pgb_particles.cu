@@ -205,23 +205,18 @@ __device__ __forceinline__ void tile_lists(const bool (&f)[NL][PGB_ITEMS], long 
     __syncthreads();
 }
 
-/* The shared deposit window holds each node's int64 sum as two 32-bit
- * sums (32-bit shared atomics are native, 64-bit ones are not): L, the sum
- * of the contributions' low 16 bits, then H, the sum of the rest (units of
- * 2^16).  The node's value is L + H 2^16.  A piece holds at most
- * PGB_PIECE_TILES * PGB_TILE = 4096 particles, so L < 2^28 and, for
- * weights in [0, 8), H < 2^31: neither wraps.  Other weights deposit
- * straight into the global int64 grid.                                   */
+/* The shared deposit window holds each node's sum as one 32-bit word
+ * (32-bit shared atomics are native, 64-bit ones are not).  A piece holds
+ * at most PGB_PIECE_TILES * PGB_TILE = 4096 particles, and a contribution
+ * of weight w < 1.99 is at most 1.99 * 2^19 + 1/2, so a node's sum stays
+ * below 2^32.
+ * Other weights deposit straight into the global int64 grid.  Both paths
+ * add the same integer round(a*w*2^19).                                  */
 #define WIN_NODES (PGB_WIN * PGB_WIN)
-#define WIN_MAX_WEIGHT 8.0f
+#define WIN_MAX_WEIGHT 1.99f
 static_assert(PGB_PIECE_TILES * PGB_TILE <= 4096, "window sums are sized for 4096 particles per piece");
-__device__ __forceinline__ void win_add(unsigned int* win, int k, long long c) {
-    atomicAdd(&win[k], (unsigned int)c & 0xFFFFu);
-    atomicAdd(&win[WIN_NODES + k], (unsigned int)((unsigned long long)c >> 16));
-}
-__device__ __forceinline__ unsigned long long win_get(const unsigned int* win, int k) {
-    return ((unsigned long long)win[WIN_NODES + k] << 16) + win[k];
-}
+static_assert((PGB_FIX_SCALE * 1.99 + 1.0) * 4096.0 < 4294967296.0, "window sums must fit 32 bits");
+__device__ __forceinline__ unsigned long long win_get(const unsigned int* win, int k) { return win[k]; }
 
 /* deposit into the CTA's shared window when the four nodes fall inside it,
  * else into the global grid                                               */
@@ -233,12 +228,13 @@ __device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned i
         float wj = xs - (float)jp, wk = ys - (float)kp;
         float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
         float a2 = wk * (1.0f - wj), a1 = wj * wk;
-        const float S = 4294967296.0f;
+        const float S = PGB_FIX_SCALE_F;
         const int k = ly * PGB_WIN + lx;
-        win_add(win, k, __float2ll_rn(a4 * w * S));
-        win_add(win, k + 1, __float2ll_rn(a3 * w * S));
-        win_add(win, k + PGB_WIN, __float2ll_rn(a2 * w * S));
-        win_add(win, k + PGB_WIN + 1, __float2ll_rn(a1 * w * S));
+        /* below 2^20: the 32-bit conversion gives the same integer */
+        atomicAdd(&win[k], (unsigned int)__float2int_rn(a4 * w * S));
+        atomicAdd(&win[k + 1], (unsigned int)__float2int_rn(a3 * w * S));
+        atomicAdd(&win[k + PGB_WIN], (unsigned int)__float2int_rn(a2 * w * S));
+        atomicAdd(&win[k + PGB_WIN + 1], (unsigned int)__float2int_rn(a1 * w * S));
     } else {
         deposit_cell(qacc, nx, xs, ys, w);
     }
@@ -393,7 +389,7 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
  * through a shared window), then every tile after the sorted region.     */
 template <bool MCC, bool DEP>
 __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
-    __shared__ unsigned int s_win[2 * WIN_NODES];
+    __shared__ unsigned int s_win[WIN_NODES];
     __shared__ ScatterQueue s_q;
     if (MCC && threadIdx.x == 0) s_q.n = 0;
     __syncthreads();
@@ -414,7 +410,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
                 win = s_win;
                 ox = (pc4.z % a.nbx) * PGB_BIN - PGB_HALO;
                 oy = (pc4.z / a.nbx) * PGB_BIN - PGB_HALO;
-                for (int k = threadIdx.x; k < 2 * WIN_NODES; k += blockDim.x) s_win[k] = 0u;
+                for (int k = threadIdx.x; k < WIN_NODES; k += blockDim.x) s_win[k] = 0u;
                 __syncthreads();
             }
             for (int t = pc4.x; t < pc4.x + pc4.y && t < ntiles; ++t)

@@ -31,14 +31,15 @@ __device__ __forceinline__ int celld(double v) {
 __device__ __forceinline__ bool is_dead(float xs) { return xs == -INFINITY; }
 
 /* CIC deposit of one particle (pic.cl:36-49) as int64 fixed point:
- * round(a*w*2^32) per node; integer sums are exact and order-free, so the
- * grid is identical run to run.  Caller checks deposit_ok().             */
+ * round(a*w*2^19) per node (1e-6 of a unit weight, below the FP32
+ * rounding of a); integer sums are exact and order-free, so the grid is
+ * identical run to run.  Caller checks deposit_ok().                     */
 __device__ __forceinline__ void deposit_cell(unsigned long long* qacc, int nx, float xs, float ys, float w) {
     int jp = cellf(xs), kp = cellf(ys);
     float wj = xs - (float)jp, wk = ys - (float)kp;
     float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
     float a2 = wk * (1.0f - wj), a1 = wj * wk;
-    const float S = 4294967296.0f;
+    const float S = PGB_FIX_SCALE_F;
     long long c4 = __float2ll_rn(a4 * w * S), c3 = __float2ll_rn(a3 * w * S);
     long long c2 = __float2ll_rn(a2 * w * S), c1 = __float2ll_rn(a1 * w * S);
     unsigned long long* q = qacc + (long long)kp * nx + jp;

@@ -17,7 +17,7 @@
  *   - the charge density qc/(DX*DY);
  *   - edge rows and columns doubled, corners doubled again
  *     (particle.cpp:663-858).
- * The per-node sums are int64 fixed point (2^32 per unit weight), so the
+ * The per-node sums are int64 fixed point (2^19 per unit weight), so the
  * grid does not depend on the order of the records.
  *
  * Scratch: one int64 accumulator per node.  It lives in the file-scope
