@@ -172,6 +172,86 @@ def cpu_sample(n_per_species, steps, threads):
     return ps / dt, dt
 
 
+# ------------------------------------------------------------------ batched
+def batched_configs(picgb, nruns, seed=1004):
+    """Independent Ar runs (the batched workload): grids of 64, 128 or 256
+    cells a side, particles per species log-uniform in [50k, 2M], neutral
+    pressure uniform in [0.005, 0.05] Torr, Te uniform in [1, 4] eV,
+    Ti = 0.026 eV, uniform positions, absorbing walls, the reference's
+    energy-dependent e-Ar and Ar+-Ar fits."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nruns):
+        nodes = int(rng.choice([65, 129, 257]))
+        n = int(round(math.exp(rng.uniform(math.log(5e4), math.log(2e6)))))
+        torr = float(rng.uniform(0.005, 0.05))
+        te = float(rng.uniform(1.0, 4.0))
+        kw = dict(X_NO_OF_CELLS=nodes, TEMPERATURE=te, GAS_PRESSURE_TORR=torr, HAVE_COLLISIONS=True,
+                  SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT", SIGMA_IONIZATION="ENERGY_DEPENDENT",
+                  STEADYSTATE="NO", SIZE_TO_CHECK=2**31 - 1, RAND_SEED=seed + k, POISSON="FMG32", SORT_INTERVAL=8)
+        L = picgb.make_params(**kw).xlength
+        size = 1.0e15 * L * L / n
+        p = picgb.make_params(E_MACROPARTICLE_SIZE=size, ION_MACROPARTICLE_SIZE=size, **kw)
+        r2 = np.random.default_rng(seed + 1000 + k)
+        st = []
+        for m, T in ((9.10939e-31, te), (p.ion_mass, 0.026)):
+            a = np.empty((n, 6))
+            a[:, 0] = r2.uniform(0.0, L, n)
+            a[:, 1] = r2.uniform(0.0, L, n)
+            a[:, 2:5] = r2.normal(0.0, math.sqrt(T * 1.602177e-19 / m), (n, 3))
+            a[:, 5] = 1.0
+            st.append(a)
+        out.append((p, st, nodes, n))
+    return out
+
+
+def run_batched(args):
+    """Plain form (one run after the other, pgb_step) against the batched form
+    (pgb_step_batch over all runs) from the same states."""
+    import picgb
+    cfgs = batched_configs(picgb, args.batch_runs)
+    runs = [picgb.Run(p) for p, _, _, _ in cfgs]
+
+    def load():
+        for r, (_, st, _, _) in zip(runs, cfgs):
+            r.load_particles(0, st[0])
+            r.load_particles(1, st[1])
+            r.set_time_step(0)
+
+    def total():
+        return sum(r.particle_size(0) + r.particle_size(1) for r in runs)
+
+    res = {}
+    for form in ("plain", "batched"):
+        load()
+        # warm-up: graphs of every run are captured outside the timed region
+        for r in runs:
+            r.step(2)
+        load()
+        n0 = total()
+        t0 = time.perf_counter()
+        if form == "plain":
+            for r in runs:
+                r.step(args.batch_steps)
+        else:
+            picgb.step_batch(runs, args.batch_steps)
+        dt = time.perf_counter() - t0
+        n1 = total()
+        ps = 0.5 * (n0 + n1) * args.batch_steps
+        res[form] = {"seconds": dt, "particle_steps_per_s": ps / dt, "runs_per_s": len(runs) / dt,
+                     "ms_per_step_of_every_run": 1000.0 * dt / args.batch_steps}
+    for r in runs:
+        r.close()
+    res["speedup"] = res["batched"]["particle_steps_per_s"] / res["plain"]["particle_steps_per_s"]
+    res["config"] = {"runs": len(cfgs), "steps_per_run": args.batch_steps,
+                     "grid_nodes": sorted(set(c[2] for c in cfgs)),
+                     "particles_per_species": [min(c[3] for c in cfgs), max(c[3] for c in cfgs)],
+                     "workload": "independent Ar runs, absorbing walls, e-Ar and Ar+-Ar collisions; grids "
+                                 "64/128/256 cells, 50k-2M particles/species log-uniform, 0.005-0.05 Torr, "
+                                 "Te 1-4 eV (seeded)"}
+    return res
+
+
 # ------------------------------------------------------------------ GPU path
 def run_gpu(args, rank, world):
     import torch
@@ -236,7 +316,9 @@ def run_gpu(args, rank, world):
         e2e = {"value": tot / wall, "unit": METRIC, "h2d_bytes_per_step": h2d // args.e2e_steps,
                "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps}
     run.close()
-    return dict(ms=ms, ps=ps, counts=(c0, c1), prof=prof, launches=launches, clocks=clk.summary(), e2e=e2e, n=n)
+    batched = run_batched(args) if (args.batch_runs > 0 and world == 1) else None
+    return dict(ms=ms, ps=ps, counts=(c0, c1), prof=prof, launches=launches, clocks=clk.summary(), e2e=e2e, n=n,
+                batched=batched)
 
 
 def main():
@@ -252,6 +334,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--poisson", default="FMG32", choices=["FMG32", "FMG_REF", "FP32_DC"])
     ap.add_argument("--sort", type=int, default=8, help="spatial sort every k steps (0 = off)")
+    ap.add_argument("--batch-runs", type=int, default=64, help="runs of the batched workload (0 = skip it)")
+    ap.add_argument("--batch-steps", type=int, default=200, help="steps per run of the batched workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -328,7 +412,8 @@ def main():
             "vs_baseline": None, "dtype": "f32 particles / f64 fields", "data": "synthetic (seeded)",
             "config": config, "e2e": res["e2e"], "roofline": roofline, "cpu_baseline": cpu,
             "gpu_launches": res["launches"], "clocks": res["clocks"],
-            "particles": {"start": [c0["n_e"], c0["n_i"]], "end": [c1["n_e"], c1["n_i"]]}}
+            "particles": {"start": [c0["n_e"], c0["n_i"]], "end": [c1["n_e"], c1["n_i"]]},
+            "batched": res.get("batched")}
     print(json.dumps(line), flush=True)
 
 

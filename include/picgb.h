@@ -180,6 +180,15 @@ PGB_API int pgb_initial_boundary(pgb_run* run);
  * kernels; same physics and call order as the per-phase entry points.      */
 PGB_API int pgb_step(pgb_run* run, int32_t nsteps);
 
+/* Step several independent runs nsteps each.  It has no counterpart in the
+ * reference, which steps one run per process (pic.cpp:1069-1250).  Each
+ * run's work is queued on its own stream, one step of every run in turn,
+ * so that the kernels of runs too small to fill the GPU overlap.  Every run
+ * ends in the same state as after pgb_step(run, nsteps) alone.  A handle
+ * may appear once only.  On failure the failing run's pgb_last_error (for
+ * an argument error, pgb_last_error(NULL)) holds the message.            */
+PGB_API int pgb_step_batch(pgb_run* const* runs, int32_t nruns, int32_t nsteps);
+
 /* ---- per-phase entry points, in pic_run order ---- */
 PGB_API int pgb_collide_electrons(pgb_run* run);        /* e_collisions::collision (e_collisions.cpp:480-597) */
 PGB_API int pgb_inject(pgb_run* run);                   /* particle::inject_more_particles, e then ions (particle.cpp:491-510) */

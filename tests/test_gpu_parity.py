@@ -425,3 +425,33 @@ def test_batch_driver_runs_and_writes_reference_files(tmp_path):
     rows = [l.split() for l in open(tmp_path / "timeData.txt")]
     assert [int(r[0]) for r in rows] == [0, 100]
     assert all(len(r) == 8 for r in rows)
+
+
+def test_batched_runs_equal_runs_alone():
+    """pgb_step_batch steps independent runs of different sizes and physics
+    on their own streams; each run ends bit-identical to stepping it alone."""
+    cases = ["core33", "arcoll33", "hsee33", "core65"]
+    alone, batched = [], []
+    for mode in ("alone", "batch"):
+        runs = []
+        for c in cases:
+            g = load_golden(c)
+            r = picgb.Run(g["p"])
+            r.load_particles(0, g["e_in"])
+            r.load_particles(1, g["i_in"])
+            r.initial_boundary()
+            runs.append(r)
+        if mode == "alone":
+            for r in runs:
+                r.step(12)
+        else:
+            picgb.step_batch(runs, 12)
+        out = alone if mode == "alone" else batched
+        for r in runs:
+            out.append((r.get_particles(0), r.get_particles(1), r.get_grid("phi"), r.counters()))
+            r.close()
+    for c, a, b in zip(cases, alone, batched):
+        assert np.array_equal(a[0], b[0], equal_nan=True), c
+        assert np.array_equal(a[1], b[1], equal_nan=True), c
+        assert np.array_equal(a[2], b[2]), c
+        assert a[3] == b[3], c

@@ -745,6 +745,42 @@ static int launch_step(pgb_run* r, bool ion_step) {
     return 0;
 }
 
+/* queue step r->time_step of r: host decisions (spatial sort or compaction),
+ * then the step's launches or graph; the host does not wait (except for
+ * profiling and for a population check that may trigger a reduction)     */
+static int issue_one_step(pgb_run* r) {
+    int rc;
+    if (r->p.sort_interval > 0) {
+        /* spatial sort (drops tombstones too) every sort_interval steps */
+        if (r->time_step % r->p.sort_interval == 0)
+            for (int s = 0; s < 2; ++s) {
+                if (pgb_launch_sort(r, s)) return PGB_ERR_CUDA;
+                r->orient[s] ^= 1;
+            }
+    } else {
+        /* compact when tombstones exceed 1/8 of the slots (counts read lazily) */
+        for (int s = 0; s < 2; ++s)
+            if (r->hs->dead[s] * 8 > r->hs->n[s] && r->hs->dead[s] > 0) {
+                if (pgb_launch_compact(r, s)) return PGB_ERR_CUDA;
+                r->orient[s] ^= 1;
+                r->hs->dead[s] = 0;
+            }
+    }
+    if (r->prof_on) {
+        if ((rc = sync_state(r))) return rc;
+        r->prof.slots_e += r->hs->n[0];
+        r->prof.slots_i += r->hs->n[1];
+    }
+    const bool ion_step = (r->time_step % r->dt_dti) == 0;
+    if ((rc = launch_step(r, ion_step))) return rc;
+    if (r->prof_on && (rc = profile_collect(r))) return rc;
+    r->time_step += 1;
+    /* counters come back asynchronously; the host reads them only to
+     * decide when to compact, which never changes results          */
+    PGB_CK(r, cudaMemcpyAsync(r->hs, r->ds, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
+    return 0;
+}
+
 extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
     if (!r || nsteps < 0) return fail(r, PGB_ERR_ARG, "pgb_step: bad argument");
     int rc = need_particles(r);
@@ -753,39 +789,45 @@ extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
     while (done < nsteps) {
         int chunk = std::min<int>(nsteps - done, (int)r->phi_tab_cap);
         if ((rc = set_device_step(r, r->time_step, chunk))) return rc;
-        for (int k = 0; k < chunk; ++k) {
-            if (r->p.sort_interval > 0) {
-                /* spatial sort (drops tombstones too) every sort_interval steps */
-                if (r->time_step % r->p.sort_interval == 0)
-                    for (int s = 0; s < 2; ++s) {
-                        if (pgb_launch_sort(r, s)) return PGB_ERR_CUDA;
-                        r->orient[s] ^= 1;
-                    }
-            } else {
-                /* compact when tombstones exceed 1/8 of the slots (counts read lazily) */
-                for (int s = 0; s < 2; ++s)
-                    if (r->hs->dead[s] * 8 > r->hs->n[s] && r->hs->dead[s] > 0) {
-                        if (pgb_launch_compact(r, s)) return PGB_ERR_CUDA;
-                        r->orient[s] ^= 1;
-                        r->hs->dead[s] = 0;
-                    }
-            }
-            if (r->prof_on) {
-                if ((rc = sync_state(r))) return rc;
-                r->prof.slots_e += r->hs->n[0];
-                r->prof.slots_i += r->hs->n[1];
-            }
-            const bool ion_step = (r->time_step % r->dt_dti) == 0;
-            if ((rc = launch_step(r, ion_step))) return rc;
-            if (r->prof_on && (rc = profile_collect(r))) return rc;
-            r->time_step += 1;
-            /* counters come back asynchronously; the host reads them only to
-             * decide when to compact, which never changes results          */
-            PGB_CK(r, cudaMemcpyAsync(r->hs, r->ds, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
-        }
+        for (int k = 0; k < chunk; ++k)
+            if ((rc = issue_one_step(r))) return rc;
         done += chunk;
     }
     return sync_state(r);
+}
+
+extern "C" int pgb_step_batch(pgb_run* const* runs, int32_t nruns, int32_t nsteps) {
+    if (!runs || nruns < 0 || nsteps < 0) return fail(nullptr, PGB_ERR_ARG, "pgb_step_batch: bad argument");
+    for (int a = 0; a < nruns; ++a) {
+        if (!runs[a]) return fail(nullptr, PGB_ERR_ARG, "pgb_step_batch: null run handle");
+        for (int b = 0; b < a; ++b)
+            if (runs[b] == runs[a]) return fail(nullptr, PGB_ERR_ARG, "pgb_step_batch: a run handle appears twice");
+        int rc = need_particles(runs[a]);
+        if (rc) return rc;
+    }
+    int done = 0;
+    while (done < nsteps) {
+        int chunk = nsteps - done;
+        for (int a = 0; a < nruns; ++a) chunk = std::min<int>(chunk, (int)runs[a]->phi_tab_cap);
+        for (int a = 0; a < nruns; ++a) {
+            int rc = set_device_step(runs[a], runs[a]->time_step, chunk);
+            if (rc) return rc;
+        }
+        /* one step of every run in turn: each run's work goes to its own
+         * stream, so the kernels of different runs overlap on the GPU    */
+        for (int k = 0; k < chunk; ++k)
+            for (int a = 0; a < nruns; ++a) {
+                int rc = issue_one_step(runs[a]);
+                if (rc) return rc;
+            }
+        done += chunk;
+    }
+    int first = 0;
+    for (int a = 0; a < nruns; ++a) {
+        int rc = sync_state(runs[a]);
+        if (rc && !first) first = rc;
+    }
+    return first;
 }
 
 /* ------------------------------------------------------------ grids */

@@ -244,6 +244,7 @@ def load_library():
         "pgb_set_time_step": (C.c_int, [R, i64]),
         "pgb_initial_boundary": (C.c_int, [R]),
         "pgb_step": (C.c_int, [R, i32]),
+        "pgb_step_batch": (C.c_int, [C.POINTER(R), i32, i32]),
         "pgb_collide_electrons": (C.c_int, [R]),
         "pgb_inject": (C.c_int, [R]),
         "pgb_gather_push": (C.c_int, [R, C.c_int]),
@@ -420,6 +421,18 @@ class Run:
 
 
 # ------------------------------------------------------------- dataDump I/O
+def step_batch(runs, n: int = 1):
+    """pgb_step_batch: step independent runs together (each on its own
+    stream); every run ends as after Run.step(n) alone."""
+    lib = load_library()
+    arr = (C.c_void_p * len(runs))(*[r.h.value for r in runs])
+    rc = lib.pgb_step_batch(arr, len(runs), n)
+    if rc != 0:
+        msgs = [r.lib.pgb_last_error(r.h).decode() for r in runs]
+        msgs.append(lib.pgb_last_error(None).decode())
+        raise PicError(f"pgb_step_batch failed ({rc}): " + "; ".join(m for m in msgs if m and m != "no error"))
+
+
 def read_datadump(path: str) -> np.ndarray:
     """particle::load_particles (particle.cpp:359-401): whitespace-separated
     records `x y vx vy vz weight`, read until the first incomplete record."""
