@@ -252,6 +252,131 @@ def run_batched(args):
     return res
 
 
+# ------------------------------------------------------------------ served
+def served_requests(picgb, nreq, max_steps, seed=1005):
+    """Run requests arriving as a Poisson process (mean 20 per second): Ar or
+    H, grids of 64 to 512 cells a side, particles per species log-uniform in
+    [50k, 8M], steps log-uniform in [max_steps/10, max_steps], uniform
+    positions, absorbing walls with the species' energy-dependent collision
+    fits."""
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    for k in range(nreq):
+        t += float(rng.exponential(1.0 / 20.0))
+        nodes = int(rng.choice([65, 129, 257, 513]))
+        n = int(round(math.exp(rng.uniform(math.log(5e4), math.log(8e6)))))
+        steps = int(round(math.exp(rng.uniform(math.log(max_steps / 10), math.log(max_steps)))))
+        hydrogen = bool(rng.integers(0, 2))
+        te = float(rng.uniform(1.0, 4.0))
+        kw = dict(X_NO_OF_CELLS=nodes, TEMPERATURE=te, GAS_PRESSURE_TORR=float(rng.uniform(0.005, 0.05)),
+                  HAVE_COLLISIONS=True, SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT",
+                  SIGMA_IONIZATION="ENERGY_DEPENDENT", STEADYSTATE="NO", SIZE_TO_CHECK=2**31 - 1,
+                  RAND_SEED=seed + k, POISSON="FMG32", SORT_INTERVAL=8)
+        if hydrogen:
+            kw.update(ION_MASS_AMU=1.0, THRESHOLD=13.6, SPECIES="HYDROGEN")
+        L = picgb.make_params(**kw).xlength
+        size = 1.0e15 * L * L / n
+        p = picgb.make_params(E_MACROPARTICLE_SIZE=size, ION_MACROPARTICLE_SIZE=size, **kw)
+        r2 = np.random.default_rng(seed + 1000 + k)
+        st = []
+        for m, T in ((9.10939e-31, te), (p.ion_mass, 0.026)):
+            a = np.empty((n, 6))
+            a[:, 0] = r2.uniform(0.0, L, n)
+            a[:, 1] = r2.uniform(0.0, L, n)
+            a[:, 2:5] = r2.normal(0.0, math.sqrt(T * 1.602177e-19 / m), (n, 3))
+            a[:, 5] = 1.0
+            st.append(a)
+        out.append((t, p, st, steps, nodes))
+    return out
+
+
+def _quantile(pairs, q):
+    """q-quantile of (value, weight) pairs"""
+    if not pairs:
+        return None
+    pairs = sorted(pairs)
+    tot = sum(w for _, w in pairs)
+    acc = 0
+    for v, w in pairs:
+        acc += w
+        if acc >= q * tot:
+            return v
+    return pairs[-1][0]
+
+
+def run_served(args):
+    """The served form (pgb_server: requests admitted by HBM footprint as they
+    arrive, resident runs stepped together in rounds) against the plain
+    form (each request run alone, in arrival order), on the same arrivals."""
+    import torch
+    import picgb
+    reqs = served_requests(picgb, args.serve_requests, args.serve_max_steps)
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(0.5 * free)
+    res = {}
+    # served
+    srv = picgb.Server(budget, round_steps=args.serve_round, max_active=64)
+    arrival, finish, particle_steps = {}, {}, 0.0
+    t0 = time.perf_counter()
+    nxt = 0
+    while len(finish) < len(reqs):
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt][0] <= now:
+            t, p, st, steps, _ = reqs[nxt]
+            rid = srv.submit(p, st[0], st[1], steps)
+            arrival[rid] = t
+            nxt += 1
+        s = srv.stats()
+        if s["active"] == 0 and s["queued"] == 0:
+            time.sleep(max(0.0, reqs[nxt][0] - now))
+            continue
+        srv.round()
+        for rid in srv.results():
+            finish[rid] = time.perf_counter() - t0
+    wall = time.perf_counter() - t0
+    s = srv.stats()
+    srv.close()
+    res["served"] = {"seconds": wall, "particle_steps_per_s": s["particle_steps"] / wall,
+                     "step_ms_p50": s["step_ms_p50"], "step_ms_p99": s["step_ms_p99"],
+                     "ttc_s_p50": _quantile([(finish[k] - arrival[k], 1) for k in finish], 0.5),
+                     "ttc_s_p99": _quantile([(finish[k] - arrival[k], 1) for k in finish], 0.99)}
+    # plain: one request at a time in arrival order
+    steps_ms, ttc, ps = [], [], 0.0
+    t0 = time.perf_counter()
+    for t, p, st, steps, _ in reqs:
+        now = time.perf_counter() - t0
+        if now < t:
+            time.sleep(t - now)
+        with picgb.Run(p) as r:
+            r.load_particles(0, st[0])
+            r.load_particles(1, st[1])
+            r.initial_boundary()
+            n0 = r.particle_size(0) + r.particle_size(1)
+            a = time.perf_counter()
+            r.step(steps)
+            b = time.perf_counter()
+            n1 = r.particle_size(0) + r.particle_size(1)
+            r.get_particles(0)
+            r.get_particles(1)
+        steps_ms.append((1000.0 * (b - a) / steps, steps))
+        ps += 0.5 * (n0 + n1) * steps
+        ttc.append((time.perf_counter() - t0 - t, 1))
+    wall = time.perf_counter() - t0
+    res["plain"] = {"seconds": wall, "particle_steps_per_s": ps / wall, "step_ms_p50": _quantile(steps_ms, 0.5),
+                    "step_ms_p99": _quantile(steps_ms, 0.99), "ttc_s_p50": _quantile(ttc, 0.5),
+                    "ttc_s_p99": _quantile(ttc, 0.99)}
+    res["speedup"] = res["served"]["particle_steps_per_s"] / res["plain"]["particle_steps_per_s"]
+    res["config"] = {"requests": len(reqs), "arrivals": "Poisson, mean 20 per second (seeded)",
+                     "grid_nodes": sorted(set(r[4] for r in reqs)),
+                     "particles_per_species": [min(r[2][0].shape[0] for r in reqs), max(r[2][0].shape[0] for r in reqs)],
+                     "steps": [min(r[3] for r in reqs), max(r[3] for r in reqs)], "round_steps": args.serve_round,
+                     "hbm_budget_bytes": budget,
+                     "workload": "Ar or H runs, absorbing walls, energy-dependent collision fits, uniform positions, "
+                                 "grids 64-512 cells, 50k-8M particles/species, 500-5000 steps; a bounded number "
+                                 "of requests of the served workload"}
+    return res
+
+
 # ------------------------------------------------------------------ GPU path
 def run_gpu(args, rank, world):
     import torch
@@ -317,8 +442,9 @@ def run_gpu(args, rank, world):
                "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps}
     run.close()
     batched = run_batched(args) if (args.batch_runs > 0 and world == 1) else None
+    served = run_served(args) if (args.serve_requests > 0 and world == 1) else None
     return dict(ms=ms, ps=ps, counts=(c0, c1), prof=prof, launches=launches, clocks=clk.summary(), e2e=e2e, n=n,
-                batched=batched)
+                batched=batched, served=served)
 
 
 def main():
@@ -336,6 +462,9 @@ def main():
     ap.add_argument("--sort", type=int, default=8, help="spatial sort every k steps (0 = off)")
     ap.add_argument("--batch-runs", type=int, default=64, help="runs of the batched workload (0 = skip it)")
     ap.add_argument("--batch-steps", type=int, default=200, help="steps per run of the batched workload")
+    ap.add_argument("--serve-requests", type=int, default=16, help="requests of the served workload (0 = skip it)")
+    ap.add_argument("--serve-max-steps", type=int, default=5000, help="longest request of the served workload")
+    ap.add_argument("--serve-round", type=int, default=10, help="steps per server round")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -413,7 +542,7 @@ def main():
             "config": config, "e2e": res["e2e"], "roofline": roofline, "cpu_baseline": cpu,
             "gpu_launches": res["launches"], "clocks": res["clocks"],
             "particles": {"start": [c0["n_e"], c0["n_i"]], "end": [c1["n_e"], c1["n_i"]]},
-            "batched": res.get("batched")}
+            "batched": res.get("batched"), "served": res.get("served")}
     print(json.dumps(line), flush=True)
 
 

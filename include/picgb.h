@@ -216,6 +216,49 @@ PGB_API int pgb_set_profiling(pgb_run* run, int on);
 PGB_API int pgb_get_profile(pgb_run* run, pgb_profile* out);
 /* Wait for all work queued on the handle's stream. */
 PGB_API int pgb_sync(pgb_run* run);
+/* Device bytes a run of these parameters holds once ne electrons and ni ions
+ * are loaded (no reference counterpart; used to admit runs by memory).   */
+PGB_API int pgb_footprint(const pgb_params* p, int64_t ne, int64_t ni, int64_t* bytes);
+
+/*
+ * Serving: a request loop that keeps many independent runs resident on the
+ * GPU and steps them together (no reference counterpart; the reference
+ * runs one simulation per process).
+ *   - pgb_server_submit copies a request (parameters, initial particles,
+ *     step count) into the server's queue.
+ *   - pgb_server_round admits queued requests, first fit in submission
+ *     order, while their pgb_footprint fits the HBM budget and fewer than
+ *     max_active runs are resident.  It then steps every resident run
+ *     min(round_steps, steps left) steps with pgb_step_batch and retires the
+ *     runs that are done.
+ *   - pgb_server_result hands back a finished request's particles and frees
+ *     them.
+ * A request's result does not depend on the other requests it ran with.
+ * One host thread drives a server.
+ */
+typedef struct pgb_server pgb_server;
+typedef struct pgb_server_stats {
+    int64_t submitted, admitted, completed, active, queued;
+    int64_t run_steps;             /* steps executed, summed over runs            */
+    double  particle_steps;        /* particles x steps, summed over runs         */
+    double  busy_seconds;          /* wall time spent inside rounds               */
+    double  step_ms_p50, step_ms_p99;  /* time per step of a resident run          */
+    double  ttc_s_p50, ttc_s_p99;  /* submission to completion                     */
+    int64_t hbm_in_use, hbm_budget;
+} pgb_server_stats;
+PGB_API int pgb_server_create(int64_t hbm_budget_bytes, int32_t round_steps, int32_t max_active, pgb_server** out);
+PGB_API int pgb_server_destroy(pgb_server* server);
+PGB_API int pgb_server_submit(pgb_server* server, const pgb_params* p, const double* e_aos6, int64_t ne,
+                              const double* i_aos6, int64_t ni, int32_t nsteps, int64_t* request_id);
+/* *completed = requests finished in this round (ids via pgb_server_done) */
+PGB_API int pgb_server_round(pgb_server* server, int32_t* completed);
+/* ids of finished requests whose results have not been taken, up to cap */
+PGB_API int pgb_server_done(pgb_server* server, int64_t* ids, int32_t cap, int32_t* n_out);
+/* counts of a finished request's particles (to size the result buffers) */
+PGB_API int pgb_server_result_size(pgb_server* server, int64_t id, int64_t* ne, int64_t* ni);
+PGB_API int pgb_server_result(pgb_server* server, int64_t id, double* e_aos6, int64_t cap_e, double* i_aos6,
+                              int64_t cap_i, pgb_counters* counters);
+PGB_API int pgb_server_get_stats(pgb_server* server, pgb_server_stats* out);
 
 /*
  * Charge grid of one species from particle records already on the device,

@@ -91,3 +91,27 @@ def test_datadump_text_format_matches_reference():
         assert head == str(g["dump_e_head"])
         back = picgb.read_datadump(path)
         np.testing.assert_allclose(back, g["e_out"], rtol=5e-6)
+
+
+def test_footprint_grows_with_particles_and_grid(lib):
+    import picgb
+    small = picgb.make_params(X_NO_OF_CELLS=65)
+    big = picgb.make_params(X_NO_OF_CELLS=257)
+    a = picgb.footprint(small, 1000, 1000)
+    b = picgb.footprint(small, 1_000_000, 1_000_000)
+    c = picgb.footprint(big, 1000, 1000)
+    assert 0 < a < b and a < c
+    # particles dominate: about 56 B per slot of capacity (2n + 65536) and species, plus lists
+    assert b - a > 2 * 56 * 2 * (1_000_000 - 1000)
+
+
+def test_server_rejects_a_run_larger_than_its_budget(lib):
+    """Admission is by memory: a request that can never fit is refused at
+    submission with PGB_ERR_CAPACITY (no GPU work is done)."""
+    import picgb
+    p = picgb.make_params(X_NO_OF_CELLS=65)
+    e = np.zeros((10, 6))
+    with picgb.Server(hbm_budget=1 << 20, round_steps=5, max_active=4) as srv:
+        with pytest.raises(picgb.PicError, match="budget"):
+            srv.submit(p, e, e, 10)
+        assert srv.stats()["submitted"] == 0

@@ -455,3 +455,62 @@ def test_batched_runs_equal_runs_alone():
         assert np.array_equal(a[1], b[1], equal_nan=True), c
         assert np.array_equal(a[2], b[2]), c
         assert a[3] == b[3], c
+
+
+def test_served_requests_equal_runs_alone():
+    """Requests submitted to the server at different times, stepped together
+    in rounds with others, end exactly as the same runs stepped alone
+    (restart load, the pre-loop boundary pass, nsteps steps)."""
+    reqs = [("core33", 12), ("arcoll33", 7), ("hsee33", 20), ("core65", 9)]
+    alone = []
+    for c, n in reqs:
+        g = load_golden(c)
+        with picgb.Run(g["p"]) as r:
+            r.load_particles(0, g["e_in"])
+            r.load_particles(1, g["i_in"])
+            r.initial_boundary()
+            r.step(n)
+            alone.append((r.get_particles(0), r.get_particles(1), r.counters()))
+    with picgb.Server(hbm_budget=8 << 30, round_steps=5, max_active=3) as srv:
+        ids = []
+        for k, (c, n) in enumerate(reqs):
+            g = load_golden(c)
+            ids.append(srv.submit(g["p"], g["e_in"], g["i_in"], n))
+            srv.round()            # later requests join runs already under way
+        got = {}
+        while len(got) < len(reqs):
+            srv.round()
+            got.update(srv.results())
+        st = srv.stats()
+    assert st["completed"] == len(reqs) and st["active"] == 0 and st["queued"] == 0
+    assert st["step_ms_p99"] >= st["step_ms_p50"] > 0
+    for (c, n), rid, a in zip(reqs, ids, alone):
+        e, i, cnt = got[rid]
+        assert np.array_equal(a[0], e, equal_nan=True), c
+        assert np.array_equal(a[1], i, equal_nan=True), c
+        assert a[2] == cnt, c
+
+
+def test_sparse_run_on_a_large_grid_with_the_bin_sort():
+    """Few particles over many bins: every non-empty bin takes at least one
+    whole tile after the sort, so the padded layout is much larger than the
+    particle count.  The run reserves room for it and matches the oracle."""
+    p = picgb.make_params(X_NO_OF_CELLS=513, STEADYSTATE="NO", RAND_SEED=5, SORT_INTERVAL=4)
+    rng = np.random.default_rng(9)
+    n = 3000
+    L = p.xlength
+    st = []
+    for m, T in ((picgb.ELECTRON_MASS, 2.0), (p.ion_mass, 0.5)):
+        a = np.empty((n, 6))
+        a[:, 0] = rng.uniform(0.0, L, n)
+        a[:, 1] = rng.uniform(0.0, L, n)
+        a[:, 2:5] = rng.normal(0.0, np.sqrt(T * picgb.CHARGE / m), (n, 3))
+        a[:, 5] = 1.0
+        st.append(a)
+    g = {"p": p, "e_in": st[0], "i_in": st[1], "nsteps": 9}
+    o, r = run_pair(g)
+    co, cr = o.counters(), r.counters()
+    for k in ("n_e", "n_i", "absorbed_e", "absorbed_i"):
+        assert cr[k] == co[k], f"{k}: gpu {cr[k]} oracle {co[k]}"
+    compare_particles(r.get_particles(0), o.get_particles(0), p, "electrons", vt=p.vte)
+    r.close()

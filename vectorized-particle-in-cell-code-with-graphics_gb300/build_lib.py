@@ -72,18 +72,22 @@ def build(verbose: bool = False, force: bool = False) -> str:
         return unit
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         list(ex.map(run, jobs))
-    host_obj = os.path.join(BUILD, "pic_host.o")
     host_src = os.path.join(HOST, "pic_host.cpp")
-    if force or _stale(host_obj, [host_src, os.path.join(HOST, "pic_host.h")] + headers):
-        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", f"-I{os.path.join(REPO, 'include')}",
-               f"-I{CSRC}", f"-I{HOST}", "-c", host_src, "-o", host_obj]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        p = subprocess.run(cmd, capture_output=True, text=True)
-        if p.returncode != 0:
-            raise RuntimeError(f"g++ failed on pic_host.cpp:\n{p.stdout}\n{p.stderr}")
-        jobs.append(("pic_host.cpp", None))
-    objs = [os.path.join(BUILD, u.replace(".cu", ".o")) for u in UNITS] + [host_obj]
+    host_objs = []
+    for name in ("pic_host.cpp", "pgb_server.cpp"):
+        src = os.path.join(HOST, name)
+        obj = os.path.join(BUILD, name.replace(".cpp", ".o"))
+        host_objs.append(obj)
+        if force or _stale(obj, [src, os.path.join(HOST, "pic_host.h")] + headers):
+            cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", f"-I{os.path.join(REPO, 'include')}",
+                   f"-I{CSRC}", f"-I{HOST}", "-c", src, "-o", obj]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            p = subprocess.run(cmd, capture_output=True, text=True)
+            if p.returncode != 0:
+                raise RuntimeError(f"g++ failed on {name}:\n{p.stdout}\n{p.stderr}")
+            jobs.append((name, None))
+    objs = [os.path.join(BUILD, u.replace(".cu", ".o")) for u in UNITS] + host_objs
     if force or jobs or _stale(OUT, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", OUT] + objs + ["-lcudart"]
         if verbose:

@@ -390,13 +390,21 @@ static int dstage(pgb_run* r, size_t bytes) {
     return 0;
 }
 
+/* slots the spatial sort may add: every bin (and the key of particles
+ * outside the deposit region) starts on a tile boundary                  */
+static long long sort_pad_slots(const pgb_params* p) {
+    if (p->sort_interval <= 0) return 0;
+    const long long nbx = (p->x_no_of_cells - 1 + PGB_BIN - 1) / PGB_BIN, nby = (p->y_no_of_cells - 1 + PGB_BIN - 1) / PGB_BIN;
+    return (nbx * nby + 2) * PGB_TILE;
+}
+
 extern "C" int pgb_load_species(pgb_run* r, int s, const double* aos6, int64_t n) {
     if (!r || s < 0 || s > 1 || n < 0 || (n > 0 && !aos6)) return fail(r, PGB_ERR_ARG, "pgb_load_species: bad argument");
     if (n > 0x7fffffffLL) return fail(r, PGB_ERR_ARG, "pgb_load_species: too many particles");
     int rc = sync_state(r);
     if (rc) return rc;
     long long want = s == 0 ? r->p.capacity_e : r->p.capacity_i;
-    long long cap = std::max<long long>(want, 2 * n + 65536);
+    long long cap = std::max<long long>(want, 2 * n + 65536 + sort_pad_slots(&r->p));
     if (cap > 0x7fffffffLL) cap = 0x7fffffffLL;
     r->hs->n[s] = 0;
     if ((rc = ensure_capacity(r, s, cap))) return rc;
@@ -427,6 +435,36 @@ extern "C" int pgb_load_species(pgb_run* r, int s, const double* aos6, int64_t n
     PGB_CK(r, cudaMemsetAsync(&r->ds->n_pieces[s], 0, sizeof(int), r->stream));
     PGB_CK(r, cudaMemsetAsync(&r->ds->sorted_tiles[s], 0, sizeof(long long), r->stream));
     PGB_CK(r, cudaStreamSynchronize(r->stream));
+    return 0;
+}
+
+/* device bytes a run holds once ne electrons and ni ions are loaded, from
+ * the allocations of pgb_create, ensure_capacity and the load staging    */
+extern "C" int pgb_footprint(const pgb_params* p, int64_t ne, int64_t ni, int64_t* bytes) {
+    if (!p || !bytes || ne < 0 || ni < 0 || p->x_no_of_cells < 3) return fail(nullptr, PGB_ERR_ARG, "pgb_footprint: bad argument");
+    const long long nx = p->x_no_of_cells, ny = p->y_no_of_cells, G = nx * ny, GE = (nx + 1) * (ny + 1);
+    const long long pad = sort_pad_slots(p);
+    auto cap_of = [pad](long long want, long long n) {
+        return std::min<long long>(std::max<long long>(want, 2 * n + 65536 + pad), 0x7fffffffLL);
+    };
+    const long long ce = cap_of(p->capacity_e, ne), ci = cap_of(p->capacity_i, ni), lc = std::max(ce, ci);
+    const long long nt = (lc + PGB_TILE - 1) / PGB_TILE + 1;
+    const long long nbx = (nx - 1 + PGB_BIN - 1) / PGB_BIN, nby = (ny - 1 + PGB_BIN - 1) / PGB_BIN, nkeys = nbx * nby + 1;
+    long long b = 0;
+    b += 2 * (16 + 4 + 4 + 4) * (ce + ci);                               /* particles, two copies */
+    b += 4 * (4 * nt * PGB_TILE + 4 * nt + 4 * lc);                      /* event lists */
+    b += 2 * 4 * std::max(lc, nt);                                        /* aux_i, aux_j */
+    b += 2 * (4 * nt + 16 * (nt + nkeys + 1));                            /* tile bins, pieces */
+    const long long chunks = (lc + PGB_SORT_CHUNK - 1) / PGB_SORT_CHUNK + 1;
+    b += 2 * 4 * nkeys * chunks + 4 * nkeys + 8 * (nkeys + 1);            /* sort scratch */
+    b += 8 * nx * ((lc + 4096 - 1) / 4096 + 1);                           /* CX tile sums */
+    b += 48 * std::max(ne, ni);                                           /* load/dump staging */
+    long long levels = 0;
+    for (long long n = nx; n >= 3; n = n / 2 + 1) { levels += n * n; if (n == 3) break; }
+    b += 4 * 8 * levels + 4 * 4 * levels;                                 /* multigrid, FP64 and FP32 */
+    b += 8 * (2 + 2 + 2 + 1) * G + 8 * 3 * GE + 8 * nx + 8 * 4096;        /* grids, phi table */
+    b += 6 * p->init_no_neutrals * 4 + (16 << 20);                        /* neutral tables, streams, graphs */
+    *bytes = b;
     return 0;
 }
 
@@ -754,6 +792,16 @@ static int issue_one_step(pgb_run* r) {
         /* spatial sort (drops tombstones too) every sort_interval steps */
         if (r->time_step % r->p.sort_interval == 0)
             for (int s = 0; s < 2; ++s) {
+                /* the padded layout needs n + pad slots; grow first if the
+                 * (lazily read) count comes near the capacity              */
+                const long long pad = sort_pad_slots(&r->p);
+                if (r->hs->n[s] + r->hs->n[s] / 8 + pad > r->sp[s].cap) {
+                    if ((rc = sync_state(r))) return rc;
+                    const long long need = 2 * r->hs->n[s] + 65536 + pad;   /* > n + n/8 + pad */
+                    if (r->hs->n[s] + r->hs->n[s] / 8 + pad > r->sp[s].cap &&
+                        (rc = ensure_capacity(r, s, std::min<long long>(need, 0x7fffffffLL))))
+                        return rc;
+                }
                 if (pgb_launch_sort(r, s)) return PGB_ERR_CUDA;
                 r->orient[s] ^= 1;
             }

@@ -57,6 +57,8 @@ struct DevState {
     long long sorted_tiles[2];  /* tiles covered by bin pieces (0 = unsorted)   */
     int n_pieces[2];
     long long t_base;        /* step of phi_tab[0]                              */
+    int sort_overflow;       /* the padded bin layout did not fit: the sort copies in place order */
+    int pad2;
 };
 
 /* dense event lists (ordered by slot) */

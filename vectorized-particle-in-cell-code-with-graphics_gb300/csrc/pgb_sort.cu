@@ -144,12 +144,22 @@ __global__ void __launch_bounds__(1024) k_sort_scan_bins(SortArgs a) {
         carry_t += tot_t;
         carry_p += tot_p;
     }
+    /* every bin starts on a tile boundary: the padded layout needs carry_t
+     * tiles.  If they do not fit the capacity, the sort copies the
+     * particles in their current order instead (no pieces, no padding) and
+     * the step reports the capacity error.                              */
+    __shared__ int s_over;
     if (threadIdx.x == 0) {
+        const int over = carry_t * PGB_TILE > a.S.cap ? 1 : 0;
+        s_over = over;
+        a.ds->sort_overflow = over;
         a.key_start[a.nbins + 1] = carry_t * PGB_TILE;
-        a.ds->n_pieces[a.s] = (int)carry_p;
-        a.ds->sorted_tiles[a.s] = carry_t;
+        a.ds->n_pieces[a.s] = over ? 0 : (int)carry_p;
+        a.ds->sorted_tiles[a.s] = over ? 0 : carry_t;
+        if (over) atomicOr(&a.ds->err, a.s == 0 ? ERR_CAP_E : ERR_CAP_I);
     }
     __syncthreads();
+    if (s_over) return;
     /* tile -> bin map: the key whose [start, next start) holds the tile */
     for (long long t = threadIdx.x; t < carry_t; t += blockDim.x) {
         const long long slot = t * PGB_TILE;
@@ -174,6 +184,16 @@ __global__ void __launch_bounds__(256) k_sort_scatter(SortArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     long long* cur = s_cur + (long long)warp * (a.nbins + 1);
     const unsigned lt = (1u << lane) - 1u;
+    if (a.ds->sort_overflow) {
+        /* the padded layout does not fit: keep the order (and the slots) */
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+            a.S.xv2[i] = a.S.xv[i];
+            a.S.vz2[i] = a.S.vz[i];
+            a.S.w2[i] = a.S.w[i];
+            a.S.id2[i] = a.S.id[i];
+        }
+        return;
+    }
     for (int c = blockIdx.x * nw + warp; c < nch; c += gridDim.x * nw) {
         for (int k = lane; k <= a.nbins; k += 32) cur[k] = a.key_start[k] + a.offs[(long long)k * a.nchunks_cap + c];
         __syncwarp();
@@ -202,7 +222,7 @@ __global__ void __launch_bounds__(256) k_sort_scatter(SortArgs a) {
                 __syncwarp();
                 if (key[u] >= 0 && (peers & lt) == 0) cur[key[u]] += __popc(peers);
                 __syncwarp();
-                if (key[u] >= 0) {
+                if (key[u] >= 0 && pos < a.S.cap) {
                     a.S.xv2[pos] = p[u];
                     a.S.vz2[pos] = vz[u];
                     a.S.w2[pos] = w[u];
@@ -216,6 +236,7 @@ __global__ void __launch_bounds__(256) k_sort_scatter(SortArgs a) {
 
 /* tombstones in the padding after each key's particles; new counts */
 __global__ void k_sort_pad(SortArgs a) {
+    if (a.ds->sort_overflow) return;   /* the copy kept n and the tombstones */
     for (int key = blockIdx.x; key <= a.nbins; key += gridDim.x) {
         long long s0 = a.key_start[key] + a.key_total[key], s1 = a.key_start[key + 1];
         for (long long i = s0 + threadIdx.x; i < s1; i += blockDim.x) {

@@ -86,6 +86,17 @@ class PgbCounters(C.Structure):
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
 
 
+class PgbServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64), ("active", C.c_int64),
+                ("queued", C.c_int64), ("run_steps", C.c_int64), ("particle_steps", C.c_double),
+                ("busy_seconds", C.c_double), ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double),
+                ("ttc_s_p50", C.c_double), ("ttc_s_p99", C.c_double), ("hbm_in_use", C.c_int64),
+                ("hbm_budget", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class PgbProfile(C.Structure):
     """ctypes image of `pgb_profile` (include/picgb.h)."""
 
@@ -245,6 +256,15 @@ def load_library():
         "pgb_initial_boundary": (C.c_int, [R]),
         "pgb_step": (C.c_int, [R, i32]),
         "pgb_step_batch": (C.c_int, [C.POINTER(R), i32, i32]),
+        "pgb_footprint": (C.c_int, [C.POINTER(PgbParams), i64, i64, C.POINTER(i64)]),
+        "pgb_server_create": (C.c_int, [i64, i32, i32, C.POINTER(R)]),
+        "pgb_server_destroy": (C.c_int, [R]),
+        "pgb_server_submit": (C.c_int, [R, C.POINTER(PgbParams), dp, i64, dp, i64, i32, C.POINTER(i64)]),
+        "pgb_server_round": (C.c_int, [R, C.POINTER(i32)]),
+        "pgb_server_done": (C.c_int, [R, C.POINTER(i64), i32, C.POINTER(i32)]),
+        "pgb_server_result_size": (C.c_int, [R, i64, C.POINTER(i64), C.POINTER(i64)]),
+        "pgb_server_result": (C.c_int, [R, i64, dp, i64, dp, i64, C.POINTER(PgbCounters)]),
+        "pgb_server_get_stats": (C.c_int, [R, C.POINTER(PgbServerStats)]),
         "pgb_collide_electrons": (C.c_int, [R]),
         "pgb_inject": (C.c_int, [R]),
         "pgb_gather_push": (C.c_int, [R, C.c_int]),
@@ -421,6 +441,83 @@ class Run:
 
 
 # ------------------------------------------------------------- dataDump I/O
+def footprint(params: PgbParams, ne: int, ni: int) -> int:
+    """Device bytes of a run of these parameters with ne + ni particles."""
+    lib = load_library()
+    out = C.c_int64()
+    if lib.pgb_footprint(C.byref(params), ne, ni, C.byref(out)) != 0:
+        raise PicError(lib.pgb_last_error(None).decode())
+    return out.value
+
+
+class Server:
+    """pgb_server_*: a request loop keeping many runs resident on the GPU.
+
+    submit() queues a run (parameters, initial particles, steps); round()
+    admits queued runs that fit the HBM budget, steps every resident run
+    together and retires finished ones; results() returns the finished
+    runs' particles and counters."""
+
+    def __init__(self, hbm_budget: int, round_steps: int = 10, max_active: int = 64):
+        self.lib = load_library()
+        h = C.c_void_p()
+        self._check(self.lib.pgb_server_create(hbm_budget, round_steps, max_active, C.byref(h)), "pgb_server_create")
+        self.h = h
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise PicError(f"{what} failed ({rc}): {self.lib.pgb_last_error(None).decode()}")
+
+    def submit(self, params: PgbParams, e: np.ndarray, i: np.ndarray, nsteps: int) -> int:
+        e = np.ascontiguousarray(e, dtype=np.float64)
+        i = np.ascontiguousarray(i, dtype=np.float64)
+        rid = C.c_int64()
+        self._check(self.lib.pgb_server_submit(self.h, C.byref(params), _dptr(e), e.shape[0], _dptr(i), i.shape[0],
+                                               nsteps, C.byref(rid)), "pgb_server_submit")
+        return rid.value
+
+    def round(self) -> int:
+        n = C.c_int32()
+        self._check(self.lib.pgb_server_round(self.h, C.byref(n)), "pgb_server_round")
+        return n.value
+
+    def results(self) -> dict:
+        """{id: (electrons, ions, counters)} for every finished request not taken yet."""
+        out = {}
+        while True:
+            ids = (C.c_int64 * 64)()
+            n = C.c_int32()
+            self._check(self.lib.pgb_server_done(self.h, ids, 64, C.byref(n)), "pgb_server_done")
+            if n.value == 0:
+                return out
+            for k in range(n.value):
+                ne, ni = C.c_int64(), C.c_int64()
+                self._check(self.lib.pgb_server_result_size(self.h, ids[k], C.byref(ne), C.byref(ni)),
+                            "pgb_server_result_size")
+                e = np.empty((max(ne.value, 1), 6))
+                i = np.empty((max(ni.value, 1), 6))
+                c = PgbCounters()
+                self._check(self.lib.pgb_server_result(self.h, ids[k], _dptr(e), ne.value, _dptr(i), ni.value,
+                                                       C.byref(c)), "pgb_server_result")
+                out[ids[k]] = (e[:ne.value], i[:ni.value], c.as_dict())
+
+    def stats(self) -> dict:
+        st = PgbServerStats()
+        self._check(self.lib.pgb_server_get_stats(self.h, C.byref(st)), "pgb_server_get_stats")
+        return st.as_dict()
+
+    def close(self):
+        if self.h:
+            self.lib.pgb_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 def step_batch(runs, n: int = 1):
     """pgb_step_batch: step independent runs together (each on its own
     stream); every run ends as after Run.step(n) alone."""
