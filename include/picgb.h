@@ -180,6 +180,14 @@ PGB_API int pgb_initial_boundary(pgb_run* run);
  * kernels; same physics and call order as the per-phase entry points.      */
 PGB_API int pgb_step(pgb_run* run, int32_t nsteps);
 
+/* pgb_step without waiting: the steps are queued on the run's stream and
+ * the call returns (no reference counterpart).  pgb_query tells when the
+ * run is idle again; pgb_sync waits for it.  Reads of the run's particles,
+ * grids or counters wait for the queued steps themselves.               */
+PGB_API int pgb_step_async(pgb_run* run, int32_t nsteps);
+/* *idle = 1 when no work of the run is queued; device errors of finished
+ * work are reported here.                                                */
+PGB_API int pgb_query(pgb_run* run, int32_t* idle);
 /* Step several independent runs nsteps each.  It has no counterpart in the
  * reference, which steps one run per process (pic.cpp:1069-1250).  Each
  * run's work is queued on its own stream, one step of every run in turn,

@@ -514,3 +514,32 @@ def test_sparse_run_on_a_large_grid_with_the_bin_sort():
         assert cr[k] == co[k], f"{k}: gpu {cr[k]} oracle {co[k]}"
     compare_particles(r.get_particles(0), o.get_particles(0), p, "electrons", vt=p.vte)
     r.close()
+
+
+def test_async_steps_equal_blocking_steps():
+    """pgb_step_async queues the steps and returns; pgb_query reports when
+    the run is idle.  The result equals pgb_step's."""
+    import ctypes as C
+    g = load_golden("arsee33")
+    out = []
+    for mode in ("blocking", "async"):
+        with picgb.Run(g["p"]) as r:
+            r.load_particles(0, g["e_in"])
+            r.load_particles(1, g["i_in"])
+            r.initial_boundary()
+            if mode == "blocking":
+                r.step(int(g["nsteps"]))
+            else:
+                assert r.lib.pgb_step_async(r.h, int(g["nsteps"])) == 0
+                idle = C.c_int32(0)
+                for _ in range(200000):
+                    assert r.lib.pgb_query(r.h, C.byref(idle)) == 0
+                    if idle.value:
+                        break
+                assert idle.value == 1
+            out.append((r.get_particles(0), r.get_particles(1), r.get_grid("phi"), r.counters()))
+    a, b = out
+    assert np.array_equal(a[0], b[0], equal_nan=True)
+    assert np.array_equal(a[1], b[1], equal_nan=True)
+    assert np.array_equal(a[2], b[2])
+    assert a[3] == b[3]

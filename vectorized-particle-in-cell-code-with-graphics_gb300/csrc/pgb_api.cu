@@ -296,6 +296,10 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
     r->phi_tab_cap = 4096;
     ok = ok && cudaMalloc(&r->inject_flag, sizeof(int) * (p->number_to_inject + 1)) == cudaSuccess;
     ok = ok && cudaMalloc(&r->phi_tab, sizeof(double) * r->phi_tab_cap) == cudaSuccess;
+    ok = ok && cudaMallocHost(&r->phi_host, sizeof(double) * r->phi_tab_cap) == cudaSuccess;
+    ok = ok && cudaMallocHost(&r->t_host, sizeof(long long) * 2) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&r->phi_ev, cudaEventDisableTiming) == cudaSuccess;
+    if (ok) r->phi_ev_ok = true;
     int ng = 0, nn = r->nx;
     while (nn >>= 1) ng++;
     r->ng = ng;
@@ -353,6 +357,9 @@ extern "C" int pgb_destroy(pgb_run* r) {
     if (r->stream) cudaStreamSynchronize(r->stream);
     drop_graphs(r);
     cudaFree(r->phi_tab);
+    if (r->phi_host) cudaFreeHost(r->phi_host);
+    if (r->t_host) cudaFreeHost(r->t_host);
+    if (r->phi_ev_ok) cudaEventDestroy(r->phi_ev);
     cudaFree(r->inject_flag);
     free_species(r->sp[0]);
     free_species(r->sp[1]);
@@ -526,13 +533,14 @@ static int need_particles(pgb_run* r) {
  * reference does                                                         */
 static int set_device_step(pgb_run* r, int64_t t0, int n) {
     if (n > r->phi_tab_cap) return fail(r, PGB_ERR_ARG, "step table too small");
-    std::vector<double> tab((size_t)n);
-    for (int k = 0; k < n; ++k) tab[k] = r->p.phi_right * cos(r->p.phi_period * (double)(t0 + k));
-    long long tt = (long long)t0;
-    PGB_CK(r, cudaMemcpyAsync(r->phi_tab, tab.data(), sizeof(double) * n, cudaMemcpyHostToDevice, r->stream));
-    PGB_CK(r, cudaMemcpyAsync(&r->ds->t, &tt, sizeof(tt), cudaMemcpyHostToDevice, r->stream));
-    PGB_CK(r, cudaMemcpyAsync(&r->ds->t_base, &tt, sizeof(tt), cudaMemcpyHostToDevice, r->stream));
-    PGB_CK(r, cudaStreamSynchronize(r->stream));
+    /* the pinned staging is reused once its previous upload has left */
+    PGB_CK(r, cudaEventSynchronize(r->phi_ev));
+    for (int k = 0; k < n; ++k) r->phi_host[k] = r->p.phi_right * cos(r->p.phi_period * (double)(t0 + k));
+    r->t_host[0] = (long long)t0;
+    PGB_CK(r, cudaMemcpyAsync(r->phi_tab, r->phi_host, sizeof(double) * n, cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaMemcpyAsync(&r->ds->t, r->t_host, sizeof(long long), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaMemcpyAsync(&r->ds->t_base, r->t_host, sizeof(long long), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaEventRecord(r->phi_ev, r->stream));
     return 0;
 }
 
@@ -842,6 +850,33 @@ extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
         done += chunk;
     }
     return sync_state(r);
+}
+
+extern "C" int pgb_step_async(pgb_run* r, int32_t nsteps) {
+    if (!r || nsteps < 0) return fail(r, PGB_ERR_ARG, "pgb_step_async: bad argument");
+    int rc = need_particles(r);
+    if (rc) return rc;
+    int done = 0;
+    while (done < nsteps) {
+        int chunk = std::min<int>(nsteps - done, (int)r->phi_tab_cap);
+        if ((rc = set_device_step(r, r->time_step, chunk))) return rc;
+        for (int k = 0; k < chunk; ++k)
+            if ((rc = issue_one_step(r))) return rc;
+        done += chunk;
+    }
+    return 0;
+}
+
+extern "C" int pgb_query(pgb_run* r, int32_t* idle) {
+    if (!r || !idle) return fail(r, PGB_ERR_ARG, "pgb_query: bad argument");
+    cudaError_t e = cudaStreamQuery(r->stream);
+    if (e == cudaErrorNotReady) {
+        *idle = 0;
+        return 0;
+    }
+    if (e != cudaSuccess) return pgb_cuda_ok(r, e, "cudaStreamQuery") ? 0 : PGB_ERR_CUDA;
+    *idle = 1;
+    return sync_state(r);   /* idle: cheap, and reports device errors */
 }
 
 extern "C" int pgb_step_batch(pgb_run* const* runs, int32_t nruns, int32_t nsteps) {

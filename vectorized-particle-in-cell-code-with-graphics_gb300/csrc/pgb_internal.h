@@ -127,6 +127,10 @@ struct pgb_run {
     double* neut64[2] = {nullptr, nullptr};
     double* prob_cx = nullptr;             /* per-column CX accumulator       */
     double* phi_tab = nullptr;             /* right-wall potential per step   */
+    double* phi_host = nullptr;            /* pinned: the table and the step number on their way */
+    long long* t_host = nullptr;
+    cudaEvent_t phi_ev;                    /* recorded after their upload     */
+    bool phi_ev_ok = false;
     long long phi_tab_cap = 0;
     /* CUDA graphs of one step, keyed by (ion step, buffer orientation e, i) */
     cudaGraphExec_t graph[8] = {};

@@ -256,6 +256,8 @@ def load_library():
         "pgb_initial_boundary": (C.c_int, [R]),
         "pgb_step": (C.c_int, [R, i32]),
         "pgb_step_batch": (C.c_int, [C.POINTER(R), i32, i32]),
+        "pgb_step_async": (C.c_int, [R, i32]),
+        "pgb_query": (C.c_int, [R, C.POINTER(i32)]),
         "pgb_footprint": (C.c_int, [C.POINTER(PgbParams), i64, i64, C.POINTER(i64)]),
         "pgb_server_create": (C.c_int, [i64, i32, i32, C.POINTER(R)]),
         "pgb_server_destroy": (C.c_int, [R]),
