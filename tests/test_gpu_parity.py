@@ -427,12 +427,17 @@ def test_batch_driver_runs_and_writes_reference_files(tmp_path):
     assert all(len(r) == 8 for r in rows)
 
 
-def test_batched_runs_equal_runs_alone():
+@pytest.mark.parametrize("nsteps", [10, 11, 12])
+def test_batched_runs_equal_runs_alone(nsteps):
     """pgb_step_batch steps independent runs of different sizes and physics
-    on their own streams; each run ends bit-identical to stepping it alone."""
+    on their own streams; each run ends bit-identical to stepping it alone,
+    batch after batch.  The step counts cover a storage growth at a sort
+    step in the middle of the batch (core65 grows while the other runs'
+    kernels occupy the GPU), after which the bin-piece tables of both
+    species must be rebuilt, not read from the new allocation."""
     cases = ["core33", "arcoll33", "hsee33", "core65"]
-    alone, batched = [], []
-    for mode in ("alone", "batch"):
+    results = {}
+    for mode in ("alone", "batch", "batch again"):
         runs = []
         for c in cases:
             g = load_golden(c)
@@ -443,18 +448,21 @@ def test_batched_runs_equal_runs_alone():
             runs.append(r)
         if mode == "alone":
             for r in runs:
-                r.step(12)
+                r.step(nsteps)
         else:
-            picgb.step_batch(runs, 12)
-        out = alone if mode == "alone" else batched
+            picgb.step_batch(runs, nsteps)
+        results[mode] = []
         for r in runs:
-            out.append((r.get_particles(0), r.get_particles(1), r.get_grid("phi"), r.counters()))
+            results[mode].append((r.get_particles(0), r.get_particles(1), r.get_grid("q_e"), r.get_grid("phi"),
+                                  r.counters()))
             r.close()
-    for c, a, b in zip(cases, alone, batched):
-        assert np.array_equal(a[0], b[0], equal_nan=True), c
-        assert np.array_equal(a[1], b[1], equal_nan=True), c
-        assert np.array_equal(a[2], b[2]), c
-        assert a[3] == b[3], c
+    for mode in ("batch", "batch again"):
+        for c, a, b in zip(cases, results["alone"], results[mode]):
+            assert np.array_equal(a[0], b[0], equal_nan=True), (mode, c)
+            assert np.array_equal(a[1], b[1], equal_nan=True), (mode, c)
+            assert np.array_equal(a[2], b[2]), (mode, c)
+            assert np.array_equal(a[3], b[3]), (mode, c)
+            assert a[4] == b[4], (mode, c)
 
 
 def test_served_requests_equal_runs_alone():

@@ -161,7 +161,13 @@ static void drop_graphs(pgb_run* r);
 
 static int ensure_capacity(pgb_run* r, int s, long long need) {
     Species& S = r->sp[s];
-    if (need > S.cap || std::max(r->sp[0].cap, r->sp[1].cap) > r->list_cap) drop_graphs(r);
+    if (need > S.cap || std::max(r->sp[0].cap, r->sp[1].cap) > r->list_cap) {
+        /* the buffers about to be replaced may still be in use by queued
+         * work (pgb_step_async): drain the run's streams first          */
+        PGB_CK(r, cudaStreamSynchronize(r->stream));
+        PGB_CK(r, cudaStreamSynchronize(r->copy_stream));
+        drop_graphs(r);
+    }
     if (need > S.cap) {
         long long cap = std::max<long long>(need, 1024);
         Species T = S;
@@ -196,7 +202,10 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
                 cudaGetLastError();
                 return fail(r, PGB_ERR_NOMEM, "device allocation of event lists failed");
             }
-            PGB_CK(r, cudaMemset(r->tile_cnt[l], 0, sizeof(int) * nt));
+            /* on the run's stream: a plain cudaMemset goes to the legacy
+             * stream, which does not order against the run's non-blocking
+             * stream                                                    */
+            PGB_CK(r, cudaMemsetAsync(r->tile_cnt[l], 0, sizeof(int) * nt, r->stream));
         }
         if (cudaMalloc(&r->aux_i, sizeof(int) * std::max(lc, nt)) != cudaSuccess ||
             cudaMalloc(&r->aux_j, sizeof(int) * std::max(lc, nt)) != cudaSuccess) {
@@ -229,6 +238,14 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
         }
         r->list_cap = lc;
         r->ntiles_cap = nt;
+        /* the bin-piece tables of both species went with the old block
+         * (a growth of the ions at a sort step drops the pieces that the
+         * electron sort has just written): both species are unsorted
+         * until their next sort, and the push walks them tile by tile   */
+        for (int q = 0; q < 2; ++q) {
+            PGB_CK(r, cudaMemsetAsync(&r->ds->n_pieces[q], 0, sizeof(int), r->stream));
+            PGB_CK(r, cudaMemsetAsync(&r->ds->sorted_tiles[q], 0, sizeof(long long), r->stream));
+        }
     }
     return 0;
 }
@@ -468,7 +485,7 @@ extern "C" int pgb_footprint(const pgb_params* p, int64_t ne, int64_t ni, int64_
     b += 48 * std::max(ne, ni);                                           /* load/dump staging */
     long long levels = 0;
     for (long long n = nx; n >= 3; n = n / 2 + 1) { levels += n * n; if (n == 3) break; }
-    b += 4 * 8 * levels + 4 * 4 * levels;                                 /* multigrid, FP64 and FP32 */
+    b += 5 * 8 * levels + 5 * 4 * levels;                                 /* multigrid, FP64 and FP32 */
     b += 8 * (2 + 2 + 2 + 1) * G + 8 * 3 * GE + 8 * nx + 8 * 4096;        /* grids, phi table */
     b += 6 * p->init_no_neutrals * 4 + (16 << 20);                        /* neutral tables, streams, graphs */
     *bytes = b;

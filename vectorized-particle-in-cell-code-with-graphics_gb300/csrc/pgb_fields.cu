@@ -128,20 +128,6 @@ __device__ __forceinline__ T prolong_point(const T* uc, int nc, int i, int j) {
 }
 
 /* ------------------------------------------------ grid-wide launches */
-/* generic indexer: covers every interior point of the colour */
-template <class T>
-__global__ void k_relax_rows(T* u, const T* f, int n, T h2, int color) {
-    const int m = n - 2, per_row = (m + 1) / 2;
-    const long long tot = (long long)m * per_row;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
-        int r = (int)(t / per_row), c = (int)(t - (long long)r * per_row);
-        int i = r + 1;
-        int j0 = 1 + ((i + 1 + color) & 1);
-        int j = j0 + 2 * c;
-        if (j > n - 2) continue;
-        u[i * n + j] = gs_point(u, f, n, i, j, h2);
-    }
-}
 /* One red-black Gauss-Seidel relaxation (both colours, mglin.cpp:116-127)
  * on a RT x RTX tile of interior points.  The tile and a two-point halo
  * of u are staged in shared memory; red points of the tile and of a
@@ -149,13 +135,19 @@ __global__ void k_relax_rows(T* u, const T* f, int n, T h2, int color) {
  * neighbouring tiles too, from the same inputs, so they agree), then the
  * black points of the tile, which read only updated red values.  The
  * result equals the two separate colour sweeps bit for bit.
- * mode 0: relax u in place
- * mode 1: u += prolong(vc) first (addint, mglin.cpp:90-97), then relax
- * mode 2: u  = prolong(vc) first (FMG interpolation, mglin.cpp:49), then relax */
+ * The sweep reads uin and writes the tile's interior to uout, a different
+ * buffer: relaxing in place would let a block load a halo that the
+ * neighbouring block has already overwritten, whenever the two blocks do
+ * not run at the same time.  uout's walls are never written (they stay 0).
+ * mode 0: relax uin
+ * mode 1: uin + prolong(vc) first (addint, mglin.cpp:90-97), then relax
+ * mode 2: prolong(vc) first (FMG interpolation, mglin.cpp:49), then relax;
+ *         uin is not read                                                 */
 #define RT 8
 #define RTX 32
 template <class T, int MODE>
-__global__ void __launch_bounds__(RT * RTX) k_relax_tile(T* u, const T* f, int n, T h2, const T* vc) {
+__global__ void __launch_bounds__(RT * RTX) k_relax_tile(const T* __restrict__ uin, T* __restrict__ uout, const T* f, int n,
+                                                          T h2, const T* vc) {
     __shared__ T su[RT + 4][RTX + 4];
     __shared__ T sf[RT + 2][RTX + 2];
     const int nc = n / 2 + 1;
@@ -168,7 +160,7 @@ __global__ void __launch_bounds__(RT * RTX) k_relax_tile(T* u, const T* f, int n
         if (i >= 0 && j >= 0 && i < n && j < n) {
             if (MODE == 2) v = prolong_point(vc, nc, i, j);
             else {
-                v = u[i * n + j];
+                v = uin[i * n + j];
                 if (MODE == 1) v = v + prolong_point(vc, nc, i, j);
             }
         }
@@ -206,7 +198,7 @@ __global__ void __launch_bounds__(RT * RTX) k_relax_tile(T* u, const T* f, int n
     {
         int li = threadIdx.y, lj = threadIdx.x;
         int i = i0 + li, j = j0 + lj;
-        if (i < n - 1 && j < n - 1) u[i * n + j] = su[li + 2][lj + 2];
+        if (i < n - 1 && j < n - 1) uout[i * n + j] = su[li + 2][lj + 2];
     }
 }
 
@@ -502,35 +494,40 @@ struct Levels {
     T** v;
     T** rr;
     T** tab;   /* device copy: u, f, v, r tables */
+    T** w;     /* pre-smoothing results */
 };
-static Levels<double> levels64(pgb_run* r) { return {r->mg_u, r->mg_f, r->mg_v, r->mg_r, r->mg_tab}; }
-static Levels<float> levels32(pgb_run* r) { return {r->mg32_u, r->mg32_f, r->mg32_v, r->mg32_r, r->mg32_tab}; }
+static Levels<double> levels64(pgb_run* r) { return {r->mg_u, r->mg_f, r->mg_v, r->mg_r, r->mg_tab, r->mg_w}; }
+static Levels<float> levels32(pgb_run* r) { return {r->mg32_u, r->mg32_f, r->mg32_v, r->mg32_r, r->mg32_tab, r->mg32_w}; }
 
 template <class T, int MODE>
-static void relax_launch(pgb_run* r, T* u, const T* f, int n, T h2, const T* vc) {
+static void relax_launch(pgb_run* r, const T* uin, T* uout, const T* f, int n, T h2, const T* vc) {
     dim3 grid((n - 2 + RTX - 1) / RTX, (n - 2 + RT - 1) / RT), block(RTX, RT);
-    k_relax_tile<T, MODE><<<grid, block, 0, r->stream>>>(u, f, n, h2, vc);
+    k_relax_tile<T, MODE><<<grid, block, 0, r->stream>>>(uin, uout, f, n, h2, vc);
     r->launches++;
 }
 
 /* V-cycle at level j > small on (u, f) (mglin.cpp:176-196).  first_mode 2
  * replaces u by the prolongation of the coarser level before the
- * pre-smoothing (the FMG interpolation of mglin.cpp:49).                */
+ * pre-smoothing (the FMG interpolation of mglin.cpp:49).  The
+ * pre-smoothing goes from u to the level's spare buffer w, the residual is
+ * taken there, and the post-smoothing goes from w back to u.  A level has
+ * one V-cycle in flight at a time, so one spare buffer per level serves.  */
 template <class T>
 static int vcycle(pgb_run* r, const Levels<T>& L, int j, int jsmall, T* u, const T* f, int first_mode,
                   const T* coarse_u) {
     int nf = r->mg_n[j], nc = r->mg_n[j - 1];
     T h = (T)r->p.xlength / (T)(nf - 1), h2 = h * h, h2i = (T)1.0 / (h * h);
-    if (first_mode == 2) relax_launch<T, 2>(r, u, f, nf, h2, coarse_u);
-    else relax_launch<T, 0>(r, u, f, nf, h2, nullptr);
-    k_resid_restrict<T><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(L.rr[j - 1], L.v[j - 1], u, f, nf, h2i);
+    T* w = L.w[j];
+    if (first_mode == 2) relax_launch<T, 2>(r, nullptr, w, f, nf, h2, coarse_u);
+    else relax_launch<T, 0>(r, u, w, f, nf, h2, nullptr);
+    k_resid_restrict<T><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(L.rr[j - 1], L.v[j - 1], w, f, nf, h2i);
     r->launches++;
     if (j - 1 <= jsmall) {
         if (small_launch<T>(r, L.tab, j - 1, 1)) return PGB_ERR_CUDA;
     } else {
         if (vcycle<T>(r, L, j - 1, jsmall, L.v[j - 1], L.rr[j - 1], 0, nullptr)) return PGB_ERR_CUDA;
     }
-    relax_launch<T, 1>(r, u, f, nf, h2, L.v[j - 1]);
+    relax_launch<T, 1>(r, w, u, f, nf, h2, L.v[j - 1]);
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -593,6 +590,8 @@ int pgb_mg_setup(pgb_run* r) {
         PGB_CK(r, cudaMalloc(&r->mg32_f[l], n2 * sizeof(float)));
         PGB_CK(r, cudaMalloc(&r->mg32_v[l], n2 * sizeof(float)));
         PGB_CK(r, cudaMalloc(&r->mg32_r[l], n2 * sizeof(float)));
+        PGB_CK(r, cudaMalloc(&r->mg_w[l], n2 * sizeof(double)));
+        PGB_CK(r, cudaMalloc(&r->mg32_w[l], n2 * sizeof(float)));
         tabs[l] = r->mg_u[l];
         tabs[PGB_MAX_LEVELS + l] = r->mg_f[l];
         tabs[2 * PGB_MAX_LEVELS + l] = r->mg_v[l];
@@ -608,6 +607,8 @@ int pgb_mg_setup(pgb_run* r) {
         PGB_CK(r, cudaMemset(r->mg_v[l], 0, n2 * sizeof(double)));
         PGB_CK(r, cudaMemset(r->mg32_u[l], 0, n2 * sizeof(float)));
         PGB_CK(r, cudaMemset(r->mg32_v[l], 0, n2 * sizeof(float)));
+        PGB_CK(r, cudaMemset(r->mg_w[l], 0, n2 * sizeof(double)));   /* walls stay 0 */
+        PGB_CK(r, cudaMemset(r->mg32_w[l], 0, n2 * sizeof(float)));
     }
     PGB_CK(r, cudaMalloc(&r->mg_tab, sizeof(tabs)));
     PGB_CK(r, cudaMemcpy(r->mg_tab, tabs, sizeof(tabs), cudaMemcpyHostToDevice));
@@ -625,6 +626,7 @@ int pgb_mg_setup(pgb_run* r) {
 void pgb_mg_free(pgb_run* r) {
     for (int l = 0; l < r->ng; ++l) {
         cudaFree(r->mg32_u[l]); cudaFree(r->mg32_f[l]); cudaFree(r->mg32_v[l]); cudaFree(r->mg32_r[l]);
+        cudaFree(r->mg_w[l]); cudaFree(r->mg32_w[l]);
     }
     cudaFree(r->mg32_tab);
     cudaFree(r->dc_u);

@@ -112,6 +112,10 @@ struct pgb_run {
     float** mg32_tab = nullptr;
     double *dc_d = nullptr, *dc_u = nullptr;        /* FP32_DC defect correction (FP64) */
     float *mg32_u[PGB_MAX_LEVELS], *mg32_f[PGB_MAX_LEVELS], *mg32_v[PGB_MAX_LEVELS], *mg32_r[PGB_MAX_LEVELS];
+    /* the pre-smoothing result of each level (the tiled smoother reads one
+     * buffer and writes another: blocks never see a neighbour's update)  */
+    double* mg_w[PGB_MAX_LEVELS] = {};
+    float* mg32_w[PGB_MAX_LEVELS] = {};
     /* event lists */
     int* tile_list[4] = {nullptr, nullptr, nullptr, nullptr};
     int* tile_cnt[4] = {nullptr, nullptr, nullptr, nullptr};
