@@ -268,6 +268,53 @@ PGB_API int pgb_server_result(pgb_server* server, int64_t id, double* e_aos6, in
                               int64_t cap_i, pgb_counters* counters);
 PGB_API int pgb_server_get_stats(pgb_server* server, pgb_server_stats* out);
 
+/* ------------------------------------------------- averaged diagnostics
+ * The graphs class (graphs.cpp, pic.cl:151-251) summed on the device.
+ * Once enabled, every step t with start_step <= t < end_step adds, after
+ * the field solve (pic.cpp:1189-1207):
+ *   - rho, phi, Ex, Ey of every node (graphs::sum_fields);
+ *   - each species' charge density / its macro charge (sum_density);
+ *   - the mean vx of the particles in each cell of row ny/2, and the mean
+ *     vy in each cell of column nx/2 (sum_av_velocities, pic.cl:154-186);
+ *   - velocity histograms of NO_BINS bins of width vt/DIVIDE_BINS_BY at
+ *     two locations (sum_av_dist, pic.cl:191-251).  The reference hands
+ *     the kernel `spread` as an 8-byte double read from its int member and
+ *     the next one, dist_locationX (graphs.cpp:865, graphs.h:281-282): the
+ *     high word is dist_locationX, which makes the effective spread
+ *     a denormal: each histogram takes the location's own cell only.  The
+ *     same rule is kept here.
+ * The reference's kernels add with plain `+=` from every work item; here
+ * the counts are exact and the velocity sums are fixed point (2^-10 m/s).
+ * Reading a graph divides by no_graph_steps as graphs::average_* do
+ * (graphs.cpp:1000-1155); the velocity profiles of both species are
+ * divided by VTE as in the reference (graphs.cpp:1114-1121).             */
+typedef struct pgb_graphs_params {
+    int64_t start_step, end_step;   /* summed steps: start <= t < end (START/END_GRAPH_TIME) */
+    int32_t no_graph_steps;         /* NO_GRAPH_STEPS: divisor of every average */
+    int32_t no_bins;                /* NO_BINS, odd */
+    int32_t divide_bins_by;         /* DIVIDE_BINS_BY */
+    int32_t spread;                 /* SPREAD */
+    int32_t dist_location_x, dist_location_y;     /* DIST_LOCATIONX/Y   */
+    int32_t dist_location2_x, dist_location2_y;   /* DIST_LOCATION2X/Y  */
+} pgb_graphs_params;
+enum {
+    PGB_GRAPH_RHO = 0, PGB_GRAPH_PHI = 1, PGB_GRAPH_EX = 2, PGB_GRAPH_EY = 3,   /* [ny][nx]             */
+    PGB_GRAPH_DENSITY = 4,                                                   /* [ny][nx], per species */
+    PGB_GRAPH_VX = 5, PGB_GRAPH_VY = 6,                                      /* [nx] / [ny], per species */
+    PGB_GRAPH_DIST_X1 = 7, PGB_GRAPH_DIST_Y1 = 8,                            /* [no_bins], per species */
+    PGB_GRAPH_DIST_X2 = 9, PGB_GRAPH_DIST_Y2 = 10,
+    PGB_GRAPH_MAXIMA = 11   /* 5 values: max phi, Ex, Ey, density e, density i (phiMax ... qMax) */
+};
+/* parameters.h's defaults for this grid (parameters.h:288-302), window empty */
+PGB_API int pgb_graphs_params_default(const pgb_params* p, pgb_graphs_params* out);
+/* allocate and zero the sums; steps queued later add to them */
+PGB_API int pgb_graphs_enable(pgb_run* run, const pgb_graphs_params* g);
+/* one averaged graph (waits for the run's queued steps) */
+PGB_API int pgb_graphs_get(pgb_run* run, int which, int species, double* out, int64_t n);
+/* the reference's graph files, names and formats, into dir
+ * (graphs::write_*_to_file, graphs.cpp:1167-1370)                       */
+PGB_API int pgb_graphs_write(pgb_run* run, const char* dir);
+
 /*
  * Charge grid of one species from particle records already on the device,
  * with no run handle and no allocation.  It has no counterpart in the

@@ -59,6 +59,13 @@ struct orc_run {
     int ng;              /* multigrid levels */
     double *mg_u[32], *mg_rhs[32], *mg_res[32], *mg_tmp[32], *mg_v[32];
     pgb_stream st;
+    /* graphs class sums (orc_graphs_enable) */
+    int gr_on;
+    pgb_graphs_params gr;
+    double* gr_f[4];       /* rho, phi, Ex, Ey [ny][nx]                     */
+    double* gr_q[2];       /* density per species [ny][nx]                  */
+    double* gr_v[2][2];    /* per-cell mean vx along row ny/2, vy along column nx/2 */
+    double* gr_d[2][4];    /* histograms X1, Y1, X2, Y2 [no_bins]           */
 };
 
 static inline int cell(double v) {
@@ -206,6 +213,11 @@ void orc_destroy(orc_run* r) {
     free(r->efx); free(r->efy); free(r->prob_cx);
     for (int t = 0; t < 2; ++t) for (int k = 0; k < 3; ++k) free(r->neut[t][k]);
     for (int j = 0; j < r->ng; ++j) { free(r->mg_u[j]); free(r->mg_rhs[j]); free(r->mg_res[j]); free(r->mg_tmp[j]); free(r->mg_v[j]); }
+    for (int k = 0; k < 4; ++k) free(r->gr_f[k]);
+    for (int s = 0; s < 2; ++s) {
+        free(r->gr_q[s]); free(r->gr_v[s][0]); free(r->gr_v[s][1]);
+        for (int k = 0; k < 4; ++k) free(r->gr_d[s][k]);
+    }
     free(r);
 }
 
@@ -1212,7 +1224,140 @@ void orc_initial_boundary(orc_run* r) {
     orc_boundary(r, PGB_BOUNDARY_ELECTRONS);
 }
 
-/* pic::pic_run loop body (pic.cpp:1069-1250), graphs and printing left out */
+/* ------------------------------------------------------------- graphs */
+/* The value sum_av_dist sees as `spread`: graphs.cpp:865 passes &spread
+ * (an int) with sizeof(cl_double), so the kernel reads spread in the low
+ * word and the next member, dist_locationX (graphs.h:281-282), in the high
+ * word of a little-endian double.                                         */
+static double gr_kernel_spread(const pgb_graphs_params* g) {
+    uint64_t bits = ((uint64_t)(uint32_t)g->dist_location_x << 32) | (uint32_t)g->spread;
+    double d;
+    memcpy(&d, &bits, sizeof d);
+    return d;
+}
+
+/* vbin = (int)((v / vt) * divide_bins_by); counted when |vbin| <= half
+ * (pic.cl:218-221).  A value outside the int range is not counted.       */
+static void gr_bin(double* d, double v, double vt, double dbb, int half) {
+    double b = (v / vt) * dbb;
+    if (!(b > -2147483649.0 && b < 2147483648.0)) return;
+    int vbin = (int)b;
+    if (abs(vbin) <= half) d[vbin + half] += 1.0;
+}
+
+int orc_graphs_enable(orc_run* r, const pgb_graphs_params* g) {
+    if (!g || g->no_bins < 1 || (g->no_bins & 1) == 0 || g->no_graph_steps < 1) return PGB_ERR_ARG;
+    const size_t G = (size_t)r->nx * r->ny;
+    r->gr = *g;
+    for (int k = 0; k < 4; ++k) { free(r->gr_f[k]); r->gr_f[k] = (double*)calloc(G, sizeof(double)); }
+    for (int s = 0; s < 2; ++s) {
+        free(r->gr_q[s]); r->gr_q[s] = (double*)calloc(G, sizeof(double));
+        free(r->gr_v[s][0]); r->gr_v[s][0] = (double*)calloc((size_t)r->nx, sizeof(double));
+        free(r->gr_v[s][1]); r->gr_v[s][1] = (double*)calloc((size_t)r->ny, sizeof(double));
+        for (int k = 0; k < 4; ++k) { free(r->gr_d[s][k]); r->gr_d[s][k] = (double*)calloc((size_t)g->no_bins, sizeof(double)); }
+    }
+    r->gr_on = 1;
+    return 0;
+}
+
+/* one graph step: graphs::sum_fields, then per species sum_density,
+ * sum_av_velocities and sum_av_dist (pic.cpp:1189-1207, graphs.cpp:412-985,
+ * pic.cl:154-251), particles in storage order                           */
+static void orc_graphs_accumulate(orc_run* r) {
+    const int nx = r->nx, ny = r->ny;
+    const int64_t G = (int64_t)nx * ny;
+    for (int64_t k = 0; k < G; ++k) {
+        r->gr_f[0][k] += r->rho[k];
+        r->gr_f[1][k] += r->phi[k];
+        r->gr_f[2][k] += r->ex[k];   /* EgridX[j*nx+i]: stride nx */
+        r->gr_f[3][k] += r->ey[k];
+    }
+    const pgb_graphs_params* g = &r->gr;
+    const double sp = gr_kernel_spread(g);
+    const double l1 = g->dist_location_x, l2 = g->dist_location2_x;
+    const double l3 = g->dist_location_y, l4 = g->dist_location2_y;
+    const double dbb = (double)g->divide_bins_by;
+    const int half = (g->no_bins - 1) / 2;
+    double* vx_t = (double*)calloc((size_t)nx, sizeof(double));
+    double* cx_t = (double*)calloc((size_t)nx, sizeof(double));
+    double* vy_t = (double*)calloc((size_t)ny, sizeof(double));
+    double* cy_t = (double*)calloc((size_t)ny, sizeof(double));
+    for (int s = 0; s < 2; ++s) {
+        const double qc = s == 0 ? -C_CHARGE : C_CHARGE;   /* ELECTRON_CHARGE, CHARGE */
+        for (int64_t k = 0; k < G; ++k) r->gr_q[s][k] += r->q[s][k] / qc;
+        const orc_sp* S = &r->sp[s];
+        memset(vx_t, 0, (size_t)nx * sizeof(double)); memset(cx_t, 0, (size_t)nx * sizeof(double));
+        memset(vy_t, 0, (size_t)ny * sizeof(double)); memset(cy_t, 0, (size_t)ny * sizeof(double));
+        const int xv = nx / 2, yv = ny / 2;   /* sum_av_velocities (pic.cl:161-162) */
+        const int xd = ny / 2, yd = ny / 2;   /* sum_av_dist (pic.cl:202-203)      */
+        for (int64_t i = 0; i < S->n; ++i) {
+            const orc_pv* p = &S->p[i];
+            const int jp = cell(p->x / r->dx), kp = cell(p->y / r->dy);
+            /* jp, kp >= 0: a position beyond the int range gives INT_MIN */
+            if (jp >= 0 && jp < nx && p->x > 0.0 && kp == yv) { vx_t[jp] += p->vx; cx_t[jp] += 1.0; }
+            if (jp == xv && kp >= 0 && kp < ny && p->y > 0.0) { vy_t[kp] += p->vy; cy_t[kp] += 1.0; }
+            if (jp >= (l1 - sp) && p->x > 0.0 && jp <= (l1 + sp) && jp < nx && kp == yd)
+                gr_bin(r->gr_d[s][0], p->vx, S->vt, dbb, half);
+            if (jp >= (l2 - sp) && p->x > 0.0 && jp <= (l2 + sp) && jp < nx && kp == yd)
+                gr_bin(r->gr_d[s][2], p->vx, S->vt, dbb, half);
+            if (kp >= (l3 - sp) && p->y > 0.0 && kp <= (l3 + sp) && kp < ny && jp == xd)
+                gr_bin(r->gr_d[s][1], p->vy, S->vt, dbb, half);
+            if (kp >= (l4 - sp) && p->y > 0.0 && kp <= (l4 + sp) && kp < ny && jp == xd)
+                gr_bin(r->gr_d[s][3], p->vy, S->vt, dbb, half);
+        }
+        for (int j = 0; j < nx; ++j)
+            if (cx_t[j] > 0.5) r->gr_v[s][0][j] += vx_t[j] / cx_t[j];
+        for (int j = 0; j < ny; ++j)
+            if (cy_t[j] > 0.5) r->gr_v[s][1][j] += vy_t[j] / cy_t[j];
+    }
+    free(vx_t); free(cx_t); free(vy_t); free(cy_t);
+}
+
+/* running maximum that starts from element `first` (graphs.cpp:1002-1028,
+ * 1093-1104)                                                             */
+static double gr_max(const double* sum, int64_t n, int64_t first, double steps) {
+    double m = sum[first] / steps;
+    for (int64_t k = 0; k < n; ++k) {
+        double v = sum[k] / steps;
+        if (m < v) m = v;
+    }
+    return m;
+}
+
+/* averages of graphs::average_fields / _density / _velocities / _dist1/2
+ * (graphs.cpp:1000-1155)                                                 */
+int orc_graphs_get(orc_run* r, int which, int species, double* out, int64_t n) {
+    if (!r->gr_on || species < 0 || species > 1) return PGB_ERR_ARG;
+    const int64_t G = (int64_t)r->nx * r->ny;
+    const double steps = (double)r->gr.no_graph_steps;
+    const double* src = NULL;
+    int64_t cnt = G;
+    double div = steps;
+    switch (which) {
+        case PGB_GRAPH_RHO: case PGB_GRAPH_PHI: case PGB_GRAPH_EX: case PGB_GRAPH_EY:
+            src = r->gr_f[which]; break;
+        case PGB_GRAPH_DENSITY: src = r->gr_q[species]; break;
+        case PGB_GRAPH_VX: src = r->gr_v[species][0]; cnt = r->nx; div = r->prm.vte * steps; break;
+        case PGB_GRAPH_VY: src = r->gr_v[species][1]; cnt = r->ny; div = r->prm.vte * steps; break;
+        case PGB_GRAPH_DIST_X1: case PGB_GRAPH_DIST_Y1: case PGB_GRAPH_DIST_X2: case PGB_GRAPH_DIST_Y2:
+            src = r->gr_d[species][which - PGB_GRAPH_DIST_X1]; cnt = r->gr.no_bins; break;
+        case PGB_GRAPH_MAXIMA:
+            if (n < 5) return PGB_ERR_ARG;
+            out[0] = gr_max(r->gr_f[1], G, 0, steps);
+            out[1] = gr_max(r->gr_f[2], G, 0, steps);
+            out[2] = gr_max(r->gr_f[3], G, 0, steps);
+            out[3] = gr_max(r->gr_q[0], G, r->nx + 1, steps);
+            out[4] = gr_max(r->gr_q[1], G, r->nx + 1, steps);
+            return 0;
+        default: return PGB_ERR_ARG;
+    }
+    if (n < cnt) return PGB_ERR_ARG;
+    for (int64_t k = 0; k < cnt; ++k) out[k] = src[k] / div;
+    return 0;
+}
+
+/* pic::pic_run loop body (pic.cpp:1069-1250) and the graphs sums of the
+ * window (pic.cpp:1189-1207); printing left out                          */
 void orc_step(orc_run* r, int nsteps) {
     for (int k = 0; k < nsteps; ++k) {
         int64_t t = r->time_step;
@@ -1239,6 +1384,7 @@ void orc_step(orc_run* r, int nsteps) {
         orc_grid_rho(r);
         orc_poisson(r, t);
         orc_efield(r);
+        if (r->gr_on && t >= r->gr.start_step && t < r->gr.end_step) orc_graphs_accumulate(r);
         r->time_step = t + 1;
         r->c.step = r->time_step;
     }

@@ -64,6 +64,10 @@ void orc_poisson_residual(orc_run* r, double* max_res, double* max_rhs);
  * correction around the full multigrid pass) -- the "exact" reference for
  * PGB_POISSON_FP32_DC                                                        */
 void orc_poisson_converged(orc_run* r, int64_t t, int iters);
+/* the graphs class (graphs.cpp): sums over the window's steps, read as
+ * the reference's averages; `which` and the layouts are PGB_GRAPH_*       */
+int  orc_graphs_enable(orc_run* r, const pgb_graphs_params* g);
+int  orc_graphs_get(orc_run* r, int which, int species, double* out, int64_t n);
 void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
 #ifdef __cplusplus

@@ -103,7 +103,7 @@ cl_int clGetProgramBuildInfo(cl_program, cl_device_id, cl_program_build_info, si
 cl_kernel clCreateKernel(cl_program, const char* name, cl_int* err) {
     _cl_kernel* k = new _cl_kernel();
     k->name = name;
-    k->args.resize(16);
+    k->args.resize(32);   /* sum_av_dist takes 17 (pic.cl:191-197) */
     if (err) *err = CL_SUCCESS;
     return k;
 }

@@ -5,11 +5,16 @@
  * golden fixtures and pin the C restatement in oracle/picport.c.
  *
  * Modes (argv[1]):
- *   run <dir> <nsteps>   chdir(dir); srand(ORC_SEED); construct the reference
+ *   run <dir> <nsteps> [<start_graph> <end_graph>]
+ *                        chdir(dir); srand(ORC_SEED); construct the reference
  *                        `pic` with restart=true (it reads dataDump_e.txt and
  *                        dataDump_i1.txt, pic.cpp:110-119) and call pic_run()
- *                        for nsteps (pic.cpp:1040-1279) with the graph window
- *                        placed after the run; then write
+ *                        for nsteps (pic.cpp:1040-1279).  Without a window the
+ *                        graph window is placed after the run.  With one, the
+ *                        graphs sum steps [start, end), average over end-start
+ *                        steps (pic::initializeGraphsForInteractive,
+ *                        pic.cpp:990-995), and the reference writes its graph
+ *                        files into dir at step end-1 (pic.cpp:1209-1247); then write
  *                          e.bin, i1.bin   particles, 6 doubles each (particleVec.h)
  *                          q_e.bin, q_i1.bin  charge after edge doubling (ny*nx)
  *                          rho.bin, phi.bin   (ny*nx, row = y index)
@@ -98,8 +103,12 @@ int main(int argc, char** argv) {
 
     if (mode == "run") {
         int nsteps = argc > 3 ? std::atoi(argv[3]) : 1;
+        const bool window = argc > 5;
+        const int start_graph = window ? std::atoi(argv[4]) : INT_MAX - 2;
+        const int end_graph = window ? std::atoi(argv[5]) : INT_MAX - 1;
         srand(RAND_SEED);
-        pic* p = new pic(true, false, nsteps, INT_MAX - 2, INT_MAX - 1);
+        pic* p = new pic(true, false, nsteps, start_graph, end_graph);
+        if (window) p->initializeGraphsForInteractive(end_graph - start_graph);
         p->pic_run();
         write_particles("e.bin", p->electrons.get_particle());
         write_particles("i1.bin", p->ions[0].get_particle());

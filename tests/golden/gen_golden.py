@@ -14,7 +14,9 @@ For every case it writes tests/golden/<case>.npz holding
   e_out, i_out       particles after the run (6 doubles each, the reference's order)
   q_e, q_i, rho, phi, ex, ey   grids after the run, reference layouts
 Field-only cases (mode "fields") hold rho and the reference's phi, ex, ey
-for one fields::grid_potential + grid_electric_field call.
+for one fields::grid_potential + grid_electric_field call.  Cases with a
+graph window also hold graph_window (start, end) and graph_<file> for every
+text file the reference's graphs class wrote at the end of the window.
 
 The states are seeded synthetic plasmas sized so that every code path of the
 case is exercised in a few steps (particles crossing walls, collisions,
@@ -62,9 +64,17 @@ CASES = {
     "reduce33": ("reduce33", dict(X_NO_OF_CELLS=33, NUMBER_TO_INJECT=20, SIZE_TO_CHECK=900, UPPER_GROUP_LIMIT=550,
                                   NEW_GROUP_SIZE=520, UPPER_GROUP_LIMIT2=200, NEW_GROUP_SIZE2=180),
                  dict(n=1000, te=3.0, ti=3.0, seed=19), 10),
+    "graphs33": ("core33", dict(X_NO_OF_CELLS=33), dict(n=4000, te=10.0, ti=2.0, seed=23, graphs=(3, 8)), 10),
     "fields65": ("core65", dict(X_NO_OF_CELLS=65), dict(mode="fields", seed=21), 0),
     "fields129": ("core129", dict(X_NO_OF_CELLS=129), dict(mode="fields", seed=22), 0),
 }
+
+
+# files the reference's graphs class writes at the end of the graph window
+# (graphs.cpp:1167-1370); e = electrons, i1 = the ion species
+GRAPH_FILES = ["rho_phi_EgridX", "rho_phi_EgridY", "rho2d", "phi2d", "egrid2dX", "egrid2dY"] + [
+    f"{stem}_{t}" for t in ("e", "i1")
+    for stem in ("density2d", "av_velocity", "first_v_distX", "first_v_distY", "second_v_distX", "second_v_distY")]
 
 
 def make_state(p: picgb.PgbParams, n: int, te: float, ti: float, seed: int, outside: float = 0.0):
@@ -119,7 +129,13 @@ def run_case(name, cfg, kw, recipe, nsteps, refdir):
             e, i = make_state(p, recipe["n"], recipe["te"], recipe["ti"], recipe["seed"], recipe.get("outside", 0.0))
             write_dump(os.path.join(d, "dataDump_e.txt"), e)
             write_dump(os.path.join(d, "dataDump_i1.txt"), i)
-            subprocess.run([exe, "run", d, str(nsteps)], check=True)
+            window = recipe.get("graphs")
+            args = [exe, "run", d, str(nsteps)] + ([str(window[0]), str(window[1])] if window else [])
+            subprocess.run(args, check=True)
+            if window:
+                rec["graph_window"] = np.array(window)
+                for stem in GRAPH_FILES:
+                    rec["graph_" + stem] = np.loadtxt(os.path.join(d, stem + ".txt"), ndmin=2)
             rec.update(mode="run", e_in=e, i_in=i, nsteps=nsteps,
                        e_out=np.fromfile(os.path.join(d, "e.bin")).reshape(-1, 6),
                        i_out=np.fromfile(os.path.join(d, "i1.bin")).reshape(-1, 6),

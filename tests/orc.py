@@ -62,6 +62,8 @@ def load():
         "orc_get_neutral_table": (C.c_int, [R, C.c_int, dp, i64]),
         "orc_poisson_residual": (None, [R, dp, dp]),
         "orc_poisson_converged": (None, [R, i64, C.c_int]),
+        "orc_graphs_enable": (C.c_int, [R, C.POINTER(picgb.PgbGraphsParams)]),
+        "orc_graphs_get": (C.c_int, [R, C.c_int, C.c_int, dp, i64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -175,6 +177,16 @@ class Oracle:
         c = picgb.PgbCounters()
         self.lib.orc_get_counters(self.h, C.byref(c))
         return c.as_dict()
+
+    def graphs_enable(self, gp):
+        self._gp = gp
+        assert self.lib.orc_graphs_enable(self.h, C.byref(gp)) == 0
+
+    def graphs_get(self, which, species=0):
+        p = self.params
+        out = np.empty(picgb.graph_size(which, p, self._gp))
+        assert self.lib.orc_graphs_get(self.h, picgb.GRAPH[which], species, _dp(out), out.size) == 0
+        return out.reshape(p.y_no_of_cells, p.x_no_of_cells) if picgb.GRAPH[which] <= 4 else out
 
     def neutral_table(self, which):
         n = self.params.init_no_neutrals

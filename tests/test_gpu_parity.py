@@ -404,14 +404,18 @@ def test_sort_leaves_deterministic_physics_unchanged():
 # ------------------------------------------------------------- host driver
 def test_batch_driver_runs_and_writes_reference_files(tmp_path):
     """picgb_run (the main.cpp batch counterpart) reads a parameters.h, loads
-    the dataDump files, runs, and writes dataDump_*.txt and timeData.txt in
-    the reference's text formats."""
+    the dataDump files, runs, and writes dataDump_*.txt, timeData.txt and the
+    averaged graph files of its graph window (steps 97-136 here) in the
+    reference's text formats."""
     import os
     import subprocess
     from test_host_driver import PARAMS_TEXT
     g = load_golden("core65")
     text = PARAMS_TEXT.replace("#define X_NO_OF_CELLS 129", "#define X_NO_OF_CELLS 65") \
-                      .replace("#define Y_NO_OF_CELLS 129", "#define Y_NO_OF_CELLS 65")
+                      .replace("#define Y_NO_OF_CELLS 129", "#define Y_NO_OF_CELLS 65") \
+                      .replace("#define NO_GRAPH_STEPS ((int)50*(int)PERIOD)", "#define NO_GRAPH_STEPS 40") \
+                      .replace("#define START_GRAPH_TIME ((int)250*(int)PERIOD)", "#define START_GRAPH_TIME 97")
+    assert "NO_GRAPH_STEPS 40" in text and "START_GRAPH_TIME 97" in text
     (tmp_path / "parameters.h").write_text(text)
     picgb.write_datadump(str(tmp_path / "dataDump_e.txt"), g["e_in"])
     picgb.write_datadump(str(tmp_path / "dataDump_i1.txt"), g["i_in"])
@@ -425,6 +429,24 @@ def test_batch_driver_runs_and_writes_reference_files(tmp_path):
     rows = [l.split() for l in open(tmp_path / "timeData.txt")]
     assert [int(r[0]) for r in rows] == [0, 100]
     assert all(len(r) == 8 for r in rows)
+    shapes = {"rho_phi_EgridX": (65, 4), "rho_phi_EgridY": (65, 4), "rho2d": (65, 65), "phi2d": (65, 65),
+              "egrid2dX": (65, 65), "egrid2dY": (65, 65)}
+    for t in ("e", "i1"):
+        shapes.update({f"density2d_{t}": (65, 65), f"av_velocity_{t}": (65, 3)})
+        for d in ("first_v_distX", "first_v_distY", "second_v_distX", "second_v_distY"):
+            shapes[f"{d}_{t}"] = (30001, 2)
+    for stem, shape in shapes.items():
+        assert np.loadtxt(tmp_path / f"{stem}.txt", ndmin=2).shape == shape, stem
+    rho = np.loadtxt(tmp_path / "rho2d.txt")
+    assert np.all(np.isfinite(rho)) and np.any(rho != 0)
+    total = 0.0
+    for t in ("e", "i1"):
+        for d in ("first_v_distX", "first_v_distY", "second_v_distX", "second_v_distY"):
+            hist = np.loadtxt(tmp_path / f"{d}_{t}.txt")
+            assert np.all(hist[:, 1] >= 0)
+            assert np.allclose(hist[:, 0], (np.arange(30001) - 15000) / 300.0)
+            total += hist[:, 1].sum()
+    assert total > 0
 
 
 @pytest.mark.parametrize("nsteps", [10, 11, 12])
@@ -551,3 +573,54 @@ def test_async_steps_equal_blocking_steps():
     assert np.array_equal(a[1], b[1], equal_nan=True)
     assert np.array_equal(a[2], b[2])
     assert a[3] == b[3]
+
+
+def test_graphs_match_oracle_and_write_reference_files(tmp_path):
+    """The averaged diagnostics (graphs class) summed on the device over a
+    window of steps, against the oracle, whose graph sums are pinned to the
+    reference's own graph files.
+    - Fields and densities: within the 1e-4 field tolerance of the step tests.
+    - Velocity profiles and histograms come from a few particles per cell, so
+      a particle whose FP32 position or velocity lands across a cell or bin
+      edge from the FP64 one moves a count: most cells and bins must agree
+      exactly, totals to within a few counts.
+    - pgb_graphs_write produces every file with the reference's name and
+      layout, holding the same values."""
+    from test_oracle_pin import graph_files_from
+    g = load_golden("graphs33")
+    p = g["p"]
+    start, end = (int(v) for v in g["graph_window"])
+    gp = picgb.graphs_params(p, start, end)
+    o = orc.Oracle(p, rng=orc.ORC_RNG_PHILOX, order=orc.ORC_ORDER_STABLE)
+    o.graphs_enable(gp)
+    with picgb.Run(p) as r:
+        r.graphs_enable(gp)
+        for x in (o, r):
+            x.load_particles(0, g["e_in"])
+            x.load_particles(1, g["i_in"])
+            x.initial_boundary()
+            x.step(int(g["nsteps"]))
+        for which in ("rho", "phi", "ex", "ey"):
+            assert rel_err(r.graphs_get(which), o.graphs_get(which)) <= 1e-4, which
+        steps = gp.no_graph_steps
+        for sp in (0, 1):
+            assert rel_err(r.graphs_get("density", sp), o.graphs_get("density", sp)) <= 1e-4
+            for which in ("vx", "vy"):
+                a, b = r.graphs_get(which, sp), o.graphs_get(which, sp)
+                agree = np.isclose(a, b, rtol=1e-4, atol=1e-9 * max(np.max(np.abs(b)), 1e-30))
+                assert agree.mean() >= 0.85, (which, sp, agree.mean())
+            for which in ("dist_x1", "dist_y1", "dist_x2", "dist_y2"):
+                a, b = r.graphs_get(which, sp) * steps, o.graphs_get(which, sp) * steps
+                assert np.array_equal(a, np.round(a)), which   # exact counts
+                assert abs(a.sum() - b.sum()) <= 0.05 * b.sum() + 2, (which, sp, a.sum(), b.sum())
+                assert np.count_nonzero(a != b) <= 0.1 * np.count_nonzero(b) + 4, (which, sp)
+        m_r, m_o = r.graphs_get("maxima"), o.graphs_get("maxima")
+        assert np.allclose(m_r, m_o, rtol=1e-3), (m_r, m_o)
+        r.graphs_write(str(tmp_path))
+        mine = graph_files_from(r.graphs_get, p, gp)
+        for key in g:
+            if key.startswith("graph_") and key != "graph_window":
+                stem = key[len("graph_"):]
+                written = np.loadtxt(tmp_path / f"{stem}.txt", ndmin=2)
+                assert written.shape == g[key].shape, stem
+                np.testing.assert_allclose(written, mine[stem], rtol=1e-6, atol=1e-300, err_msg=stem)

@@ -90,3 +90,55 @@ def test_philox_known_answers():
         o = (C.c_uint32 * 4)()
         lib.orc_philox4x32(c, k, o)
         assert list(o) == want
+
+
+def graph_files_from(get, p, gp):
+    """The reference's graph files (graphs.cpp:1167-1370) assembled from
+    averaged graphs; get(which, species) returns one graph."""
+    nx, ny = p.x_no_of_cells, p.y_no_of_cells
+    yp, xp = ny // 2, nx // 2
+    rho, phi, ex, ey = (get(w, 0) for w in ("rho", "phi", "ex", "ey"))
+    i = np.arange(nx, dtype=np.float64)
+    files = {
+        "rho_phi_EgridX": np.column_stack([i, rho[yp, :], phi[yp, :], ex[yp, :]]),
+        "rho_phi_EgridY": np.column_stack([i, rho[:nx, xp], phi[:nx, xp], ey[:nx, xp]]),
+        "rho2d": rho, "phi2d": phi, "egrid2dX": ex, "egrid2dY": ey,
+    }
+    half = (gp.no_bins - 1) // 2
+    vbin = (np.arange(gp.no_bins) - half) / float(gp.divide_bins_by)
+    for s, t in ((0, "e"), (1, "i1")):
+        files[f"density2d_{t}"] = get("density", s)
+        files[f"av_velocity_{t}"] = np.column_stack([i, get("vx", s)[:nx], get("vy", s)[:nx]])
+        for stem, w in (("first_v_distX", "dist_x1"), ("first_v_distY", "dist_y1"),
+                        ("second_v_distX", "dist_x2"), ("second_v_distY", "dist_y2")):
+            files[f"{stem}_{t}"] = np.column_stack([vbin, get(w, s)])
+    return files
+
+
+def test_port_graphs_match_reference_files():
+    """The oracle's graph sums over a window of steps reproduce the files the
+    reference's graphs class wrote (printed with %e, so to 6 digits),
+    including the histograms taken from the location's own cell only."""
+    import picgb
+    g = load_golden("graphs33")
+    p = g["p"]
+    start, end = (int(v) for v in g["graph_window"])
+    gp = picgb.graphs_params(p, start, end)
+    o = orc.Oracle(p, rng=orc.ORC_RNG_LIBC, order=orc.ORC_ORDER_REF)
+    o.graphs_enable(gp)
+    o.load_particles(0, g["e_in"])
+    o.load_particles(1, g["i_in"])
+    o.initial_boundary()
+    o.step(int(g["nsteps"]))
+    mine = graph_files_from(o.graphs_get, p, gp)
+    counted = 0
+    for stem, a in mine.items():
+        ref = g["graph_" + stem]
+        assert a.shape == ref.shape, (stem, a.shape, ref.shape)
+        np.testing.assert_allclose(a, ref, rtol=1e-6, atol=1e-300, err_msg=stem)
+        if "dist" in stem:
+            counted += a[:, 1].sum()
+    assert counted > 0, "the window's histograms are empty"
+    m = o.graphs_get("maxima")
+    assert m[0] == np.max(mine["phi2d"]) and m[3] == np.max(mine["density2d_e"])
+

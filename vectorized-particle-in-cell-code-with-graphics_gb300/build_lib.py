@@ -31,6 +31,7 @@ UNITS = {
     "pgb_fields.cu": ["--fmad=false"],
     "pgb_sort.cu": [],
     "pgb_reduce.cu": [],
+    "pgb_graphs.cu": [],
     "pgb_static.cu": [],
 }
 

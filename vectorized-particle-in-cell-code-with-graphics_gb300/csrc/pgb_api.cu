@@ -393,6 +393,7 @@ extern "C" int pgb_destroy(pgb_run* r) {
     if (r->h_stage) cudaFreeHost(r->h_stage);
     cudaFree(r->d_stage);
     cudaFree(r->kh);
+    cudaFree(r->gr.buf);
     if (r->prof_ev_ok)
         for (int k = 0; k < 12; ++k) cudaEventDestroy(r->prof_ev[k]);
     if (r->copy_ev_ok)
@@ -847,6 +848,10 @@ static int issue_one_step(pgb_run* r) {
     const bool ion_step = (r->time_step % r->dt_dti) == 0;
     if ((rc = launch_step(r, ion_step))) return rc;
     if (r->prof_on && (rc = profile_collect(r))) return rc;
+    /* the graphs class sums after the field solve (pic.cpp:1189-1207) */
+    if (r->gr.on && r->time_step >= r->gr.g.start_step && r->time_step < r->gr.g.end_step &&
+        (rc = pgb_launch_graphs(r)))
+        return rc;
     r->time_step += 1;
     /* counters come back asynchronously; the host reads them only to
      * decide when to compact, which never changes results          */

@@ -154,6 +154,18 @@ struct pgb_run {
     long long sort_chunks_cap = 0;
     /* population control (Kunhardt): group counts and digit histograms */
     void* kh = nullptr;
+    /* averaged diagnostics (graphs class): sums on the device, one buffer */
+    struct Graphs {
+        bool on = false;
+        pgb_graphs_params g{};
+        double* f[4] = {};                /* rho, phi, Ex, Ey sums [ny][nx]          */
+        double* q[2] = {};                /* density sums per species [ny][nx]       */
+        double* v[2][2] = {};             /* per-cell mean vx [nx] / vy [ny] sums    */
+        long long* vsum[2][2] = {};       /* this step's velocity sums, 2^10 per m/s */
+        unsigned int* vcnt[2][2] = {};    /* this step's particle counts             */
+        unsigned long long* d[2][4] = {}; /* histogram counts X1, Y1, X2, Y2         */
+        void* buf = nullptr;
+    } gr;
     /* host staging */
     double* h_stage = nullptr;
     size_t h_stage_bytes = 0;
@@ -202,6 +214,7 @@ int pgb_launch_sort(pgb_run* r, int s);
 int pgb_sort_setup(pgb_run* r);
 void pgb_bins(pgb_run* r, int* nbx, int* nby);
 int pgb_launch_reduce(pgb_run* r, int s);
+int pgb_launch_graphs(pgb_run* r);
 int pgb_poisson_solve(pgb_run* r);
 int pgb_launch_efield(pgb_run* r, int advance);
 int pgb_launch_rhs(pgb_run* r);

@@ -391,6 +391,25 @@ Pic::Pic(const MacroTable& m, const std::string& dir, bool restart, uint64_t see
         point[k][0] = m.has(px[k]) ? (int)m.number(px[k]) : 0;
         point[k][1] = m.has(py[k]) ? (int)m.number(py[k]) : 0;
     }
+    /* the graphs of pic::initialize_graph_parameters (pic.cpp:539-577) and
+     * the window of pic::pic (pic.h:89): sums over time steps
+     * [START_GRAPH_TIME, END_GRAPH_TIME), averaged over NO_GRAPH_STEPS    */
+    check(pgb_graphs_params_default(&p_, &graphs_), "pgb_graphs_params_default");
+    const struct { const char* name; int32_t* i32; int64_t* i64; } gm[] = {
+        {"START_GRAPH_TIME", nullptr, &graphs_.start_step}, {"END_GRAPH_TIME", nullptr, &graphs_.end_step},
+        {"NO_GRAPH_STEPS", &graphs_.no_graph_steps, nullptr}, {"NO_BINS", &graphs_.no_bins, nullptr},
+        {"DIVIDE_BINS_BY", &graphs_.divide_bins_by, nullptr}, {"SPREAD", &graphs_.spread, nullptr},
+        {"DIST_LOCATIONX", &graphs_.dist_location_x, nullptr}, {"DIST_LOCATIONY", &graphs_.dist_location_y, nullptr},
+        {"DIST_LOCATION2X", &graphs_.dist_location2_x, nullptr},
+        {"DIST_LOCATION2Y", &graphs_.dist_location2_y, nullptr},
+    };
+    for (auto& g : gm) {
+        if (!m.has(g.name)) continue;
+        const double v = m.number(g.name);
+        if (g.i32) *g.i32 = (int32_t)v;
+        else *g.i64 = (int64_t)v;
+    }
+    if (graphs_.end_step > graphs_.start_step) check(pgb_graphs_enable(run_, &graphs_), "pgb_graphs_enable");
     const char* types[2] = {"e", "i1"};   /* ELECTRON_TYPE, ION_TYPE */
     for (int s = 0; s < 2; ++s) {
         std::vector<double> a;
@@ -461,6 +480,9 @@ void Pic::pic_run(int run_time, bool verbose) {
         if (!verbose) {
             int next = ((t / time_data_frequency_) + 1) * time_data_frequency_;
             if (t % time_data_frequency_ == 0) next = t + 1;
+            /* stop after step END_GRAPH_TIME-1 to write the graph files */
+            const int64_t gend = graphs_.end_step;
+            if (gend > graphs_.start_step && gend > t && gend < next) next = (int)gend;
             chunk = std::min(run_time, next) - t;
         }
         check(pgb_step(run_, chunk), "pgb_step");
@@ -479,6 +501,9 @@ void Pic::pic_run(int run_time, bool verbose) {
             s.iden_r = qi[(size_t)point[2][1] * nx + point[2][0]];
             samples_.push_back(s);
         }
+        /* pic.cpp:1209-1247 */
+        if (write_graphs_ && graphs_.end_step > graphs_.start_step && last == graphs_.end_step - 1)
+            check(pgb_graphs_write(run_, dir_.c_str()), "pgb_graphs_write");
         if (verbose) {
             pgb_counters c = counters();
             std::printf("time is %d no of electrons= %lld no ions of species1  %lld\n", last, (long long)c.n_e,

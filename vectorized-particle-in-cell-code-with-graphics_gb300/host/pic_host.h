@@ -68,6 +68,9 @@ public:
      * TIME_DATA_FREQUENCY steps (pic.cpp:1167-1180); verbose prints the
      * reference's per-step line (pic.cpp:1183-1186)                      */
     void pic_run(int run_time, bool verbose);
+    /* pic::setWriteGraphDataToFiles (pic.cpp:980-983): the averaged graph
+     * files are written when step END_GRAPH_TIME-1 completes            */
+    void set_write_graph_data_to_files(bool on) { write_graphs_ = on; }
     void dump_data();                       /* dataDump_e.txt, dataDump_i1.txt */
     void write_time_data();                 /* timeData.txt (pic.cpp:1261-1274) */
     pgb_counters counters();
@@ -83,6 +86,8 @@ private:
     struct Sample { long long t, ne, ni; double phi_l, phi_m, phi_r, eden_r, iden_r; };
     std::vector<Sample> samples_;
     bool first_run_ = true;
+    pgb_graphs_params graphs_{};
+    bool write_graphs_ = true;
 };
 
 }  // namespace picgb

@@ -4,9 +4,11 @@
  * run pic_run, write the particle dump and timeData.txt.
  *
  *   picgb_run <parameters.h> <dir> [--steps N] [--seed S] [--restart|--fresh]
- *             [--verbose] [--no-dump]
+ *             [--verbose] [--no-dump] [--no-graphs]
  * dir holds dataDump_e.txt / dataDump_i1.txt for a restart and receives the
- * outputs.  Without --steps the run length is TOTAL_RUN_TIME.
+ * outputs: dataDump_*.txt, timeData.txt and, when the run reaches
+ * END_GRAPH_TIME, the averaged graph files (pic.cpp:1209-1247).  Without
+ * --steps the run length is TOTAL_RUN_TIME.
  */
 #include <chrono>
 #include <cstdio>
@@ -18,7 +20,8 @@
 int main(int argc, char** argv) {
     if (argc < 3) {
         std::fprintf(stderr,
-                     "usage: %s <parameters.h> <dir> [--steps N] [--seed S] [--restart|--fresh] [--verbose] [--no-dump]\n",
+                     "usage: %s <parameters.h> <dir> [--steps N] [--seed S] [--restart|--fresh] [--verbose] [--no-dump] "
+                     "[--no-graphs]\n",
                      argv[0]);
         return 2;
     }
@@ -26,7 +29,7 @@ int main(int argc, char** argv) {
     long long steps = -1;
     unsigned long long seed = 1;
     int restart = -1;
-    bool verbose = false, dump = true;
+    bool verbose = false, dump = true, graphs = true;
     for (int k = 3; k < argc; ++k) {
         if (!std::strcmp(argv[k], "--steps") && k + 1 < argc) steps = std::atoll(argv[++k]);
         else if (!std::strcmp(argv[k], "--seed") && k + 1 < argc) seed = std::strtoull(argv[++k], nullptr, 10);
@@ -34,6 +37,7 @@ int main(int argc, char** argv) {
         else if (!std::strcmp(argv[k], "--fresh")) restart = 0;
         else if (!std::strcmp(argv[k], "--verbose")) verbose = true;
         else if (!std::strcmp(argv[k], "--no-dump")) dump = false;
+        else if (!std::strcmp(argv[k], "--no-graphs")) graphs = false;
         else { std::fprintf(stderr, "unknown argument %s\n", argv[k]); return 2; }
     }
     try {
@@ -41,6 +45,7 @@ int main(int argc, char** argv) {
         if (restart < 0) restart = m.has("RESTART") ? (m.flag("RESTART") ? 1 : 0) : 0;
         if (steps < 0) steps = (long long)m.number("TOTAL_RUN_TIME");
         picgb::Pic pic(m, dir, restart == 1, seed);
+        pic.set_write_graph_data_to_files(graphs);
         auto t0 = std::chrono::steady_clock::now();
         pic.pic_run((int)steps, verbose);
         auto t1 = std::chrono::steady_clock::now();

@@ -97,6 +97,48 @@ class PgbServerStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class PgbGraphsParams(C.Structure):
+    """pgb_graphs_params: window and settings of the averaged diagnostics
+    (the graphs class, graphs.cpp; parameters.h:227-302)."""
+    _fields_ = [("start_step", C.c_int64), ("end_step", C.c_int64), ("no_graph_steps", C.c_int32),
+                ("no_bins", C.c_int32), ("divide_bins_by", C.c_int32), ("spread", C.c_int32),
+                ("dist_location_x", C.c_int32), ("dist_location_y", C.c_int32),
+                ("dist_location2_x", C.c_int32), ("dist_location2_y", C.c_int32)]
+
+
+# PGB_GRAPH_*: which averaged graph to read
+GRAPH = {"rho": 0, "phi": 1, "ex": 2, "ey": 3, "density": 4, "vx": 5, "vy": 6, "dist_x1": 7, "dist_y1": 8,
+         "dist_x2": 9, "dist_y2": 10, "maxima": 11}
+
+
+def graphs_params(p, start: int, end: int, no_graph_steps: int = None, **kw) -> PgbGraphsParams:
+    """parameters.h's graph settings for this grid (NO_BINS, DIVIDE_BINS_BY,
+    SPREAD, DIST_LOCATION*; parameters.h:288-302), summing steps
+    [start, end) and averaging over no_graph_steps (default end - start).
+    Keyword arguments override single fields."""
+    g = PgbGraphsParams()
+    nx, ny = p.x_no_of_cells, p.y_no_of_cells
+    f32 = lambda v: float(np.float32(v))   # the (float) casts of parameters.h
+    g.start_step, g.end_step = start, end
+    g.no_graph_steps = no_graph_steps if no_graph_steps is not None else max(end - start, 1)
+    g.no_bins = 30001
+    g.divide_bins_by = (g.no_bins - 1) // 100
+    g.spread = int(0.05 * f32(nx))
+    g.dist_location_x, g.dist_location_y = int(0.9 * f32(nx)), int(0.5 * f32(ny))
+    g.dist_location2_x, g.dist_location2_y = int(0.1 * f32(nx)), int(0.5 * f32(ny))
+    for k, v in kw.items():
+        setattr(g, k, v)
+    return g
+
+
+def graph_size(which: str, p, gp: PgbGraphsParams) -> int:
+    """number of values pgb_graphs_get returns for `which`"""
+    w = GRAPH[which]
+    if w <= 4:
+        return p.x_no_of_cells * p.y_no_of_cells
+    return {5: p.x_no_of_cells, 6: p.y_no_of_cells, 11: 5}.get(w, gp.no_bins)
+
+
 class PgbProfile(C.Structure):
     """ctypes image of `pgb_profile` (include/picgb.h)."""
 
@@ -257,6 +299,10 @@ def load_library():
         "pgb_step": (C.c_int, [R, i32]),
         "pgb_step_batch": (C.c_int, [C.POINTER(R), i32, i32]),
         "pgb_step_async": (C.c_int, [R, i32]),
+        "pgb_graphs_params_default": (C.c_int, [C.POINTER(PgbParams), C.POINTER(PgbGraphsParams)]),
+        "pgb_graphs_enable": (C.c_int, [R, C.POINTER(PgbGraphsParams)]),
+        "pgb_graphs_get": (C.c_int, [R, C.c_int, C.c_int, dp, i64]),
+        "pgb_graphs_write": (C.c_int, [R, C.c_char_p]),
         "pgb_query": (C.c_int, [R, C.POINTER(i32)]),
         "pgb_footprint": (C.c_int, [C.POINTER(PgbParams), i64, i64, C.POINTER(i64)]),
         "pgb_server_create": (C.c_int, [i64, i32, i32, C.POINTER(R)]),
@@ -429,6 +475,24 @@ class Run:
         pr = PgbProfile()
         self._check(self.lib.pgb_get_profile(self.h, C.byref(pr)), "pgb_get_profile")
         return pr.as_dict()
+
+    # averaged diagnostics (the graphs class)
+    def graphs_enable(self, gp: PgbGraphsParams):
+        """sum the graphs over steps [gp.start_step, gp.end_step) of what is
+        stepped from now on"""
+        self._gp = gp
+        self._check(self.lib.pgb_graphs_enable(self.h, C.byref(gp)), "pgb_graphs_enable")
+
+    def graphs_get(self, which: str, species: int = 0) -> np.ndarray:
+        """one averaged graph: [ny, nx] for the grids, 1-D otherwise"""
+        p = self.params
+        out = np.empty(graph_size(which, p, self._gp))
+        self._check(self.lib.pgb_graphs_get(self.h, GRAPH[which], species, _dptr(out), out.size), "pgb_graphs_get")
+        return out.reshape(p.y_no_of_cells, p.x_no_of_cells) if GRAPH[which] <= 4 else out
+
+    def graphs_write(self, directory: str):
+        """the reference's graph text files, written into directory"""
+        self._check(self.lib.pgb_graphs_write(self.h, os.fsencode(directory)), "pgb_graphs_write")
 
     def load_particles_ptr(self, species: int, ptr: int, n: int):
         """Load n records from a host address (e.g. pinned memory)."""
