@@ -378,6 +378,27 @@ def run_served(args):
 
 
 # ------------------------------------------------------------------ GPU path
+def run_render(run, args, picgb, size=1024):
+    """Wall time of one pgb_render call (the viewer's plots at size x size,
+    the 3 MB image copied to host memory) on the bench state after its
+    steps.  The reference draws these with OpenGL, which is unavailable on
+    this box, so no reference time exists."""
+    frames = {}
+    cases = [("particle_xy", 0), ("particle_xy", picgb.NUM_PARTICLES_TO_PLOT), ("electron_vx_vy", 0), ("phi", 0),
+             ("e_density", 0)]
+    for plot, max_points in cases:
+        run.render(plot, size, size, max_points)   # allocation and warm-up
+        t0 = time.perf_counter()
+        for k in range(args.render_frames):
+            run.render(plot, size, size, max_points, seed=k)
+        ms = 1000.0 * (time.perf_counter() - t0) / args.render_frames
+        frames[f"{plot}{'' if max_points == 0 else f'_{max_points}_per_species'}"] = ms
+    return {"ms_per_frame": frames, "width": size, "height": size,
+            "particles_per_species": [run.particle_size(0), run.particle_size(1)],
+            "note": "wall time of pgb_render through the C ABI, image copied to pageable host memory; "
+                    "OpenGL reference unavailable on this box"}
+
+
 def run_gpu(args, rank, world):
     import torch
     import picgb
@@ -440,11 +461,12 @@ def run_gpu(args, rank, world):
         wall = time.perf_counter() - t0
         e2e = {"value": tot / wall, "unit": METRIC, "h2d_bytes_per_step": h2d // args.e2e_steps,
                "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps}
+    render = run_render(run, args, picgb) if args.render_frames > 0 else None
     run.close()
     batched = run_batched(args) if (args.batch_runs > 0 and world == 1) else None
     served = run_served(args) if (args.serve_requests > 0 and world == 1) else None
     return dict(ms=ms, ps=ps, counts=(c0, c1), prof=prof, launches=launches, clocks=clk.summary(), e2e=e2e, n=n,
-                batched=batched, served=served)
+                batched=batched, served=served, render=render)
 
 
 def main():
@@ -465,6 +487,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=16, help="requests of the served workload (0 = skip it)")
     ap.add_argument("--serve-max-steps", type=int, default=5000, help="longest request of the served workload")
     ap.add_argument("--serve-round", type=int, default=10, help="steps per server round")
+    ap.add_argument("--render-frames", type=int, default=10, help="frames per viewer plot timed (0 = skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -542,7 +565,7 @@ def main():
             "config": config, "e2e": res["e2e"], "roofline": roofline, "cpu_baseline": cpu,
             "gpu_launches": res["launches"], "clocks": res["clocks"],
             "particles": {"start": [c0["n_e"], c0["n_i"]], "end": [c1["n_e"], c1["n_i"]]},
-            "batched": res.get("batched"), "served": res.get("served")}
+            "batched": res.get("batched"), "served": res.get("served"), "render": res.get("render")}
     print(json.dumps(line), flush=True)
 
 

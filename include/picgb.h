@@ -315,6 +315,35 @@ PGB_API int pgb_graphs_get(pgb_run* run, int which, int species, double* out, in
  * (graphs::write_*_to_file, graphs.cpp:1167-1370)                       */
 PGB_API int pgb_graphs_write(pgb_run* run, const char* dir);
 
+/* ------------------------------------------------ headless viewer plots
+ * The interactive viewer's plots (the radio buttons of graphics.cpp:68-77,
+ * drawn by graphics.cpp:245-607) rasterised with CUDA into an RGB image;
+ * no graphics API is involved.  Row 0 of the image is the top; background
+ * black.  Titles, labels and axes are not drawn.
+ *   PARTICLE_XY   electrons (lime), then ions (hot pink) on top, as 2x2
+ *                 pixel points over the domain (draw_particleXY, :512-607);
+ *   *_VX_VY       vx-vy points of one species scaled by the integer part of
+ *                 the largest |vx|, |vy| among the plotted particles (at
+ *                 least 1), points with |v| below it (drawParticlePhase,
+ *                 :396-509);
+ *   PHI ... ION_DENSITY   one flat quad per grid cell, inset by a tenth of a
+ *                 cell, coloured by |mean of its four corners| / |max| with
+ *                 the five-band red-orange-yellow-green-blue-purple ramp
+ *                 of drawField (:245-378); the densities skip the outer
+ *                 ring (gridStart 1).  The field is the averaged graph when
+ *                 graphs are enabled (the viewer's source, pic.cpp:918-960),
+ *                 otherwise the current grid; the maximum is taken as
+ *                 graphs::average_* take it (NaN values ignored).
+ * max_points: particles per species (NUM_PARTICLES_TO_PLOT, 5000 in
+ * graphics.h:77); <= 0 plots all.  Where a species has more, a particle is
+ * plotted when a hash of its id and sample_seed falls below
+ * max_points/n, instead of the viewer's rand() picks, so the sample does
+ * not depend on the particle order.  rgb: width*height*3 host bytes.     */
+enum { PGB_PLOT_PARTICLE_XY = 0, PGB_PLOT_ELECTRON_VX_VY = 1, PGB_PLOT_ION_VX_VY = 2, PGB_PLOT_PHI = 3,
+       PGB_PLOT_EFIELD_X = 4, PGB_PLOT_EFIELD_Y = 5, PGB_PLOT_E_DENSITY = 6, PGB_PLOT_ION_DENSITY = 7 };
+PGB_API int pgb_render(pgb_run* run, int plot, int32_t width, int32_t height, int32_t max_points,
+                       uint32_t sample_seed, uint8_t* rgb, int64_t cap);
+
 /*
  * Charge grid of one species from particle records already on the device,
  * with no run handle and no allocation.  It has no counterpart in the

@@ -1356,6 +1356,150 @@ int orc_graphs_get(orc_run* r, int which, int species, double* out, int64_t n) {
     return 0;
 }
 
+/* ------------------------------------------------------------- plots */
+/* CPU restatement of the headless viewer plots of pgb_render, written
+ * separately from the CUDA code: the same selection, mapping and colour
+ * rules (graphics.cpp:245-607), in the same FP32/FP64 operations, with
+ * -ffp-contract=off.  Particles are converted to FP32 cell units as the
+ * library's load does.                                                    */
+static unsigned char plot_byte(float c) {
+    float v = c * 255.0f + 0.5f;
+    if (v < 0.0f) v = 0.0f;
+    if (v > 255.0f) v = 255.0f;
+    return (unsigned char)(int)v;
+}
+static uint32_t plot_hash(uint32_t id, uint32_t seed) {   /* lowbias32 */
+    uint32_t x = id ^ (seed * 0x9E3779B9u);
+    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+    return x;
+}
+static int plot_keep(uint32_t id, uint32_t seed, int64_t nlive, int max_points) {
+    if (max_points <= 0 || nlive <= max_points) return 1;
+    uint64_t thresh = (uint64_t)((double)max_points / (double)nlive * 4294967296.0);
+    return (uint64_t)plot_hash(id, seed) < thresh;
+}
+static void plot_point(unsigned char* img, int W, int H, int px, int py, const unsigned char* c) {
+    for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+            int x = px + dx, y = py - dy;
+            if (x < 0 || x >= W || y < 0 || y >= H) continue;
+            memcpy(img + 3 * ((size_t)y * W + x), c, 3);
+        }
+}
+static void plot_species(orc_run* r, int s, int phase, int W, int H, int max_points, uint32_t seed,
+                         const unsigned char* colour, unsigned char* img) {
+    const orc_sp* S = &r->sp[s];
+    const float lx = (float)(r->nx - 1), ly = (float)(r->ny - 1);
+    int mvx = 1, mvy = 1;
+    if (phase) {
+        float mx = 0.0f, my = 0.0f;
+        for (int64_t i = 0; i < S->n; ++i) {
+            float xs = (float)(S->p[i].x / r->dx), ys = (float)(S->p[i].y / r->dy);
+            if (!(xs > 0.0f && xs < lx && ys > 0.0f && ys < ly) || !plot_keep(S->id[i], seed, S->n, max_points)) continue;
+            float ax = fabsf((float)S->p[i].vx), ay = fabsf((float)S->p[i].vy);
+            if (ax == ax && ax > mx) mx = ax;
+            if (ay == ay && ay > my) my = ay;
+        }
+        mvx = mx < 2147483520.0f ? (int)mx : 2147483647;
+        mvy = my < 2147483520.0f ? (int)my : 2147483647;
+        if (mvx < 1) mvx = 1;
+        if (mvy < 1) mvy = 1;
+    }
+    for (int64_t i = 0; i < S->n; ++i) {
+        float xs = (float)(S->p[i].x / r->dx), ys = (float)(S->p[i].y / r->dy);
+        if (!(xs > 0.0f && xs < lx && ys > 0.0f && ys < ly) || !plot_keep(S->id[i], seed, S->n, max_points)) continue;
+        float fx, fy;
+        if (phase) {
+            float vx = (float)S->p[i].vx, vy = (float)S->p[i].vy;
+            if (!(fabsf(vx) < (float)mvx && fabsf(vy) < (float)mvy)) continue;
+            fx = (vx / (float)mvx + 1.0f) * 0.5f;
+            fy = (vy / (float)mvy + 1.0f) * 0.5f;
+        } else {
+            fx = xs / lx;
+            fy = ys / ly;
+        }
+        int px = (int)(fx * (float)W), py = H - 1 - (int)(fy * (float)H);
+        px = px < 0 ? 0 : (px > W - 1 ? W - 1 : px);
+        py = py < 0 ? 0 : (py > H - 1 ? H - 1 : py);
+        plot_point(img, W, H, px, py, colour);
+    }
+}
+/* drawField's ramp (graphics.cpp:303-356) */
+static void plot_ramp(float zAv, float c[3]) {
+    static const float red[3] = {1.0f, 0.0f, 0.0f}, orange[3] = {1.0f, 0.396f, 0.0f},
+                       yellow[3] = {1.0f, 1.0f, 0.0f}, green[3] = {0.0f, 1.0f, 0.0f},
+                       blue[3] = {0.0f, 0.0f, 1.0f}, purple[3] = {0.396f, 0.0f, 1.0f};
+    const float rd = 0.2f;
+    float alpha = zAv < 1.0f ? zAv : 1.0f;
+    const float *c1, *c2;
+    if (zAv < rd) { alpha /= rd; c1 = red; c2 = orange; }
+    else if ((double)zAv < 2.0 * (double)rd) { alpha = (alpha - rd) / rd; c1 = orange; c2 = yellow; }
+    else if ((double)zAv < 3.0 * (double)rd) { alpha = (float)(((double)alpha - 2.0 * (double)rd) / (double)rd); c1 = yellow; c2 = green; }
+    else if ((double)zAv < 4.0 * (double)rd) { alpha = (float)(((double)alpha - 3.0 * (double)rd) / (double)rd); c1 = green; c2 = blue; }
+    else { alpha = (float)(((double)alpha - 4.0 * (double)rd) / (double)rd); c1 = blue; c2 = purple; }
+    for (int k = 0; k < 3; ++k) c[k] = c1[k] * (1.0f - alpha) + c2[k] * alpha;
+}
+
+int orc_render(orc_run* r, int plot, int W, int H, int max_points, uint32_t seed, unsigned char* img, int64_t cap) {
+    if (W < 1 || H < 1 || cap < 3LL * W * H || plot < 0 || plot > PGB_PLOT_ION_DENSITY) return PGB_ERR_ARG;
+    static const unsigned char lime[3] = {142, 255, 29}, pink[3] = {255, 29, 142};
+    memset(img, 0, (size_t)3 * W * H);
+    if (plot == PGB_PLOT_PARTICLE_XY) {
+        plot_species(r, 0, 0, W, H, max_points, seed, lime, img);
+        plot_species(r, 1, 0, W, H, max_points, seed, pink, img);
+        return 0;
+    }
+    if (plot == PGB_PLOT_ELECTRON_VX_VY || plot == PGB_PLOT_ION_VX_VY) {
+        int s = plot == PGB_PLOT_ELECTRON_VX_VY ? 0 : 1;
+        plot_species(r, s, 1, W, H, max_points, seed, s == 0 ? lime : pink, img);
+        return 0;
+    }
+    const int n = r->nx, G = r->nx * r->ny;
+    const double* src;
+    double div = 1.0;
+    int gs = 0;
+    switch (plot) {
+        case PGB_PLOT_PHI: src = r->gr_on ? r->gr_f[1] : r->phi; break;
+        case PGB_PLOT_EFIELD_X: src = r->gr_on ? r->gr_f[2] : r->ex; break;
+        case PGB_PLOT_EFIELD_Y: src = r->gr_on ? r->gr_f[3] : r->ey; break;
+        default: {
+            int s = plot == PGB_PLOT_E_DENSITY ? 0 : 1;
+            gs = 1;
+            src = r->gr_on ? r->gr_q[s] : r->q[s];
+            if (!r->gr_on) div = s == 0 ? -C_CHARGE : C_CHARGE;
+        }
+    }
+    if (r->gr_on) div = (double)r->gr.no_graph_steps;
+    int have = 0;
+    double mx = 0.0;
+    for (int k = 0; k < G; ++k) {
+        double v = src[k] / div;
+        if (v == v && (!have || v > mx)) { mx = v; have = 1; }
+    }
+    double fmax = fabs(mx);
+    if (!have || !(fmax >= 1.0)) fmax = 1.0;
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            unsigned char* q = img + 3 * ((size_t)py * W + px);
+            float u = ((float)px + 0.5f) * (float)(n - 1) / (float)W;
+            float v = ((float)(H - 1 - py) + 0.5f) * (float)(n - 1) / (float)H;
+            int i = (int)u, j = (int)v;
+            float fu = u - (float)i, fv = v - (float)j;
+            if (i < gs || i >= n - gs - 1 || j < gs || j >= n - gs - 1 || fu < 0.1f || fu > 0.9f || fv < 0.1f ||
+                fv > 0.9f)
+                continue;
+            float z0 = (float)(src[(size_t)(j + 1) * n + i] / div / fmax);
+            float z1 = (float)(src[(size_t)(j + 1) * n + i + 1] / div / fmax);
+            float z2 = (float)(src[(size_t)j * n + i + 1] / div / fmax);
+            float z3 = (float)(src[(size_t)j * n + i] / div / fmax);
+            float zAv = (float)fabs((double)(z0 + z1 + z2 + z3) / 4.0);
+            float c[3];
+            plot_ramp(zAv, c);
+            q[0] = plot_byte(c[0]); q[1] = plot_byte(c[1]); q[2] = plot_byte(c[2]);
+        }
+    return 0;
+}
+
 /* pic::pic_run loop body (pic.cpp:1069-1250) and the graphs sums of the
  * window (pic.cpp:1189-1207); printing left out                          */
 void orc_step(orc_run* r, int nsteps) {

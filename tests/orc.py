@@ -64,6 +64,7 @@ def load():
         "orc_poisson_converged": (None, [R, i64, C.c_int]),
         "orc_graphs_enable": (C.c_int, [R, C.POINTER(picgb.PgbGraphsParams)]),
         "orc_graphs_get": (C.c_int, [R, C.c_int, C.c_int, dp, i64]),
+        "orc_render": (C.c_int, [R, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32, C.POINTER(C.c_uint8), i64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -187,6 +188,12 @@ class Oracle:
         out = np.empty(picgb.graph_size(which, p, self._gp))
         assert self.lib.orc_graphs_get(self.h, picgb.GRAPH[which], species, _dp(out), out.size) == 0
         return out.reshape(p.y_no_of_cells, p.x_no_of_cells) if picgb.GRAPH[which] <= 4 else out
+
+    def render(self, plot, width=512, height=512, max_points=picgb.NUM_PARTICLES_TO_PLOT, seed=0):
+        img = np.empty((height, width, 3), dtype=np.uint8)
+        assert self.lib.orc_render(self.h, picgb.PLOT[plot], width, height, max_points, seed,
+                                   img.ctypes.data_as(C.POINTER(C.c_uint8)), img.size) == 0
+        return img
 
     def neutral_table(self, which):
         n = self.params.init_no_neutrals

@@ -624,3 +624,79 @@ def test_graphs_match_oracle_and_write_reference_files(tmp_path):
                 written = np.loadtxt(tmp_path / f"{stem}.txt", ndmin=2)
                 assert written.shape == g[key].shape, stem
                 np.testing.assert_allclose(written, mine[stem], rtol=1e-6, atol=1e-300, err_msg=stem)
+
+
+# ------------------------------------------------------- viewer plots
+@pytest.mark.parametrize("size", [(256, 256), (300, 200)])
+def test_particle_plots_equal_oracle(size):
+    """pgb_render's particle plots (X-Y, electron and ion vx-vy) of the same
+    particles equal the oracle's restatement of the same rules pixel for
+    pixel, for all particles and for a hashed sample of 500 per species."""
+    g = load_golden("core65")
+    w, h = size
+    o = orc.Oracle(g["p"], rng=orc.ORC_RNG_PHILOX, order=orc.ORC_ORDER_STABLE)
+    with picgb.Run(g["p"]) as r:
+        for x in (o, r):
+            x.load_particles(0, g["e_in"])
+            x.load_particles(1, g["i_in"])
+        for plot in ("particle_xy", "electron_vx_vy", "ion_vx_vy"):
+            for max_points, seed in ((0, 0), (500, 7)):
+                a = r.render(plot, w, h, max_points, seed)
+                b = o.render(plot, w, h, max_points, seed)
+                assert np.array_equal(a, b), (plot, max_points, np.count_nonzero(np.any(a != b, axis=2)))
+                assert np.any(a != 0), plot
+
+
+def test_field_plots_equal_oracle():
+    """Field plots of bit-identical fields (the FP64 Poisson solve of a fixed
+    rho) are bit-identical images; the density plots, from the FP32 deposit,
+    differ from the FP64 oracle in at most a few colour levels of a few
+    pixels."""
+    g = load_golden("fields65")
+    p = g["p"]
+    rho = g["rho"].reshape(p.y_no_of_cells, -1)
+    o = orc.Oracle(p)
+    with picgb.Run(p) as r:
+        for x in (o, r):
+            x.set_rho(rho)
+            x.poisson(0)
+            x.efield()
+        for plot in ("phi", "efield_x", "efield_y"):
+            a, b = r.render(plot, 320, 320), o.render(plot, 320, 320)
+            assert np.array_equal(a, b), (plot, np.count_nonzero(np.any(a != b, axis=2)))
+    c = load_golden("core65")
+    o = orc.Oracle(c["p"], rng=orc.ORC_RNG_PHILOX, order=orc.ORC_ORDER_STABLE)
+    with picgb.Run(c["p"]) as r:
+        for x in (o, r):
+            x.load_particles(0, c["e_in"])
+            x.load_particles(1, c["i_in"])
+            x.deposit(0)
+            x.deposit(1)
+        for plot in ("e_density", "ion_density"):
+            a, b = r.render(plot, 320, 320).astype(int), o.render(plot, 320, 320).astype(int)
+            assert np.max(np.abs(a - b)) <= 2, plot
+            assert np.count_nonzero(np.any(a != b, axis=2)) <= 0.005 * a.shape[0] * a.shape[1], plot
+
+
+def test_averaged_field_plots_follow_the_graphs():
+    """With graphs enabled the field plots show the averaged graphs, as the
+    viewer does; after a stepped window they match the oracle's plots of its
+    averages to a colour level or two on all but a few pixels."""
+    g = load_golden("graphs33")
+    p = g["p"]
+    start, end = (int(v) for v in g["graph_window"])
+    gp = picgb.graphs_params(p, start, end)
+    o = orc.Oracle(p, rng=orc.ORC_RNG_PHILOX, order=orc.ORC_ORDER_STABLE)
+    o.graphs_enable(gp)
+    with picgb.Run(p) as r:
+        r.graphs_enable(gp)
+        for x in (o, r):
+            x.load_particles(0, g["e_in"])
+            x.load_particles(1, g["i_in"])
+            x.initial_boundary()
+            x.step(int(g["nsteps"]))
+        for plot in ("phi", "efield_x", "efield_y", "e_density", "ion_density"):
+            a, b = r.render(plot, 256, 256).astype(int), o.render(plot, 256, 256).astype(int)
+            differ = np.count_nonzero(np.any(a != b, axis=2))
+            assert differ <= 0.05 * 256 * 256, (plot, differ)
+            assert np.max(np.abs(a - b)) <= 3 or differ <= 0.01 * 256 * 256, (plot, np.max(np.abs(a - b)))

@@ -32,6 +32,7 @@ UNITS = {
     "pgb_sort.cu": [],
     "pgb_reduce.cu": [],
     "pgb_graphs.cu": [],
+    "pgb_render.cu": ["--fmad=false"],
     "pgb_static.cu": [],
 }
 

@@ -394,6 +394,8 @@ extern "C" int pgb_destroy(pgb_run* r) {
     cudaFree(r->d_stage);
     cudaFree(r->kh);
     cudaFree(r->gr.buf);
+    cudaFree(r->rd_img);
+    cudaFree(r->rd_scratch);
     if (r->prof_ev_ok)
         for (int k = 0; k < 12; ++k) cudaEventDestroy(r->prof_ev[k]);
     if (r->copy_ev_ok)

@@ -166,6 +166,10 @@ struct pgb_run {
         unsigned long long* d[2][4] = {}; /* histogram counts X1, Y1, X2, Y2         */
         void* buf = nullptr;
     } gr;
+    /* headless viewer plots: the image and a 16-byte scratch (pgb_render) */
+    void* rd_img = nullptr;
+    long long rd_cap = 0;
+    void* rd_scratch = nullptr;
     /* host staging */
     double* h_stage = nullptr;
     size_t h_stage_bytes = 0;

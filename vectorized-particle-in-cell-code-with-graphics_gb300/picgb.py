@@ -131,6 +131,20 @@ def graphs_params(p, start: int, end: int, no_graph_steps: int = None, **kw) -> 
     return g
 
 
+# PGB_PLOT_*: the viewer's plot selector (graphics.cpp:68-77)
+PLOT = {"particle_xy": 0, "electron_vx_vy": 1, "ion_vx_vy": 2, "phi": 3, "efield_x": 4, "efield_y": 5,
+        "e_density": 6, "ion_density": 7}
+NUM_PARTICLES_TO_PLOT = 5000   # graphics.h:77
+
+
+def write_ppm(path: str, img: np.ndarray):
+    """an (H, W, 3) uint8 image as binary PPM"""
+    h, w, _ = img.shape
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(img, dtype=np.uint8).tobytes())
+
+
 def graph_size(which: str, p, gp: PgbGraphsParams) -> int:
     """number of values pgb_graphs_get returns for `which`"""
     w = GRAPH[which]
@@ -303,6 +317,7 @@ def load_library():
         "pgb_graphs_enable": (C.c_int, [R, C.POINTER(PgbGraphsParams)]),
         "pgb_graphs_get": (C.c_int, [R, C.c_int, C.c_int, dp, i64]),
         "pgb_graphs_write": (C.c_int, [R, C.c_char_p]),
+        "pgb_render": (C.c_int, [R, C.c_int, i32, i32, i32, C.c_uint32, C.POINTER(C.c_uint8), i64]),
         "pgb_query": (C.c_int, [R, C.POINTER(i32)]),
         "pgb_footprint": (C.c_int, [C.POINTER(PgbParams), i64, i64, C.POINTER(i64)]),
         "pgb_server_create": (C.c_int, [i64, i32, i32, C.POINTER(R)]),
@@ -493,6 +508,15 @@ class Run:
     def graphs_write(self, directory: str):
         """the reference's graph text files, written into directory"""
         self._check(self.lib.pgb_graphs_write(self.h, os.fsencode(directory)), "pgb_graphs_write")
+
+    def render(self, plot: str, width: int = 512, height: int = 512, max_points: int = NUM_PARTICLES_TO_PLOT,
+               seed: int = 0) -> np.ndarray:
+        """one of the viewer's plots as an (height, width, 3) uint8 image,
+        row 0 at the top (pgb_render)"""
+        img = np.empty((height, width, 3), dtype=np.uint8)
+        self._check(self.lib.pgb_render(self.h, PLOT[plot], width, height, max_points, seed,
+                                        img.ctypes.data_as(C.POINTER(C.c_uint8)), img.size), "pgb_render")
+        return img
 
     def load_particles_ptr(self, species: int, ptr: int, n: int):
         """Load n records from a host address (e.g. pinned memory)."""
