@@ -115,3 +115,24 @@ def test_server_rejects_a_run_larger_than_its_budget(lib):
         with pytest.raises(picgb.PicError, match="budget"):
             srv.submit(p, e, e, 10)
         assert srv.stats()["submitted"] == 0
+
+
+def test_binary_datadump_round_trips_exactly(tmp_path):
+    """The binary restart format keeps every double, NaN and infinities
+    included, and rejects files that are not dumps or are cut short."""
+    import picgb
+    rng = np.random.default_rng(1)
+    a = rng.standard_normal((1000, 6)) * 1e-3
+    a[3, 2], a[5, 0], a[7, 4] = np.nan, np.inf, -0.0
+    path = tmp_path / "dataDump_e.bin"
+    picgb.write_datadump_bin(str(path), a)
+    b = picgb.read_datadump_bin(str(path))
+    assert b.shape == a.shape and np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    assert path.stat().st_size == 16 + 48 * 1000
+    picgb.write_datadump_bin(str(path), np.empty((0, 6)))
+    assert picgb.read_datadump_bin(str(path)).shape == (0, 6)
+    (tmp_path / "bad.bin").write_bytes(b"NOTADUMP" + bytes(8))
+    (tmp_path / "cut.bin").write_bytes(path.read_bytes()[:8] + np.array([5], "<i8").tobytes() + bytes(40))
+    for bad in ("bad.bin", "cut.bin"):
+        with pytest.raises(picgb.PicError):
+            picgb.read_datadump_bin(str(tmp_path / bad))

@@ -449,6 +449,49 @@ def test_batch_driver_runs_and_writes_reference_files(tmp_path):
     assert total > 0
 
 
+def test_batch_driver_binary_restart_is_lossless(tmp_path):
+    """picgb_run --binary-dump writes dataDump_*.bin beside the text dumps,
+    holding the same records to full precision; restarting from them and
+    dumping again (no steps) reproduces the files byte for byte."""
+    import os
+    import shutil
+    import subprocess
+    from test_host_driver import PARAMS_TEXT
+    g = load_golden("core65")
+    text = PARAMS_TEXT.replace("#define X_NO_OF_CELLS 129", "#define X_NO_OF_CELLS 65") \
+                      .replace("#define Y_NO_OF_CELLS 129", "#define Y_NO_OF_CELLS 65")
+    exe = os.path.join(os.path.dirname(picgb.library_path()), "picgb_run")
+    a, b = tmp_path / "a", tmp_path / "b"
+    a.mkdir()
+    b.mkdir()
+    (a / "parameters.h").write_text(text)
+    picgb.write_datadump(str(a / "dataDump_e.txt"), g["e_in"])
+    picgb.write_datadump(str(a / "dataDump_i1.txt"), g["i_in"])
+    out = subprocess.run([exe, str(a / "parameters.h"), str(a), "--steps", "30", "--restart", "--binary-dump",
+                          "--no-graphs"], capture_output=True, text=True, timeout=300)
+    assert out.returncode != 0 and "dataDump_e.bin" in out.stderr   # restarts need the binary files
+    out = subprocess.run([exe, str(a / "parameters.h"), str(a), "--steps", "30", "--restart", "--no-graphs"],
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    out = subprocess.run([exe, str(a / "parameters.h"), str(a), "--steps", "30", "--fresh", "--binary-dump",
+                          "--no-graphs"], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    for t in ("e", "i1"):
+        full = picgb.read_datadump_bin(str(a / f"dataDump_{t}.bin"))
+        txt = picgb.read_datadump(str(a / f"dataDump_{t}.txt"))
+        assert full.shape == txt.shape and full.shape[0] > 0
+        assert np.allclose(full, txt, rtol=1e-5, atol=0, equal_nan=True)
+        shutil.copy(a / f"dataDump_{t}.bin", b / f"dataDump_{t}.bin")
+    shutil.copy(a / "parameters.h", b / "parameters.h")
+    for t in ("e", "i1"):
+        shutil.copy(b / f"dataDump_{t}.bin", b / f"start_{t}.bin")
+    out = subprocess.run([exe, str(b / "parameters.h"), str(b), "--steps", "0", "--restart", "--binary-dump",
+                          "--no-graphs"], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    for t in ("e", "i1"):
+        assert (b / f"dataDump_{t}.bin").read_bytes() == (b / f"start_{t}.bin").read_bytes(), t
+
+
 @pytest.mark.parametrize("nsteps", [10, 11, 12])
 def test_batched_runs_equal_runs_alone(nsteps):
     """pgb_step_batch steps independent runs of different sizes and physics

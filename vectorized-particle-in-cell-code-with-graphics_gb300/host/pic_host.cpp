@@ -375,12 +375,47 @@ void write_datadump(const std::string& path, const std::vector<double>& a) {
     std::fclose(f);
 }
 
+/* ------------------------------------------------------- binary files */
+/* Lossless restart records, an addition to the reference's text format:
+ * "PGBDUMP1", an int64 record count, then the records as little-endian
+ * doubles {x, y, vx, vy, vz, weight}.  The text format keeps 6 digits;
+ * this one keeps the state exactly, so a restart continues the same run. */
+static const char kDumpMagic[8] = {'P', 'G', 'B', 'D', 'U', 'M', 'P', '1'};
+
+std::vector<double> read_datadump_bin(const std::string& path) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) throw Error("cannot open " + path, PGB_ERR_IO);
+    char magic[8];
+    int64_t n = -1;
+    if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kDumpMagic, 8) != 0 ||
+        std::fread(&n, sizeof n, 1, f) != 1 || n < 0 || n > ((int64_t)1 << 40)) {
+        std::fclose(f);
+        throw Error(path + ": not a binary particle dump", PGB_ERR_IO);
+    }
+    std::vector<double> out((size_t)n * 6);
+    const size_t got = n ? std::fread(out.data(), sizeof(double), out.size(), f) : 0;
+    std::fclose(f);
+    if (got != out.size()) throw Error(path + ": truncated binary particle dump", PGB_ERR_IO);
+    return out;
+}
+
+void write_datadump_bin(const std::string& path, const std::vector<double>& a) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) throw Error("cannot write " + path, PGB_ERR_IO);
+    const int64_t n = (int64_t)(a.size() / 6);
+    bool ok = std::fwrite(kDumpMagic, 1, 8, f) == 8 && std::fwrite(&n, sizeof n, 1, f) == 1 &&
+              (n == 0 || std::fwrite(a.data(), sizeof(double), (size_t)n * 6, f) == (size_t)n * 6);
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) throw Error("cannot write " + path, PGB_ERR_IO);
+}
+
 /* --------------------------------------------------------------- Pic */
 void Pic::check(int rc, const char* what) {
     if (rc != 0) throw Error(std::string(what) + ": " + pgb_last_error(run_), rc);
 }
 
-Pic::Pic(const MacroTable& m, const std::string& dir, bool restart, uint64_t seed) : dir_(dir) {
+Pic::Pic(const MacroTable& m, const std::string& dir, bool restart, uint64_t seed, bool binary_dump)
+    : dir_(dir), binary_dump_(binary_dump) {
     p_ = params_from_macros(m, seed);
     int rc = pgb_create(&p_, &run_);
     if (rc != 0) throw Error(std::string("pgb_create: ") + pgb_last_error(nullptr), rc);
@@ -414,7 +449,8 @@ Pic::Pic(const MacroTable& m, const std::string& dir, bool restart, uint64_t see
     for (int s = 0; s < 2; ++s) {
         std::vector<double> a;
         if (restart) {
-            a = read_datadump(dir_ + "/dataDump_" + types[s] + ".txt");
+            a = binary_dump_ ? read_datadump_bin(dir_ + "/dataDump_" + types[s] + ".bin")
+                             : read_datadump(dir_ + "/dataDump_" + types[s] + ".txt");
         } else {
             /* create_particles + initiate_positions + initiate_velocities
              * (particle.cpp:321-482): a lattice of spacing DXP, repeated
@@ -523,6 +559,7 @@ void Pic::dump_data() {
         check(pgb_dump_species(run_, s, a.data(), n, &got), "pgb_dump_species");
         a.resize((size_t)std::min<int64_t>(got, n) * 6);
         write_datadump(dir_ + "/dataDump_" + types[s] + ".txt", a);
+        if (binary_dump_) write_datadump_bin(dir_ + "/dataDump_" + types[s] + ".bin", a);
     }
 }
 

@@ -45,6 +45,10 @@ pgb_params params_from_macros(const MacroTable& m, uint64_t seed);
  * (particle.cpp:359-401, 1361-1382)                                      */
 std::vector<double> read_datadump(const std::string& path);
 void write_datadump(const std::string& path, const std::vector<double>& aos6);
+/* lossless binary form of the same records (no reference counterpart):
+ * "PGBDUMP1", int64 count, little-endian doubles                       */
+std::vector<double> read_datadump_bin(const std::string& path);
+void write_datadump_bin(const std::string& path, const std::vector<double>& aos6);
 
 class Error : public std::runtime_error {
 public:
@@ -58,8 +62,10 @@ public:
     /* restart = true loads dataDump_e.txt and dataDump_i1.txt from dir
      * (pic.cpp:110-119); otherwise INIT_PARTICLE_NO particles per species
      * are placed on the lattice of particle::initiate_positions
-     * (particle.cpp:410-443) with Maxwellian velocities.                  */
-    Pic(const MacroTable& macros, const std::string& dir, bool restart, uint64_t seed);
+     * (particle.cpp:410-443) with Maxwellian velocities.  binary_dump
+     * restarts from dataDump_*.bin and makes dump_data() write them beside
+     * the text files.                                                     */
+    Pic(const MacroTable& macros, const std::string& dir, bool restart, uint64_t seed, bool binary_dump = false);
     ~Pic();
     Pic(const Pic&) = delete;
     Pic& operator=(const Pic&) = delete;
@@ -71,7 +77,7 @@ public:
     /* pic::setWriteGraphDataToFiles (pic.cpp:980-983): the averaged graph
      * files are written when step END_GRAPH_TIME-1 completes            */
     void set_write_graph_data_to_files(bool on) { write_graphs_ = on; }
-    void dump_data();                       /* dataDump_e.txt, dataDump_i1.txt */
+    void dump_data();                       /* dataDump_e.txt, dataDump_i1.txt (+ .bin) */
     void write_time_data();                 /* timeData.txt (pic.cpp:1261-1274) */
     pgb_counters counters();
     pgb_run* handle() { return run_; }
@@ -88,6 +94,7 @@ private:
     bool first_run_ = true;
     pgb_graphs_params graphs_{};
     bool write_graphs_ = true;
+    bool binary_dump_ = false;
 };
 
 }  // namespace picgb

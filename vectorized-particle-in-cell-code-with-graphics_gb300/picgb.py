@@ -638,6 +638,31 @@ def write_datadump(path: str, aos6: np.ndarray):
             f.write(" ".join(_ostream_double(v) for v in row) + "\n")
 
 
+DUMP_MAGIC = b"PGBDUMP1"
+
+
+def read_datadump_bin(path: str) -> np.ndarray:
+    """The lossless binary dump (no reference counterpart): "PGBDUMP1", an
+    int64 record count, then little-endian doubles {x, y, vx, vy, vz, w}."""
+    with open(path, "rb") as f:
+        head = f.read(16)
+        if len(head) != 16 or head[:8] != DUMP_MAGIC:
+            raise PicError(f"{path}: not a binary particle dump")
+        n = int(np.frombuffer(head[8:], dtype="<i8")[0])
+        a = np.fromfile(f, dtype="<f8", count=6 * n)
+    if a.size != 6 * n:
+        raise PicError(f"{path}: truncated binary particle dump")
+    return a.reshape(n, 6).astype(np.float64)
+
+
+def write_datadump_bin(path: str, aos6: np.ndarray):
+    a = np.ascontiguousarray(aos6, dtype="<f8").reshape(-1, 6)
+    with open(path, "wb") as f:
+        f.write(DUMP_MAGIC)
+        f.write(np.array([a.shape[0]], dtype="<i8").tobytes())
+        f.write(a.tobytes())
+
+
 def _ostream_double(v: float) -> str:
     if v != v:
         return "nan" if math.copysign(1.0, v) > 0 else "-nan"
