@@ -57,6 +57,7 @@ __device__ __forceinline__ double rhs_node(double rho, int i, int j, const Final
 }
 
 __global__ void k_finalize(FinalizeArgs a) {
+    pgb_pdl_entry();
     const int G = a.nx * a.ny;
     const double phirx = a.phi_tab[a.ds->t - a.ds->t_base];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x) {
@@ -74,6 +75,7 @@ __global__ void k_finalize(FinalizeArgs a) {
 }
 
 __global__ void k_rhs(FinalizeArgs a) {
+    pgb_pdl_entry();
     const int G = a.nx * a.ny;
     const double phirx = a.phi_tab[a.ds->t - a.ds->t_base];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x) {
@@ -148,6 +150,7 @@ __device__ __forceinline__ T prolong_point(const T* uc, int nc, int i, int j) {
 template <class T, int MODE>
 __global__ void __launch_bounds__(RT * RTX) k_relax_tile(const T* __restrict__ uin, T* __restrict__ uout, const T* f, int n,
                                                           T h2, const T* vc) {
+    pgb_pdl_entry();
     __shared__ T su[RT + 4][RTX + 4];
     __shared__ T sf[RT + 2][RTX + 2];
     const int nc = n / 2 + 1;
@@ -206,6 +209,7 @@ __global__ void __launch_bounds__(RT * RTX) k_relax_tile(const T* __restrict__ u
  * also zeroes the coarse correction vc that the next level starts from    */
 template <class T>
 __global__ void k_resid_restrict(T* rc, T* vc, const T* u, const T* f, int nf, T h2i) {
+    pgb_pdl_entry();
     const int nc = (nf + 1) / 2;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc * nc; k += gridDim.x * blockDim.x) {
         int ic = k / nc, jc = k - ic * nc;
@@ -217,6 +221,7 @@ __global__ void k_resid_restrict(T* rc, T* vc, const T* u, const T* f, int nf, T
 }
 template <class T>
 __global__ void k_restrict(T* uc, const T* uf, int nc) {
+    pgb_pdl_entry();
     const int nf = 2 * nc - 1;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc * nc; k += gridDim.x * blockDim.x) {
         int ic = k / nc, jc = k - ic * nc;
@@ -228,6 +233,7 @@ __global__ void k_restrict(T* uc, const T* uf, int nc) {
 }
 template <class T>
 __global__ void k_prolong(T* uf, const T* uc, int nf, int add) {
+    pgb_pdl_entry();
     const int nc = nf / 2 + 1;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nf * nf; k += gridDim.x * blockDim.x) {
         int i = k / nf, j = k - i * nf;
@@ -242,12 +248,19 @@ __global__ void k_prolong(T* uf, const T* uc, int nf, int add) {
  * restricted residual of the levels below.                              */
 template <class T>
 struct SmallMG {
-    T* U[8];
-    T* F[8];
-    T* V[8];
-    T* R[8];
-    int n[8];
+    T* base;
     T length;
+    __device__ __forceinline__ int n(int l) const { return (1 << (l + 1)) + 1; }
+    /* the levels below l hold sum_{m<l} (2^(m+1)+1)^2 = 4(4^l-1)/3 + 4(2^l-1) + l
+     * nodes per array, four arrays each: addresses are register arithmetic
+     * (a pointer table indexed by level would live in local memory)      */
+    __device__ __forceinline__ T* U(int l) const {
+        const int below = (4 * ((1 << (2 * l)) - 1)) / 3 + 4 * ((1 << l) - 1) + l;
+        return base + 4 * below;
+    }
+    __device__ __forceinline__ T* F(int l) const { return U(l) + n(l) * n(l); }
+    __device__ __forceinline__ T* V(int l) const { return U(l) + 2 * n(l) * n(l); }
+    __device__ __forceinline__ T* R(int l) const { return U(l) + 3 * n(l) * n(l); }
 };
 
 /* Loops of the one-CTA solver run over flat point indices so that every
@@ -282,12 +295,12 @@ __device__ void sm_coarsest(T* u, const T* f, T length) {
 }
 /* V-cycle at level j on (u, f) using V/R of the levels below */
 template <class T>
-__device__ void sm_vcycle(SmallMG<T>& s, int j, T* u, const T* f) {
+__device__ __forceinline__ void sm_vcycle(const SmallMG<T> s, int j, T* u, const T* f) {
     if (j == 0) { sm_coarsest(u, f, s.length); return; }
     for (int l = j; l >= 1; --l) {
-        T* ul = (l == j) ? u : s.V[l];
-        const T* fl = (l == j) ? f : s.R[l];
-        int nf = s.n[l], nc = s.n[l - 1];
+        T* ul = (l == j) ? u : s.V(l);
+        const T* fl = (l == j) ? f : s.R(l);
+        int nf = s.n(l), nc = s.n(l - 1);
         T h = s.length / (T)(nf - 1), h2i = (T)1.0 / (h * h);
         sm_relax(ul, fl, nf, s.length);
         const float inv = 1.0f / (float)nc;
@@ -295,20 +308,20 @@ __device__ void sm_vcycle(SmallMG<T>& s, int j, T* u, const T* f) {
             int ic = sm_row(k, inv), jc = k - ic * nc;
             T v = (T)0;
             if (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) v = restrict_resid_point(ul, fl, nf, ic, jc, h2i);
-            s.R[l - 1][k] = v;
-            s.V[l - 1][k] = (T)0;
+            s.R(l - 1)[k] = v;
+            s.V(l - 1)[k] = (T)0;
         }
         __syncthreads();
     }
-    sm_coarsest(s.V[0], s.R[0], s.length);
+    sm_coarsest(s.V(0), s.R(0), s.length);
     for (int l = 1; l <= j; ++l) {
-        T* ul = (l == j) ? u : s.V[l];
-        const T* fl = (l == j) ? f : s.R[l];
-        int nf = s.n[l], nc = s.n[l - 1];
+        T* ul = (l == j) ? u : s.V(l);
+        const T* fl = (l == j) ? f : s.R(l);
+        int nf = s.n(l), nc = s.n(l - 1);
         const float inv = 1.0f / (float)nf;
         for (int k = threadIdx.x; k < nf * nf; k += blockDim.x) {
             int i = sm_row(k, inv), jj = k - i * nf;
-            ul[k] = ul[k] + prolong_point(s.V[l - 1], nc, i, jj);
+            ul[k] = ul[k] + prolong_point(s.V(l - 1), nc, i, jj);
         }
         __syncthreads();
         sm_relax(ul, fl, nf, s.length);
@@ -320,53 +333,56 @@ __device__ void sm_vcycle(SmallMG<T>& s, int j, T* u, const T* f) {
  * mode 1: one V-cycle at level J on (g_v[J], g_r[J]) in place.          */
 template <class T>
 __global__ void __launch_bounds__(1024, 1) k_mg_small(int J, int mode, T length, T** g_u, T** g_f, T** g_v, T** g_r) {
+    pgb_pdl_entry();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmallMG<T> s;
+    s.base = reinterpret_cast<T*>(smem_raw);
     s.length = length;
-    T* p = reinterpret_cast<T*>(smem_raw);
-    for (int l = 0; l <= J; ++l) {
-        int n = (1 << (l + 1)) + 1;
-        s.n[l] = n;
-        s.U[l] = p; p += n * n;
-        s.F[l] = p; p += n * n;
-        s.V[l] = p; p += n * n;
-        s.R[l] = p; p += n * n;
-    }
     if (mode == 0) {
-        for (int k = threadIdx.x; k < s.n[J] * s.n[J]; k += blockDim.x) s.F[J][k] = g_f[J][k];
+        const T* gf = g_f[J];
+        T* const fJ = s.F(J);
+        for (int k = threadIdx.x; k < s.n(J) * s.n(J); k += blockDim.x) fJ[k] = gf[k];
         __syncthreads();
         /* right-hand sides of the coarser levels, as k_restrict computes them */
         for (int l = J - 1; l >= 0; --l) {
-            const int nc = s.n[l], nf = s.n[l + 1];
+            const int nc = s.n(l), nf = s.n(l + 1);
             const float inv = 1.0f / (float)nc;
             for (int k = threadIdx.x; k < nc * nc; k += blockDim.x) {
                 int ic = sm_row(k, inv), jc = k - ic * nc;
-                s.F[l][k] = (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) ? restrict_point(s.F[l + 1], nf, ic, jc)
-                                                                             : s.F[l + 1][(2 * ic) * nf + 2 * jc];
+                s.F(l)[k] = (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) ? restrict_point(s.F(l + 1), nf, ic, jc)
+                                                                             : s.F(l + 1)[(2 * ic) * nf + 2 * jc];
             }
             __syncthreads();
         }
-        sm_coarsest(s.U[0], s.F[0], length);
+        sm_coarsest(s.U(0), s.F(0), length);
         for (int l = 1; l <= J; ++l) {
-            int nf = s.n[l], nc = s.n[l - 1];
+            int nf = s.n(l), nc = s.n(l - 1);
             const float inv = 1.0f / (float)nf;
+            T* const uf = s.U(l);
+            const T* uc = s.U(l - 1);
             for (int k = threadIdx.x; k < nf * nf; k += blockDim.x) {
                 int i = sm_row(k, inv), jj = k - i * nf;
-                s.U[l][k] = prolong_point(s.U[l - 1], nc, i, jj);
+                uf[k] = prolong_point(uc, nc, i, jj);
             }
             __syncthreads();
-            for (int c = 0; c < 2; ++c) sm_vcycle(s, l, s.U[l], s.F[l]);
+            for (int c = 0; c < 2; ++c) sm_vcycle(s, l, s.U(l), s.F(l));
         }
-        for (int k = threadIdx.x; k < s.n[J] * s.n[J]; k += blockDim.x) g_u[J][k] = s.U[J][k];
+        T* const gu = g_u[J];
+        const T* uJ = s.U(J);
+        for (int k = threadIdx.x; k < s.n(J) * s.n(J); k += blockDim.x) gu[k] = uJ[k];
     } else {
-        int n = s.n[J];
+        int n = s.n(J);
+        T* const gv = g_v[J];
+        const T* gr = g_r[J];
+        T* const uJ = s.U(J);
+        T* const fJ = s.F(J);
         for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
-            s.U[J][k] = g_v[J][k];
-            s.F[J][k] = g_r[J][k];
+            uJ[k] = gv[k];
+            fJ[k] = gr[k];
         }
         __syncthreads();
-        sm_vcycle(s, J, s.U[J], s.F[J]);
-        for (int k = threadIdx.x; k < n * n; k += blockDim.x) g_v[J][k] = s.U[J][k];
+        sm_vcycle(s, J, uJ, fJ);
+        for (int k = threadIdx.x; k < n * n; k += blockDim.x) gv[k] = uJ[k];
     }
 }
 
@@ -393,6 +409,7 @@ __device__ __forceinline__ double ey_interior(const double* phi, int nx, int ny,
 }
 __global__ void k_efield(const double* phi, double* Ex, double* Ey, float2* exy, int nx, int ny, double twoDX,
                          DevState* ds, int advance) {
+    pgb_pdl_entry();
     /* the last kernel of a step moves the device step counter on */
     if (advance && blockIdx.x == 0 && threadIdx.x == 0) ds->t += 1;
     const int GE = (nx + 1) * (ny + 1);
@@ -415,6 +432,7 @@ __global__ void k_efield(const double* phi, double* Ex, double* Ey, float2* exy,
 
 __global__ void k_walls(double* phi, int nx, int ny, double phi0x, const double* phi_tab, const DevState* ds,
                         double phi0y, double phily) {
+    pgb_pdl_entry();
     const double phirx = phi_tab[ds->t - ds->t_base];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx * ny; k += gridDim.x * blockDim.x) {
         int j = k / nx, i = k - j * nx;
@@ -446,7 +464,7 @@ static FinalizeArgs fin_args(pgb_run* r, int mask, bool rhs) {
 int pgb_launch_finalize(pgb_run* r, int mask, bool make_rhs) {
     FinalizeArgs a = fin_args(r, mask, make_rhs);
     int G = r->nx * r->ny;
-    k_finalize<<<(G + 255) / 256, 256, 0, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_finalize, dim3((G + 255) / 256), dim3(256), 0, r->stream, a));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -455,7 +473,7 @@ int pgb_launch_finalize(pgb_run* r, int mask, bool make_rhs) {
 int pgb_launch_rhs(pgb_run* r) {
     FinalizeArgs a = fin_args(r, 0, true);
     int G = r->nx * r->ny;
-    k_rhs<<<(G + 255) / 256, 256, 0, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_rhs, dim3((G + 255) / 256), dim3(256), 0, r->stream, a));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -479,8 +497,8 @@ struct MgTables {
 template <class T>
 static int small_launch(pgb_run* r, T** tab, int J, int mode) {
     size_t smem = small_smem_bytes(J, sizeof(T));
-    k_mg_small<T><<<1, 1024, smem, r->stream>>>(J, mode, (T)r->p.xlength, tab, tab + PGB_MAX_LEVELS,
-                                                tab + 2 * PGB_MAX_LEVELS, tab + 3 * PGB_MAX_LEVELS);
+    PGB_CK(r, pgb_launch_pdl(k_mg_small<T>, dim3(1), dim3(1024), smem, r->stream, J, mode, (T)r->p.xlength, tab, tab + PGB_MAX_LEVELS,
+                                                tab + 2 * PGB_MAX_LEVELS, tab + 3 * PGB_MAX_LEVELS));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -500,10 +518,11 @@ static Levels<double> levels64(pgb_run* r) { return {r->mg_u, r->mg_f, r->mg_v, 
 static Levels<float> levels32(pgb_run* r) { return {r->mg32_u, r->mg32_f, r->mg32_v, r->mg32_r, r->mg32_tab, r->mg32_w}; }
 
 template <class T, int MODE>
-static void relax_launch(pgb_run* r, const T* uin, T* uout, const T* f, int n, T h2, const T* vc) {
+static int relax_launch(pgb_run* r, const T* uin, T* uout, const T* f, int n, T h2, const T* vc) {
     dim3 grid((n - 2 + RTX - 1) / RTX, (n - 2 + RT - 1) / RT), block(RTX, RT);
-    k_relax_tile<T, MODE><<<grid, block, 0, r->stream>>>(uin, uout, f, n, h2, vc);
+    PGB_CK(r, pgb_launch_pdl(k_relax_tile<T, MODE>, dim3(grid), dim3(block), 0, r->stream, uin, uout, f, n, h2, vc));
     r->launches++;
+    return 0;
 }
 
 /* V-cycle at level j > small on (u, f) (mglin.cpp:176-196).  first_mode 2
@@ -518,16 +537,17 @@ static int vcycle(pgb_run* r, const Levels<T>& L, int j, int jsmall, T* u, const
     int nf = r->mg_n[j], nc = r->mg_n[j - 1];
     T h = (T)r->p.xlength / (T)(nf - 1), h2 = h * h, h2i = (T)1.0 / (h * h);
     T* w = L.w[j];
-    if (first_mode == 2) relax_launch<T, 2>(r, nullptr, w, f, nf, h2, coarse_u);
-    else relax_launch<T, 0>(r, u, w, f, nf, h2, nullptr);
-    k_resid_restrict<T><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(L.rr[j - 1], L.v[j - 1], w, f, nf, h2i);
+    int rc = first_mode == 2 ? relax_launch<T, 2>(r, nullptr, w, f, nf, h2, coarse_u)
+                             : relax_launch<T, 0>(r, u, w, f, nf, h2, nullptr);
+    if (rc) return rc;
+    PGB_CK(r, pgb_launch_pdl(k_resid_restrict<T>, dim3(blocks_for((long long)nc * nc)), dim3(256), 0, r->stream, L.rr[j - 1], L.v[j - 1], w, f, nf, h2i));
     r->launches++;
     if (j - 1 <= jsmall) {
         if (small_launch<T>(r, L.tab, j - 1, 1)) return PGB_ERR_CUDA;
     } else {
         if (vcycle<T>(r, L, j - 1, jsmall, L.v[j - 1], L.rr[j - 1], 0, nullptr)) return PGB_ERR_CUDA;
     }
-    relax_launch<T, 1>(r, w, u, f, nf, h2, L.v[j - 1]);
+    if ((rc = relax_launch<T, 1>(r, w, u, f, nf, h2, L.v[j - 1]))) return rc;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
@@ -550,7 +570,7 @@ static int fmg(pgb_run* r, const Levels<T>& L) {
     /* the one-CTA solver restricts the levels below jsmall itself */
     for (int j = ng - 2; j >= jsmall; --j) {
         int nc = r->mg_n[j];
-        k_restrict<T><<<blocks_for((long long)nc * nc), 256, 0, r->stream>>>(L.f[j], L.f[j + 1], nc);
+        PGB_CK(r, pgb_launch_pdl(k_restrict<T>, dim3(blocks_for((long long)nc * nc)), dim3(256), 0, r->stream, L.f[j], L.f[j + 1], nc));
         r->launches++;
     }
     if (small_launch<T>(r, L.tab, jsmall, 0)) return PGB_ERR_CUDA;
@@ -563,6 +583,7 @@ static int fmg(pgb_run* r, const Levels<T>& L) {
 
 /* FP64 defect d = f - L u on the interior (zero on the walls), as FP32 */
 __global__ void k_defect32(const double* u, const double* f, float* d, int n, double h2i) {
+    pgb_pdl_entry();
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n * n; k += gridDim.x * blockDim.x) {
         int i = k / n, j = k - i * n;
         double v = 0.0;
@@ -572,12 +593,15 @@ __global__ void k_defect32(const double* u, const double* f, float* d, int n, do
     }
 }
 __global__ void k_add32(double* u, const float* e, int count) {
+    pgb_pdl_entry();
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) u[k] += (double)e[k];
 }
 __global__ void k_to32(float* d, const double* s, int count) {
+    pgb_pdl_entry();
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) d[k] = (float)s[k];
 }
 __global__ void k_to64(double* d, const float* s, int count) {
+    pgb_pdl_entry();
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) d[k] = (double)s[k];
 }
 
@@ -645,10 +669,10 @@ int pgb_poisson_solve(pgb_run* r) {
         PGB_CK(r, cudaMemcpyAsync(r->phi, r->mg_u[top], sizeof(double) * G, cudaMemcpyDeviceToDevice, r->stream));
     } else if (r->p.poisson_mode == PGB_POISSON_FMG32) {
         Levels<float> L = levels32(r);
-        k_to32<<<gb, 256, 0, r->stream>>>(L.f[top], r->mg_f[top], G);
+        PGB_CK(r, pgb_launch_pdl(k_to32, dim3(gb), dim3(256), 0, r->stream, L.f[top], r->mg_f[top], G));
         r->launches++;
         if (fmg<float>(r, L)) return PGB_ERR_CUDA;
-        k_to64<<<gb, 256, 0, r->stream>>>(r->phi, L.u[top], G);
+        PGB_CK(r, pgb_launch_pdl(k_to64, dim3(gb), dim3(256), 0, r->stream, r->phi, L.u[top], G));
         r->launches++;
     } else {
         Levels<float> L = levels32(r);
@@ -656,16 +680,16 @@ int pgb_poisson_solve(pgb_run* r) {
         PGB_CK(r, cudaMemsetAsync(r->dc_u, 0, sizeof(double) * G, r->stream));
         int iters = r->p.dc_max_iters > 0 ? r->p.dc_max_iters : 1;
         for (int it = 0; it < iters; ++it) {
-            k_defect32<<<gb, 256, 0, r->stream>>>(r->dc_u, r->mg_f[top], L.f[top], n, h2i);
+            PGB_CK(r, pgb_launch_pdl(k_defect32, dim3(gb), dim3(256), 0, r->stream, r->dc_u, r->mg_f[top], L.f[top], n, h2i));
             r->launches++;
             if (fmg<float>(r, L)) return PGB_ERR_CUDA;
-            k_add32<<<gb, 256, 0, r->stream>>>(r->dc_u, L.u[top], G);
+            PGB_CK(r, pgb_launch_pdl(k_add32, dim3(gb), dim3(256), 0, r->stream, r->dc_u, L.u[top], G));
             r->launches++;
         }
         PGB_CK(r, cudaMemcpyAsync(r->phi, r->dc_u, sizeof(double) * G, cudaMemcpyDeviceToDevice, r->stream));
     }
-    k_walls<<<blocks_for((long long)r->nx * r->ny), 256, 0, r->stream>>>(r->phi, r->nx, r->ny, r->p.phi_left, r->phi_tab,
-                                                                         r->ds, r->p.phi_bottom, r->p.phi_top);
+    PGB_CK(r, pgb_launch_pdl(k_walls, dim3(blocks_for((long long)r->nx * r->ny)), dim3(256), 0, r->stream, r->phi, r->nx, r->ny, r->p.phi_left, r->phi_tab,
+                                                                         r->ds, r->p.phi_bottom, r->p.phi_top));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -673,7 +697,7 @@ int pgb_poisson_solve(pgb_run* r) {
 
 int pgb_launch_efield(pgb_run* r, int advance) {
     int GE = (r->nx + 1) * (r->ny + 1);
-    k_efield<<<blocks_for(GE), 256, 0, r->stream>>>(r->phi, r->ex, r->ey, r->exy, r->nx, r->ny, 2.0 * r->dx, r->ds, advance);
+    PGB_CK(r, pgb_launch_pdl(k_efield, dim3(blocks_for(GE)), dim3(256), 0, r->stream, r->phi, r->ex, r->ey, r->exy, r->nx, r->ny, 2.0 * r->dx, r->ds, advance));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;

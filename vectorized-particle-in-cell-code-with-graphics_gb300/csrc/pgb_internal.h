@@ -190,6 +190,36 @@ struct pgb_run {
 bool pgb_cuda_ok(pgb_run* r, cudaError_t e, const char* what);
 /* message for pgb_last_error(NULL), from entry points without a handle */
 void pgb_set_unbound_error(const std::string& msg);
+/* Programmatic dependent launch.  A kernel launched with pgb_launch_pdl may
+ * be scheduled while the previous kernel on its stream is still running;
+ * its first statement is pgb_pdl_entry(), whose griddepcontrol.wait blocks
+ * until that kernel has completed and its writes are visible.  No memory is
+ * touched before it, so the order of results is that of plain launches.
+ * The launch_dependents that follows lets the next kernel be scheduled
+ * early in turn: what it saves is the launch gap, not any ordering.  On a
+ * kernel launched without the attribute both instructions do nothing.    */
+#ifdef __CUDACC__
+__device__ __forceinline__ void pgb_pdl_entry() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+template <typename... KArgs, typename... Args>
+inline cudaError_t pgb_launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                  Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+#endif
+
 #define PGB_CK(r, call)                                  \
     do {                                                 \
         if (!pgb_cuda_ok((r), (call), #call)) return PGB_ERR_CUDA; \
