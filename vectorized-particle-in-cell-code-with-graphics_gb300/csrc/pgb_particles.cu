@@ -389,6 +389,7 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
  * through a shared window), then every tile after the sorted region.     */
 template <bool MCC, bool DEP>
 __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
+    pgb_pdl_entry();
     __shared__ unsigned int s_win[WIN_NODES];
     __shared__ ScatterQueue s_q;
     if (MCC && threadIdx.x == 0) s_q.n = 0;
@@ -437,6 +438,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
 /* flag-only pass (wall classification without a push) */
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_flag(const float4* xv, DevState* ds, int s, int nx, int ny,
                                                            int steady, int* tl, int* tc) {
+    pgb_pdl_entry();
     const long long n = ds->n[s];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -460,6 +462,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_flag(const float4* xv, Dev
 /* standalone deposit (particle::collect_charge) */
 __global__ void __launch_bounds__(256) k_deposit(const float4* xv, const float* w, DevState* ds, int s, int nx, int ny,
                                                  unsigned long long* qacc) {
+    pgb_pdl_entry();
     const long long n = ds->n[s];
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float4 p = xv[i];
@@ -469,6 +472,7 @@ __global__ void __launch_bounds__(256) k_deposit(const float4* xv, const float* 
 
 /* standalone electron collisions (e_collisions::collision) */
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_mcc(PushArgs a) {
+    pgb_pdl_entry();
     const long long n = a.ds->n[0];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     int st_loc[2] = {0, 0};
@@ -543,6 +547,7 @@ __device__ __forceinline__ long long block_excl_scan8(const int* cnt, int* off, 
 
 __global__ void __launch_bounds__(1024) k_scan_small(const int* cnt, int* off, const long long* n_ptr, long long m_const,
                                                      long long* total) {
+    pgb_pdl_entry();
     /* n_ptr: particle count whose tiles are scanned; else m_const entries */
     const long long m = n_ptr ? (*n_ptr + PGB_TILE - 1) / PGB_TILE : m_const;
     long long t = block_excl_scan8(cnt, off, m, 0);
@@ -551,12 +556,14 @@ __global__ void __launch_bounds__(1024) k_scan_small(const int* cnt, int* off, c
 
 /* exclusive scan of a list-length array (length read from device memory) */
 __global__ void __launch_bounds__(1024) k_scan_list(const int* cnt, int* off, const long long* m_ptr, long long* total) {
+    pgb_pdl_entry();
     long long t = block_excl_scan8(cnt, off, *m_ptr, 0);
     if (threadIdx.x == 0) *total = t;
 }
 
 /* gather per-tile lists into one dense list in slot order */
 __global__ void k_gather_lists(const int* tl, const int* tc, const int* toff, const long long* n_ptr, int* out) {
+    pgb_pdl_entry();
     const long long n = *n_ptr;
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -586,6 +593,7 @@ struct InjectArgs {
     int* flag;                   /* per new electron: outside after its push */
 };
 __global__ void k_inject(InjectArgs a) {
+    pgb_pdl_entry();
     /* one thread per new particle; electrons first, then ions, in id order */
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int total = a.k * ((a.species_mask & 1) + ((a.species_mask >> 1) & 1));
@@ -624,6 +632,7 @@ __global__ void k_inject(InjectArgs a) {
 
 /* after k_inject: counts, ids, and the wall list entries of new electrons */
 __global__ void k_inject_commit(InjectArgs a) {
+    pgb_pdl_entry();
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     for (int s = 0; s < 2; ++s) {
         if (!(a.species_mask & (1 << s))) continue;
@@ -662,6 +671,7 @@ struct IonizeAppendArgs {
     int store_e, store_i;
 };
 __global__ void k_ionize_append(IonizeAppendArgs a) {
+    pgb_pdl_entry();
     const long long m = a.ds->list_n[LIST_ION_EV];
     const long long ne0 = a.ds->n[0], ni0 = a.ds->n[1];
     const unsigned int ide0 = a.ds->next_id[0], idi0 = a.ds->next_id[1];
@@ -702,6 +712,7 @@ __global__ void k_ionize_append(IonizeAppendArgs a) {
     }
 }
 __global__ void k_ionize_commit(DevState* ds, int store_e, int store_i, long long cap_e, long long cap_i) {
+    pgb_pdl_entry();
     long long m = ds->list_n[LIST_ION_EV];
     ds->next_id[0] += (unsigned int)m;
     ds->next_id[1] += (unsigned int)m;
@@ -713,6 +724,7 @@ __global__ void k_ionize_commit(DevState* ds, int store_e, int store_i, long lon
 
 /* ------------------------------------------------------------ compaction */
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_alive_count(const float4* xv, DevState* ds, int s, int* tc) {
+    pgb_pdl_entry();
     const long long n = ds->n[s];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     __shared__ int s_w[PGB_PUSH_THREADS / 32];
@@ -734,6 +746,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_alive_count(const float4* 
     }
 }
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_compact(Species S, DevState* ds, int s, const int* toff) {
+    pgb_pdl_entry();
     const long long n = ds->n[s];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     bool f[1][PGB_ITEMS];
@@ -767,6 +780,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_compact(Species S, DevStat
     }
 }
 __global__ void k_compact_commit(DevState* ds, int s, const long long* total) {
+    pgb_pdl_entry();
     ds->n[s] = *total;
     ds->dead[s] = 0;
     ds->n_pieces[s] = 0;       /* slot order changed: the bin pieces are gone */
@@ -776,6 +790,7 @@ __global__ void k_compact_commit(DevState* ds, int s, const long long* total) {
 /* ------------------------------------------------------------ load / dump */
 /* slots [i0, i1) from records aos[6 i ..] */
 __global__ void k_load(Species S, const double* aos, long long i0, long long i1, double dx, double dy) {
+    pgb_pdl_entry();
     for (long long i = i0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < i1; i += (long long)gridDim.x * blockDim.x) {
         const double* r = aos + 6 * i;
         S.xv[i] = make_float4((float)(r[0] / dx), (float)(r[1] / dy), (float)r[2], (float)r[3]);
@@ -789,6 +804,7 @@ __global__ void k_load(Species S, const double* aos, long long i0, long long i1,
 /* tiles [t0, t1) of the live-slot order */
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_dump(Species S, DevState* ds, int s, const int* toff, double dx,
                                                            double dy, double* out, long long cap, int t0, int t1) {
+    pgb_pdl_entry();
     const long long n = ds->n[s];
     const int ntiles = min(t1, (int)((n + PGB_TILE - 1) / PGB_TILE));
     __shared__ int s_off[PGB_ITEMS][PGB_PUSH_THREADS / 32];
@@ -895,10 +911,9 @@ int pgb_launch_push(pgb_run* r, int s, bool mcc, bool deposit, bool flag_ion) {
     (void)flag_ion;
     PushArgs a = push_args(r, s);
     int g = grid_for(r, 8);
-    if (mcc && deposit) k_push<true, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
-    else if (mcc) k_push<true, false><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
-    else if (deposit) k_push<false, true><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
-    else k_push<false, false><<<g, PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    void (*kp)(PushArgs) = mcc ? (deposit ? k_push<true, true> : k_push<true, false>)
+                               : (deposit ? k_push<false, true> : k_push<false, false>);
+    PGB_CK(r, pgb_launch_pdl(kp, dim3(g), dim3(PGB_PUSH_THREADS), 0, r->stream, a));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -906,8 +921,8 @@ int pgb_launch_push(pgb_run* r, int s, bool mcc, bool deposit, bool flag_ion) {
 
 int pgb_launch_flag_outside(pgb_run* r, int s) {
     int l = s == 0 ? LIST_OUT_E : LIST_OUT_I;
-    k_flag<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s].xv, r->ds, s, r->nx, r->ny, r->p.steadystate,
-                                                               r->tile_list[l], r->tile_cnt[l]);
+    PGB_CK(r, pgb_launch_pdl(k_flag, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, r->sp[s].xv, r->ds, s, r->nx, r->ny, r->p.steadystate,
+                                                               r->tile_list[l], r->tile_cnt[l]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -915,7 +930,7 @@ int pgb_launch_flag_outside(pgb_run* r, int s) {
 
 int pgb_launch_mcc(pgb_run* r) {
     PushArgs a = push_args(r, 0);
-    k_mcc<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_mcc, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, a));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -924,17 +939,17 @@ int pgb_launch_mcc(pgb_run* r) {
 /* per-tile list `which` (tiles of species s) -> dense list + count */
 int pgb_build_list(pgb_run* r, int which, int s) {
     int* toff = r->aux_j;
-    k_scan_small<<<1, 1024, 0, r->stream>>>(r->tile_cnt[which], toff, &r->ds->n[s], 0, &r->ds->list_n[which]);
+    PGB_CK(r, pgb_launch_pdl(k_scan_small, dim3(1), dim3(1024), 0, r->stream, r->tile_cnt[which], toff, &r->ds->n[s], 0, &r->ds->list_n[which]));
     r->launches++;
-    k_gather_lists<<<grid_for(r, 4), 256, 0, r->stream>>>(r->tile_list[which], r->tile_cnt[which], toff,
-                                                           &r->ds->n[s], r->list[which]);
+    PGB_CK(r, pgb_launch_pdl(k_gather_lists, dim3(grid_for(r, 4)), dim3(256), 0, r->stream, r->tile_list[which], r->tile_cnt[which], toff,
+                                                           &r->ds->n[s], r->list[which]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
 
 int pgb_launch_deposit(pgb_run* r, int s) {
-    k_deposit<<<grid_for(r, 8), 256, 0, r->stream>>>(r->sp[s].xv, r->sp[s].w, r->ds, s, r->nx, r->ny, r->qacc[s]);
+    PGB_CK(r, pgb_launch_pdl(k_deposit, dim3(grid_for(r, 8)), dim3(256), 0, r->stream, r->sp[s].xv, r->sp[s].w, r->ds, s, r->nx, r->ny, r->qacc[s]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -951,8 +966,8 @@ int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e) {
     a.flag = r->inject_flag;
     int tot = 2 * a.k;
     if (tot <= 0) return 0;
-    k_inject<<<(tot + 127) / 128, 128, 0, r->stream>>>(a);
-    k_inject_commit<<<1, 32, 0, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_inject, dim3((tot + 127) / 128), dim3(128), 0, r->stream, a));
+    PGB_CK(r, pgb_launch_pdl(k_inject_commit, dim3(1), dim3(32), 0, r->stream, a));
     r->launches += 2;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -965,10 +980,10 @@ int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i) {
     a.dx = r->dx; a.dy = r->dy;
     a.store_e = store_e;
     a.store_i = store_i;
-    k_ionize_append<<<r->sms * 2, 256, 0, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_ionize_append, dim3(r->sms * 2), dim3(256), 0, r->stream, a));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
-    k_ionize_commit<<<1, 1, 0, r->stream>>>(r->ds, a.store_e, a.store_i, r->sp[0].cap, r->sp[1].cap);
+    PGB_CK(r, pgb_launch_pdl(k_ionize_commit, dim3(1), dim3(1), 0, r->stream, r->ds, a.store_e, a.store_i, r->sp[0].cap, r->sp[1].cap));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -979,13 +994,13 @@ int pgb_launch_compact(pgb_run* r, int s) {
     int* tc = r->tile_cnt[LIST_SPARE];
     int* toff = r->aux_j;
     PGB_CK(r, cudaMemsetAsync(tc, 0, sizeof(int) * r->ntiles_cap, r->stream));
-    k_alive_count<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(S.xv, r->ds, s, tc);
+    PGB_CK(r, pgb_launch_pdl(k_alive_count, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, S.xv, r->ds, s, tc));
     r->launches++;
-    k_scan_small<<<1, 1024, 0, r->stream>>>(tc, toff, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]);
+    PGB_CK(r, pgb_launch_pdl(k_scan_small, dim3(1), dim3(1024), 0, r->stream, tc, toff, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]));
     r->launches++;
-    k_compact<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(S, r->ds, s, toff);
+    PGB_CK(r, pgb_launch_pdl(k_compact, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, S, r->ds, s, toff));
     r->launches++;
-    k_compact_commit<<<1, 1, 0, r->stream>>>(r->ds, s, &r->ds->list_n[LIST_SPARE]);
+    PGB_CK(r, pgb_launch_pdl(k_compact_commit, dim3(1), dim3(1), 0, r->stream, r->ds, s, &r->ds->list_n[LIST_SPARE]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     std::swap(S.xv, S.xv2);
@@ -996,7 +1011,7 @@ int pgb_launch_compact(pgb_run* r, int s) {
 }
 
 int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long i0, long long i1) {
-    k_load<<<grid_for(r, 4), 256, 0, r->stream>>>(r->sp[s], d_aos, i0, i1, r->dx, r->dy);
+    PGB_CK(r, pgb_launch_pdl(k_load, dim3(grid_for(r, 4)), dim3(256), 0, r->stream, r->sp[s], d_aos, i0, i1, r->dx, r->dy));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -1006,17 +1021,17 @@ int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long i0, long l
 int pgb_launch_dump_offsets(pgb_run* r, int s) {
     int* tc = r->tile_cnt[LIST_SPARE];
     PGB_CK(r, cudaMemsetAsync(tc, 0, sizeof(int) * r->ntiles_cap, r->stream));
-    k_alive_count<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s].xv, r->ds, s, tc);
+    PGB_CK(r, pgb_launch_pdl(k_alive_count, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, r->sp[s].xv, r->ds, s, tc));
     r->launches++;
-    k_scan_small<<<1, 1024, 0, r->stream>>>(tc, r->aux_j, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]);
+    PGB_CK(r, pgb_launch_pdl(k_scan_small, dim3(1), dim3(1024), 0, r->stream, tc, r->aux_j, &r->ds->n[s], 0, &r->ds->list_n[LIST_SPARE]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
 }
 
 int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap, int t0, int t1) {
-    k_dump<<<grid_for(r, 8), PGB_PUSH_THREADS, 0, r->stream>>>(r->sp[s], r->ds, s, r->aux_j, r->dx, r->dy, d_out, cap,
-                                                               t0, t1);
+    PGB_CK(r, pgb_launch_pdl(k_dump, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, r->sp[s], r->ds, s, r->aux_j, r->dx, r->dy, d_out, cap,
+                                                               t0, t1));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;

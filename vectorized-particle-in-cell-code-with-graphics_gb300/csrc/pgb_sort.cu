@@ -50,6 +50,7 @@ __device__ __forceinline__ int bin_key(float4 p, int nx, int ny, int nbx, int nb
 }
 
 __global__ void __launch_bounds__(256) k_sort_count(SortArgs a) {
+    pgb_pdl_entry();
     extern __shared__ int s_hist[];
     const long long n = a.ds->n[a.s];
     const int nch = (int)((n + SORT_CHUNK - 1) / SORT_CHUNK);
@@ -96,6 +97,7 @@ __device__ __forceinline__ long long block_excl_scan_ll(long long v, long long* 
 
 /* per key: exclusive scan over the live chunks (one CTA per key) */
 __global__ void __launch_bounds__(1024) k_sort_scan_keys(SortArgs a) {
+    pgb_pdl_entry();
     const long long n = a.ds->n[a.s];
     const int nch = (int)((n + SORT_CHUNK - 1) / SORT_CHUNK);
     __shared__ long long s_w[32];
@@ -119,6 +121,7 @@ __global__ void __launch_bounds__(1024) k_sort_scan_keys(SortArgs a) {
  * key's thread writes its pieces, then every tile finds its key by binary
  * search over the starts.                                               */
 __global__ void __launch_bounds__(1024) k_sort_scan_bins(SortArgs a) {
+    pgb_pdl_entry();
     __shared__ long long s_w[32];
     long long carry_t = 0, carry_p = 0;
     for (int base = 0; base <= a.nbins; base += blockDim.x) {
@@ -178,6 +181,7 @@ __global__ void __launch_bounds__(1024) k_sort_scan_bins(SortArgs a) {
  * slot order.                                                           */
 #define SCATTER_BATCHES 4
 __global__ void __launch_bounds__(256) k_sort_scatter(SortArgs a) {
+    pgb_pdl_entry();
     extern __shared__ long long s_cur[];   /* [warp][key] */
     const long long n = a.ds->n[a.s];
     const int nch = (int)((n + SORT_CHUNK - 1) / SORT_CHUNK);
@@ -236,6 +240,7 @@ __global__ void __launch_bounds__(256) k_sort_scatter(SortArgs a) {
 
 /* tombstones in the padding after each key's particles; new counts */
 __global__ void k_sort_pad(SortArgs a) {
+    pgb_pdl_entry();
     if (a.ds->sort_overflow) return;   /* the copy kept n and the tombstones */
     for (int key = blockIdx.x; key <= a.nbins; key += gridDim.x) {
         long long s0 = a.key_start[key] + a.key_total[key], s1 = a.key_start[key + 1];
@@ -271,16 +276,16 @@ int pgb_launch_sort(pgb_run* r, int s) {
     a.key_start = r->sort_key_start; a.tile_bin = r->tile_bin[s]; a.pieces = r->pieces[s];
     a.piece_tiles = PGB_PIECE_TILES;
     size_t hist = sizeof(int) * (a.nbins + 1);
-    k_sort_count<<<r->sms * 4, 256, hist, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_sort_count, dim3(r->sms * 4), dim3(256), hist, r->stream, a));
     r->launches++;
-    k_sort_scan_keys<<<r->sms * 2, 1024, 0, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_sort_scan_keys, dim3(r->sms * 2), dim3(1024), 0, r->stream, a));
     r->launches++;
-    k_sort_scan_bins<<<1, 1024, 0, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_sort_scan_bins, dim3(1), dim3(1024), 0, r->stream, a));
     r->launches++;
     size_t cur = sizeof(long long) * (a.nbins + 1) * 8;
-    k_sort_scatter<<<r->sms * 4, 256, cur, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_sort_scatter, dim3(r->sms * 4), dim3(256), cur, r->stream, a));
     r->launches++;
-    k_sort_pad<<<r->sms, 256, 0, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_sort_pad, dim3(r->sms), dim3(256), 0, r->stream, a));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     Species& S = r->sp[s];

@@ -85,6 +85,7 @@ __device__ __forceinline__ double ion_yield(const WallArgs& a, double energy) {
 }
 
 __global__ void k_iwall1(WallArgs a) {
+    pgb_pdl_entry();
     const long long m = a.ds->list_n[LIST_OUT_I];
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
         int slot = a.list_i[k];
@@ -101,6 +102,7 @@ __global__ void k_iwall1(WallArgs a) {
 
 /* boundary::i_secondary_vel (boundary.cpp:687-756) */
 __global__ void k_iwall2(WallArgs a) {
+    pgb_pdl_entry();
     const long long m = a.ds->list_n[LIST_OUT_I];
     const long long ne0 = a.ds->n[0];
     const unsigned int id0 = a.ds->next_id[0];
@@ -214,6 +216,7 @@ __device__ int e_wall_event(const WallArgs& a, pgb_stream* st, double& x, double
 }
 
 __global__ void k_ewall1(WallArgs a) {
+    pgb_pdl_entry();
     const long long m = a.ds->list_n[LIST_OUT_E];
     int cnt[4] = {0, 0, 0, 0};   /* absorbed, reflected, backscattered, see events */
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
@@ -255,6 +258,7 @@ __global__ void k_ewall1(WallArgs a) {
 
 /* boundary::secondary_electrons (boundary.cpp:494-529) */
 __global__ void k_ewall2(WallArgs a) {
+    pgb_pdl_entry();
     const long long m = a.ds->list_n[LIST_OUT_E];
     const long long ne0 = a.ds->n[0];
     const unsigned int id0 = a.ds->next_id[0];
@@ -293,6 +297,7 @@ __global__ void k_ewall2(WallArgs a) {
 
 /* n, next id and statistics after a wall pass that appended `total` electrons */
 __global__ void k_wall_commit(DevState* ds, const long long* total, int which, long long cap_e, int stat_emit) {
+    pgb_pdl_entry();
     long long t = *total;
     long long v = ds->n[0] + t;
     ds->n[0] = v < cap_e ? v : cap_e;
@@ -333,6 +338,7 @@ __device__ __forceinline__ void block_scan2(int a, int b, int& ea, int& eb, int&
 }
 
 __global__ void __launch_bounds__(1024) k_steady(WallArgs a, int* ion_by_rank) {
+    pgb_pdl_entry();
     const long long me_ = a.ds->list_n[LIST_OUT_E], mi_ = a.ds->list_n[LIST_OUT_I];
     __shared__ int s_plops;
     if (threadIdx.x == 0) s_plops = 0;
@@ -438,6 +444,7 @@ __device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, fl
 }
 
 __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
+    pgb_pdl_entry();
     extern __shared__ unsigned long long s_sum[];
     const long long n = a.ds->n[1];
     const int ntiles = (int)((n + CX_TILE - 1) / CX_TILE);
@@ -472,6 +479,7 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
 }
 
 __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
+    pgb_pdl_entry();
     const int lane = threadIdx.x & 31;
     const int col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (col >= a.nx) return;
@@ -572,29 +580,29 @@ int pgb_launch_walls(pgb_run* r, int which) {
     int g = r->sms * 4;
     if (r->p.steadystate) {
         if (which == PGB_BOUNDARY_ELECTRONS) {
-            k_steady<<<1, 1024, 0, r->stream>>>(a, r->aux_i);
+            PGB_CK(r, pgb_launch_pdl(k_steady, dim3(1), dim3(1024), 0, r->stream, a, r->aux_i));
             r->launches++;
             PGB_CK(r, cudaGetLastError());
         }
         return 0;
     }
     if (which == PGB_BOUNDARY_IONS) {
-        k_iwall1<<<g, 256, 0, r->stream>>>(a);
+        PGB_CK(r, pgb_launch_pdl(k_iwall1, dim3(g), dim3(256), 0, r->stream, a));
         r->launches++;
-        k_scan_list<<<1, 1024, 0, r->stream>>>(r->aux_i, r->aux_j, &r->ds->list_n[LIST_OUT_I], &r->ds->list_n[LIST_SPARE]);
+        PGB_CK(r, pgb_launch_pdl(k_scan_list, dim3(1), dim3(1024), 0, r->stream, r->aux_i, r->aux_j, &r->ds->list_n[LIST_OUT_I], &r->ds->list_n[LIST_SPARE]));
         r->launches++;
-        k_iwall2<<<g, 256, 0, r->stream>>>(a);
+        PGB_CK(r, pgb_launch_pdl(k_iwall2, dim3(g), dim3(256), 0, r->stream, a));
         r->launches++;
-        k_wall_commit<<<1, 1, 0, r->stream>>>(r->ds, &r->ds->list_n[LIST_SPARE], 0, r->sp[0].cap, ST_ISEE_EM);
+        PGB_CK(r, pgb_launch_pdl(k_wall_commit, dim3(1), dim3(1), 0, r->stream, r->ds, &r->ds->list_n[LIST_SPARE], 0, r->sp[0].cap, ST_ISEE_EM));
         r->launches++;
     } else {
-        k_ewall1<<<g, 256, 0, r->stream>>>(a);
+        PGB_CK(r, pgb_launch_pdl(k_ewall1, dim3(g), dim3(256), 0, r->stream, a));
         r->launches++;
-        k_scan_list<<<1, 1024, 0, r->stream>>>(r->aux_i, r->aux_j, &r->ds->list_n[LIST_OUT_E], &r->ds->list_n[LIST_SPARE]);
+        PGB_CK(r, pgb_launch_pdl(k_scan_list, dim3(1), dim3(1024), 0, r->stream, r->aux_i, r->aux_j, &r->ds->list_n[LIST_OUT_E], &r->ds->list_n[LIST_SPARE]));
         r->launches++;
-        k_ewall2<<<g, 256, 0, r->stream>>>(a);
+        PGB_CK(r, pgb_launch_pdl(k_ewall2, dim3(g), dim3(256), 0, r->stream, a));
         r->launches++;
-        k_wall_commit<<<1, 1, 0, r->stream>>>(r->ds, &r->ds->list_n[LIST_SPARE], 1, r->sp[0].cap, ST_SEE_EM);
+        PGB_CK(r, pgb_launch_pdl(k_wall_commit, dim3(1), dim3(1), 0, r->stream, r->ds, &r->ds->list_n[LIST_SPARE], 1, r->sp[0].cap, ST_SEE_EM));
         r->launches++;
     }
     PGB_CK(r, cudaGetLastError());
@@ -611,10 +619,10 @@ int pgb_launch_cx(pgb_run* r) {
     a.col_acc = (long long*)r->prob_cx;
     a.neut_i = r->neut[1];
     a.seed = r->p.seed;
-    k_cx_tiles<<<r->sms * 4, 256, sizeof(unsigned long long) * r->nx, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_cx_tiles, dim3(r->sms * 4), dim3(256), sizeof(unsigned long long) * r->nx, r->stream, a));
     r->launches++;
     int warps = 8;
-    k_cx_walk<<<(r->nx + warps - 1) / warps, warps * 32, 0, r->stream>>>(a);
+    PGB_CK(r, pgb_launch_pdl(k_cx_walk, dim3((r->nx + warps - 1) / warps), dim3(warps * 32), 0, r->stream, a));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
