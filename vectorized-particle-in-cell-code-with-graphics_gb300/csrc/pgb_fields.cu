@@ -271,61 +271,109 @@ struct SmallMG {
  * of n.                                                                  */
 __device__ __forceinline__ int sm_row(int k, float inv_n) { return (int)(((float)k + 0.5f) * inv_n); }
 
-template <class T>
-__device__ void sm_relax(T* u, const T* f, int n, T length) {
+/* Who works on a level.  Levels of 33 nodes and more use the whole CTA
+ * and __syncthreads.  Levels of 17 nodes and fewer (at most 289 points)
+ * use threads 0..255 and named barrier 1: with all 32 warps, every phase
+ * of a small level would cost each scheduler the issue of eight warps'
+ * loop code for a handful of points.  Every point is updated by the same
+ * arithmetic whichever team updates it.                                  */
+struct TeamCta {
+    static __device__ __forceinline__ int size() { return blockDim.x; }
+    static __device__ __forceinline__ void sync() { __syncthreads(); }
+};
+struct TeamSmall {   /* threads 0..255 only */
+    static __device__ __forceinline__ int size() { return 256; }
+    static __device__ __forceinline__ void sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+};
+
+template <class T, class Tm>
+__device__ __forceinline__ void sm_relax(T* u, const T* f, int n, T length) {
     T h = length / (T)(n - 1), h2 = h * h;
     const int m = n - 2, per_row = (n - 1) >> 1, sh = __ffs(per_row) - 1;
     for (int color = 0; color < 2; ++color) {
-        for (int t = threadIdx.x; t < m * per_row; t += blockDim.x) {
+        for (int t = threadIdx.x; t < m * per_row; t += Tm::size()) {
             int r = t >> sh, c = t & (per_row - 1);
             int i = r + 1, j = 1 + ((i + 1 + color) & 1) + 2 * c;
             if (j <= n - 2) u[i * n + j] = gs_point(u, f, n, i, j, h2);
         }
-        __syncthreads();
+        Tm::sync();
     }
 }
-template <class T>
-__device__ void sm_coarsest(T* u, const T* f, T length) {
+template <class T, class Tm>
+__device__ __forceinline__ void sm_coarsest(T* u, const T* f, T length) {
     if (threadIdx.x == 0) {
         T h = (T)0.5 * length;
         for (int k = 0; k < 9; ++k) u[k] = (T)0;
         u[4] = -h * h * f[4] / (T)4.0;   /* mglin.cpp:103-110 */
     }
-    __syncthreads();
+    Tm::sync();
 }
-/* V-cycle at level j on (u, f) using V/R of the levels below */
+/* level l of a V-cycle whose top is j, on the way down: smooth, then the
+ * restricted residual and a zero correction on level l-1               */
+template <class T, class Tm>
+__device__ __forceinline__ void sm_down(const SmallMG<T>& s, int j, int l, T* u, const T* f) {
+    T* ul = (l == j) ? u : s.V(l);
+    const T* fl = (l == j) ? f : s.R(l);
+    const int nf = s.n(l), nc = s.n(l - 1);
+    const T h = s.length / (T)(nf - 1), h2i = (T)1.0 / (h * h);
+    sm_relax<T, Tm>(ul, fl, nf, s.length);
+    const float inv = 1.0f / (float)nc;
+    T* const rc = s.R(l - 1);
+    T* const vc = s.V(l - 1);
+    for (int k = threadIdx.x; k < nc * nc; k += Tm::size()) {
+        int ic = sm_row(k, inv), jc = k - ic * nc;
+        T v = (T)0;
+        if (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) v = restrict_resid_point(ul, fl, nf, ic, jc, h2i);
+        rc[k] = v;
+        vc[k] = (T)0;
+    }
+    Tm::sync();
+}
+/* level l on the way up: add the prolongated correction, then smooth */
+template <class T, class Tm>
+__device__ __forceinline__ void sm_up(const SmallMG<T>& s, int j, int l, T* u, const T* f) {
+    T* ul = (l == j) ? u : s.V(l);
+    const T* fl = (l == j) ? f : s.R(l);
+    const int nf = s.n(l), nc = s.n(l - 1);
+    const float inv = 1.0f / (float)nf;
+    const T* vc = s.V(l - 1);
+    for (int k = threadIdx.x; k < nf * nf; k += Tm::size()) {
+        int i = sm_row(k, inv), jj = k - i * nf;
+        ul[k] = ul[k] + prolong_point(vc, nc, i, jj);
+    }
+    Tm::sync();
+    sm_relax<T, Tm>(ul, fl, nf, s.length);
+}
+/* FMG interpolation of level l from level l-1 */
+template <class T, class Tm>
+__device__ __forceinline__ void sm_prolong_u(const SmallMG<T>& s, int l) {
+    const int nf = s.n(l), nc = s.n(l - 1);
+    const float inv = 1.0f / (float)nf;
+    T* const uf = s.U(l);
+    const T* uc = s.U(l - 1);
+    for (int k = threadIdx.x; k < nf * nf; k += Tm::size()) {
+        int i = sm_row(k, inv), jj = k - i * nf;
+        uf[k] = prolong_point(uc, nc, i, jj);
+    }
+    Tm::sync();
+}
+/* the part of a V-cycle (top j) from level l (at most 17 nodes) down to
+ * the coarsest solve and back up to l; entered by threads 0..255 only   */
+template <class T>
+__device__ __forceinline__ void sm_vcycle_small(const SmallMG<T>& s, int j, int l, T* u, const T* f) {
+    for (int m = l; m >= 1; --m) sm_down<T, TeamSmall>(s, j, m, u, f);
+    if (j == 0) sm_coarsest<T, TeamSmall>(u, f, s.length);
+    else sm_coarsest<T, TeamSmall>(s.V(0), s.R(0), s.length);
+    for (int m = 1; m <= l; ++m) sm_up<T, TeamSmall>(s, j, m, u, f);
+}
+/* V-cycle at level j on (u, f) using V/R of the levels below; all threads */
 template <class T>
 __device__ __forceinline__ void sm_vcycle(const SmallMG<T> s, int j, T* u, const T* f) {
-    if (j == 0) { sm_coarsest(u, f, s.length); return; }
-    for (int l = j; l >= 1; --l) {
-        T* ul = (l == j) ? u : s.V(l);
-        const T* fl = (l == j) ? f : s.R(l);
-        int nf = s.n(l), nc = s.n(l - 1);
-        T h = s.length / (T)(nf - 1), h2i = (T)1.0 / (h * h);
-        sm_relax(ul, fl, nf, s.length);
-        const float inv = 1.0f / (float)nc;
-        for (int k = threadIdx.x; k < nc * nc; k += blockDim.x) {
-            int ic = sm_row(k, inv), jc = k - ic * nc;
-            T v = (T)0;
-            if (ic > 0 && jc > 0 && ic < nc - 1 && jc < nc - 1) v = restrict_resid_point(ul, fl, nf, ic, jc, h2i);
-            s.R(l - 1)[k] = v;
-            s.V(l - 1)[k] = (T)0;
-        }
-        __syncthreads();
-    }
-    sm_coarsest(s.V(0), s.R(0), s.length);
-    for (int l = 1; l <= j; ++l) {
-        T* ul = (l == j) ? u : s.V(l);
-        const T* fl = (l == j) ? f : s.R(l);
-        int nf = s.n(l), nc = s.n(l - 1);
-        const float inv = 1.0f / (float)nf;
-        for (int k = threadIdx.x; k < nf * nf; k += blockDim.x) {
-            int i = sm_row(k, inv), jj = k - i * nf;
-            ul[k] = ul[k] + prolong_point(s.V(l - 1), nc, i, jj);
-        }
-        __syncthreads();
-        sm_relax(ul, fl, nf, s.length);
-    }
+    int l = j;
+    for (; l >= 1 && s.n(l) >= 33; --l) sm_down<T, TeamCta>(s, j, l, u, f);
+    if (threadIdx.x < 256) sm_vcycle_small(s, j, l, u, f);
+    __syncthreads();
+    for (int m = l + 1; m <= j; ++m) sm_up<T, TeamCta>(s, j, m, u, f);
 }
 
 /* mode 0: full multigrid from level 0 to J on the rhs g_f[J] (the coarser
@@ -354,17 +402,18 @@ __global__ void __launch_bounds__(1024, 1) k_mg_small(int J, int mode, T length,
             }
             __syncthreads();
         }
-        sm_coarsest(s.U(0), s.F(0), length);
-        for (int l = 1; l <= J; ++l) {
-            int nf = s.n(l), nc = s.n(l - 1);
-            const float inv = 1.0f / (float)nf;
-            T* const uf = s.U(l);
-            const T* uc = s.U(l - 1);
-            for (int k = threadIdx.x; k < nf * nf; k += blockDim.x) {
-                int i = sm_row(k, inv), jj = k - i * nf;
-                uf[k] = prolong_point(uc, nc, i, jj);
+        /* the FMG levels of at most 17 nodes (l <= 3) by threads 0..255 */
+        const int ls = J < 3 ? J : 3;
+        if (threadIdx.x < 256) {
+            sm_coarsest<T, TeamSmall>(s.U(0), s.F(0), length);
+            for (int l = 1; l <= ls; ++l) {
+                sm_prolong_u<T, TeamSmall>(s, l);
+                for (int c = 0; c < 2; ++c) sm_vcycle_small(s, l, l, s.U(l), s.F(l));
             }
-            __syncthreads();
+        }
+        __syncthreads();
+        for (int l = ls + 1; l <= J; ++l) {
+            sm_prolong_u<T, TeamCta>(s, l);
             for (int c = 0; c < 2; ++c) sm_vcycle(s, l, s.U(l), s.F(l));
         }
         T* const gu = g_u[J];
