@@ -191,18 +191,18 @@ bool pgb_cuda_ok(pgb_run* r, cudaError_t e, const char* what);
 /* message for pgb_last_error(NULL), from entry points without a handle */
 void pgb_set_unbound_error(const std::string& msg);
 /* Programmatic dependent launch.  A kernel launched with pgb_launch_pdl may
- * be scheduled while the previous kernel on its stream is still running;
- * its first statement is pgb_pdl_entry(), whose griddepcontrol.wait blocks
- * until that kernel has completed and its writes are visible.  No memory is
- * touched before it, so the order of results is that of plain launches.
- * The launch_dependents that follows lets the next kernel be scheduled
- * early in turn: what it saves is the launch gap, not any ordering.  On a
- * kernel launched without the attribute both instructions do nothing.    */
+ * be launched while the previous kernel on its stream finishes: as that
+ * kernel's blocks exit, the next one's are scheduled.  Its first statement
+ * is pgb_pdl_entry(), whose griddepcontrol.wait blocks until the previous
+ * kernel has completed and its writes are visible.  No memory is touched
+ * before it, so results are those of plain launches; what it saves is the
+ * launch gap.  No kernel triggers its dependents early: blocks parked at
+ * the wait would hold SM slots that other runs' streams need when many
+ * runs share the GPU (pgb_step_batch), which cost those a third of their
+ * throughput.  On a kernel launched without the attribute the wait does
+ * nothing.                                                                */
 #ifdef __CUDACC__
-__device__ __forceinline__ void pgb_pdl_entry() {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
+__device__ __forceinline__ void pgb_pdl_entry() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 template <typename... KArgs, typename... Args>
 inline cudaError_t pgb_launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
                                   Args... args) {
