@@ -499,21 +499,25 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_mcc(PushArgs a) {
 }
 
 /* ------------------------------------------------------------ scans */
-/* exclusive scan of cnt[0..m) (m read from *m_ptr or given) into off[];
- * total written to *total.  Single block; m up to a few 1e5.             */
-__device__ __forceinline__ long long block_excl_scan8(const int* cnt, int* off, long long m, long long carry0) {
-    /* exclusive scan of cnt[0..m) with 8 consecutive items per thread; returns the total */
+/* exclusive scan of cnt[0..m) into off[]; returns the total.  One block of
+ * 1024 threads, 8 consecutive items per thread and 8192 entries per pass.
+ * (32 items per thread, one pass for the bench's 16.7K tiles, measured
+ * slower: a warp's load then touches 32 lines instead of 8.)            */
+#define SCAN_ITEMS 8
+__device__ __forceinline__ long long block_excl_scan(const int* cnt, int* off, long long m, long long carry0) {
     __shared__ long long s_warp[32];
     __shared__ long long s_carry;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_carry = carry0;
     __syncthreads();
-    for (long long b = 0; b < m; b += 8 * 1024) {
-        long long i0 = b + 8 * (long long)threadIdx.x;
-        int v[8];
+    for (long long b = 0; b < m; b += SCAN_ITEMS * 1024) {
+        long long i0 = b + SCAN_ITEMS * (long long)threadIdx.x;
+        int v[SCAN_ITEMS];
         long long sum = 0;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) { v[q] = (i0 + q < m) ? cnt[i0 + q] : 0; sum += v[q]; }
+        for (int q = 0; q < SCAN_ITEMS; ++q) v[q] = (i0 + q < m) ? cnt[i0 + q] : 0;
+#pragma unroll
+        for (int q = 0; q < SCAN_ITEMS; ++q) sum += v[q];
         long long x = sum;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -534,7 +538,7 @@ __device__ __forceinline__ long long block_excl_scan8(const int* cnt, int* off, 
         __syncthreads();
         long long excl = s_carry + (warp ? s_warp[warp - 1] : 0) + x - sum;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
+        for (int q = 0; q < SCAN_ITEMS; ++q) {
             if (i0 + q < m) off[i0 + q] = (int)excl;
             excl += v[q];
         }
@@ -550,25 +554,30 @@ __global__ void __launch_bounds__(1024) k_scan_small(const int* cnt, int* off, c
     pgb_pdl_entry();
     /* n_ptr: particle count whose tiles are scanned; else m_const entries */
     const long long m = n_ptr ? (*n_ptr + PGB_TILE - 1) / PGB_TILE : m_const;
-    long long t = block_excl_scan8(cnt, off, m, 0);
+    long long t = block_excl_scan(cnt, off, m, 0);
     if (threadIdx.x == 0) *total = t;
 }
 
 /* exclusive scan of a list-length array (length read from device memory) */
 __global__ void __launch_bounds__(1024) k_scan_list(const int* cnt, int* off, const long long* m_ptr, long long* total) {
     pgb_pdl_entry();
-    long long t = block_excl_scan8(cnt, off, *m_ptr, 0);
+    long long t = block_excl_scan(cnt, off, *m_ptr, 0);
     if (threadIdx.x == 0) *total = t;
 }
 
-/* gather per-tile lists into one dense list in slot order */
+/* gather per-tile lists into one dense list in slot order.  A warp per
+ * tile: lists hold about one particle in a hundred, so a tile has a few
+ * entries, and a block walking its tiles one after another would wait on
+ * each tile's count and offset in turn.                                 */
 __global__ void k_gather_lists(const int* tl, const int* tc, const int* toff, const long long* n_ptr, int* out) {
     pgb_pdl_entry();
     const long long n = *n_ptr;
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        int c = tc[t], o = toff[t];
-        for (int k = threadIdx.x; k < c; k += blockDim.x) out[o + k] = tl[(long long)t * PGB_TILE + k];
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int t = blockIdx.x * wpb + (threadIdx.x >> 5); t < ntiles; t += gridDim.x * wpb) {
+        const int c = tc[t], o = toff[t];
+        for (int k = lane; k < c; k += 32) out[o + k] = tl[(long long)t * PGB_TILE + k];
     }
 }
 
