@@ -14,7 +14,15 @@
  * (absorb, reflect, backscatter); an exclusive scan of the secondary counts
  * gives every new electron its slot and id in list order; pass 2 writes
  * the secondaries and removes their parents.  Results therefore do not
- * depend on thread scheduling.  Event arithmetic is FP64.
+ * depend on thread scheduling.
+ *
+ * Event arithmetic (energies, angles, yields, speeds) is FP32, like the
+ * particle state it starts from; positions are placed in FP64.  A wall
+ * kernel handles a few wall hits per thread, so its time is the latency
+ * of the longest event chain, and FP64 acos/pow/exp chains made it three
+ * to four times longer.  Random numbers are the same in either precision
+ * (pgb_u01f and pgb_u01d give the same value), so every comparison with a
+ * draw sees the same draw.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -47,40 +55,49 @@ __device__ __forceinline__ void store_particle(const Species& S, long long slot,
 }
 
 /* boundary::secondary_vel (boundary.cpp:427-486) on a particle state */
-__device__ void secondary_vel_d(const WallArgs& a, pgb_stream* st, double& x, double& y, double& vx, double& vy,
-                                double& vz, double velocity, int jp, int kp) {
+__device__ void secondary_vel_f(const WallArgs& a, pgb_stream* st, double& x, double& y, float& vx, float& vy,
+                                float& vz, float velocity, int jp, int kp) {
     const double lengthX = a.dx * a.nx, lengthY = a.dy * a.ny;
+    const float two_pi = (float)(2.0 * PGB_PI);
     if (jp < 0 || jp >= a.nx) {
-        double R = pgb_u01d(pgb_stream_u32(st)), Rphi = pgb_u01d(pgb_stream_u32(st)), Rchi = pgb_u01d(pgb_stream_u32(st));
-        double chi = asin(sqrt(Rchi)), phi = 2.0 * PGB_PI * Rphi;
-        vx = fabs(velocity * cos(chi));
-        vy = velocity * sin(chi) * cos(phi);
-        vz = velocity * sin(chi) * sin(phi);
-        x = R * a.dt * fabs(vx);
-        if (jp >= a.nx) { x = lengthX - x; vx = -fabs(velocity * cos(chi)); }
+        float R = pgb_u01f(pgb_stream_u32(st)), Rphi = pgb_u01f(pgb_stream_u32(st)), Rchi = pgb_u01f(pgb_stream_u32(st));
+        float chi = asinf(sqrtf(Rchi)), phi = two_pi * Rphi;
+        float sc, cc, sp, cp;
+        sincosf(chi, &sc, &cc);
+        sincosf(phi, &sp, &cp);
+        vx = fabsf(velocity * cc);
+        vy = velocity * sc * cp;
+        vz = velocity * sc * sp;
+        x = (double)R * a.dt * fabs((double)vx);
+        if (jp >= a.nx) { x = lengthX - x; vx = -fabsf(velocity * cc); }
     }
     if (kp < 0 || kp >= a.ny) {
-        double R = pgb_u01d(pgb_stream_u32(st)), Rphi = pgb_u01d(pgb_stream_u32(st)), Rchi = pgb_u01d(pgb_stream_u32(st));
-        double chi = asin(sqrt(Rchi)), phi = 2.0 * PGB_PI * Rphi;
-        vy = fabs(velocity * cos(chi));
-        vx = velocity * sin(chi) * cos(phi);
-        vz = velocity * sin(chi) * sin(phi);
-        y = R * a.dt * fabs(vy);
-        if (kp >= a.ny) { y = lengthY - y; vy = -fabs(velocity * cos(chi)); }
+        float R = pgb_u01f(pgb_stream_u32(st)), Rphi = pgb_u01f(pgb_stream_u32(st)), Rchi = pgb_u01f(pgb_stream_u32(st));
+        float chi = asinf(sqrtf(Rchi)), phi = two_pi * Rphi;
+        float sc, cc, sp, cp;
+        sincosf(chi, &sc, &cc);
+        sincosf(phi, &sp, &cp);
+        vy = fabsf(velocity * cc);
+        vx = velocity * sc * cp;
+        vz = velocity * sc * sp;
+        y = (double)R * a.dt * fabs((double)vy);
+        if (kp >= a.ny) { y = lengthY - y; vy = -fabsf(velocity * cc); }
     }
 }
 
-__device__ __forceinline__ double see_velocity(const WallArgs& a, double R) {
-    return sqrt((2.0 * R * PGB_CHARGE * (a.threshold - 2.0 * a.work_function) / a.me));
+/* sqrt(2 R q (THRESHOLD - 2 WORK_FUNCTION) / me) (boundary.cpp:510-512, 700-702) */
+__device__ __forceinline__ float see_velocity(const WallArgs& a, float R) {
+    return sqrtf(R * (float)(2.0 * PGB_CHARGE * (a.threshold - 2.0 * a.work_function) / a.me));
 }
 
 /* --------------------------------------------------------- ion walls */
 /* i_impact_see_yield_Ar (boundary.cpp:310-317) */
-__device__ __forceinline__ double ion_yield(const WallArgs& a, double energy) {
-    if (!a.ion_see) return 0.0;
-    double y = 0.0;
-    if (energy >= 80.0)
-        y = 0.006 * energy / (1.0 + (energy / 10.0)) + 1.05e-4 * (sqrt((energy - 80.0)) / (1.0 + pow((energy / 8000.0), 1.5)));
+__device__ __forceinline__ float ion_yield(const WallArgs& a, float energy) {
+    if (!a.ion_see) return 0.0f;
+    float y = 0.0f;
+    if (energy >= 80.0f)
+        y = 0.006f * energy / (1.0f + (energy / 10.0f)) +
+            1.05e-4f * (sqrtf((energy - 80.0f)) / (1.0f + powf((energy / 8000.0f), 1.5f)));
     return y;
 }
 
@@ -90,13 +107,13 @@ __global__ void k_iwall1(WallArgs a) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
         int slot = a.list_i[k];
         float4 p = a.i.xv[slot];
-        double vx = p.z, vy = p.w, vz = a.i.vz[slot];
-        double energy = (0.5 / PGB_CHARGE) * a.mi * (vx * vx + vy * vy + vz * vz);
-        double yield = ion_yield(a, energy);
+        float vx = p.z, vy = p.w, vz = a.i.vz[slot];
+        float energy = (float)((0.5 / PGB_CHARGE) * a.mi) * (vx * vx + vy * vy + vz * vz);
+        float yield = ion_yield(a, energy);
         pgb_stream st;
         pgb_stream_init(&st, a.seed, a.i.id[slot], (unsigned int)a.ds->t, PGB_STREAM_IWALL, 1);
-        double R = pgb_u01d(pgb_stream_u32(&st));
-        a.aux[k] = (R < yield) ? (int)floor(yield) + 1 : 0;
+        float R = pgb_u01f(pgb_stream_u32(&st));
+        a.aux[k] = (R < yield) ? (int)floorf(yield) + 1 : 0;
     }
 }
 
@@ -120,33 +137,41 @@ __global__ void k_iwall2(WallArgs a) {
                 unsigned int id = id0 + (unsigned int)(a.off[k] + j);
                 pgb_stream st;
                 pgb_stream_init(&st, a.seed, id, (unsigned int)a.ds->t, PGB_STREAM_SEE, 0);
-                double x = 0.0, y = 0.0, vx = 0.0, vy = 0.0, vz = 0.0, ww = 1.0;
+                double x = 0.0, y = 0.0;
+                float vx = 0.0f, vy = 0.0f, vz = 0.0f, ww = 1.0f;
+                const float two_pi = (float)(2.0 * PGB_PI);
                 if (jp < 0 || jp >= a.nx) {
-                    double R = pgb_u01d(pgb_stream_u32(&st));
-                    double velocity = see_velocity(a, R);
-                    double Rphi = pgb_u01d(pgb_stream_u32(&st)), Rchi = pgb_u01d(pgb_stream_u32(&st));
-                    double chi = asin(sqrt(Rchi)), phi = 2.0 * PGB_PI * Rphi;
-                    vx = fabs(velocity * cos(chi));
-                    vy = velocity * sin(chi) * cos(phi);
-                    vz = velocity * sin(chi) * sin(phi);
-                    ww = w;
-                    x = R * a.dt * fabs(vx);
-                    if (jp >= a.nx) { x = lengthX - x; vx = -fabs(velocity * cos(chi)); }
+                    float R = pgb_u01f(pgb_stream_u32(&st));
+                    float velocity = see_velocity(a, R);
+                    float Rphi = pgb_u01f(pgb_stream_u32(&st)), Rchi = pgb_u01f(pgb_stream_u32(&st));
+                    float chi = asinf(sqrtf(Rchi)), phi = two_pi * Rphi;
+                    float sc, cc, sp, cp;
+                    sincosf(chi, &sc, &cc);
+                    sincosf(phi, &sp, &cp);
+                    vx = fabsf(velocity * cc);
+                    vy = velocity * sc * cp;
+                    vz = velocity * sc * sp;
+                    ww = (float)w;
+                    x = (double)R * a.dt * fabs((double)vx);
+                    if (jp >= a.nx) { x = lengthX - x; vx = -fabsf(velocity * cc); }
                 }
                 if (kp < 0 || kp >= a.ny) {
-                    double R = pgb_u01d(pgb_stream_u32(&st));
-                    double velocity = see_velocity(a, R);
-                    double Rphi = pgb_u01d(pgb_stream_u32(&st)), Rchi = pgb_u01d(pgb_stream_u32(&st));
-                    double chi = asin(sqrt(Rchi)), phi = 2.0 * PGB_PI * Rphi;
-                    vy = fabs(velocity * cos(chi));
-                    vx = velocity * sin(chi) * cos(phi);
-                    vz = velocity * sin(chi) * sin(phi);
-                    ww = w;
-                    y = R * a.dt * fabs(vy);
-                    if (kp >= a.ny) { y = lengthY - y; vy = -fabs(velocity * cos(chi)); }
+                    float R = pgb_u01f(pgb_stream_u32(&st));
+                    float velocity = see_velocity(a, R);
+                    float Rphi = pgb_u01f(pgb_stream_u32(&st)), Rchi = pgb_u01f(pgb_stream_u32(&st));
+                    float chi = asinf(sqrtf(Rchi)), phi = two_pi * Rphi;
+                    float sc, cc, sp, cp;
+                    sincosf(chi, &sc, &cc);
+                    sincosf(phi, &sp, &cp);
+                    vy = fabsf(velocity * cc);
+                    vx = velocity * sc * cp;
+                    vz = velocity * sc * sp;
+                    ww = (float)w;
+                    y = (double)R * a.dt * fabs((double)vy);
+                    if (kp >= a.ny) { y = lengthY - y; vy = -fabsf(velocity * cc); }
                 }
                 store_particle(a.e, es, x, y, vx, vy, vz, a.dx, a.dy);
-                a.e.w[es] = (float)ww;
+                a.e.w[es] = ww;
                 a.e.id[es] = id;
                 float4 q = a.e.xv[es];
                 maybe_deposit(a.qacc_e, a.nx, a.ny, q.x, q.y, (float)ww);
@@ -157,53 +182,54 @@ __global__ void k_iwall2(WallArgs a) {
 }
 
 /* ---------------------------------------------------- electron walls */
-struct WallState { double energy, angleX, angleY; int onX; };
-
+struct WallState { float energy, angleX, angleY; int onX; };
 /* e_impact_see_yield_v (boundary.cpp:281-300) */
-__device__ __forceinline__ double e_yield(const WallArgs& a, const WallState& w) {
-    if (!a.e_see) return 0.0;
-    double twoPi = 2.0 * PGB_PI;
-    double v = (w.energy - a.e0) / (a.emax0 - a.e0);
-    double k = (v > 1) ? 0.25 : 0.62;
-    double ang = w.onX ? w.angleX : w.angleY;
-    double ww = (w.energy - a.e0) / (a.emax0 * (1.0 + k * (ang * ang / twoPi)) - a.e0);
-    return a.max_yield * (1.0 + k * (ang * ang / twoPi)) * pow((ww * exp((1.0 - ww))), k);
+__device__ __forceinline__ float e_yield(const WallArgs& a, const WallState& w) {
+    if (!a.e_see) return 0.0f;
+    const float twoPi = (float)(2.0 * PGB_PI);
+    const float e0 = (float)a.e0, emax0 = (float)a.emax0;
+    float v = (w.energy - e0) / (emax0 - e0);
+    float k = (v > 1.0f) ? 0.25f : 0.62f;
+    float ang = w.onX ? w.angleX : w.angleY;
+    float ww = (w.energy - e0) / (emax0 * (1.0f + k * (ang * ang / twoPi)) - e0);
+    return (float)a.max_yield * (1.0f + k * (ang * ang / twoPi)) * powf((ww * expf((1.0f - ww))), k);
 }
 
 /* outcome codes of one electron wall interaction */
 enum { EW_STAY = 0, EW_ABSORB = 1, EW_SEE = 2, EW_RETRY = -1 };
 
-__device__ int e_wall_event(const WallArgs& a, pgb_stream* st, double& x, double& y, double& vx, double& vy,
-                            double& vz, int jp, int kp, int& nsec, int& kind) {
+__device__ int e_wall_event(const WallArgs& a, pgb_stream* st, double& x, double& y, float& vx, float& vy,
+                            float& vz, int jp, int kp, int& nsec, int& kind) {
     const double lengthX = a.dx * a.nx, lengthY = a.dy * a.ny;
+    const float me = (float)a.me;
     WallState w;
     w.onX = (jp < 0 || jp >= a.nx);
-    double u2 = vx * vx + vy * vy + vz * vz;
-    w.energy = (0.5 / PGB_CHARGE) * a.me * u2;
-    double uu = 2.0 * w.energy / a.me;
-    w.angleX = acos(vx / (sqrt(uu) + 1.0e-6));
-    w.angleY = acos(vy / (sqrt(uu) + 1.0e-6));
-    double yield = e_yield(a, w);
-    double R = pgb_u01d(pgb_stream_u32(st));
+    float u2 = vx * vx + vy * vy + vz * vz;
+    w.energy = (float)((0.5 / PGB_CHARGE) * a.me) * u2;
+    float uu = 2.0f * w.energy / me;
+    w.angleX = acosf(vx / (sqrtf(uu) + 1.0e-6f));
+    w.angleY = acosf(vy / (sqrtf(uu) + 1.0e-6f));
+    float yield = e_yield(a, w);
+    float R = pgb_u01f(pgb_stream_u32(st));
     if (R < yield) {
-        double refl = (a.refl && w.energy > 50.0) ? 0.1 * yield : 0.0;
-        double back = (a.back && w.energy > 50.0) ? 0.1 * yield : 0.0;
-        int no_inject = (int)floor(fabs((yield - refl - back))) + 1;
-        const double offset = 1.0e-6;
-        R = pgb_u01d(pgb_stream_u32(st));
+        float refl = (a.refl && w.energy > 50.0f) ? 0.1f * yield : 0.0f;
+        float back = (a.back && w.energy > 50.0f) ? 0.1f * yield : 0.0f;
+        int no_inject = (int)floorf(fabsf((yield - refl - back))) + 1;
+        const float offset = 1.0e-6f;
+        R = pgb_u01f(pgb_stream_u32(st));
         if (R < refl / (yield + offset)) {
             /* reflect_electron (boundary.cpp:374-417) */
             double Rr = pgb_u01d(pgb_stream_u32(st));
-            if (jp >= a.nx) { vx = -vx; x = lengthX - Rr * a.dt * fabs(vx); }
-            else if (jp < 0) { vx = -vx; x = Rr * a.dt * fabs(vx); }
-            if (kp >= a.ny) { vy = -vy; y = lengthY - Rr * a.dt * fabs(vy); }
-            else if (kp < 0) { vy = -vy; y = Rr * a.dt * fabs(vy); }
+            if (jp >= a.nx) { vx = -vx; x = lengthX - Rr * a.dt * fabs((double)vx); }
+            else if (jp < 0) { vx = -vx; x = Rr * a.dt * fabs((double)vx); }
+            if (kp >= a.ny) { vy = -vy; y = lengthY - Rr * a.dt * fabs((double)vy); }
+            else if (kp < 0) { vy = -vy; y = Rr * a.dt * fabs((double)vy); }
             kind = ST_REFL;
             return EW_STAY;
         } else if (R > refl / yield && R < (refl + back) / (yield + offset)) {
-            double R3 = (double)(pgb_stream_u32(st) % 10000u) / 10000.0;
-            double velocity = R3 * sqrt((2.0 * PGB_CHARGE * w.energy) / a.me);
-            secondary_vel_d(a, st, x, y, vx, vy, vz, velocity, jp, kp);
+            float R3 = (float)(pgb_stream_u32(st) % 10000u) / 10000.0f;
+            float velocity = R3 * sqrtf((float)(2.0 * PGB_CHARGE / a.me) * w.energy);
+            secondary_vel_f(a, st, x, y, vx, vy, vz, velocity, jp, kp);
             kind = ST_BACK;
             return EW_STAY;
         } else if (R > (refl + back) / (yield + offset)) {
@@ -222,7 +248,8 @@ __global__ void k_ewall1(WallArgs a) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
         int slot = a.list_e[k];
         float4 p = a.e.xv[slot];
-        double x = (double)p.x * a.dx, y = (double)p.y * a.dy, vx = p.z, vy = p.w, vz = a.e.vz[slot];
+        double x = (double)p.x * a.dx, y = (double)p.y * a.dy;
+        float vx = p.z, vy = p.w, vz = a.e.vz[slot];
         pgb_stream st;
         pgb_stream_init(&st, a.seed, a.e.id[slot], (unsigned int)a.ds->t, PGB_STREAM_EWALL, 0);
         int res = EW_RETRY, nsec = 0, kind = 0;
@@ -274,17 +301,18 @@ __global__ void k_ewall2(WallArgs a) {
             long long es = ne0 + a.off[k] + j;
             if (es >= a.e.cap) { atomicOr(&a.ds->err, ERR_CAP_E); break; }
             unsigned int id = id0 + (unsigned int)(a.off[k] + j);
-            double x = 0.0, y = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+            double x = 0.0, y = 0.0;
+            float vx = 0.0f, vy = 0.0f, vz = 0.0f;
             if (jpp < 0 || jpp >= a.nx) x = px;
             else y = py;
             pgb_stream st;
             pgb_stream_init(&st, a.seed, id, (unsigned int)a.ds->t, PGB_STREAM_SEE, 0);
-            double R = pgb_u01d(pgb_stream_u32(&st));
-            double velocity = see_velocity(a, R);
+            float R = pgb_u01f(pgb_stream_u32(&st));
+            float velocity = see_velocity(a, R);
             /* the new electron sits at the parent's x (left/right wall) or y */
             int jp = (jpp < 0 || jpp >= a.nx) ? jpp : 0;
             int kp = (jpp < 0 || jpp >= a.nx) ? 0 : cellf(p.y);
-            secondary_vel_d(a, &st, x, y, vx, vy, vz, velocity, jp, kp);
+            secondary_vel_f(a, &st, x, y, vx, vy, vz, velocity, jp, kp);
             store_particle(a.e, es, x, y, vx, vy, vz, a.dx, a.dy);
             a.e.w[es] = w;
             a.e.id[es] = id;
