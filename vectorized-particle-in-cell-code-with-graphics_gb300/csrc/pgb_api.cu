@@ -166,6 +166,7 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
          * work (pgb_step_async): drain the run's streams first          */
         PGB_CK(r, cudaStreamSynchronize(r->stream));
         PGB_CK(r, cudaStreamSynchronize(r->copy_stream));
+        if (r->side) PGB_CK(r, cudaStreamSynchronize(r->side));
         drop_graphs(r);
     }
     if (need > S.cap) {
@@ -296,6 +297,15 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
             return bail(PGB_ERR_CUDA);
         }
     r->copy_ev_ok = true;
+    /* the side stream only speeds steps up: without it steps run in turn */
+    if (cudaStreamCreateWithFlags(&r->side, cudaStreamNonBlocking) == cudaSuccess) {
+        if (cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming) == cudaSuccess) {
+            if (cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming) == cudaSuccess) r->side_ok = true;
+            else cudaEventDestroy(r->ev_fork);
+        }
+        if (!r->side_ok) { cudaStreamDestroy(r->side); r->side = nullptr; }
+    }
+    cudaGetLastError();
     const size_t G = (size_t)r->nx * r->ny, GE = (size_t)(r->nx + 1) * (r->ny + 1);
     bool ok = true;
     ok = ok && cudaMalloc(&r->ds, sizeof(DevState)) == cudaSuccess;
@@ -372,6 +382,7 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
 extern "C" int pgb_destroy(pgb_run* r) {
     if (!r) return 0;
     if (r->stream) cudaStreamSynchronize(r->stream);
+    if (r->side) cudaStreamSynchronize(r->side);
     drop_graphs(r);
     cudaFree(r->phi_tab);
     if (r->phi_host) cudaFreeHost(r->phi_host);
@@ -400,6 +411,8 @@ extern "C" int pgb_destroy(pgb_run* r) {
         for (int k = 0; k < 12; ++k) cudaEventDestroy(r->prof_ev[k]);
     if (r->copy_ev_ok)
         for (int k = 0; k < PGB_COPY_EVENTS; ++k) cudaEventDestroy(r->copy_ev[k]);
+    if (r->side_ok) { cudaEventDestroy(r->ev_fork); cudaEventDestroy(r->ev_join); }
+    if (r->side) cudaStreamDestroy(r->side);
     if (r->copy_stream) cudaStreamDestroy(r->copy_stream);
     if (r->stream) cudaStreamDestroy(r->stream);
     delete r;
@@ -560,6 +573,7 @@ static int set_device_step(pgb_run* r, int64_t t0, int n) {
     PGB_CK(r, cudaMemcpyAsync(r->phi_tab, r->phi_host, sizeof(double) * n, cudaMemcpyHostToDevice, r->stream));
     PGB_CK(r, cudaMemcpyAsync(&r->ds->t, r->t_host, sizeof(long long), cudaMemcpyHostToDevice, r->stream));
     PGB_CK(r, cudaMemcpyAsync(&r->ds->t_base, r->t_host, sizeof(long long), cudaMemcpyHostToDevice, r->stream));
+    PGB_CK(r, cudaMemcpyAsync(&r->ds->tf, r->t_host, sizeof(long long), cudaMemcpyHostToDevice, r->stream));
     PGB_CK(r, cudaEventRecord(r->phi_ev, r->stream));
     return 0;
 }
@@ -685,22 +699,42 @@ extern "C" int pgb_efield(pgb_run* r) {
 #define PROF_MARK(r, k) \
     do { if ((r)->prof_on) PGB_CK((r), cudaEventRecord((r)->prof_ev[k], (r)->stream)); } while (0)
 
-/* one pic_run iteration; the device step counter ds->t selects the random
- * streams and the right-wall potential, so the same launches can be
- * replayed as a CUDA graph for every step                               */
-static int step_once(pgb_run* r, bool ion_step) {
+/* One pic_run iteration in three parts.  The device counters ds->t
+ * (particle phases) and ds->tf (field solve) select the random streams
+ * and the right-wall potential, so the same launches can be replayed as
+ * CUDA graphs for every step.
+ *   step_mcc:       e_collisions::collision (pic.cpp:1071-1075): collision
+ *                   tests, scattering and the list of ionization events;
+ *                   reads no field
+ *   step_particles: charge reset, electron push and deposit, ionization
+ *                   products, injection,
+ *                   ion charge exchange and push, walls, population control
+ *                   (pic.cpp:1080-1141), then ds->t += 1
+ *   step_fields:    charge finalisation, grid_rho, grid_potential,
+ *                   grid_electric_field (pic.cpp:1143-1161), then ds->tf += 1
+ * Run in this order they are the reference's step.  The collisions of step
+ * t+1 need the particles after step t's walls, not step t's fields, so the
+ * pipelined path (issue_one_step) runs them while step t's field solve is
+ * still in flight on the run's side stream.                              */
+static int step_mcc(pgb_run* r, bool) {
+    if (!r->p.have_collisions) return 0;
+    if (pgb_launch_mcc_q(r) || pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
+    return 0;
+}
+
+static int step_particles(pgb_run* r, bool ion_step) {
     const bool coll = r->p.have_collisions != 0;
     const size_t G = (size_t)r->nx * r->ny;
     PGB_CK(r, cudaMemsetAsync(r->qacc[0], 0, sizeof(unsigned long long) * G, r->stream));
     PGB_CK(r, cudaMemsetAsync(r->qacc[1], 0, sizeof(unsigned long long) * G, r->stream));
-    /* e_collisions::collision + get_particle_electric_field + move_particles */
-    PROF_MARK(r, 0);
-    if (pgb_launch_push(r, 0, coll, true, coll)) return PGB_ERR_CUDA;
+    /* get_particle_electric_field + move_particles, charge deposit */
+    if (pgb_launch_push(r, 0, false, true, false)) return PGB_ERR_CUDA;
     PROF_MARK(r, 7);
     if (pgb_build_list(r, LIST_OUT_E, 0)) return PGB_ERR_CUDA;
     PROF_MARK(r, 1);
     if (coll) {
-        if (pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
+        /* the ionization products join after the push: an ion takes its
+         * parent electron's new position                                */
         int store_e = r->p.steadystate ? 1 : 0;
         int store_i = (r->p.steadystate || !ion_step) ? 1 : 0;
         if (pgb_launch_ionize_appends(r, store_e, store_i)) return PGB_ERR_CUDA;
@@ -740,12 +774,24 @@ static int step_once(pgb_run* r, bool ion_step) {
             }
         }
     }
+    return pgb_launch_step_advance(r);
+}
+
+static int step_fields(pgb_run* r, bool) {
     /* collect_charge edge doubling, grid_rho, grid_potential, grid_electric_field */
     PROF_MARK(r, 5);
     if (pgb_launch_finalize(r, 3, true)) return PGB_ERR_CUDA;
     if (pgb_poisson_solve(r)) return PGB_ERR_CUDA;
     if (pgb_launch_efield(r, 1)) return PGB_ERR_CUDA;
     PROF_MARK(r, 6);
+    return 0;
+}
+
+static int step_once(pgb_run* r, bool ion_step) {
+    PROF_MARK(r, 0);
+    int rc;
+    if ((rc = step_mcc(r, ion_step)) || (rc = step_particles(r, ion_step)) || (rc = step_fields(r, ion_step)))
+        return rc;
     return 0;
 }
 
@@ -767,8 +813,12 @@ static int profile_collect(pgb_run* r) {
 }
 
 static void drop_graphs(pgb_run* r) {
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < 8; ++k) {
         if (r->graph[k]) { cudaGraphExecDestroy(r->graph[k]); r->graph[k] = nullptr; }
+        if (r->graph_a[k]) { cudaGraphExecDestroy(r->graph_a[k]); r->graph_a[k] = nullptr; }
+        if (r->graph_b[k]) { cudaGraphExecDestroy(r->graph_b[k]); r->graph_b[k] = nullptr; }
+    }
+    if (r->graph_f) { cudaGraphExecDestroy(r->graph_f); r->graph_f = nullptr; }
 }
 
 /* graphs are usable when no step needs a host decision: no profiling and
@@ -779,43 +829,85 @@ static bool graphs_ok(pgb_run* r) {
     return true;
 }
 
-static int launch_step(pgb_run* r, bool ion_step) {
-    if (!graphs_ok(r)) return step_once(r, ion_step);
-    int key = (ion_step ? 4 : 0) | (r->orient[0] << 1) | r->orient[1];
-    if (!r->graph[key]) {
-        cudaGraph_t g = nullptr;
-        PGB_CK(r, cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
-        long long l0 = r->launches;
-        int rc = step_once(r, ion_step);
-        cudaError_t e = cudaStreamEndCapture(r->stream, &g);
-        if (rc || e != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            cudaGetLastError();
-            r->use_graphs = 0;   /* run the launches directly from now on */
-            r->launches = l0;
-            return step_once(r, ion_step);
-        }
-        r->graph_launches[key] = r->launches - l0;
+/* capture fn(r, ion_step) as a graph; -1 if the launches cannot be captured */
+static int capture(pgb_run* r, int (*fn)(pgb_run*, bool), bool ion_step, cudaGraphExec_t* out, long long* nl) {
+    cudaGraph_t g = nullptr;
+    PGB_CK(r, cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
+    long long l0 = r->launches;
+    int rc = fn(r, ion_step);
+    cudaError_t e = cudaStreamEndCapture(r->stream, &g);
+    if (rc || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
         r->launches = l0;
-        e = cudaGraphInstantiate(&r->graph[key], g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            r->graph[key] = nullptr;
-            r->use_graphs = 0;
-            return step_once(r, ion_step);
-        }
+        return -1;
     }
-    PGB_CK(r, cudaGraphLaunch(r->graph[key], r->stream));
-    r->launches += r->graph_launches[key];
+    *nl = r->launches - l0;
+    r->launches = l0;
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return -1;
+    }
     return 0;
 }
 
+/* run fn as graph *slot (captured on first use), or launch it directly
+ * when graphs are off or cannot be captured                            */
+static int replay(pgb_run* r, int (*fn)(pgb_run*, bool), bool ion_step, cudaGraphExec_t* slot, long long* nl) {
+    if (graphs_ok(r) && !*slot && capture(r, fn, ion_step, slot, nl)) r->use_graphs = 0;
+    if (!*slot || !graphs_ok(r)) return fn(r, ion_step);
+    PGB_CK(r, cudaGraphLaunch(*slot, r->stream));
+    r->launches += *nl;
+    return 0;
+}
+
+static int graph_key(pgb_run* r, bool ion_step) { return (ion_step ? 4 : 0) | (r->orient[0] << 1) | r->orient[1]; }
+
+static int launch_step(pgb_run* r, bool ion_step) {
+    const int key = graph_key(r, ion_step);
+    return replay(r, step_once, ion_step, &r->graph[key], &r->graph_launches[key]);
+}
+
+/* the field solve of the last step issued, if it is still to be issued */
+static int flush_fields(pgb_run* r) {
+    if (!r->fields_pending) return 0;
+    r->fields_pending = false;
+    return replay(r, step_fields, false, &r->graph_f, &r->graph_f_launches);
+}
+
+/* pipelining needs collisions to overlap and graphs to replay the parts */
+static bool pipelined(pgb_run* r) { return r->side_ok && r->p.have_collisions && r->use_graphs && graphs_ok(r); }
+
 /* queue step r->time_step of r: host decisions (spatial sort or compaction),
- * then the step's launches or graph; the host does not wait (except for
- * profiling and for a population check that may trigger a reduction)     */
+ * then the step's launches or graphs; the host does not wait (except for
+ * profiling and for a population check that may trigger a reduction).
+ * Pipelined, the previous step's field solve (graph F) runs on the side
+ * stream while this step's collisions (graph A) run on the run's stream;
+ * the rest of the step (graph B) waits for both, and this step's field
+ * solve is left pending.                                                */
 static int issue_one_step(pgb_run* r) {
     int rc;
+    const bool pipe = pipelined(r);
+    bool forked = false;
+    if (r->fields_pending) {
+        if (pipe && !r->graph_f &&
+            capture(r, step_fields, false, &r->graph_f, &r->graph_f_launches))
+            r->use_graphs = 0;
+        if (pipe && r->graph_f && pipelined(r)) {
+            PGB_CK(r, cudaEventRecord(r->ev_fork, r->stream));
+            PGB_CK(r, cudaStreamWaitEvent(r->side, r->ev_fork, 0));
+            PGB_CK(r, cudaGraphLaunch(r->graph_f, r->side));
+            r->launches += r->graph_f_launches;
+            PGB_CK(r, cudaEventRecord(r->ev_join, r->side));
+            r->fields_pending = false;
+            forked = true;
+        } else if ((rc = flush_fields(r))) {
+            return rc;
+        }
+    }
     if (r->p.sort_interval > 0) {
         /* spatial sort (drops tombstones too) every sort_interval steps */
         if (r->time_step % r->p.sort_interval == 0)
@@ -848,12 +940,21 @@ static int issue_one_step(pgb_run* r) {
         r->prof.slots_i += r->hs->n[1];
     }
     const bool ion_step = (r->time_step % r->dt_dti) == 0;
-    if ((rc = launch_step(r, ion_step))) return rc;
-    if (r->prof_on && (rc = profile_collect(r))) return rc;
+    if (pipe || forked) {
+        const int key = graph_key(r, ion_step);
+        if ((rc = replay(r, step_mcc, ion_step, &r->graph_a[key], &r->graph_a_launches[key]))) return rc;
+        if (forked) PGB_CK(r, cudaStreamWaitEvent(r->stream, r->ev_join, 0));
+        if ((rc = replay(r, step_particles, ion_step, &r->graph_b[key], &r->graph_b_launches[key])))
+            return rc;
+        r->fields_pending = true;
+    } else {
+        if ((rc = launch_step(r, ion_step))) return rc;
+        if (r->prof_on && (rc = profile_collect(r))) return rc;
+    }
     /* the graphs class sums after the field solve (pic.cpp:1189-1207) */
-    if (r->gr.on && r->time_step >= r->gr.g.start_step && r->time_step < r->gr.g.end_step &&
-        (rc = pgb_launch_graphs(r)))
-        return rc;
+    if (r->gr.on && r->time_step >= r->gr.g.start_step && r->time_step < r->gr.g.end_step) {
+        if ((rc = flush_fields(r)) || (rc = pgb_launch_graphs(r))) return rc;
+    }
     r->time_step += 1;
     /* counters come back asynchronously; the host reads them only to
      * decide when to compact, which never changes results          */
@@ -871,6 +972,7 @@ extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
         if ((rc = set_device_step(r, r->time_step, chunk))) return rc;
         for (int k = 0; k < chunk; ++k)
             if ((rc = issue_one_step(r))) return rc;
+        if ((rc = flush_fields(r))) return rc;
         done += chunk;
     }
     return sync_state(r);
@@ -886,6 +988,7 @@ extern "C" int pgb_step_async(pgb_run* r, int32_t nsteps) {
         if ((rc = set_device_step(r, r->time_step, chunk))) return rc;
         for (int k = 0; k < chunk; ++k)
             if ((rc = issue_one_step(r))) return rc;
+        if ((rc = flush_fields(r))) return rc;
         done += chunk;
     }
     return 0;
@@ -927,6 +1030,10 @@ extern "C" int pgb_step_batch(pgb_run* const* runs, int32_t nruns, int32_t nstep
                 int rc = issue_one_step(runs[a]);
                 if (rc) return rc;
             }
+        for (int a = 0; a < nruns; ++a) {
+            int rc = flush_fields(runs[a]);
+            if (rc) return rc;
+        }
         done += chunk;
     }
     int first = 0;

@@ -59,7 +59,7 @@ __device__ __forceinline__ double rhs_node(double rho, int i, int j, const Final
 __global__ void k_finalize(FinalizeArgs a) {
     pgb_pdl_entry();
     const int G = a.nx * a.ny;
-    const double phirx = a.phi_tab[a.ds->t - a.ds->t_base];
+    const double phirx = a.phi_tab[a.ds->tf - a.ds->t_base];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x) {
         int j = k / a.nx, i = k - j * a.nx;
         double ef = edge_factor(i, j, a.nx, a.ny);
@@ -77,7 +77,7 @@ __global__ void k_finalize(FinalizeArgs a) {
 __global__ void k_rhs(FinalizeArgs a) {
     pgb_pdl_entry();
     const int G = a.nx * a.ny;
-    const double phirx = a.phi_tab[a.ds->t - a.ds->t_base];
+    const double phirx = a.phi_tab[a.ds->tf - a.ds->t_base];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x) {
         int j = k / a.nx, i = k - j * a.nx;
         a.f[k] = rhs_node(a.rho[k], i, j, a, phirx);
@@ -459,8 +459,8 @@ __device__ __forceinline__ double ey_interior(const double* phi, int nx, int ny,
 __global__ void k_efield(const double* phi, double* Ex, double* Ey, float2* exy, int nx, int ny, double twoDX,
                          DevState* ds, int advance) {
     pgb_pdl_entry();
-    /* the last kernel of a step moves the device step counter on */
-    if (advance && blockIdx.x == 0 && threadIdx.x == 0) ds->t += 1;
+    /* the last kernel of a field solve moves the field step counter on */
+    if (advance && blockIdx.x == 0 && threadIdx.x == 0) ds->tf += 1;
     const int GE = (nx + 1) * (ny + 1);
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < GE; k += gridDim.x * blockDim.x) {
         double ex = 0.0, ey = 0.0;
@@ -482,7 +482,7 @@ __global__ void k_efield(const double* phi, double* Ex, double* Ey, float2* exy,
 __global__ void k_walls(double* phi, int nx, int ny, double phi0x, const double* phi_tab, const DevState* ds,
                         double phi0y, double phily) {
     pgb_pdl_entry();
-    const double phirx = phi_tab[ds->t - ds->t_base];
+    const double phirx = phi_tab[ds->tf - ds->t_base];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx * ny; k += gridDim.x * blockDim.x) {
         int j = k / nx, i = k - j * nx;
         /* fields.cpp:209-219: columns first, then rows overwrite the corners */

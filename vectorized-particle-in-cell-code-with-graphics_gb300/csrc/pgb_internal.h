@@ -53,12 +53,15 @@ struct DevState {
     long long stats[ST_COUNT];
     int err;
     int pad1;
-    long long t;             /* the reference's time_step of the step being run */
+    long long t;             /* the reference's time_step of the particle phases being run */
     long long sorted_tiles[2];  /* tiles covered by bin pieces (0 = unsorted)   */
     int n_pieces[2];
     long long t_base;        /* step of phi_tab[0]                              */
     int sort_overflow;       /* the padded bin layout did not fit: the sort copies in place order */
     int pad2;
+    long long tf;            /* time_step of the field solve being run (its right-wall
+                                potential); trails t while a solve overlaps the next
+                                step's collisions                                      */
 };
 
 /* dense event lists (ordered by slot) */
@@ -141,6 +144,15 @@ struct pgb_run {
     int orient[2] = {0, 0};                /* which particle buffer is live   */
     long long graph_launches[8] = {};      /* kernels in each graph           */
     int use_graphs = 1;
+    /* pipelined steps: graph A (collisions) and B (the other particle
+     * phases) per key as above, graph F (field solve); F of step t runs on
+     * the side stream while A of step t+1 runs on the run's stream        */
+    cudaGraphExec_t graph_a[8] = {}, graph_b[8] = {}, graph_f = nullptr;
+    long long graph_a_launches[8] = {}, graph_b_launches[8] = {}, graph_f_launches = 0;
+    bool fields_pending = false;           /* last step's field solve not yet issued */
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork, ev_join;
+    bool side_ok = false;
     float* cx_p = nullptr;                 /* per-ion CX probability          */
     float* cx_tile_sum = nullptr;          /* [column][tile] (int64)          */
     long long cx_tiles_cap = 0;
@@ -248,6 +260,8 @@ int pgb_launch_sort(pgb_run* r, int s);
 int pgb_sort_setup(pgb_run* r);
 void pgb_bins(pgb_run* r, int* nbx, int* nby);
 int pgb_launch_reduce(pgb_run* r, int s);
+int pgb_launch_mcc_q(pgb_run* r);
+int pgb_launch_step_advance(pgb_run* r);
 int pgb_launch_graphs(pgb_run* r);
 int pgb_poisson_solve(pgb_run* r);
 int pgb_launch_efield(pgb_run* r, int advance);

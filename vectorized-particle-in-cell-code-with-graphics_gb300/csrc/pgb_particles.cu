@@ -498,6 +498,90 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_mcc(PushArgs a) {
     flush_stats(st_loc, a.ds->stats);
 }
 
+/* e_collisions::collision (e_collisions.cpp:480-597) as a pass of its own,
+ * the first of a step: collision tests, the tile's scatterings queued so
+ * that full warps run them, ionization of the parent electrons, and the
+ * ordered list of ionization events.  It reads no field, so it can run
+ * while the previous step's field solve is still in flight.              */
+__global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_mcc_q(PushArgs a) {
+    pgb_pdl_entry();
+    __shared__ ScatterQueue q;
+    if (threadIdx.x == 0) q.n = 0;
+    __syncthreads();
+    const long long n = a.ds->n[0];
+    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    const unsigned step = (unsigned)a.ds->t;
+    int st_loc[2] = {0, 0};
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long base = (long long)tile * PGB_TILE;
+        int code[PGB_ITEMS];
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            code[k] = -1;
+            long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+            if (i >= n) continue;
+            const float4 p = a.xv[i];
+            if (is_dead(p.x)) continue;
+            const float vz = a.vz[i];
+            const unsigned int id = a.id[i];
+            float energy;
+            pgb_stream st;
+            int ev = mcc_test(a.cc, id, step, a.pc.nx, a.pc.ny, p, vz, &energy, &st);
+            if (ev & MCC_SCATTER) {
+                st_loc[0] += 1;
+                int slot = atomicAdd(&q.n, 1);
+                q.v[slot] = make_float4(p.z, p.w, vz, energy);
+                q.id[slot] = id;
+                ev |= (slot + 1) << 2;
+            }
+            code[k] = ev;
+        }
+        __syncthreads();
+        const int qn = q.n;
+        for (int e = threadIdx.x; e < qn; e += blockDim.x) {
+            float4 v = q.v[e];
+            pgb_stream st;
+            pgb_stream_init(&st, a.cc.seed, q.id[e], step, PGB_STREAM_EMCC, 0);
+            (void)pgb_stream_u32(&st);   /* the collision test's draw */
+            scatter_f32(&st, a.neut, a.cc.n_neutral, v.w, (float)a.cc.reduced_mass, v.x, v.y, v.z);
+            q.v[e] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) q.n = 0;   /* read again only after the list barriers */
+        bool f[1][PGB_ITEMS];
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            f[0][k] = false;
+            if (code[k] <= 0) continue;
+            long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+            float4 p = a.xv[i];
+            float vz = a.vz[i];
+            int slot = (code[k] >> 2) - 1;
+            if (slot >= 0) {
+                float4 v = q.v[slot];
+                p.z = v.x; p.w = v.y; vz = v.z;
+            }
+            if (code[k] & MCC_IONIZE) {
+                mcc_ionize(a.cc, a.neut, a.id[i], step, p, vz);
+                st_loc[1] += 1;
+                f[0][k] = true;
+            }
+            a.xv[i] = p;
+            a.vz[i] = vz;
+        }
+        int* const tla[1] = {a.tl_ev};
+        int* const tca[1] = {a.tc_ev};
+        tile_lists<1>(f, base, tile, tla, tca);
+    }
+    flush_stats(st_loc, a.ds->stats);
+}
+
+/* the last kernel of a step's particle phases moves the step counter on */
+__global__ void k_step_advance(DevState* ds) {
+    pgb_pdl_entry();
+    ds->t += 1;
+}
+
 /* ------------------------------------------------------------ scans */
 /* exclusive scan of cnt[0..m) into off[]; returns the total.  One block of
  * 1024 threads, 8 consecutive items per thread and 8192 entries per pass.
@@ -934,6 +1018,19 @@ int pgb_launch_flag_outside(pgb_run* r, int s) {
                                                                r->tile_list[l], r->tile_cnt[l]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_mcc_q(pgb_run* r) {
+    PushArgs a = push_args(r, 0);
+    PGB_CK(r, pgb_launch_pdl(k_mcc_q, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, a));
+    r->launches++;
+    return 0;
+}
+
+int pgb_launch_step_advance(pgb_run* r) {
+    PGB_CK(r, pgb_launch_pdl(k_step_advance, dim3(1), dim3(1), 0, r->stream, r->ds));
+    r->launches++;
     return 0;
 }
 
