@@ -43,7 +43,7 @@ sys.path.insert(0, PKG)
 
 N_PER_SPECIES = 16 * 1024 * 1024
 GRID_NODES = 513
-ALG_BYTES = 44          # per particle slot: read x,y,vx,vy,vz,w,id (28 B) + write x,y,vx,vy (16 B)
+ALG_BYTES = 36          # electron push, per slot: read x,y,vx,vy,w (20 B) + write x,y,vx,vy (16 B); B = 0, so no vz
 METRIC = "particle-steps/s"
 
 
@@ -545,10 +545,11 @@ def main():
     tr = ncu_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": (tr or {}).get("bytes_per_launch_scaled"), "kernel": "k_push<MCC,DEP,FLAG> (electrons)",
+                "traffic": (tr or {}).get("bytes_per_launch_scaled"), "kernel": "k_push<DEP> (electrons: gather, push, deposit, wall list)",
                 "alg_bytes_per_particle": ALG_BYTES, "peak_kind": f"{peak_kind} hbm_gbs",
                 "phase_ms_per_step": {k: prof[k] / max(prof["steps"], 1) for k in
-                                      ("ms_push_e", "ms_push_i", "ms_collide_ions", "ms_walls", "ms_fields")}}
+                                      ("ms_push_e", "ms_push_e_kernel", "ms_collide_e", "ms_push_i", "ms_collide_ions", "ms_walls",
+                                       "ms_fields")}}
     cpu = None
     if not args.no_cpu:
         try:

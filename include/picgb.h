@@ -137,6 +137,7 @@ typedef struct pgb_profile {
     int64_t slots_e, slots_i;      /* particle slots swept by the push kernels     */
     int64_t launches;              /* kernel launches issued since pgb_create      */
     double ms_push_e_kernel;       /* the electron push kernel alone (in ms_push_e) */
+    double ms_collide_e;           /* electron collision pass and its event list (in ms_push_e) */
 } pgb_profile;
 
 typedef struct pgb_run pgb_run;

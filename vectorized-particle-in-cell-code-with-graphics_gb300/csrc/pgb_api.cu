@@ -297,8 +297,12 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
             return bail(PGB_ERR_CUDA);
         }
     r->copy_ev_ok = true;
-    /* the side stream only speeds steps up: without it steps run in turn */
-    if (cudaStreamCreateWithFlags(&r->side, cudaStreamNonBlocking) == cudaSuccess) {
+    /* the side stream only speeds steps up: without it steps run in turn.
+     * It takes the highest priority, so that the field solve's short
+     * kernels get SMs ahead of queued blocks of the run's own stream.     */
+    int prio_lo = 0, prio_hi = 0;
+    if (cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) == cudaSuccess &&
+        cudaStreamCreateWithPriority(&r->side, cudaStreamNonBlocking, prio_hi) == cudaSuccess) {
         if (cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming) == cudaSuccess) {
             if (cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming) == cudaSuccess) r->side_ok = true;
             else cudaEventDestroy(r->ev_fork);
@@ -373,7 +377,7 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
             cudaMemcpy(r->neut[w], tab32.data(), sizeof(float) * nn, cudaMemcpyHostToDevice);
         }
     }
-    if (pgb_mg_setup(r) || pgb_sort_setup(r)) { g_create_error = r->err; return bail(PGB_ERR_CUDA); }
+    if (pgb_mg_setup(r) || pgb_sort_setup(r) || pgb_particles_setup(r)) { g_create_error = r->err; return bail(PGB_ERR_CUDA); }
     if (!pgb_cuda_ok(nullptr, cudaDeviceSynchronize(), "create")) return bail(PGB_ERR_CUDA);
     *out = r;
     return 0;
@@ -620,7 +624,7 @@ extern "C" int pgb_collide_electrons(pgb_run* r) {
     int rc = need_particles(r);
     if (rc) return rc;
     if ((rc = set_device_step(r, r->time_step, 1))) return rc;
-    if (pgb_launch_mcc(r) || pgb_build_list(r, LIST_ION_EV, 0) || pgb_launch_ionize_appends(r, 1, 1))
+    if (pgb_launch_mcc(r, 0) || pgb_build_list(r, LIST_ION_EV, 0) || pgb_launch_ionize_appends(r, 1, 1))
         return PGB_ERR_CUDA;
     return sync_state(r);
 }
@@ -638,7 +642,7 @@ extern "C" int pgb_gather_push(pgb_run* r, int s) {
     if (!r || s < 0 || s > 1) return fail(r, PGB_ERR_ARG, "pgb_gather_push: bad argument");
     int rc = need_particles(r);
     if (rc) return rc;
-    if (pgb_launch_push(r, s, false, false, false)) return PGB_ERR_CUDA;
+    if (pgb_launch_push(r, s, false)) return PGB_ERR_CUDA;
     return sync_state(r);
 }
 
@@ -716,11 +720,15 @@ extern "C" int pgb_efield(pgb_run* r) {
  * t+1 need the particles after step t's walls, not step t's fields, so the
  * pipelined path (issue_one_step) runs them while step t's field solve is
  * still in flight on the run's side stream.                              */
-static int step_mcc(pgb_run* r, bool) {
+static int mcc_part(pgb_run* r, int leave_sms) {
     if (!r->p.have_collisions) return 0;
-    if (pgb_launch_mcc_q(r) || pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
+    if (pgb_launch_mcc(r, leave_sms) || pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
     return 0;
 }
+static int step_mcc(pgb_run* r, bool) { return mcc_part(r, 0); }
+/* beside a field solve: the one-CTA multigrid needs SMs of its own */
+#define PGB_FIELD_SMS 8
+static int step_mcc_beside(pgb_run* r, bool) { return mcc_part(r, PGB_FIELD_SMS); }
 
 static int step_particles(pgb_run* r, bool ion_step) {
     const bool coll = r->p.have_collisions != 0;
@@ -728,7 +736,8 @@ static int step_particles(pgb_run* r, bool ion_step) {
     PGB_CK(r, cudaMemsetAsync(r->qacc[0], 0, sizeof(unsigned long long) * G, r->stream));
     PGB_CK(r, cudaMemsetAsync(r->qacc[1], 0, sizeof(unsigned long long) * G, r->stream));
     /* get_particle_electric_field + move_particles, charge deposit */
-    if (pgb_launch_push(r, 0, false, true, false)) return PGB_ERR_CUDA;
+    PROF_MARK(r, 8);
+    if (pgb_launch_push(r, 0, true)) return PGB_ERR_CUDA;
     PROF_MARK(r, 7);
     if (pgb_build_list(r, LIST_OUT_E, 0)) return PGB_ERR_CUDA;
     PROF_MARK(r, 1);
@@ -745,7 +754,7 @@ static int step_particles(pgb_run* r, bool ion_step) {
     if (ion_step) {
         if (coll && pgb_launch_cx(r)) return PGB_ERR_CUDA;
         PROF_MARK(r, 3);
-        if (pgb_launch_push(r, 1, false, true, false)) return PGB_ERR_CUDA;
+        if (pgb_launch_push(r, 1, true)) return PGB_ERR_CUDA;
         if (pgb_build_list(r, LIST_OUT_I, 1)) return PGB_ERR_CUDA;
         PROF_MARK(r, 4);
         if (pgb_launch_walls(r, PGB_BOUNDARY_IONS)) return PGB_ERR_CUDA;
@@ -802,8 +811,10 @@ static int profile_collect(pgb_run* r) {
     for (int k = 0; k < 6; ++k) PGB_CK(r, cudaEventElapsedTime(&ms[k], r->prof_ev[k], r->prof_ev[k + 1]));
     r->prof.ms_push_e += ms[0];
     float mk;
-    PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[0], r->prof_ev[7]));
+    PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[8], r->prof_ev[7]));
     r->prof.ms_push_e_kernel += mk;
+    PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[0], r->prof_ev[8]));
+    r->prof.ms_collide_e += mk;
     r->prof.ms_walls += ms[1] + ms[4];
     r->prof.ms_collide_ions += ms[2];
     r->prof.ms_push_i += ms[3];
@@ -942,7 +953,7 @@ static int issue_one_step(pgb_run* r) {
     const bool ion_step = (r->time_step % r->dt_dti) == 0;
     if (pipe || forked) {
         const int key = graph_key(r, ion_step);
-        if ((rc = replay(r, step_mcc, ion_step, &r->graph_a[key], &r->graph_a_launches[key]))) return rc;
+        if ((rc = replay(r, step_mcc_beside, ion_step, &r->graph_a[key], &r->graph_a_launches[key]))) return rc;
         if (forked) PGB_CK(r, cudaStreamWaitEvent(r->stream, r->ev_join, 0));
         if ((rc = replay(r, step_particles, ion_step, &r->graph_b[key], &r->graph_b_launches[key])))
             return rc;

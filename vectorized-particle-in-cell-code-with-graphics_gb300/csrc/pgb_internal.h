@@ -239,14 +239,15 @@ inline cudaError_t pgb_launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, si
 
 /* kernels launched from the host side (defined in the .cu files) */
 struct CollConsts;
-int pgb_launch_push(pgb_run* r, int s, bool mcc, bool deposit, bool flag_ion);
+int pgb_launch_push(pgb_run* r, int s, bool deposit);
 int pgb_launch_flag_outside(pgb_run* r, int s);
 int pgb_build_list(pgb_run* r, int which, int species_for_tiles);
 int pgb_launch_deposit(pgb_run* r, int s);
 int pgb_launch_finalize(pgb_run* r, int which_species_mask, bool make_rhs);
 int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e);
 int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i);
-int pgb_launch_mcc(pgb_run* r);
+int pgb_launch_mcc(pgb_run* r, int leave_sms);
+int pgb_particles_setup(pgb_run* r);
 int pgb_launch_cx(pgb_run* r);
 int pgb_launch_walls(pgb_run* r, int which);
 int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long i0, long long i1);
@@ -260,7 +261,6 @@ int pgb_launch_sort(pgb_run* r, int s);
 int pgb_sort_setup(pgb_run* r);
 void pgb_bins(pgb_run* r, int* nbx, int* nby);
 int pgb_launch_reduce(pgb_run* r, int s);
-int pgb_launch_mcc_q(pgb_run* r);
 int pgb_launch_step_advance(pgb_run* r);
 int pgb_launch_graphs(pgb_run* r);
 int pgb_poisson_solve(pgb_run* r);

@@ -1,6 +1,7 @@
 /*
- * Particle kernels: fused collision + gather + push + deposit, ordered event
- * lists, injection, ionization products, compaction, load and dump.
+ * Particle kernels: electron-neutral collisions, gather + push + deposit,
+ * ordered event lists, injection, ionization products, compaction, load
+ * and dump.
  *
  * Reference path: e_collisions::collision (e_collisions.cpp:480-597),
  * particle::get_particle_electric_field + move_particles
@@ -8,14 +9,16 @@
  * (particle.cpp:663-858, pic.cl:22-52), particle::inject_more_particles
  * (particle.cpp:491-510).
  *
- * One pass of k_push reads a particle once (16 B position/velocity, 4 B vz,
- * 4 B weight, 4 B id when collisions are on), applies the electron-neutral
- * collision test, gathers E bilinearly from the FP32 node grid (L2
- * resident), pushes, deposits the new position into the int64 fixed-point
- * charge grid and records wall crossings and ionization events in per-tile
- * lists that keep slot order.  Grids are sized from the SM count and loop
- * over tiles, reading the particle count from device memory, so a step
- * needs no host round trip.
+ * k_mcc reads each electron (16 B position/velocity, 4 B vz, 4 B id) for
+ * the collision test and writes back only the ~5% whose velocity changes;
+ * it reads no field, so it runs beside the previous step's field solve.
+ * One pass of k_push then reads a particle once (16 B, plus 4 B vz with a
+ * magnetic field and 4 B weight), gathers E bilinearly from the FP32 node
+ * grid (L2 resident), pushes, deposits the new position into the int64
+ * fixed-point charge grid and records wall crossings in per-tile lists
+ * that keep slot order.  Grids are sized from the SM count and loop over
+ * tiles, reading the particle count from device memory, so a step needs
+ * no host round trip.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -133,26 +136,6 @@ __device__ __forceinline__ void mcc_ionize(const CollConsts& cc, const float* ne
     }
 }
 
-/* test and events of one electron in place (e_collisions.cpp:504-562).
- * Returns true if the electron ionized (its velocity is then NaN).        */
-__device__ __forceinline__ bool mcc_one(const CollConsts& cc, const float* neut, unsigned int id, unsigned int step,
-                                        int nx, int ny, float4& p, float& vz, bool& vchanged, int* stats) {
-    float energy;
-    pgb_stream st;
-    int ev = mcc_test(cc, id, step, nx, ny, p, vz, &energy, &st);
-    if (ev & MCC_SCATTER) {
-        scatter_f32(&st, neut, cc.n_neutral, energy, (float)cc.reduced_mass, p.z, p.w, vz);
-        vchanged = true;
-        stats[0] += 1;
-    }
-    if (ev & MCC_IONIZE) {
-        mcc_ionize(cc, neut, id, step, p, vz);
-        vchanged = true;
-        stats[1] += 1;
-    }
-    return (ev & MCC_IONIZE) != 0;
-}
-
 /* add per-thread event counts (elastic, ionization) with one atomic per warp */
 __device__ __forceinline__ void flush_stats(int (&st)[2], long long* stats) {
 #pragma unroll
@@ -252,104 +235,8 @@ struct ScatterQueue {
 };
 
 template <bool DEP>
-__device__ __forceinline__ void push_tile_mcc(const PushArgs& a, const PushConsts& pc, int tile, long long n,
-                                              unsigned int* win, int ox, int oy, unsigned step,
-                                              int (&st_loc)[2], ScatterQueue& q) {
-    const long long base = (long long)tile * PGB_TILE;
-    int code[PGB_ITEMS];   /* -1 absent; else MCC bits | (queue slot + 1) << 2 */
-    /* 1: collision tests; scattering events go to the queue.  Only the
-     * codes live across the barriers; step 3 reads the particle again
-     * (from L1/L2)                                                     */
-    float4 pa[PGB_ITEMS];
-    float vza[PGB_ITEMS];
-    unsigned int ida[PGB_ITEMS];
-#pragma unroll
-    for (int k = 0; k < PGB_ITEMS; ++k) {
-        long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
-        pa[k] = make_float4(-INFINITY, 0.0f, 0.0f, 0.0f);
-        vza[k] = 0.0f;
-        ida[k] = 0u;
-        if (i < n) {
-            pa[k] = a.xv[i];
-            vza[k] = a.vz[i];
-            ida[k] = a.id[i];
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < PGB_ITEMS; ++k) {
-        code[k] = -1;
-        const float4 p = pa[k];
-        if (is_dead(p.x)) continue;
-        const float vz = vza[k];
-        const unsigned int id = ida[k];
-        float energy;
-        pgb_stream st;
-        int ev = mcc_test(a.cc, id, step, pc.nx, pc.ny, p, vz, &energy, &st);
-        if (ev & MCC_SCATTER) {
-            st_loc[0] += 1;
-            int slot = atomicAdd(&q.n, 1);   /* < PGB_TILE: one entry per slot at most */
-            q.v[slot] = make_float4(p.z, p.w, vz, energy);
-            q.id[slot] = id;
-            ev |= (slot + 1) << 2;
-        }
-        code[k] = ev;
-    }
-    __syncthreads();
-    /* 2: the queued scatterings, one per thread */
-    const int qn = q.n;
-    for (int e = threadIdx.x; e < qn; e += blockDim.x) {
-        float4 v = q.v[e];
-        pgb_stream st;
-        pgb_stream_init(&st, a.cc.seed, q.id[e], step, PGB_STREAM_EMCC, 0);
-        (void)pgb_stream_u32(&st);   /* the collision test's draw */
-        scatter_f32(&st, a.neut, a.cc.n_neutral, v.w, (float)a.cc.reduced_mass, v.x, v.y, v.z);
-        q.v[e] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) q.n = 0;   /* read again only after the list barriers */
-    /* 3: ionization, gather, push, deposit, wall and event flags */
-    bool f[2][PGB_ITEMS];
-#pragma unroll
-    for (int k = 0; k < PGB_ITEMS; ++k) {
-        f[0][k] = false;
-        f[1][k] = false;
-        if (code[k] < 0) continue;
-        long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
-        float4 p = a.xv[i];
-        float vz = a.vz[i];
-        bool vchanged = false;
-        int slot = (code[k] >> 2) - 1;
-        if (slot >= 0) {
-            float4 v = q.v[slot];
-            p.z = v.x; p.w = v.y; vz = v.z;
-            vchanged = true;
-        }
-        if (code[k] & MCC_IONIZE) {
-            mcc_ionize(a.cc, a.neut, a.id[i], step, p, vz);
-            vchanged = true;
-            st_loc[1] += 1;
-            f[1][k] = true;
-        }
-        bool moved;
-        gather_push_one(pc, a.exy, p, vz, moved);
-        if (moved || vchanged) a.xv[i] = p;
-        if (vchanged || (pc.bfield && moved)) a.vz[i] = vz;
-        if (DEP && deposit_ok(p.x, p.y, pc.nx, pc.ny)) deposit_win(a.qacc, win, ox, oy, pc.nx, p.x, p.y, a.w[i]);
-        f[0][k] = pc.steady ? outside_steady(p.x, p.y, pc.nx, pc.ny) : outside_absorbing(p.x, p.y, pc.nx, pc.ny);
-    }
-    int* const tl[2] = {a.tl_out, a.tl_ev};
-    int* const tc[2] = {a.tc_out, a.tc_ev};
-    tile_lists<2>(f, base, tile, tl, tc);
-}
-
-template <bool MCC, bool DEP>
 __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& pc, int tile, long long n,
-                                          unsigned int* win, int ox, int oy, unsigned step, int (&st_loc)[2],
-                                          ScatterQueue& q) {
-    if (MCC) {
-        push_tile_mcc<DEP>(a, pc, tile, n, win, ox, oy, step, st_loc, q);
-        return;
-    }
+                                          unsigned int* win, int ox, int oy) {
     const long long base = (long long)tile * PGB_TILE;
     bool f[1][PGB_ITEMS];
     /* all loads of the thread's items first, so that they are in flight
@@ -387,21 +274,16 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
 
 /* Work items: the bin pieces of the last sort (tiles of one bin, deposited
  * through a shared window), then every tile after the sorted region.     */
-template <bool MCC, bool DEP>
+template <bool DEP>
 __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
     pgb_pdl_entry();
     __shared__ unsigned int s_win[WIN_NODES];
-    __shared__ ScatterQueue s_q;
-    if (MCC && threadIdx.x == 0) s_q.n = 0;
-    __syncthreads();
     const long long n = a.ds->n[a.s];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     const int npieces = a.ds->n_pieces[a.s];
     const int tile0 = (int)a.ds->sorted_tiles[a.s];
     const int nitems = npieces + (ntiles > tile0 ? ntiles - tile0 : 0);
-    const unsigned step = (unsigned)a.ds->t;
     const PushConsts pc = a.pc;
-    int st_loc[2] = {0, 0};
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         if (item < npieces) {
             int4 pc4 = a.pieces[item];
@@ -415,7 +297,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
                 __syncthreads();
             }
             for (int t = pc4.x; t < pc4.x + pc4.y && t < ntiles; ++t)
-                push_tile<MCC, DEP>(a, pc, t, n, win, ox, oy, step, st_loc, s_q);
+                push_tile<DEP>(a, pc, t, n, win, ox, oy);
             if (win) {
                 __syncthreads();
                 for (int k = threadIdx.x; k < WIN_NODES; k += blockDim.x) {
@@ -429,10 +311,9 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
                 __syncthreads();
             }
         } else {
-            push_tile<MCC, DEP>(a, pc, tile0 + (item - npieces), n, nullptr, 0, 0, step, st_loc, s_q);
+            push_tile<DEP>(a, pc, tile0 + (item - npieces), n, nullptr, 0, 0);
         }
     }
-    if (MCC) flush_stats(st_loc, a.ds->stats);
 }
 
 /* flag-only pass (wall classification without a push) */
@@ -470,55 +351,46 @@ __global__ void __launch_bounds__(256) k_deposit(const float4* xv, const float* 
     }
 }
 
-/* standalone electron collisions (e_collisions::collision) */
-__global__ void __launch_bounds__(PGB_PUSH_THREADS) k_mcc(PushArgs a) {
-    pgb_pdl_entry();
-    const long long n = a.ds->n[0];
-    const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
-    int st_loc[2] = {0, 0};
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long long base = (long long)tile * PGB_TILE;
-        bool f[1][PGB_ITEMS];
-#pragma unroll
-        for (int k = 0; k < PGB_ITEMS; ++k) {
-            f[0][k] = false;
-            long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
-            if (i >= n) continue;
-            float4 p = a.xv[i];
-            if (is_dead(p.x)) continue;
-            float vz = a.vz[i];
-            bool vchanged = false;
-            f[0][k] = mcc_one(a.cc, a.neut, a.id[i], (unsigned int)a.ds->t, a.pc.nx, a.pc.ny, p, vz, vchanged, st_loc);
-            if (vchanged) { a.xv[i] = p; a.vz[i] = vz; }
-        }
-        int* const tla[1] = {a.tl_ev};
-        int* const tca[1] = {a.tc_ev};
-        tile_lists<1>(f, base, tile, tla, tca);
-    }
-    flush_stats(st_loc, a.ds->stats);
-}
-
 /* e_collisions::collision (e_collisions.cpp:480-597) as a pass of its own,
  * the first of a step: collision tests, the tile's scatterings queued so
  * that full warps run them, ionization of the parent electrons, and the
  * ordered list of ionization events.  It reads no field, so it can run
- * while the previous step's field solve is still in flight.              */
-__global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_mcc_q(PushArgs a) {
+ * while the previous step's field solve is still in flight.
+ *
+ * A block is MCC_GROUPS independent groups of 256 threads, each with its
+ * own queue, list scratch and named barrier, each taking one tile at a
+ * time.  At 64 registers a thread the block fills an SM's register file,
+ * so a grid of sms - k blocks leaves k SMs wholly free: the field solve's
+ * one-CTA multigrid (1024 threads) needs an SM of its own.               */
+#define MCC_GROUPS 4
+#define MCC_THREADS (MCC_GROUPS * PGB_PUSH_THREADS)
+struct MccGroupSmem {
+    ScatterQueue q;
+    int off[PGB_ITEMS][PGB_PUSH_THREADS / 32];
+};
+__device__ __forceinline__ void group_sync(int g) {
+    asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "n"(PGB_PUSH_THREADS) : "memory");
+}
+__global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a) {
     pgb_pdl_entry();
-    __shared__ ScatterQueue q;
-    if (threadIdx.x == 0) q.n = 0;
-    __syncthreads();
+    extern __shared__ __align__(16) unsigned char mcc_smem[];
+    const int g = threadIdx.x / PGB_PUSH_THREADS, t = threadIdx.x % PGB_PUSH_THREADS;
+    const int lane = t & 31, warp = t >> 5;
+    MccGroupSmem& S = reinterpret_cast<MccGroupSmem*>(mcc_smem)[g];
+    ScatterQueue& q = S.q;
+    if (t == 0) q.n = 0;
+    group_sync(g);
     const long long n = a.ds->n[0];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     const unsigned step = (unsigned)a.ds->t;
     int st_loc[2] = {0, 0};
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int tile = blockIdx.x * MCC_GROUPS + g; tile < ntiles; tile += gridDim.x * MCC_GROUPS) {
         const long long base = (long long)tile * PGB_TILE;
         int code[PGB_ITEMS];
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
             code[k] = -1;
-            long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+            long long i = base + k * PGB_PUSH_THREADS + t;
             if (i >= n) continue;
             const float4 p = a.xv[i];
             if (is_dead(p.x)) continue;
@@ -529,16 +401,16 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_mcc_q(PushArgs a) {
             int ev = mcc_test(a.cc, id, step, a.pc.nx, a.pc.ny, p, vz, &energy, &st);
             if (ev & MCC_SCATTER) {
                 st_loc[0] += 1;
-                int slot = atomicAdd(&q.n, 1);
+                int slot = atomicAdd(&q.n, 1);   /* < PGB_TILE: one entry per slot at most */
                 q.v[slot] = make_float4(p.z, p.w, vz, energy);
                 q.id[slot] = id;
                 ev |= (slot + 1) << 2;
             }
             code[k] = ev;
         }
-        __syncthreads();
+        group_sync(g);
         const int qn = q.n;
-        for (int e = threadIdx.x; e < qn; e += blockDim.x) {
+        for (int e = t; e < qn; e += PGB_PUSH_THREADS) {
             float4 v = q.v[e];
             pgb_stream st;
             pgb_stream_init(&st, a.cc.seed, q.id[e], step, PGB_STREAM_EMCC, 0);
@@ -546,14 +418,14 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_mcc_q(PushArgs a) {
             scatter_f32(&st, a.neut, a.cc.n_neutral, v.w, (float)a.cc.reduced_mass, v.x, v.y, v.z);
             q.v[e] = v;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) q.n = 0;   /* read again only after the list barriers */
-        bool f[1][PGB_ITEMS];
+        group_sync(g);
+        if (t == 0) q.n = 0;   /* read again only after the list barriers */
+        bool f[PGB_ITEMS];
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
-            f[0][k] = false;
+            f[k] = false;
             if (code[k] <= 0) continue;
-            long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
+            long long i = base + k * PGB_PUSH_THREADS + t;
             float4 p = a.xv[i];
             float vz = a.vz[i];
             int slot = (code[k] >> 2) - 1;
@@ -564,14 +436,35 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_mcc_q(PushArgs a) {
             if (code[k] & MCC_IONIZE) {
                 mcc_ionize(a.cc, a.neut, a.id[i], step, p, vz);
                 st_loc[1] += 1;
-                f[0][k] = true;
+                f[k] = true;
             }
             a.xv[i] = p;
             a.vz[i] = vz;
         }
-        int* const tla[1] = {a.tl_ev};
-        int* const tca[1] = {a.tc_ev};
-        tile_lists<1>(f, base, tile, tla, tca);
+        /* the tile's ionization events in slot order (as tile_lists) */
+        const unsigned lt = (1u << lane) - 1u;
+        unsigned m[PGB_ITEMS];
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            m[k] = __ballot_sync(0xffffffffu, f[k]);
+            if (lane == 0) S.off[k][warp] = __popc(m[k]);
+        }
+        group_sync(g);
+        if (t == 0) {
+            int acc = 0;
+            for (int k = 0; k < PGB_ITEMS; ++k)
+                for (int w = 0; w < PGB_PUSH_THREADS / 32; ++w) {
+                    int c = S.off[k][w];
+                    S.off[k][w] = acc;
+                    acc += c;
+                }
+            a.tc_ev[tile] = acc;
+        }
+        group_sync(g);
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k)
+            if (f[k]) a.tl_ev[(long long)tile * PGB_TILE + S.off[k][warp] + __popc(m[k] & lt)] = (int)(base + k * PGB_PUSH_THREADS + t);
+        group_sync(g);
     }
     flush_stats(st_loc, a.ds->stats);
 }
@@ -1000,12 +893,10 @@ static PushArgs push_args(pgb_run* r, int s) {
     return a;
 }
 
-int pgb_launch_push(pgb_run* r, int s, bool mcc, bool deposit, bool flag_ion) {
-    (void)flag_ion;
+int pgb_launch_push(pgb_run* r, int s, bool deposit) {
     PushArgs a = push_args(r, s);
     int g = grid_for(r, 8);
-    void (*kp)(PushArgs) = mcc ? (deposit ? k_push<true, true> : k_push<true, false>)
-                               : (deposit ? k_push<false, true> : k_push<false, false>);
+    void (*kp)(PushArgs) = deposit ? k_push<true> : k_push<false>;
     PGB_CK(r, pgb_launch_pdl(kp, dim3(g), dim3(PGB_PUSH_THREADS), 0, r->stream, a));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
@@ -1021,12 +912,6 @@ int pgb_launch_flag_outside(pgb_run* r, int s) {
     return 0;
 }
 
-int pgb_launch_mcc_q(pgb_run* r) {
-    PushArgs a = push_args(r, 0);
-    PGB_CK(r, pgb_launch_pdl(k_mcc_q, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, a));
-    r->launches++;
-    return 0;
-}
 
 int pgb_launch_step_advance(pgb_run* r) {
     PGB_CK(r, pgb_launch_pdl(k_step_advance, dim3(1), dim3(1), 0, r->stream, r->ds));
@@ -1034,9 +919,17 @@ int pgb_launch_step_advance(pgb_run* r) {
     return 0;
 }
 
-int pgb_launch_mcc(pgb_run* r) {
+int pgb_particles_setup(pgb_run* r) {
+    PGB_CK(r, cudaFuncSetAttribute(k_mcc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(MCC_GROUPS * sizeof(MccGroupSmem))));
+    return 0;
+}
+
+/* leave_sms: SMs the collision pass leaves free (one block fills an SM) */
+int pgb_launch_mcc(pgb_run* r, int leave_sms) {
     PushArgs a = push_args(r, 0);
-    PGB_CK(r, pgb_launch_pdl(k_mcc, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, a));
+    const int g = std::max(1, r->sms - leave_sms);
+    PGB_CK(r, pgb_launch_pdl(k_mcc, dim3(g), dim3(MCC_THREADS), MCC_GROUPS * sizeof(MccGroupSmem), r->stream, a));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;

@@ -131,7 +131,7 @@ struct CollConsts {
     float i_pcoef;            /* DTI*1e-20*NEUTRAL_DENSITY */
     double me, mi, dt, dti, threshold, reduced_mass;
     /* electron speed below which e_collisions::ionization certainly gives
-     * a negative excess energy, hence NaN velocities (see mcc_one)      */
+     * a negative excess energy, hence NaN velocities (see mcc_ionize)  */
     float ion_vcap;
     int n_neutral;
     uint64_t seed;
