@@ -137,7 +137,8 @@ typedef struct pgb_profile {
     int64_t slots_e, slots_i;      /* particle slots swept by the push kernels     */
     int64_t launches;              /* kernel launches issued since pgb_create      */
     double ms_push_e_kernel;       /* the electron push kernel alone (in ms_push_e) */
-    double ms_collide_e;           /* electron collision pass and its event list (in ms_push_e) */
+    double ms_collide_e;           /* the electron collision-test kernel alone (in ms_push_e) */
+    double ms_scatter_e;           /* the electron scattering kernel alone (in ms_push_e)     */
 } pgb_profile;
 
 typedef struct pgb_run pgb_run;

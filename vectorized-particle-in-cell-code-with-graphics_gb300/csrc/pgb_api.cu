@@ -624,7 +624,8 @@ extern "C" int pgb_collide_electrons(pgb_run* r) {
     int rc = need_particles(r);
     if (rc) return rc;
     if ((rc = set_device_step(r, r->time_step, 1))) return rc;
-    if (pgb_launch_mcc(r, 0) || pgb_build_list(r, LIST_ION_EV, 0) || pgb_launch_ionize_appends(r, 1, 1))
+    if (pgb_launch_mcc(r, 0) || pgb_launch_scatter(r, 0) || pgb_build_list(r, LIST_ION_EV, 0) ||
+        pgb_launch_ionize_appends(r, 1, 1))
         return PGB_ERR_CUDA;
     return sync_state(r);
 }
@@ -722,12 +723,16 @@ extern "C" int pgb_efield(pgb_run* r) {
  * still in flight on the run's side stream.                              */
 static int mcc_part(pgb_run* r, int leave_sms) {
     if (!r->p.have_collisions) return 0;
-    if (pgb_launch_mcc(r, leave_sms) || pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
+    if (pgb_launch_mcc(r, leave_sms)) return PGB_ERR_CUDA;
+    PROF_MARK(r, 9);
+    if (pgb_launch_scatter(r, leave_sms)) return PGB_ERR_CUDA;
+    PROF_MARK(r, 10);
+    if (pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
     return 0;
 }
 static int step_mcc(pgb_run* r, bool) { return mcc_part(r, 0); }
 /* beside a field solve: the one-CTA multigrid needs SMs of its own */
-#define PGB_FIELD_SMS 8
+#define PGB_FIELD_SMS 16
 static int step_mcc_beside(pgb_run* r, bool) { return mcc_part(r, PGB_FIELD_SMS); }
 
 static int step_particles(pgb_run* r, bool ion_step) {
@@ -813,8 +818,12 @@ static int profile_collect(pgb_run* r) {
     float mk;
     PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[8], r->prof_ev[7]));
     r->prof.ms_push_e_kernel += mk;
-    PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[0], r->prof_ev[8]));
-    r->prof.ms_collide_e += mk;
+    if (r->p.have_collisions) {
+        PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[0], r->prof_ev[9]));
+        r->prof.ms_collide_e += mk;
+        PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[9], r->prof_ev[10]));
+        r->prof.ms_scatter_e += mk;
+    }
     r->prof.ms_walls += ms[1] + ms[4];
     r->prof.ms_collide_ions += ms[2];
     r->prof.ms_push_i += ms[3];

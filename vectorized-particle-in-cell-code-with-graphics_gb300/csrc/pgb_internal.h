@@ -62,6 +62,7 @@ struct DevState {
     long long tf;            /* time_step of the field solve being run (its right-wall
                                 potential); trails t while a solve overlaps the next
                                 step's collisions                                      */
+    unsigned long long scat_n;   /* scattering events queued by the collision pass */
 };
 
 /* dense event lists (ordered by slot) */
@@ -247,6 +248,7 @@ int pgb_launch_finalize(pgb_run* r, int which_species_mask, bool make_rhs);
 int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e);
 int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i);
 int pgb_launch_mcc(pgb_run* r, int leave_sms);
+int pgb_launch_scatter(pgb_run* r, int leave_sms);
 int pgb_particles_setup(pgb_run* r);
 int pgb_launch_cx(pgb_run* r);
 int pgb_launch_walls(pgb_run* r, int which);

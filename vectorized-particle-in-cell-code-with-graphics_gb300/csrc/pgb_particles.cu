@@ -85,11 +85,16 @@ __device__ __forceinline__ void gather_push_one(const PushConsts& pc, const floa
  * the EMCC stream after its first draw, as the scattering continues it.  */
 #define MCC_SCATTER 1
 #define MCC_IONIZE 2
+/* |v|^2 with its roundings spelled out: the collision test and the
+ * scattering kernel must derive the same energy from the same velocity */
+__device__ __forceinline__ float speed2(const float4& p, float vz) {
+    return __fmaf_rn(vz, vz, __fmaf_rn(p.w, p.w, __fmul_rn(p.z, p.z)));
+}
 __device__ __forceinline__ int mcc_test(const CollConsts& cc, unsigned int id, unsigned int step, int nx, int ny,
                                         const float4& p, float vz, float* energy_out, pgb_stream* st) {
     int jp = cellf(p.x), kp = cellf(p.y);
     if (!(jp >= 0 && jp < nx && kp >= 0 && kp < ny)) return 0;
-    float u2 = p.z * p.z + p.w * p.w + vz * vz;
+    float u2 = speed2(p, vz);
     float energy = cc.e_energy_coef * u2;
     float u = sqrtf(u2);
     pgb_stream_init(st, cc.seed, id, step, PGB_STREAM_EMCC, 0);
@@ -223,17 +228,6 @@ __device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned i
     }
 }
 
-/* Elastic-scattering events of one tile, queued so that full warps run
- * them: about one electron in twenty scatters per step, and inline the
- * event would hold a whole warp for one or two active lanes.  The queue
- * holds a whole tile, so it never overflows.                            */
-#define SCATTER_QCAP PGB_TILE
-struct ScatterQueue {
-    float4 v[SCATTER_QCAP];        /* vx, vy, vz; energy (eV) */
-    unsigned int id[SCATTER_QCAP];
-    int n;
-};
-
 template <bool DEP>
 __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& pc, int tile, long long n,
                                           unsigned int* win, int ox, int oy) {
@@ -351,98 +345,94 @@ __global__ void __launch_bounds__(256) k_deposit(const float4* xv, const float* 
     }
 }
 
-/* e_collisions::collision (e_collisions.cpp:480-597) as a pass of its own,
- * the first of a step: collision tests, the tile's scatterings queued so
- * that full warps run them, ionization of the parent electrons, and the
- * ordered list of ionization events.  It reads no field, so it can run
- * while the previous step's field solve is still in flight.
+/* e_collisions::collision (e_collisions.cpp:480-597) in two kernels, the
+ * first of a step.  They read no field, so they run while the previous
+ * step's field solve is still in flight.
+ *   k_mcc      the collision test of every electron; the ionizations of
+ *              electrons that do not also scatter; the ordered per-tile
+ *              list of ionization events; the scattering events (about one
+ *              electron in twenty) appended, unordered, to a dense list
+ *   k_scatter  one thread per listed event: the scattering, then the
+ *              ionization of the parent if it also ionizes
+ * Each event touches only its own electron and draws from that electron's
+ * stream, so the order of the scattering list changes nothing.
  *
  * A block is MCC_GROUPS independent groups of 256 threads, each with its
- * own queue, list scratch and named barrier, each taking one tile at a
- * time.  At 64 registers a thread the block fills an SM's register file,
- * so a grid of sms - k blocks leaves k SMs wholly free: the field solve's
- * one-CTA multigrid (1024 threads) needs an SM of its own.               */
+ * own list scratch and named barrier, each taking one tile at a time.  At
+ * 64 registers a thread the block fills an SM's register file, so a grid
+ * of sms - k blocks leaves k SMs wholly free: the field solve's one-CTA
+ * multigrid (1024 threads) needs an SM of its own.                       */
 #define MCC_GROUPS 4
 #define MCC_THREADS (MCC_GROUPS * PGB_PUSH_THREADS)
+#define MCC_ION_BIT 0x80000000u
 struct MccGroupSmem {
-    ScatterQueue q;
     int off[PGB_ITEMS][PGB_PUSH_THREADS / 32];
 };
 __device__ __forceinline__ void group_sync(int g) {
     asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "n"(PGB_PUSH_THREADS) : "memory");
 }
-__global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a) {
+__global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
     pgb_pdl_entry();
-    extern __shared__ __align__(16) unsigned char mcc_smem[];
+    __shared__ MccGroupSmem s_grp[MCC_GROUPS];
     const int g = threadIdx.x / PGB_PUSH_THREADS, t = threadIdx.x % PGB_PUSH_THREADS;
     const int lane = t & 31, warp = t >> 5;
-    MccGroupSmem& S = reinterpret_cast<MccGroupSmem*>(mcc_smem)[g];
-    ScatterQueue& q = S.q;
-    if (t == 0) q.n = 0;
-    group_sync(g);
+    const unsigned lt = (1u << lane) - 1u;
+    MccGroupSmem& S = s_grp[g];
     const long long n = a.ds->n[0];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     const unsigned step = (unsigned)a.ds->t;
     int st_loc[2] = {0, 0};
     for (int tile = blockIdx.x * MCC_GROUPS + g; tile < ntiles; tile += gridDim.x * MCC_GROUPS) {
         const long long base = (long long)tile * PGB_TILE;
-        int code[PGB_ITEMS];
+        /* all loads of the thread's items first, then the tests */
+        float4 pa[PGB_ITEMS];
+        float vza[PGB_ITEMS];
+        unsigned int ida[PGB_ITEMS];
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
-            code[k] = -1;
             long long i = base + k * PGB_PUSH_THREADS + t;
-            if (i >= n) continue;
-            const float4 p = a.xv[i];
-            if (is_dead(p.x)) continue;
-            const float vz = a.vz[i];
-            const unsigned int id = a.id[i];
-            float energy;
-            pgb_stream st;
-            int ev = mcc_test(a.cc, id, step, a.pc.nx, a.pc.ny, p, vz, &energy, &st);
-            if (ev & MCC_SCATTER) {
-                st_loc[0] += 1;
-                int slot = atomicAdd(&q.n, 1);   /* < PGB_TILE: one entry per slot at most */
-                q.v[slot] = make_float4(p.z, p.w, vz, energy);
-                q.id[slot] = id;
-                ev |= (slot + 1) << 2;
+            pa[k] = make_float4(-INFINITY, 0.0f, 0.0f, 0.0f);
+            vza[k] = 0.0f;
+            ida[k] = 0u;
+            if (i < n) {
+                pa[k] = a.xv[i];
+                vza[k] = a.vz[i];
+                ida[k] = a.id[i];
             }
-            code[k] = ev;
         }
-        group_sync(g);
-        const int qn = q.n;
-        for (int e = t; e < qn; e += PGB_PUSH_THREADS) {
-            float4 v = q.v[e];
-            pgb_stream st;
-            pgb_stream_init(&st, a.cc.seed, q.id[e], step, PGB_STREAM_EMCC, 0);
-            (void)pgb_stream_u32(&st);   /* the collision test's draw */
-            scatter_f32(&st, a.neut, a.cc.n_neutral, v.w, (float)a.cc.reduced_mass, v.x, v.y, v.z);
-            q.v[e] = v;
-        }
-        group_sync(g);
-        if (t == 0) q.n = 0;   /* read again only after the list barriers */
         bool f[PGB_ITEMS];
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
-            f[k] = false;
-            if (code[k] <= 0) continue;
-            long long i = base + k * PGB_PUSH_THREADS + t;
-            float4 p = a.xv[i];
-            float vz = a.vz[i];
-            int slot = (code[k] >> 2) - 1;
-            if (slot >= 0) {
-                float4 v = q.v[slot];
-                p.z = v.x; p.w = v.y; vz = v.z;
+            const int i = (int)(base + k * PGB_PUSH_THREADS + t);
+            int ev = 0;
+            if (!is_dead(pa[k].x)) {
+                float energy;
+                pgb_stream st;
+                ev = mcc_test(a.cc, ida[k], step, a.pc.nx, a.pc.ny, pa[k], vza[k], &energy, &st);
             }
-            if (code[k] & MCC_IONIZE) {
-                mcc_ionize(a.cc, a.neut, a.id[i], step, p, vz);
-                st_loc[1] += 1;
-                f[k] = true;
+            const bool sc = (ev & MCC_SCATTER) != 0;
+            f[k] = (ev & MCC_IONIZE) != 0;
+            st_loc[0] += sc ? 1 : 0;
+            st_loc[1] += f[k] ? 1 : 0;
+            /* scattering events: one counter update per warp */
+            const unsigned ms = __ballot_sync(0xffffffffu, sc);
+            if (ms) {
+                const int leader = __ffs(ms) - 1;
+                unsigned long long b0 = 0;
+                if (lane == leader) b0 = atomicAdd(&a.ds->scat_n, (unsigned long long)__popc(ms));
+                b0 = __shfl_sync(0xffffffffu, b0, leader);
+                if (sc) scat[b0 + __popc(ms & lt)] = (int)((unsigned)i | (f[k] ? MCC_ION_BIT : 0u));
             }
-            a.xv[i] = p;
-            a.vz[i] = vz;
+            /* an ionization without scattering is applied here */
+            if (f[k] && !sc) {
+                float4 p = pa[k];
+                float vz = vza[k];
+                mcc_ionize(a.cc, a.neut, ida[k], step, p, vz);
+                a.xv[i] = p;
+                a.vz[i] = vz;
+            }
         }
         /* the tile's ionization events in slot order (as tile_lists) */
-        const unsigned lt = (1u << lane) - 1u;
         unsigned m[PGB_ITEMS];
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
@@ -467,6 +457,27 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a) {
         group_sync(g);
     }
     flush_stats(st_loc, a.ds->stats);
+}
+
+__global__ void __launch_bounds__(MCC_THREADS, 1) k_scatter(PushArgs a, const int* scat) {
+    pgb_pdl_entry();
+    const long long m = (long long)a.ds->scat_n;
+    const unsigned step = (unsigned)a.ds->t;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < m; r += (long long)gridDim.x * blockDim.x) {
+        const unsigned e = (unsigned)scat[r];
+        const int slot = (int)(e & ~MCC_ION_BIT);
+        float4 p = a.xv[slot];
+        float vz = a.vz[slot];
+        const unsigned int id = a.id[slot];
+        const float energy = a.cc.e_energy_coef * speed2(p, vz);
+        pgb_stream st;
+        pgb_stream_init(&st, a.cc.seed, id, step, PGB_STREAM_EMCC, 0);
+        (void)pgb_stream_u32(&st);   /* the collision test's draw */
+        scatter_f32(&st, a.neut, a.cc.n_neutral, energy, (float)a.cc.reduced_mass, p.z, p.w, vz);
+        if (e & MCC_ION_BIT) mcc_ionize(a.cc, a.neut, id, step, p, vz);
+        a.xv[slot] = p;
+        a.vz[slot] = vz;
+    }
 }
 
 /* the last kernel of a step's particle phases moves the step counter on */
@@ -919,17 +930,24 @@ int pgb_launch_step_advance(pgb_run* r) {
     return 0;
 }
 
-int pgb_particles_setup(pgb_run* r) {
-    PGB_CK(r, cudaFuncSetAttribute(k_mcc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)(MCC_GROUPS * sizeof(MccGroupSmem))));
-    return 0;
-}
+int pgb_particles_setup(pgb_run*) { return 0; }
 
-/* leave_sms: SMs the collision pass leaves free (one block fills an SM) */
+/* leave_sms: SMs the collision kernels leave free (one block fills an SM).
+ * The scattering list is the spare dense list (capacity >= electron slots). */
 int pgb_launch_mcc(pgb_run* r, int leave_sms) {
     PushArgs a = push_args(r, 0);
     const int g = std::max(1, r->sms - leave_sms);
-    PGB_CK(r, pgb_launch_pdl(k_mcc, dim3(g), dim3(MCC_THREADS), MCC_GROUPS * sizeof(MccGroupSmem), r->stream, a));
+    PGB_CK(r, cudaMemsetAsync(&r->ds->scat_n, 0, sizeof(unsigned long long), r->stream));
+    PGB_CK(r, pgb_launch_pdl(k_mcc, dim3(g), dim3(MCC_THREADS), 0, r->stream, a, r->list[LIST_SPARE]));
+    r->launches++;
+    PGB_CK(r, cudaGetLastError());
+    return 0;
+}
+
+int pgb_launch_scatter(pgb_run* r, int leave_sms) {
+    PushArgs a = push_args(r, 0);
+    const int g = std::max(1, r->sms - leave_sms);
+    PGB_CK(r, pgb_launch_pdl(k_scatter, dim3(g), dim3(MCC_THREADS), 0, r->stream, a, (const int*)r->list[LIST_SPARE]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;

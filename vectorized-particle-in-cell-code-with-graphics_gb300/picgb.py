@@ -159,7 +159,8 @@ class PgbProfile(C.Structure):
     _fields_ = [("ms_push_e", C.c_double), ("ms_push_i", C.c_double), ("ms_collide_ions", C.c_double),
                 ("ms_walls", C.c_double), ("ms_fields", C.c_double), ("steps", C.c_int64),
                 ("slots_e", C.c_int64), ("slots_i", C.c_int64), ("launches", C.c_int64),
-                ("ms_push_e_kernel", C.c_double), ("ms_collide_e", C.c_double)]
+                ("ms_push_e_kernel", C.c_double), ("ms_collide_e", C.c_double),
+                ("ms_scatter_e", C.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
