@@ -933,10 +933,18 @@ int pgb_launch_step_advance(pgb_run* r) {
 int pgb_particles_setup(pgb_run*) { return 0; }
 
 /* leave_sms: SMs the collision kernels leave free (one block fills an SM).
+ * Small runs take fewer blocks: one per MCC_GROUPS tiles for k_mcc, one per
+ * 16 Ki electrons for k_scatter (about a scattering per thread), from the
+ * electron count last read back; both kernels loop grid-stride.
  * The scattering list is the spare dense list (capacity >= electron slots). */
+static int mcc_blocks(pgb_run* r, int leave_sms, long long per_block) {
+    const long long n = std::max<long long>(r->hs->n[0], 0);
+    const long long want = std::max<long long>(1, (n + per_block - 1) / per_block);
+    return (int)std::min<long long>(std::max(1, r->sms - leave_sms), want);
+}
 int pgb_launch_mcc(pgb_run* r, int leave_sms) {
     PushArgs a = push_args(r, 0);
-    const int g = std::max(1, r->sms - leave_sms);
+    const int g = mcc_blocks(r, leave_sms, (long long)MCC_GROUPS * PGB_TILE);
     PGB_CK(r, cudaMemsetAsync(&r->ds->scat_n, 0, sizeof(unsigned long long), r->stream));
     PGB_CK(r, pgb_launch_pdl(k_mcc, dim3(g), dim3(MCC_THREADS), 0, r->stream, a, r->list[LIST_SPARE]));
     r->launches++;
@@ -946,7 +954,7 @@ int pgb_launch_mcc(pgb_run* r, int leave_sms) {
 
 int pgb_launch_scatter(pgb_run* r, int leave_sms) {
     PushArgs a = push_args(r, 0);
-    const int g = std::max(1, r->sms - leave_sms);
+    const int g = mcc_blocks(r, leave_sms, 16384);
     PGB_CK(r, pgb_launch_pdl(k_scatter, dim3(g), dim3(MCC_THREADS), 0, r->stream, a, (const int*)r->list[LIST_SPARE]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
