@@ -91,7 +91,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             jobs.append((name, None))
     objs = [os.path.join(BUILD, u.replace(".cu", ".o")) for u in UNITS] + host_objs
     if force or jobs or _stale(OUT, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", OUT] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", OUT] + objs + ["-lcudart", "-ldl"]
         if verbose:
             print(" ".join(cmd), flush=True)
         p = subprocess.run(cmd, capture_output=True, text=True)

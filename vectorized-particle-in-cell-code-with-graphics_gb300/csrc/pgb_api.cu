@@ -14,6 +14,7 @@
  * time.
  */
 #include <cuda_runtime.h>
+#include <cstdlib>
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
@@ -21,7 +22,17 @@
 #include <new>
 #include <string>
 #include <vector>
+#include <nvtx3/nvToolsExt.h>
 #include "pgb_internal.h"
+
+/* NVTX ranges around the entry points and each issued step: host-side
+ * enqueue spans for a timeline tool (no cost without one attached)     */
+namespace {
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+};
+}
 #include "pgb_physics.cuh"
 #include "pgb_rng.h"
 
@@ -171,13 +182,19 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
     }
     if (need > S.cap) {
         long long cap = std::max<long long>(need, 1024);
-        Species T = S;
+        Species T;   /* the new storage; S keeps the old until it is copied */
+        T.qc = S.qc; T.q_over_m = S.q_over_m; T.mass = S.mass; T.vt = S.vt; T.dt = S.dt;
         T.cap = cap;
-        if (cudaMalloc(&T.xv, sizeof(float4) * cap) != cudaSuccess || cudaMalloc(&T.vz, sizeof(float) * cap) != cudaSuccess ||
-            cudaMalloc(&T.w, sizeof(float) * cap) != cudaSuccess || cudaMalloc(&T.id, sizeof(unsigned) * cap) != cudaSuccess ||
-            cudaMalloc(&T.xv2, sizeof(float4) * cap) != cudaSuccess || cudaMalloc(&T.vz2, sizeof(float) * cap) != cudaSuccess ||
-            cudaMalloc(&T.w2, sizeof(float) * cap) != cudaSuccess || cudaMalloc(&T.id2, sizeof(unsigned) * cap) != cudaSuccess) {
+        /* host-side fault injection (tests): the handle's fault_alloc-th
+         * growth fails as if the device were out of memory              */
+        const bool injected = r->fault_alloc > 0 && ++r->alloc_events == r->fault_alloc;
+        if (injected || cudaMalloc(&T.xv, sizeof(float4) * cap) != cudaSuccess ||
+            cudaMalloc(&T.vz, sizeof(float) * cap) != cudaSuccess || cudaMalloc(&T.w, sizeof(float) * cap) != cudaSuccess ||
+            cudaMalloc(&T.id, sizeof(unsigned) * cap) != cudaSuccess || cudaMalloc(&T.xv2, sizeof(float4) * cap) != cudaSuccess ||
+            cudaMalloc(&T.vz2, sizeof(float) * cap) != cudaSuccess || cudaMalloc(&T.w2, sizeof(float) * cap) != cudaSuccess ||
+            cudaMalloc(&T.id2, sizeof(unsigned) * cap) != cudaSuccess) {
             cudaGetLastError();
+            free_species(T);   /* what was allocated before the failure */
             return fail(r, PGB_ERR_NOMEM, "device allocation of particle storage failed");
         }
         if (S.cap > 0) {
@@ -297,6 +314,7 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
             return bail(PGB_ERR_CUDA);
         }
     r->copy_ev_ok = true;
+    if (const char* fa = std::getenv("PGB_FAULT_ALLOC")) r->fault_alloc = std::atoi(fa);
     /* the side stream only speeds steps up: without it steps run in turn.
      * It takes the highest priority, so that the field solve's short
      * kernels get SMs ahead of queued blocks of the run's own stream.     */
@@ -443,6 +461,7 @@ static long long sort_pad_slots(const pgb_params* p) {
 }
 
 extern "C" int pgb_load_species(pgb_run* r, int s, const double* aos6, int64_t n) {
+    Range range("pgb_load_species");
     if (!r || s < 0 || s > 1 || n < 0 || (n > 0 && !aos6)) return fail(r, PGB_ERR_ARG, "pgb_load_species: bad argument");
     if (n > 0x7fffffffLL) return fail(r, PGB_ERR_ARG, "pgb_load_species: too many particles");
     int rc = sync_state(r);
@@ -521,6 +540,7 @@ extern "C" int pgb_species_count(pgb_run* r, int s, int64_t* n_out) {
 }
 
 extern "C" int pgb_dump_species(pgb_run* r, int s, double* aos6, int64_t cap, int64_t* n_out) {
+    Range range("pgb_dump_species");
     if (!r || s < 0 || s > 1 || cap < 0 || (cap > 0 && !aos6)) return fail(r, PGB_ERR_ARG, "pgb_dump_species: bad argument");
     int rc = sync_state(r);
     if (rc) return rc;
@@ -909,6 +929,7 @@ static bool pipelined(pgb_run* r) { return r->side_ok && r->p.have_collisions &&
  * the rest of the step (graph B) waits for both, and this step's field
  * solve is left pending.                                                */
 static int issue_one_step(pgb_run* r) {
+    Range range("step");
     int rc;
     const bool pipe = pipelined(r);
     bool forked = false;
@@ -983,6 +1004,7 @@ static int issue_one_step(pgb_run* r) {
 }
 
 extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
+    Range range("pgb_step");
     if (!r || nsteps < 0) return fail(r, PGB_ERR_ARG, "pgb_step: bad argument");
     int rc = need_particles(r);
     if (rc) return rc;
@@ -999,6 +1021,7 @@ extern "C" int pgb_step(pgb_run* r, int32_t nsteps) {
 }
 
 extern "C" int pgb_step_async(pgb_run* r, int32_t nsteps) {
+    Range range("pgb_step_async");
     if (!r || nsteps < 0) return fail(r, PGB_ERR_ARG, "pgb_step_async: bad argument");
     int rc = need_particles(r);
     if (rc) return rc;
@@ -1027,6 +1050,7 @@ extern "C" int pgb_query(pgb_run* r, int32_t* idle) {
 }
 
 extern "C" int pgb_step_batch(pgb_run* const* runs, int32_t nruns, int32_t nsteps) {
+    Range range("pgb_step_batch");
     if (!runs || nruns < 0 || nsteps < 0) return fail(nullptr, PGB_ERR_ARG, "pgb_step_batch: bad argument");
     for (int a = 0; a < nruns; ++a) {
         if (!runs[a]) return fail(nullptr, PGB_ERR_ARG, "pgb_step_batch: null run handle");

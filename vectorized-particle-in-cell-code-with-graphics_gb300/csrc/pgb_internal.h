@@ -193,6 +193,9 @@ struct pgb_run {
     bool copy_ev_ok = false;
     /* instrumentation */
     long long launches = 0;        /* kernel launches issued                     */
+    /* host-side fault injection for tests: PGB_FAULT_ALLOC=k at pgb_create
+     * makes the handle's k-th particle-storage growth fail (PGB_ERR_NOMEM) */
+    int fault_alloc = 0, alloc_events = 0;
     int prof_on = 0;
     pgb_profile prof;
     cudaEvent_t prof_ev[12];

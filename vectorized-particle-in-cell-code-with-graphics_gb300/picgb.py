@@ -361,8 +361,16 @@ def _dptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+PGB_ERR_ARG, PGB_ERR_CUDA, PGB_ERR_NOMEM, PGB_ERR_CAPACITY, PGB_ERR_STATE, PGB_ERR_IO = -1, -2, -3, -4, -5, -6
+
+
 class PicError(RuntimeError):
-    pass
+    """A failed call; `code` is the library's PGB_ERR_* status (0 when the
+    error was found on the Python side)."""
+
+    def __init__(self, msg: str, code: int = 0):
+        super().__init__(msg)
+        self.code = code
 
 
 class Run:
@@ -383,7 +391,7 @@ class Run:
 
     def _check(self, rc: int, what: str):
         if rc != 0:
-            raise PicError(f"{what} failed ({rc}): {self.lib.pgb_last_error(self.h).decode()}")
+            raise PicError(f"{what} failed ({rc}): {self.lib.pgb_last_error(self.h).decode()}", rc)
 
     def close(self):
         if self.h:
@@ -557,7 +565,7 @@ class Server:
 
     def _check(self, rc, what):
         if rc != 0:
-            raise PicError(f"{what} failed ({rc}): {self.lib.pgb_last_error(None).decode()}")
+            raise PicError(f"{what} failed ({rc}): {self.lib.pgb_last_error(None).decode()}", rc)
 
     def submit(self, params: PgbParams, e: np.ndarray, i: np.ndarray, nsteps: int) -> int:
         e = np.ascontiguousarray(e, dtype=np.float64)
@@ -623,9 +631,21 @@ def step_batch(runs, n: int = 1):
 
 def read_datadump(path: str) -> np.ndarray:
     """particle::load_particles (particle.cpp:359-401): whitespace-separated
-    records `x y vx vy vz weight`, read until the first incomplete record."""
+    records `x y vx vy vz weight`, read while `in >> x >> ... >> weight`
+    succeeds: up to the first incomplete record or the first token that is
+    not a number."""
     with open(path, "rb") as f:
-        vals = np.array(f.read().split(), dtype=np.float64)
+        toks = f.read().split()
+    try:
+        vals = np.array(toks, dtype=np.float64)
+    except ValueError:
+        good = []
+        for t in toks:
+            try:
+                good.append(float(t))
+            except ValueError:
+                break
+        vals = np.array(good, dtype=np.float64)
     n = vals.size // 6
     return vals[: n * 6].reshape(n, 6)
 
