@@ -490,7 +490,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--poisson", default="FMG32", choices=["FMG32", "FMG_REF", "FP32_DC"])
-    ap.add_argument("--sort", type=int, default=16, help="spatial sort every k steps (0 = off)")
+    ap.add_argument("--sort", type=int, default=12,
+                    help="spatial sort of the electrons every k steps, of the ions every 4k (0 = off)")
     ap.add_argument("--batch-runs", type=int, default=64, help="runs of the batched workload (0 = skip it)")
     ap.add_argument("--batch-steps", type=int, default=200, help="steps per run of the batched workload")
     ap.add_argument("--serve-requests", type=int, default=16, help="requests of the served workload (0 = skip it)")

@@ -43,6 +43,11 @@ extern "C" {
 #define PGB_ERR_STATE    -5   /* call not valid in the handle's current state  */
 #define PGB_ERR_IO       -6   /* file could not be read or written             */
 
+/* Ions move far less per step than electrons, so their slot order stays
+ * close to the cell order for longer: they are sorted this many times
+ * less often.  The order of slots changes no deterministic result.      */
+#define PGB_ION_SORT_FACTOR 4
+
 /* ---- enumerations (string-valued macros of parameters.h) ---- */
 enum { PGB_ELECTRONS = 0, PGB_IONS = 1 };
 enum { PGB_ARGON = 0, PGB_HYDROGEN = 1 };                 /* SPECIES            */
@@ -108,7 +113,8 @@ typedef struct pgb_params {
     int32_t poisson_mode;          /* PGB_POISSON_*                               */
     int32_t dc_max_iters;          /* FP32_DC: max defect-correction passes       */
     double  dc_tolerance;          /* FP32_DC: stop when max|r| <= tol*max|f|     */
-    int32_t sort_interval;         /* cell-sort particles every k steps (0 = off) */
+    int32_t sort_interval;         /* cell-sort electrons every k steps, ions every
+                                      PGB_ION_SORT_FACTOR * k (0 = off)            */
     int64_t capacity_e, capacity_i;/* particle slots to reserve (0 = automatic)   */
 } pgb_params;
 

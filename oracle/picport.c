@@ -1178,7 +1178,8 @@ void orc_contain_growth(orc_run* r, int spi) {
 }
 
 /* Stable sort of a species by spatial bin, as the CUDA library orders its
- * particle slots every sort_interval steps (bins of 32x32 cells inside the
+ * particle slots (electrons every sort_interval steps, ions every
+ * PGB_ION_SORT_FACTOR * sort_interval; bins of 32x32 cells inside the
  * deposit region of pic.cl:35, then everything else).  Only the order
  * changes; it matters for the order-dependent rules (charge-exchange
  * accumulation, wall lists).                                              */
@@ -1506,9 +1507,9 @@ void orc_step(orc_run* r, int nsteps) {
     for (int k = 0; k < nsteps; ++k) {
         int64_t t = r->time_step;
         r->rng_step = (uint32_t)t;
-        if (r->order_mode == ORC_ORDER_STABLE && r->prm.sort_interval > 0 && t % r->prm.sort_interval == 0) {
-            orc_sort_bins(r, PGB_ELECTRONS);
-            orc_sort_bins(r, PGB_IONS);
+        if (r->order_mode == ORC_ORDER_STABLE && r->prm.sort_interval > 0) {
+            if (t % r->prm.sort_interval == 0) orc_sort_bins(r, PGB_ELECTRONS);
+            if (t % ((int64_t)r->prm.sort_interval * PGB_ION_SORT_FACTOR) == 0) orc_sort_bins(r, PGB_IONS);
         }
         if (r->prm.have_collisions) orc_collide_electrons(r);
         orc_inject(r);

@@ -950,9 +950,10 @@ static int issue_one_step(pgb_run* r) {
         }
     }
     if (r->p.sort_interval > 0) {
-        /* spatial sort (drops tombstones too) every sort_interval steps */
-        if (r->time_step % r->p.sort_interval == 0)
-            for (int s = 0; s < 2; ++s) {
+        /* spatial sort (drops tombstones too): electrons every sort_interval
+         * steps, ions every PGB_ION_SORT_FACTOR * sort_interval           */
+        for (int s = 0; s < 2; ++s)
+            if (r->time_step % ((long long)r->p.sort_interval * (s ? PGB_ION_SORT_FACTOR : 1)) == 0) {
                 /* the padded layout needs n + pad slots; grow first if the
                  * (lazily read) count comes near the capacity              */
                 const long long pad = sort_pad_slots(&r->p);
