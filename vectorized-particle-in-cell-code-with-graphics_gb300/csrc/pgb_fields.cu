@@ -329,20 +329,40 @@ __device__ __forceinline__ void sm_down(const SmallMG<T>& s, int j, int l, T* u,
     }
     Tm::sync();
 }
-/* level l on the way up: add the prolongated correction, then smooth */
+/* level l on the way up: add the prolongated correction (addint,
+ * mglin.cpp:90-97), then smooth.  The red sweep reads only black points
+ * and walls, the black sweep only red points and walls, and neither reads
+ * the point it updates; so the red sweep adds the correction to the values
+ * it reads (the same sums as after a separate pass, so the same bits), the
+ * red points' own corrected values would be overwritten unread, and the
+ * black sweep then overwrites the black points.  The walls' correction is
+ * +0 and leaves them as they are.  One pass and one barrier fewer.       */
 template <class T, class Tm>
 __device__ __forceinline__ void sm_up(const SmallMG<T>& s, int j, int l, T* u, const T* f) {
     T* ul = (l == j) ? u : s.V(l);
     const T* fl = (l == j) ? f : s.R(l);
-    const int nf = s.n(l), nc = s.n(l - 1);
-    const float inv = 1.0f / (float)nf;
+    const int n = s.n(l), nc = s.n(l - 1);
     const T* vc = s.V(l - 1);
-    for (int k = threadIdx.x; k < nf * nf; k += Tm::size()) {
-        int i = sm_row(k, inv), jj = k - i * nf;
-        ul[k] = ul[k] + prolong_point(vc, nc, i, jj);
+    T h = s.length / (T)(n - 1), h2 = h * h;
+    const int m = n - 2, per_row = (n - 1) >> 1, sh = __ffs(per_row) - 1;
+    for (int t = threadIdx.x; t < m * per_row; t += Tm::size()) {
+        int r = t >> sh, c = t & (per_row - 1);
+        int i = r + 1, jj = 1 + ((i + 1) & 1) + 2 * c;
+        if (jj <= n - 2) {
+            T a = ul[(i + 1) * n + jj] + prolong_point(vc, nc, i + 1, jj);
+            T b = ul[(i - 1) * n + jj] + prolong_point(vc, nc, i - 1, jj);
+            T e = ul[i * n + jj + 1] + prolong_point(vc, nc, i, jj + 1);
+            T w = ul[i * n + jj - 1] + prolong_point(vc, nc, i, jj - 1);
+            ul[i * n + jj] = (T)0.25 * (a + b + e + w - h2 * fl[i * n + jj]);
+        }
     }
     Tm::sync();
-    sm_relax<T, Tm>(ul, fl, nf, s.length);
+    for (int t = threadIdx.x; t < m * per_row; t += Tm::size()) {
+        int r = t >> sh, c = t & (per_row - 1);
+        int i = r + 1, jj = 1 + (i & 1) + 2 * c;
+        if (jj <= n - 2) ul[i * n + jj] = gs_point(ul, fl, n, i, jj, h2);
+    }
+    Tm::sync();
 }
 /* FMG interpolation of level l from level l-1 */
 template <class T, class Tm>
