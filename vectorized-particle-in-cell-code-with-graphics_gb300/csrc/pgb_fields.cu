@@ -299,6 +299,39 @@ __device__ __forceinline__ void sm_relax(T* u, const T* f, int n, T length) {
         Tm::sync();
     }
 }
+/* the FMG interpolation u = P(uc) (mglin.cpp:49) followed by one
+ * red-black sweep, as one sweep fewer: the red sweep reads only black
+ * points and walls, so it interpolates the ones it reads (the same values,
+ * so the same bits); the walls get their interpolated values; the black
+ * sweep then overwrites the black points, whose interpolated values
+ * nothing else would have read.                                          */
+template <class T, class Tm>
+__device__ __forceinline__ void sm_relax_from_coarse(T* u, const T* f, int n, T length, const T* uc, int nc) {
+    T h = length / (T)(n - 1), h2 = h * h;
+    const int m = n - 2, per_row = (n - 1) >> 1, sh = __ffs(per_row) - 1;
+    for (int t = threadIdx.x; t < m * per_row; t += Tm::size()) {
+        int r = t >> sh, c = t & (per_row - 1);
+        int i = r + 1, j = 1 + ((i + 1) & 1) + 2 * c;
+        if (j <= n - 2) {
+            T a = prolong_point(uc, nc, i + 1, j), b = prolong_point(uc, nc, i - 1, j);
+            T e = prolong_point(uc, nc, i, j + 1), w = prolong_point(uc, nc, i, j - 1);
+            u[i * n + j] = (T)0.25 * (a + b + e + w - h2 * f[i * n + j]);
+        }
+    }
+    for (int t = threadIdx.x; t < 4 * (n - 1); t += Tm::size()) {
+        const int side = t / (n - 1), k = t - side * (n - 1);
+        const int i = side == 0 ? 0 : side == 1 ? k : side == 2 ? n - 1 : n - 1 - k;
+        const int j = side == 0 ? k : side == 1 ? n - 1 : side == 2 ? n - 1 - k : 0;
+        u[i * n + j] = prolong_point(uc, nc, i, j);
+    }
+    Tm::sync();
+    for (int t = threadIdx.x; t < m * per_row; t += Tm::size()) {
+        int r = t >> sh, c = t & (per_row - 1);
+        int i = r + 1, j = 1 + (i & 1) + 2 * c;
+        if (j <= n - 2) u[i * n + j] = gs_point(u, f, n, i, j, h2);
+    }
+    Tm::sync();
+}
 template <class T, class Tm>
 __device__ __forceinline__ void sm_coarsest(T* u, const T* f, T length) {
     if (threadIdx.x == 0) {
@@ -311,12 +344,13 @@ __device__ __forceinline__ void sm_coarsest(T* u, const T* f, T length) {
 /* level l of a V-cycle whose top is j, on the way down: smooth, then the
  * restricted residual and a zero correction on level l-1               */
 template <class T, class Tm>
-__device__ __forceinline__ void sm_down(const SmallMG<T>& s, int j, int l, T* u, const T* f) {
+__device__ __forceinline__ void sm_down(const SmallMG<T>& s, int j, int l, T* u, const T* f, const T* from = nullptr) {
     T* ul = (l == j) ? u : s.V(l);
     const T* fl = (l == j) ? f : s.R(l);
     const int nf = s.n(l), nc = s.n(l - 1);
     const T h = s.length / (T)(nf - 1), h2i = (T)1.0 / (h * h);
-    sm_relax<T, Tm>(ul, fl, nf, s.length);
+    if (from) sm_relax_from_coarse<T, Tm>(ul, fl, nf, s.length, from, nc);
+    else sm_relax<T, Tm>(ul, fl, nf, s.length);
     const float inv = 1.0f / (float)nc;
     T* const rc = s.R(l - 1);
     T* const vc = s.V(l - 1);
@@ -364,34 +398,23 @@ __device__ __forceinline__ void sm_up(const SmallMG<T>& s, int j, int l, T* u, c
     }
     Tm::sync();
 }
-/* FMG interpolation of level l from level l-1 */
-template <class T, class Tm>
-__device__ __forceinline__ void sm_prolong_u(const SmallMG<T>& s, int l) {
-    const int nf = s.n(l), nc = s.n(l - 1);
-    const float inv = 1.0f / (float)nf;
-    T* const uf = s.U(l);
-    const T* uc = s.U(l - 1);
-    for (int k = threadIdx.x; k < nf * nf; k += Tm::size()) {
-        int i = sm_row(k, inv), jj = k - i * nf;
-        uf[k] = prolong_point(uc, nc, i, jj);
-    }
-    Tm::sync();
-}
 /* the part of a V-cycle (top j) from level l (at most 17 nodes) down to
  * the coarsest solve and back up to l; entered by threads 0..255 only   */
 template <class T>
-__device__ __forceinline__ void sm_vcycle_small(const SmallMG<T>& s, int j, int l, T* u, const T* f) {
-    for (int m = l; m >= 1; --m) sm_down<T, TeamSmall>(s, j, m, u, f);
+__device__ __forceinline__ void sm_vcycle_small(const SmallMG<T>& s, int j, int l, T* u, const T* f,
+                                                const T* from = nullptr) {
+    for (int m = l; m >= 1; --m) sm_down<T, TeamSmall>(s, j, m, u, f, m == j ? from : nullptr);
     if (j == 0) sm_coarsest<T, TeamSmall>(u, f, s.length);
     else sm_coarsest<T, TeamSmall>(s.V(0), s.R(0), s.length);
     for (int m = 1; m <= l; ++m) sm_up<T, TeamSmall>(s, j, m, u, f);
 }
-/* V-cycle at level j on (u, f) using V/R of the levels below; all threads */
+/* V-cycle at level j on (u, f) using V/R of the levels below; all threads.
+ * from: the coarser level to interpolate u from first (FMG), or null.   */
 template <class T>
-__device__ __forceinline__ void sm_vcycle(const SmallMG<T> s, int j, T* u, const T* f) {
+__device__ __forceinline__ void sm_vcycle(const SmallMG<T> s, int j, T* u, const T* f, const T* from = nullptr) {
     int l = j;
-    for (; l >= 1 && s.n(l) >= 33; --l) sm_down<T, TeamCta>(s, j, l, u, f);
-    if (threadIdx.x < 256) sm_vcycle_small(s, j, l, u, f);
+    for (; l >= 1 && s.n(l) >= 33; --l) sm_down<T, TeamCta>(s, j, l, u, f, l == j ? from : nullptr);
+    if (threadIdx.x < 256) sm_vcycle_small(s, j, l, u, f, l == j ? from : nullptr);
     __syncthreads();
     for (int m = l + 1; m <= j; ++m) sm_up<T, TeamCta>(s, j, m, u, f);
 }
@@ -426,16 +449,12 @@ __global__ void __launch_bounds__(1024, 1) k_mg_small(int J, int mode, T length,
         const int ls = J < 3 ? J : 3;
         if (threadIdx.x < 256) {
             sm_coarsest<T, TeamSmall>(s.U(0), s.F(0), length);
-            for (int l = 1; l <= ls; ++l) {
-                sm_prolong_u<T, TeamSmall>(s, l);
-                for (int c = 0; c < 2; ++c) sm_vcycle_small(s, l, l, s.U(l), s.F(l));
-            }
+            for (int l = 1; l <= ls; ++l)
+                for (int c = 0; c < 2; ++c) sm_vcycle_small(s, l, l, s.U(l), s.F(l), c == 0 ? s.U(l - 1) : nullptr);
         }
         __syncthreads();
-        for (int l = ls + 1; l <= J; ++l) {
-            sm_prolong_u<T, TeamCta>(s, l);
-            for (int c = 0; c < 2; ++c) sm_vcycle(s, l, s.U(l), s.F(l));
-        }
+        for (int l = ls + 1; l <= J; ++l)
+            for (int c = 0; c < 2; ++c) sm_vcycle(s, l, s.U(l), s.F(l), c == 0 ? s.U(l - 1) : nullptr);
         T* const gu = g_u[J];
         const T* uJ = s.U(J);
         for (int k = threadIdx.x; k < s.n(J) * s.n(J); k += blockDim.x) gu[k] = uJ[k];
