@@ -395,7 +395,7 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
             cudaMemcpy(r->neut[w], tab32.data(), sizeof(float) * nn, cudaMemcpyHostToDevice);
         }
     }
-    if (pgb_mg_setup(r) || pgb_sort_setup(r) || pgb_particles_setup(r)) { g_create_error = r->err; return bail(PGB_ERR_CUDA); }
+    if (pgb_mg_setup(r) || pgb_sort_setup(r)) { g_create_error = r->err; return bail(PGB_ERR_CUDA); }
     if (!pgb_cuda_ok(nullptr, cudaDeviceSynchronize(), "create")) return bail(PGB_ERR_CUDA);
     *out = r;
     return 0;

@@ -231,17 +231,6 @@ __global__ void k_restrict(T* uc, const T* uf, int nc) {
         uc[k] = v;
     }
 }
-template <class T>
-__global__ void k_prolong(T* uf, const T* uc, int nf, int add) {
-    pgb_pdl_entry();
-    const int nc = nf / 2 + 1;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nf * nf; k += gridDim.x * blockDim.x) {
-        int i = k / nf, j = k - i * nf;
-        T v = prolong_point(uc, nc, i, j);
-        uf[k] = add ? uf[k] + v : v;
-    }
-}
-
 /* --------------------------------------- one-CTA solver for coarse levels */
 /* Shared-memory image of levels 0..J (n_l = 2^(l+1)+1).  U/F: the current
  * level's solution and right-hand side at the top, V/R: correction and

@@ -930,8 +930,6 @@ int pgb_launch_step_advance(pgb_run* r) {
     return 0;
 }
 
-int pgb_particles_setup(pgb_run*) { return 0; }
-
 /* leave_sms: SMs the collision kernels leave free (one block fills an SM).
  * Small runs take fewer blocks: one per MCC_GROUPS tiles for k_mcc, one per
  * 16 Ki electrons for k_scatter (about a scattering per thread), from the
