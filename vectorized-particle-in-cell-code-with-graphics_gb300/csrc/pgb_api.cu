@@ -752,7 +752,7 @@ static int mcc_part(pgb_run* r, int leave_sms) {
 }
 static int step_mcc(pgb_run* r, bool) { return mcc_part(r, 0); }
 /* beside a field solve: the one-CTA multigrid needs SMs of its own */
-#define PGB_FIELD_SMS 16
+#define PGB_FIELD_SMS 32
 static int step_mcc_beside(pgb_run* r, bool) { return mcc_part(r, PGB_FIELD_SMS); }
 
 static int step_particles(pgb_run* r, bool ion_step) {
