@@ -478,6 +478,20 @@ def run_gpu(args, rank, world):
                 batched=batched, served=served, render=render)
 
 
+def combine_ranks(ms: float, ps: float):
+    """Every rank steps its own replica (weak scaling, no data-path
+    collective): the job's time is the slowest rank's, its work the sum of
+    the ranks' particle-steps.  Needs an initialised process group."""
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    tmax = torch.tensor([ms], dtype=torch.float64, device=dev)
+    tsum = torch.tensor([ps], dtype=torch.float64, device=dev)
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(tsum[0])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -535,15 +549,7 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     res = run_gpu(args, rank, world)
-    if world > 1:
-        import torch
-        t = torch.tensor([res["ms"], res["ps"]], dtype=torch.float64, device="cuda")
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
-        ms, ps = float(tmax[0]), float(t[1])
-    else:
-        ms, ps = res["ms"], res["ps"]
+    ms, ps = combine_ranks(res["ms"], res["ps"]) if world > 1 else (res["ms"], res["ps"])
     if rank != 0:
         return
     value = ps / (ms / 1000.0)
