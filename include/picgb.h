@@ -175,6 +175,11 @@ PGB_API int pgb_load_species(pgb_run* run, int species, const double* aos6, int6
  * copy the live particles out as 6 doubles each.  *n_out = live count; at
  * most cap records are written.                                             */
 PGB_API int pgb_dump_species(pgb_run* run, int species, double* aos6, int64_t cap, int64_t* n_out);
+/* No reference counterpart (the reference's particles carry no identity):
+ * the id of every live particle, in pgb_dump_species's order.  Ids key the
+ * particle's random streams: loaded particles get 0..n-1, new ones the next
+ * ids in creation order.  *n_out = live count; at most cap ids are written. */
+PGB_API int pgb_dump_ids(pgb_run* run, int species, uint32_t* ids, int64_t cap, int64_t* n_out);
 /* particle::particle_size */
 PGB_API int pgb_species_count(pgb_run* run, int species, int64_t* n_out);
 

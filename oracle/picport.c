@@ -481,12 +481,21 @@ static void assemble_rhs(orc_run* r, double* f, double phi_right) {
         f[(ny - 2) * nx + i] = f[(ny - 2) * nx + i] - r->prm.phi_top * divdxdy;
     }
 }
+/* FP64 full-multigrid passes of the converged solve: each divides the
+ * error by more than 1e3, so 12 reach FP64 rounding at 513^2           */
+#define ORC_CONVERGED_PASSES 12
 static void apply_walls(orc_run* r, double* phi, double phi_right) {
     const int nx = r->nx, ny = r->ny;
     for (int j = 0; j < ny; j++) { phi[j * nx] = r->prm.phi_left; phi[j * nx + nx - 1] = phi_right; }
     for (int i = 0; i < nx; i++) { phi[i] = r->prm.phi_bottom; phi[(ny - 1) * nx + i] = r->prm.phi_top; }
 }
 void orc_poisson(orc_run* r, int64_t t) {
+    /* PGB_POISSON_FP32_DC approximates the exact discrete solution: its
+     * FP64 oracle is that solution (defect correction to convergence)   */
+    if (r->prm.poisson_mode == PGB_POISSON_FP32_DC) {
+        orc_poisson_converged(r, t, ORC_CONVERGED_PASSES);
+        return;
+    }
     double phi_right = r->prm.phi_right * cos(r->prm.phi_period * (double)t);
     assemble_rhs(r, r->phi, phi_right);
     memcpy(r->rhs, r->phi, sizeof(double) * (size_t)r->nx * r->ny);

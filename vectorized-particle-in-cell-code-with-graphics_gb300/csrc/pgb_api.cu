@@ -564,13 +564,32 @@ extern "C" int pgb_dump_species(pgb_run* r, int s, double* aos6, int64_t cap, in
         const int t1 = std::min(ntiles, t0 + per);
         const long long a = std::min<long long>(toff[t0], m), b = std::min<long long>(t1 < ntiles ? toff[t1] : live, m);
         cudaEvent_t ev = r->copy_ev[k % PGB_COPY_EVENTS];
-        ok = pgb_launch_dump(r, s, r->d_stage, live, t0, t1) == 0 && cudaEventRecord(ev, r->stream) == cudaSuccess &&
+        ok = pgb_launch_dump(r, s, r->d_stage, nullptr, live, t0, t1) == 0 && cudaEventRecord(ev, r->stream) == cudaSuccess &&
              cudaStreamWaitEvent(r->copy_stream, ev, 0) == cudaSuccess &&
              (b <= a || cudaMemcpyAsync(aos6 + 6 * a, r->d_stage + 6 * a, sizeof(double) * 6 * (b - a),
                                         cudaMemcpyDeviceToHost, r->copy_stream) == cudaSuccess);
     }
     if (!ok || cudaStreamSynchronize(r->copy_stream) != cudaSuccess || cudaStreamSynchronize(r->stream) != cudaSuccess)
         return fail(r, PGB_ERR_CUDA, "pgb_dump_species: download failed");
+    return 0;
+}
+
+extern "C" int pgb_dump_ids(pgb_run* r, int s, uint32_t* ids, int64_t cap, int64_t* n_out) {
+    Range range("pgb_dump_ids");
+    if (!r || s < 0 || s > 1 || cap < 0 || (cap > 0 && !ids)) return fail(r, PGB_ERR_ARG, "pgb_dump_ids: bad argument");
+    int rc = sync_state(r);
+    if (rc) return rc;
+    long long live = r->hs->n[s] - r->hs->dead[s];
+    if (n_out) *n_out = live;
+    long long m = std::min<long long>(live, cap);
+    if (m <= 0 || r->sp[s].cap == 0) return 0;
+    if ((rc = dstage(r, sizeof(double) * 6 * live))) return rc;
+    const int ntiles = (int)((r->hs->n[s] + PGB_TILE - 1) / PGB_TILE);
+    unsigned int* d_ids = reinterpret_cast<unsigned int*>(r->d_stage);
+    if (pgb_launch_dump_offsets(r, s) || pgb_launch_dump(r, s, nullptr, d_ids, m, 0, ntiles) ||
+        cudaMemcpyAsync(ids, d_ids, sizeof(uint32_t) * (size_t)m, cudaMemcpyDeviceToHost, r->stream) != cudaSuccess ||
+        cudaStreamSynchronize(r->stream) != cudaSuccess)
+        return fail(r, PGB_ERR_CUDA, "pgb_dump_ids: download failed");
     return 0;
 }
 

@@ -144,7 +144,9 @@ __device__ __forceinline__ T prolong_point(const T* uc, int nc, int i, int j) {
  * mode 0: relax uin
  * mode 1: uin + prolong(vc) first (addint, mglin.cpp:90-97), then relax
  * mode 2: prolong(vc) first (FMG interpolation, mglin.cpp:49), then relax;
- *         uin is not read                                                 */
+ *         uin is not read
+ * mode 3: relax from u = 0 (a correction's first smoothing); neither uin
+ *         nor vc is read                                                  */
 #define RT 8
 #define RTX 32
 template <class T, int MODE>
@@ -161,7 +163,8 @@ __global__ void __launch_bounds__(RT * RTX) k_relax_tile(const T* __restrict__ u
         int i = i0 - 2 + li, j = j0 - 2 + lj;
         T v = (T)0;
         if (i >= 0 && j >= 0 && i < n && j < n) {
-            if (MODE == 2) v = prolong_point(vc, nc, i, j);
+            if (MODE == 3) v = (T)0;
+            else if (MODE == 2) v = prolong_point(vc, nc, i, j);
             else {
                 v = uin[i * n + j];
                 if (MODE == 1) v = v + prolong_point(vc, nc, i, j);
@@ -604,7 +607,8 @@ static int relax_launch(pgb_run* r, const T* uin, T* uout, const T* f, int n, T 
 
 /* V-cycle at level j > small on (u, f) (mglin.cpp:176-196).  first_mode 2
  * replaces u by the prolongation of the coarser level before the
- * pre-smoothing (the FMG interpolation of mglin.cpp:49).  The
+ * pre-smoothing (the FMG interpolation of mglin.cpp:49); first_mode 3
+ * starts from u = 0 without reading it (a defect correction).  The
  * pre-smoothing goes from u to the level's spare buffer w, the residual is
  * taken there, and the post-smoothing goes from w back to u.  A level has
  * one V-cycle in flight at a time, so one spare buffer per level serves.  */
@@ -614,8 +618,9 @@ static int vcycle(pgb_run* r, const Levels<T>& L, int j, int jsmall, T* u, const
     int nf = r->mg_n[j], nc = r->mg_n[j - 1];
     T h = (T)r->p.xlength / (T)(nf - 1), h2 = h * h, h2i = (T)1.0 / (h * h);
     T* w = L.w[j];
-    int rc = first_mode == 2 ? relax_launch<T, 2>(r, nullptr, w, f, nf, h2, coarse_u)
-                             : relax_launch<T, 0>(r, u, w, f, nf, h2, nullptr);
+    int rc = first_mode == 2   ? relax_launch<T, 2>(r, nullptr, w, f, nf, h2, coarse_u)
+             : first_mode == 3 ? relax_launch<T, 3>(r, nullptr, w, f, nf, h2, nullptr)
+                               : relax_launch<T, 0>(r, u, w, f, nf, h2, nullptr);
     if (rc) return rc;
     PGB_CK(r, pgb_launch_pdl(k_resid_restrict<T>, dim3(blocks_for((long long)nc * nc)), dim3(256), 0, r->stream, L.rr[j - 1], L.v[j - 1], w, f, nf, h2i));
     r->launches++;
@@ -658,20 +663,30 @@ static int fmg(pgb_run* r, const Levels<T>& L) {
     return 0;
 }
 
-/* FP64 defect d = f - L u on the interior (zero on the walls), as FP32 */
-__global__ void k_defect32(const double* u, const double* f, float* d, int n, double h2i) {
+/* One defect-correction update: u' = u + e in FP64 (u' = e on the first
+ * pass, when u is null), written to a second buffer so that neighbours
+ * read the old values, and the FP64 defect d = f - L u' of the interior
+ * (zero on the walls) stored as FP32 for the next FP32 correction.  The
+ * walls of u, e and so u' are 0.                                         */
+__global__ void k_dc_update(const double* __restrict__ u, const float* __restrict__ e, double* __restrict__ uout,
+                            const double* __restrict__ f, float* __restrict__ d, int n, double h2i) {
     pgb_pdl_entry();
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n * n; k += gridDim.x * blockDim.x) {
         int i = k / n, j = k - i * n;
-        double v = 0.0;
+        auto U = [&](int q) { return u ? u[q] + (double)e[q] : (double)e[q]; };
+        double c = U(k), v = 0.0;
         if (i > 0 && j > 0 && i < n - 1 && j < n - 1)
-            v = f[k] - h2i * (u[k + n] + u[k - n] + u[k + 1] + u[k - 1] - 4.0 * u[k]);
+            v = f[k] - h2i * (U(k + n) + U(k - n) + U(k + 1) + U(k - 1) - 4.0 * c);
+        uout[k] = c;
         d[k] = (float)v;
     }
 }
-__global__ void k_add32(double* u, const float* e, int count) {
+/* the last correction: phi = u + e in FP64 (the walls are set after) */
+__global__ void k_dc_final(double* __restrict__ phi, const double* __restrict__ u, const float* __restrict__ e,
+                           int count) {
     pgb_pdl_entry();
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) u[k] += (double)e[k];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x)
+        phi[k] = u[k] + (double)e[k];
 }
 __global__ void k_to32(float* d, const double* s, int count) {
     pgb_pdl_entry();
@@ -717,6 +732,7 @@ int pgb_mg_setup(pgb_run* r) {
     PGB_CK(r, cudaMemcpy(r->mg32_tab, tabs32, sizeof(tabs32), cudaMemcpyHostToDevice));
     size_t G = (size_t)r->nx * r->ny;
     PGB_CK(r, cudaMalloc(&r->dc_u, G * sizeof(double)));
+    PGB_CK(r, cudaMalloc(&r->dc_u2, G * sizeof(double)));
     PGB_CK(r, cudaFuncSetAttribute(k_mg_small<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)small_smem_bytes(small_top(r, sizeof(double)), sizeof(double))));
     PGB_CK(r, cudaFuncSetAttribute(k_mg_small<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -731,12 +747,18 @@ void pgb_mg_free(pgb_run* r) {
     }
     cudaFree(r->mg32_tab);
     cudaFree(r->dc_u);
+    cudaFree(r->dc_u2);
 }
 
 /* fields::grid_potential after the right-hand side is in mg_f[ng-1]:
  *   FMG_REF  FP64 full multigrid with the reference's schedule (bitwise)
  *   FMG32    the same schedule in FP32
- *   FP32_DC  FP32 full multigrid inside an FP64 defect-correction loop   */
+ *   FP32_DC  FP64 defect correction around FP32 multigrid: the FMG32 pass
+ *            on the right-hand side, then dc_max_iters - 1 passes of
+ *            (FP64 defect of the FP64 solution, one FP32 V-cycle on it
+ *            from zero, FP64 addition of that correction).  The FP32 pass
+ *            leaves an error of a few 1e-5 of phi; each V-cycle divides it
+ *            by about ten, down to the FP64 discrete solution.          */
 int pgb_poisson_solve(pgb_run* r) {
     const int top = r->ng - 1, n = r->nx;
     const int G = n * n;
@@ -744,26 +766,43 @@ int pgb_poisson_solve(pgb_run* r) {
     if (r->p.poisson_mode == PGB_POISSON_FMG_REF) {
         if (fmg<double>(r, levels64(r))) return PGB_ERR_CUDA;
         PGB_CK(r, cudaMemcpyAsync(r->phi, r->mg_u[top], sizeof(double) * G, cudaMemcpyDeviceToDevice, r->stream));
-    } else if (r->p.poisson_mode == PGB_POISSON_FMG32) {
+    } else {
         Levels<float> L = levels32(r);
         PGB_CK(r, pgb_launch_pdl(k_to32, dim3(gb), dim3(256), 0, r->stream, L.f[top], r->mg_f[top], G));
         r->launches++;
         if (fmg<float>(r, L)) return PGB_ERR_CUDA;
-        PGB_CK(r, pgb_launch_pdl(k_to64, dim3(gb), dim3(256), 0, r->stream, r->phi, L.u[top], G));
-        r->launches++;
-    } else {
-        Levels<float> L = levels32(r);
-        double h = r->p.xlength / (n - 1), h2i = 1.0 / (h * h);
-        PGB_CK(r, cudaMemsetAsync(r->dc_u, 0, sizeof(double) * G, r->stream));
-        int iters = r->p.dc_max_iters > 0 ? r->p.dc_max_iters : 1;
-        for (int it = 0; it < iters; ++it) {
-            PGB_CK(r, pgb_launch_pdl(k_defect32, dim3(gb), dim3(256), 0, r->stream, r->dc_u, r->mg_f[top], L.f[top], n, h2i));
+        const int passes = r->p.poisson_mode == PGB_POISSON_FP32_DC && r->p.dc_max_iters > 1 ? r->p.dc_max_iters : 1;
+        if (passes == 1) {
+            PGB_CK(r, pgb_launch_pdl(k_to64, dim3(gb), dim3(256), 0, r->stream, r->phi, L.u[top], G));
             r->launches++;
-            if (fmg<float>(r, L)) return PGB_ERR_CUDA;
-            PGB_CK(r, pgb_launch_pdl(k_add32, dim3(gb), dim3(256), 0, r->stream, r->dc_u, L.u[top], G));
+        } else {
+            const double h = r->p.xlength / (n - 1), h2i = 1.0 / (h * h);
+            const int jsmall = small_top(r, sizeof(float));
+            /* a grid solved inside one CTA takes its V-cycle there, on the
+             * level's correction and residual arrays (v, r)              */
+            const bool one_cta = top <= jsmall;
+            float* const dtop = one_cta ? L.rr[top] : L.f[top];
+            float* const etop = one_cta ? L.v[top] : L.u[top];
+            const float* e = L.u[top];   /* the FMG pass's result        */
+            double* ua = nullptr;        /* FP64 solution so far (null: 0) */
+            double* ub = r->dc_u;
+            for (int it = 1; it < passes; ++it) {
+                PGB_CK(r, pgb_launch_pdl(k_dc_update, dim3(gb), dim3(256), 0, r->stream, (const double*)ua, e, ub,
+                                         (const double*)r->mg_f[top], dtop, n, h2i));
+                r->launches++;
+                ua = ub;
+                ub = (ub == r->dc_u) ? r->dc_u2 : r->dc_u;
+                if (one_cta) {
+                    PGB_CK(r, cudaMemsetAsync(etop, 0, sizeof(float) * G, r->stream));
+                    if (small_launch<float>(r, L.tab, top, 1)) return PGB_ERR_CUDA;
+                } else if (vcycle<float>(r, L, top, jsmall, etop, dtop, 3, nullptr)) {
+                    return PGB_ERR_CUDA;
+                }
+                e = etop;
+            }
+            PGB_CK(r, pgb_launch_pdl(k_dc_final, dim3(gb), dim3(256), 0, r->stream, r->phi, (const double*)ua, e, G));
             r->launches++;
         }
-        PGB_CK(r, cudaMemcpyAsync(r->phi, r->dc_u, sizeof(double) * G, cudaMemcpyDeviceToDevice, r->stream));
     }
     PGB_CK(r, pgb_launch_pdl(k_walls, dim3(blocks_for((long long)r->nx * r->ny)), dim3(256), 0, r->stream, r->phi, r->nx, r->ny, r->p.phi_left, r->phi_tab,
                                                                          r->ds, r->p.phi_bottom, r->p.phi_top));

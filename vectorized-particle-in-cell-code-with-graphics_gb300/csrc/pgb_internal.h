@@ -114,7 +114,7 @@ struct pgb_run {
     double *mg_u[PGB_MAX_LEVELS], *mg_f[PGB_MAX_LEVELS], *mg_v[PGB_MAX_LEVELS], *mg_r[PGB_MAX_LEVELS];
     double** mg_tab = nullptr;                       /* device table of the level pointers */
     float** mg32_tab = nullptr;
-    double *dc_d = nullptr, *dc_u = nullptr;        /* FP32_DC defect correction (FP64) */
+    double *dc_u = nullptr, *dc_u2 = nullptr;       /* FP32_DC: FP64 solution, two buffers */
     float *mg32_u[PGB_MAX_LEVELS], *mg32_f[PGB_MAX_LEVELS], *mg32_v[PGB_MAX_LEVELS], *mg32_r[PGB_MAX_LEVELS];
     /* the pre-smoothing result of each level (the tiled smoother reads one
      * buffer and writes another: blocks never see a neighbour's update)  */
@@ -256,7 +256,7 @@ int pgb_launch_cx(pgb_run* r);
 int pgb_launch_walls(pgb_run* r, int which);
 int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long i0, long long i1);
 int pgb_launch_dump_offsets(pgb_run* r, int s);
-int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap, int t0, int t1);
+int pgb_launch_dump(pgb_run* r, int s, double* d_out, unsigned int* d_ids, long long cap, int t0, int t1);
 int pgb_mg_setup(pgb_run* r);
 void pgb_mg_free(pgb_run* r);
 CollConsts pgb_coll_consts(pgb_run* r);

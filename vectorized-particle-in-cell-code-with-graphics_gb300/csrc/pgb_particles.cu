@@ -799,8 +799,11 @@ __global__ void k_load(Species S, const double* aos, long long i0, long long i1,
 /* dump live slots in order: out[j] for the j-th live slot; pos[] = exclusive
  * scan of the per-tile live counts                                        */
 /* tiles [t0, t1) of the live-slot order */
+/* out (6 doubles per particle) and ids (the particle's id) are each
+ * written when not null                                                  */
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_dump(Species S, DevState* ds, int s, const int* toff, double dx,
-                                                           double dy, double* out, long long cap, int t0, int t1) {
+                                                           double dy, double* out, unsigned int* ids, long long cap,
+                                                           int t0, int t1) {
     pgb_pdl_entry();
     const long long n = ds->n[s];
     const int ntiles = min(t1, (int)((n + PGB_TILE - 1) / PGB_TILE));
@@ -826,12 +829,13 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_dump(Species S, DevState* 
             if (f[k]) {
                 long long i = (long long)tile * PGB_TILE + k * PGB_PUSH_THREADS + threadIdx.x;
                 long long pos = s_off[k][warp] + __popc(m[k] & ((1u << lane) - 1u));
-                if (pos < cap) {
+                if (pos < cap && out) {
                     float4 p = S.xv[i];
                     double* o = out + 6 * pos;
                     o[0] = (double)p.x * dx; o[1] = (double)p.y * dy;
                     o[2] = p.z; o[3] = p.w; o[4] = S.vz[i]; o[5] = S.w[i];
                 }
+                if (pos < cap && ids) ids[pos] = S.id[i];
             }
         __syncthreads();
     }
@@ -1052,9 +1056,9 @@ int pgb_launch_dump_offsets(pgb_run* r, int s) {
     return 0;
 }
 
-int pgb_launch_dump(pgb_run* r, int s, double* d_out, long long cap, int t0, int t1) {
-    PGB_CK(r, pgb_launch_pdl(k_dump, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, r->sp[s], r->ds, s, r->aux_j, r->dx, r->dy, d_out, cap,
-                                                               t0, t1));
+int pgb_launch_dump(pgb_run* r, int s, double* d_out, unsigned int* d_ids, long long cap, int t0, int t1) {
+    PGB_CK(r, pgb_launch_pdl(k_dump, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, r->sp[s], r->ds, s, r->aux_j, r->dx, r->dy, d_out,
+                             d_ids, cap, t0, t1));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;

@@ -309,6 +309,7 @@ def load_library():
         "pgb_load_species": (C.c_int, [R, C.c_int, dp, i64]),
         "pgb_dump_species": (C.c_int, [R, C.c_int, dp, i64, C.POINTER(i64)]),
         "pgb_species_count": (C.c_int, [R, C.c_int, C.POINTER(i64)]),
+        "pgb_dump_ids": (C.c_int, [R, C.c_int, C.POINTER(C.c_uint32), i64, C.POINTER(i64)]),
         "pgb_set_time_step": (C.c_int, [R, i64]),
         "pgb_initial_boundary": (C.c_int, [R]),
         "pgb_step": (C.c_int, [R, i32]),
@@ -425,6 +426,16 @@ class Run:
         out = np.empty((max(n, 1), 6), dtype=np.float64)
         got = C.c_int64()
         self._check(self.lib.pgb_dump_species(self.h, species, _dptr(out), n, C.byref(got)), "pgb_dump_species")
+        return out[: got.value].copy()
+
+    def get_ids(self, species: int) -> np.ndarray:
+        """Particle ids in get_particles' order (the key of each particle's
+        random streams)."""
+        n = self.particle_size(species)
+        out = np.empty(max(n, 1), dtype=np.uint32)
+        got = C.c_int64()
+        self._check(self.lib.pgb_dump_ids(self.h, species, out.ctypes.data_as(C.POINTER(C.c_uint32)), n,
+                                          C.byref(got)), "pgb_dump_ids")
         return out[: got.value].copy()
 
     # driver
