@@ -388,6 +388,9 @@ PGB_API int pgb_render(pgb_run* run, int plot, int32_t width, int32_t height, in
  *   - The first call on a device looks up the array with
  *     cudaGetSymbolAddress.  Make that first call with the device current,
  *     before any stream capture begins.
+ *   - That address is kept for the life of the process.  A cudaDeviceReset
+ *     of the device invalidates it: do not call this entry point on a
+ *     device after resetting it.
  *
  * Errors: other failures return PGB_ERR_ARG or PGB_ERR_CUDA, with the
  * message in pgb_last_error(NULL).

@@ -1186,6 +1186,37 @@ void orc_contain_growth(orc_run* r, int spi) {
     if (spi == 0) r->c.reductions_e++; else r->c.reductions_i++;
 }
 
+/* The library keeps a position as a signed 32-bit fixed-point number of
+ * cells with ps fraction bits (pgb_pos_shift of the grid), saturated at
+ * +-2^30 units; NaN is its own code.  These restate that rounding where the
+ * oracle must decide as the library decides (bin order, plot pixels).    */
+#define LIB_POS_NAN INT64_MIN
+static int64_t lib_fixed(double x, double d, int ps) {
+    double c = x / d;
+    if (c != c) return LIB_POS_NAN;
+    double v = ldexp(c, ps);
+    v = v < -1073741824.0 ? -1073741824.0 : (v > 1073741824.0 ? 1073741824.0 : v);
+    return (int64_t)nearbyint(v);
+}
+/* (int)(x/DX) of a fixed-point position: toward zero, INT_MIN for NaN */
+static int lib_cell(int64_t v, int ps) {
+    if (v == LIB_POS_NAN) return INT_MIN;
+    return v >= 0 ? (int)(v >> ps) : -(int)((-v) >> ps);
+}
+/* A position in FP32 cells as the library plots it: x/DX rounded to its
+ * fixed-point grid of 2^-ps of a cell (saturated at +-2^30 units), then to
+ * FP32 (the library keeps positions in that fixed point).              */
+static float plot_cells(double x, double d, int ps) {
+    int64_t v = lib_fixed(x, d, ps);
+    return v == LIB_POS_NAN ? (float)(x / d) : (float)ldexp((double)v, -ps);
+}
+static int lib_shift(const orc_run* r) {   /* the library's fraction bits for this grid (pgb_pos_shift) */
+    int cells = (r->nx > r->ny ? r->nx : r->ny) - 1, b = 0;
+    while ((1 << b) < cells) ++b;
+    int ps = 29 - b;
+    return ps > 23 ? 23 : (ps < 8 ? 8 : ps);
+}
+
 /* Stable sort of a species by spatial bin, as the CUDA library orders its
  * particle slots (electrons every sort_interval steps, ions every
  * PGB_ION_SORT_FACTOR * sort_interval; bins of 32x32 cells inside the
@@ -1203,16 +1234,16 @@ static void orc_sort_bins(orc_run* r, int spi) {
     orc_sp* S = &r->sp[spi];
     const int nx = r->nx, ny = r->ny, BIN = 32;
     const int nbx = (nx - 1 + BIN - 1) / BIN, nby = (ny - 1 + BIN - 1) / BIN, nbins = nbx * nby;
+    const int ps = lib_shift(r);
     int64_t n = S->n;
     if (n == 0) return;
     int64_t* keys = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
     int64_t* idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
     for (int64_t i = 0; i < n; ++i) {
-        /* the library classifies in FP32 cell units */
-        float xs = (float)(S->p[i].x / r->dx), ys = (float)(S->p[i].y / r->dy);
-        int jp = (xs >= -2147483648.0f && xs < 2147483648.0f) ? (int)xs : INT_MIN;
-        int kp = (ys >= -2147483648.0f && ys < 2147483648.0f) ? (int)ys : INT_MIN;
-        keys[i] = (jp < nx - 1 && xs > 0.0f && kp < ny - 1 && ys > 0.0f) ? (kp / BIN) * nbx + jp / BIN : nbins;
+        /* the library classifies its fixed-point positions (2^-ps of a cell) */
+        int64_t xf = lib_fixed(S->p[i].x, r->dx, ps), yf = lib_fixed(S->p[i].y, r->dy, ps);
+        int jp = lib_cell(xf, ps), kp = lib_cell(yf, ps);
+        keys[i] = (jp < nx - 1 && xf > 0 && kp < ny - 1 && yf > 0) ? (kp / BIN) * nbx + jp / BIN : nbins;
         idx[i] = i;
     }
     g_sort_keys = keys;
@@ -1398,13 +1429,14 @@ static void plot_point(unsigned char* img, int W, int H, int px, int py, const u
 }
 static void plot_species(orc_run* r, int s, int phase, int W, int H, int max_points, uint32_t seed,
                          const unsigned char* colour, unsigned char* img) {
+    const int ps = lib_shift(r);
     const orc_sp* S = &r->sp[s];
     const float lx = (float)(r->nx - 1), ly = (float)(r->ny - 1);
     int mvx = 1, mvy = 1;
     if (phase) {
         float mx = 0.0f, my = 0.0f;
         for (int64_t i = 0; i < S->n; ++i) {
-            float xs = (float)(S->p[i].x / r->dx), ys = (float)(S->p[i].y / r->dy);
+            float xs = plot_cells(S->p[i].x, r->dx, ps), ys = plot_cells(S->p[i].y, r->dy, ps);
             if (!(xs > 0.0f && xs < lx && ys > 0.0f && ys < ly) || !plot_keep(S->id[i], seed, S->n, max_points)) continue;
             float ax = fabsf((float)S->p[i].vx), ay = fabsf((float)S->p[i].vy);
             if (ax == ax && ax > mx) mx = ax;
@@ -1416,7 +1448,7 @@ static void plot_species(orc_run* r, int s, int phase, int W, int H, int max_poi
         if (mvy < 1) mvy = 1;
     }
     for (int64_t i = 0; i < S->n; ++i) {
-        float xs = (float)(S->p[i].x / r->dx), ys = (float)(S->p[i].y / r->dy);
+        float xs = plot_cells(S->p[i].x, r->dx, ps), ys = plot_cells(S->p[i].y, r->dy, ps);
         if (!(xs > 0.0f && xs < lx && ys > 0.0f && ys < ly) || !plot_keep(S->id[i], seed, S->n, max_points)) continue;
         float fx, fy;
         if (phase) {

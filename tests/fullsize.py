@@ -35,6 +35,12 @@ Reported errors (max norm relative to the oracle's max |value|):
   grids_tie_corrected            the same grids against the oracle's deposit and
                                  solve of its final particles with the ties
                                  replaced by the device's: the FP32 error alone
+  grids_away_from_ties           the tie-corrected comparison at nodes farther
+                                 than TIE_RADIUS cells from every tie particle
+                                 (nodes_near_ties: how many are nearer): a tie
+                                 particle's charge changed the field around it
+                                 in the steps after the decision and so moved
+                                 its neighbours, which the swap cannot undo
   solver                         phi, ex, ey against the oracle's solve of the
                                  device's own rho: the Poisson mode's error alone
   mean energy                    relative difference of the mean kinetic energy
@@ -60,6 +66,7 @@ GRIDS = ("q_e", "q_i", "rho", "phi", "ex", "ey")
 COUNTS = ("n_e", "n_i", "absorbed_e", "absorbed_i", "reflected", "backscattered", "see_events", "see_emitted",
           "ion_see_emitted", "elastic", "ionization", "charge_exchange", "injected_e", "injected_i")
 TIE_VT = 1e-2
+TIE_RADIUS = 6   # cells around a tie particle whose field moved its neighbours
 
 
 def rel_err(a, b):
@@ -70,10 +77,13 @@ def rel_err(a, b):
     return d / scale if scale > 0 else d
 
 
-def argon_257_params(n_per_species, poisson="FP32_DC", dc_passes=4, sort_interval=12, seed=1002):
+def argon_257_params(n_per_species, poisson="FP32_DC", dc_passes=5, sort_interval=12, seed=1002):
     """257^2 nodes, Ar at 0.01 Torr, Te = 2 eV, absorbing walls, energy-dependent
     e-Ar and Ar+-Ar fits; the macro-particle size gives the design density
-    1e15 m^-3 for n_per_species particles."""
+    1e15 m^-3 for n_per_species particles.  A uniform quasi-neutral plasma
+    has a charge density of nearly white noise, the slowest right-hand side
+    for the multigrid: five FP32_DC passes keep phi within 2e-6 of the FP64
+    solution (four leave 9e-6)."""
     kw = dict(X_NO_OF_CELLS=257, TEMPERATURE=2.0, GAS_PRESSURE_TORR=0.01, HAVE_COLLISIONS=True,
               SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT", SIGMA_IONIZATION="ENERGY_DEPENDENT",
               STEADYSTATE="NO", SIZE_TO_CHECK=2**31 - 1, RAND_SEED=seed, POISSON=poisson, DC_MAX_ITERS=dc_passes,
@@ -177,6 +187,35 @@ def _tie_corrected_fields(p, t, parts):
         o.close()
 
 
+def _far_from_ties(p, parts):
+    """Nodes farther than TIE_RADIUS cells from every tie particle (its final
+    position on either side).  A tie particle's different charge changed
+    the field around it in the steps after the decision, which moved its
+    neighbours together; the tie-corrected grids still hold that.  The rest
+    of the grid carries the FP32 error alone."""
+    nx, ny = p.x_no_of_cells, p.y_no_of_cells
+    dx, dy = p.xlength / (nx - 1), p.ylength / (ny - 1)
+    near = np.zeros((ny, nx), dtype=bool)
+    r = TIE_RADIUS
+    for a, ia, b, ib, ties in parts:
+        for P, I in ((a, ia), (b, ib)):
+            sel = P[_isin(I, ties)]
+            for x, y in sel[:, :2]:
+                if not (np.isfinite(x) and np.isfinite(y)):
+                    continue
+                cx, cy = int(round(x / dx)), int(round(y / dy))
+                near[max(cy - r, 0):max(cy + r + 1, 0), max(cx - r, 0):max(cx + r + 1, 0)] = True
+    return ~near.ravel()
+
+
+def _far_e(far, p):
+    """the node mask on the stride-nx E layout ((nx+1)(ny+1) entries)"""
+    nx, ny = p.x_no_of_cells, p.y_no_of_cells
+    m = np.ones((nx + 1) * (ny + 1), dtype=bool)
+    m[: nx * ny] = far
+    return m
+
+
 def _solver_only(p, t, gg):
     """The device's phi and E against the oracle's solve of the device's own
     rho (the FP64 solve the mode approximates): the solver's error alone."""
@@ -223,6 +262,15 @@ def compare(p, e, i, steps, threads=None, run=None):
         fixed = _tie_corrected_fields(p, steps - 1, parts) if out["ties"] else None
         out["grids_tie_corrected"] = ({g: rel_err(gg[g], fixed[g]) for g in GRIDS} if fixed is not None
                                       else dict(out["grids"]))
+        ref = fixed if fixed is not None else {g: o.get_grid(g) for g in GRIDS}
+        far = _far_from_ties(p, parts)
+        out["nodes_near_ties"] = int((~far).sum())
+        out["grids_away_from_ties"] = {}
+        for g in GRIDS:
+            a_, b_ = gg[g].ravel(), ref[g].ravel()
+            m = far if a_.size == far.size else _far_e(far, p)
+            scale = np.max(np.abs(b_))
+            out["grids_away_from_ties"][g] = float(np.max(np.abs(a_[m] - b_[m])) / scale) if scale > 0 else 0.0
         out["solver"] = _solver_only(p, steps - 1, gg)
         return out
     finally:

@@ -1,0 +1,99 @@
+"""Parity with the FP64 oracle at the benchmark's own sizes.
+
+The CUDA library (through its C ABI) and the oracle (oracle/picport.c in its
+library mode: the same Philox draws, the same stable particle order, OpenMP
+over the host cores; its Poisson solve for FP32_DC is the converged FP64
+solution) step the same seeded state for three steps, across a spatial sort
+step (the sort runs every 2 steps here), and tests/fullsize.py compares them.
+
+Workloads (tests/fullsize.py):
+  hydrogen_513  the benchmark's state: 513^2 nodes, 16Mi particles per species,
+                H plasma with the collisional boundary
+  argon_257     257^2 nodes, 4Mi particles per species, Ar, absorbing walls
+
+Why ties are counted rather than forbidden: the device keeps particles in
+FP32, the oracle in FP64.  A decision whose input lies within FP32 rounding of
+its threshold (an electron within ~1e-6 relative of the 13.6 eV ionization
+energy, P within rounding of 2R for an elastic collision, a position within
+rounding of a wall or of x = 0) can go either way.  At 16Mi electrons about
+one such decision happens per step.  Particles created after it take ids one
+apart on the two sides, and a secondary's velocity is drawn from its own id,
+so those particles pair up differently too.  Ties are therefore matched by
+id, counted, and bounded below.
+
+Tolerances (max norm relative to the oracle's max |value|):
+  fields away from ties ........ q, rho, phi, E within 1e-5 of the oracle's
+                                 deposit and solve of its final particles with
+                                 the tie particles taken from the device, at
+                                 nodes more than 6 cells from every tie particle
+  fields, tie-corrected ........ phi, E within 1e-5 everywhere; q, rho within
+                                 1e-4 everywhere (next to a tie, the tie
+                                 particle's field in the steps after the decision
+                                 moved its neighbours together, which no swap of
+                                 particles undoes)
+  Poisson solver alone ......... phi, E within 1e-5 of the converged FP64 solve
+                                 of the device's own rho
+  positions / velocities ....... 2e-4 cell / 1e-3 thermal speed (non-tie particles;
+                                 a particle next to a tie sees its field)
+  mean energy per species ...... 1e-5 relative
+  ties ......................... at most the particles created in the run (wall
+                                 secondaries, injected particles) plus 1e-6 of the
+                                 particle-steps
+  event counts ................. |device - oracle| <= 2 + 1e-5 * count
+"""
+import os
+import sys
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+import bench  # noqa: E402
+import fullsize  # noqa: E402
+import picgb  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+STEPS = 3
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(lib):
+    return lib
+
+
+def check(d, name):
+    print(name, {k: d[k] for k in ("grids", "grids_tie_corrected", "grids_away_from_ties", "nodes_near_ties",
+                                   "solver", "ties", "counts")})
+    print(name, d["particles"])
+    for g, e in d["grids_away_from_ties"].items():
+        assert e <= 1e-5, f"{name} {g}: {e:.3g} (away from ties)"
+    for g, e in d["grids_tie_corrected"].items():
+        assert e <= (1e-5 if g in ("phi", "ex", "ey") else 1e-4), f"{name} {g}: {e:.3g} (tie-corrected)"
+    for g, e in d["solver"].items():
+        assert e <= 1e-5, f"{name} solver {g}: {e:.3g}"
+    n_steps = 0
+    for sp, x in d["particles"].items():
+        assert x["pos_cells"] <= 2e-4, f"{name} {sp} positions {x['pos_cells']:.3g} cells"
+        assert x["vel_vt"] <= 1e-3, f"{name} {sp} velocities {x['vel_vt']:.3g} vt"
+        assert x["mean_energy_rel"] <= 1e-5, f"{name} {sp} mean energy {x['mean_energy_rel']:.3g}"
+        assert x["weights_equal"], f"{name} {sp} weights"
+        n_steps += x["n_oracle"] * d["steps"]
+    oc = d["oracle_counts"]
+    created = oc["see_emitted"] + oc["ion_see_emitted"] + oc["injected_e"] + oc["injected_i"]
+    assert d["ties"] <= created + 1e-6 * n_steps, f"{name}: {d['ties']} ties"
+    for k, dv in d["counts"].items():
+        assert abs(dv) <= 2 + 1e-5 * oc[k], f"{name} {k}: device - oracle = {dv} (oracle {oc[k]})"
+
+
+def test_hydrogen_513_bench_state_matches_oracle():
+    n = bench.N_PER_SPECIES
+    p = bench.workload_params(picgb, n_per_species=n, sort_interval=2)
+    e, i = bench.gaussian_state(p, n, 3.0, 0.026, 1003, p.ion_mass)
+    check(fullsize.compare(p, e, i, STEPS), "hydrogen_513")
+
+
+def test_argon_257_matches_oracle():
+    n = 4 * 1024 * 1024
+    p = fullsize.argon_257_params(n, sort_interval=2)
+    e, i = fullsize.uniform_state(p, n, 2.0, 0.026, 1002)
+    check(fullsize.compare(p, e, i, STEPS), "argon_257")

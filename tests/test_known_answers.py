@@ -89,8 +89,9 @@ def test_free_streaming_and_gyration_with_zero_field(b):
     x, y, v = _orbit(e[:, 2:5], e[:, 0], e[:, 1], p, steps, b)
     dx = L / (p.x_no_of_cells - 1)
     assert got.shape[0] == n
-    # FP32 cell-unit positions round to ~2e-6 cells per step; velocities to 1e-7 per rotation
-    assert np.max(np.abs(got[:, 0] - x)) / dx < 5e-5 and np.max(np.abs(got[:, 1] - y)) / dx < 5e-5
+    # fixed-point positions round to 2^-23 of a cell per step (33 nodes), the FP32
+    # displacement to 6e-8 of itself; velocities to 1e-7 per rotation
+    assert np.max(np.abs(got[:, 0] - x)) / dx < 2e-6 and np.max(np.abs(got[:, 1] - y)) / dx < 2e-6
     assert np.max(np.abs(got[:, 2:5] - v)) < 1e-5 * np.max(np.abs(v))
     if b > 0:   # the rotation really happened
         assert np.max(np.abs(v - e[:, 2:5])) > 0.1 * p.vte
@@ -129,8 +130,8 @@ def test_gather_push_uses_the_cic_average_of_the_field():
         r.step(1)
         after = r.get_particles(0)
     assert before.shape == after.shape == (ne, 6)
-    xs = (before[:, 0] / dx).astype(np.float32).astype(np.float64)
-    ys = (before[:, 1] / dx).astype(np.float32).astype(np.float64)
+    # the dumped position is the library's fixed-point position times DX
+    xs, ys = before[:, 0] / dx, before[:, 1] / dx
     exp_, eyp = _gather(ex, ey, xs, ys, nx)
     dv = p.dt * p.q_over_me
     want_vx, want_vy = before[:, 2] + dv * exp_, before[:, 3] + dv * eyp

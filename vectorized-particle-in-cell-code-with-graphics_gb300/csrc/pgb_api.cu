@@ -294,6 +294,7 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
     r->p = *p;
     r->nx = p->x_no_of_cells;
     r->ny = p->y_no_of_cells;
+    r->ps = pgb_pos_shift(r->nx, r->ny);
     r->dx = p->xlength / (double)(r->nx - 1);
     r->dy = p->ylength / (double)(r->ny - 1);
     r->dt_dti = std::max(1, (int)(p->dti / p->dt));

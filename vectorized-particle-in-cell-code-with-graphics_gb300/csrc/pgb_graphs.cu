@@ -48,7 +48,7 @@ __global__ void k_gr_fields(int nodes, const double* rho, const double* phi, con
 struct GrParticleArgs {
     const float4* xv;
     const DevState* ds;
-    int s, nx, ny;
+    int s, nx, ny, ps;
     double vt, dbb, spread;
     int half;
     double l1, l2, l3, l4;           /* DIST_LOCATIONX, 2X, Y, 2Y */
@@ -66,7 +66,7 @@ __device__ __forceinline__ void gr_bin(unsigned long long* d, float v, const GrP
     if (abs(vbin) <= a.half) atomicAdd(&d[vbin + a.half], 1ull);
 }
 
-/* particles in cell units: jp = (int)(x/DX) is cellf(xs) (pic.cl:164-165) */
+/* jp = (int)(x/DX) (pic.cl:164-165) is the position's cell field */
 __global__ void __launch_bounds__(256) k_gr_particles(GrParticleArgs a) {
     const long long n = a.ds->n[a.s];
     const int xv = a.nx / 2, yv = a.ny / 2;   /* sum_av_velocities (pic.cl:161-162) */
@@ -74,8 +74,8 @@ __global__ void __launch_bounds__(256) k_gr_particles(GrParticleArgs a) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float4 p = a.xv[i];
         if (is_dead(p.x)) continue;
-        const int jp = cellf(p.x), kp = cellf(p.y);
-        const bool xin = p.x > 0.0f, yin = p.y > 0.0f;
+        const int jp = pcell(p.x, a.ps), kp = pcell(p.y, a.ps);
+        const bool xin = pos_gt0(p.x), yin = pos_gt0(p.y);
         if (kp != yv && kp != yd && jp != xv && jp != xd) continue;   /* off both slices */
         /* jp >= 0, kp >= 0: a position beyond the int range converts to
          * INT_MIN, which the reference would use as an index            */
@@ -129,7 +129,7 @@ int pgb_launch_graphs(pgb_run* r) {
     r->launches++;
     for (int s = 0; s < 2; ++s) {
         GrParticleArgs a;
-        a.xv = r->sp[s].xv; a.ds = r->ds; a.s = s; a.nx = r->nx; a.ny = r->ny;
+        a.xv = r->sp[s].xv; a.ds = r->ds; a.s = s; a.nx = r->nx; a.ny = r->ny; a.ps = r->ps;
         a.vt = s == 0 ? r->p.vte : r->p.vti;   /* set_vt(VTE / VTI) (pic.cpp:543-552) */
         a.dbb = (double)G.g.divide_bins_by;
         a.spread = kernel_spread(G.g);

@@ -2,15 +2,19 @@
  * Internal definitions shared by the libpicgb translation units.
  *
  * Device layout of one species (structure of arrays, slot order):
- *   xv  float4 {xs, ys, vx, vy}   xs = x/DX, ys = y/DY (cell units), v in m/s
+ *   xv  float4 {xs, ys, vx, vy}   xs, ys: x/DX, y/DY as signed 32-bit fixed
+ *                                 point with ps fraction bits (the bit
+ *                                 patterns sit in the float lanes; see the
+ *                                 position helpers in pgb_physics.cuh);
+ *                                 vx, vy in m/s
  *   vz  float                     m/s
  *   w   float                     macro-particle weight
  *   id  uint32                    stable identity: keys the random streams
- * A removed particle keeps its slot with xs = -inf (a tombstone) until the
- * next compaction, which keeps the surviving slots in order.  Cell units make
- * the cell index trunc(xs) and the CIC weight xs - trunc(xs) exact in FP32;
- * the reference computes the same quantities from x/DX in FP64
- * (pic.cl:31-37).
+ * A removed particle keeps its slot with the tombstone code in xs until the
+ * next compaction, which keeps the surviving slots in order.  The cell index
+ * (int)(x/DX) and the CIC weight x/DX - (int)(x/DX) are bit fields of the
+ * fixed-point position; the reference computes the same quantities from
+ * x/DX in FP64 (pic.cl:31-37).
  *
  * Counters that change on the device (slot counts, next id, statistics) live
  * in one DevState block so that a step never waits for the host.
@@ -82,9 +86,21 @@ struct Species {
     double qc = 0, q_over_m = 0, mass = 0, vt = 0, dt = 0;
 };
 
+/* fraction bits of a fixed-point position for a grid of nx x ny nodes:
+ * 2^-ps of a cell (20 bits at 513 nodes, at most 23 so that the fraction
+ * is exact in FP32), with room for two grid lengths on either side of the
+ * origin before a position saturates at +-2^30                            */
+inline int pgb_pos_shift(int nx, int ny) {
+    int cells = (nx > ny ? nx : ny) - 1, b = 0;
+    while ((1 << b) < cells) ++b;
+    int ps = 29 - b;
+    return ps > 23 ? 23 : (ps < 8 ? 8 : ps);
+}
+
 struct PushConsts {
     int nx, ny;
-    float dtdx, dtdy;      /* dt/DX, dt/DY: cell units per (m/s)            */
+    int ps;                /* fraction bits of the fixed-point positions    */
+    float dtdx, dtdy;      /* dt/DX*2^ps, dt/DY*2^ps: position units per (m/s) */
     float coef;            /* 0.5*dt*q/m                                     */
     float ca, sa, co, so;  /* cos/sin of ANGLE and of omega*dt               */
     int bfield;            /* MAGNETIC_FIELD > 0                             */
@@ -97,6 +113,7 @@ struct pgb_run {
     int dev = 0, sms = 0;
     cudaStream_t stream = nullptr;
     int nx = 0, ny = 0, dt_dti = 1;
+    int ps = 20;                  /* pgb_pos_shift(nx, ny) */
     double dx = 0, dy = 0;
     int64_t time_step = 0;
     Species sp[2];

@@ -49,10 +49,10 @@ struct PushArgs {
 /* gather (pic.cl:56-92) + push (pic.cl:95-149) of one particle in cell units */
 __device__ __forceinline__ void gather_push_one(const PushConsts& pc, const float2* exy, float4& p, float& vz,
                                                 bool& moved) {
-    int jp = cellf(p.x), kp = cellf(p.y);
+    int jp = pcell(p.x, pc.ps), kp = pcell(p.y, pc.ps);
     moved = false;
-    if (jp < pc.nx && p.x > 0.0f && kp < pc.ny && p.y > 0.0f) {
-        float wj = p.x - (float)jp, wk = p.y - (float)kp;
+    if (jp < pc.nx && pos_gt0(p.x) && kp < pc.ny && pos_gt0(p.y)) {
+        float wj = pfrac(p.x, pc.ps), wk = pfrac(p.y, pc.ps);
         float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
         float a2 = wk * (1.0f - wj), a1 = wj * wk;
         const float2* e = exy + (long long)kp * pc.nx + jp;
@@ -71,8 +71,8 @@ __device__ __forceinline__ void gather_push_one(const PushConsts& pc, const floa
         }
         vx += pc.coef * Exp;
         vy += pc.coef * Eyp;
-        p.x += pc.dtdx * vx;
-        p.y += pc.dtdy * vy;
+        p.x = pos_step(p.x, pc.dtdx * vx);
+        p.y = pos_step(p.y, pc.dtdy * vy);
         p.z = vx;
         p.w = vy;
         moved = true;
@@ -91,8 +91,8 @@ __device__ __forceinline__ float speed2(const float4& p, float vz) {
     return __fmaf_rn(vz, vz, __fmaf_rn(p.w, p.w, __fmul_rn(p.z, p.z)));
 }
 __device__ __forceinline__ int mcc_test(const CollConsts& cc, unsigned int id, unsigned int step, int nx, int ny,
-                                        const float4& p, float vz, float* energy_out, pgb_stream* st) {
-    int jp = cellf(p.x), kp = cellf(p.y);
+                                        int ps, const float4& p, float vz, float* energy_out, pgb_stream* st) {
+    int jp = pcell(p.x, ps), kp = pcell(p.y, ps);
     if (!(jp >= 0 && jp < nx && kp >= 0 && kp < ny)) return 0;
     float u2 = speed2(p, vz);
     float energy = cc.e_energy_coef * u2;
@@ -209,11 +209,11 @@ __device__ __forceinline__ unsigned long long win_get(const unsigned int* win, i
 /* deposit into the CTA's shared window when the four nodes fall inside it,
  * else into the global grid                                               */
 __device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned int* win, int ox, int oy, int nx,
-                                            float xs, float ys, float w) {
-    int jp = cellf(xs), kp = cellf(ys);
+                                            int ps, float xs, float ys, float w) {
+    int jp = pcell(xs, ps), kp = pcell(ys, ps);
     int lx = jp - ox, ly = kp - oy;
     if (win && lx >= 0 && ly >= 0 && lx < PGB_WIN - 1 && ly < PGB_WIN - 1 && w >= 0.0f && w < WIN_MAX_WEIGHT) {
-        float wj = xs - (float)jp, wk = ys - (float)kp;
+        float wj = pfrac(xs, ps), wk = pfrac(ys, ps);
         float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
         float a2 = wk * (1.0f - wj), a1 = wj * wk;
         const float S = PGB_FIX_SCALE_F;
@@ -224,7 +224,7 @@ __device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned i
         atomicAdd(&win[k + PGB_WIN], (unsigned int)__float2int_rn(a2 * w * S));
         atomicAdd(&win[k + PGB_WIN + 1], (unsigned int)__float2int_rn(a1 * w * S));
     } else {
-        deposit_cell(qacc, nx, xs, ys, w);
+        deposit_cell(qacc, nx, ps, xs, ys, w);
     }
 }
 
@@ -240,7 +240,7 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
 #pragma unroll
     for (int k = 0; k < PGB_ITEMS; ++k) {
         long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
-        p[k] = make_float4(-INFINITY, 0.0f, 0.0f, 0.0f);
+        p[k] = make_float4(pos_dead(), 0.0f, 0.0f, 0.0f);
         vz[k] = 0.0f;
         w[k] = 0.0f;
         if (i < n) {
@@ -258,8 +258,10 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
         gather_push_one(pc, a.exy, p[k], vz[k], moved);
         if (moved) a.xv[i] = p[k];
         if (pc.bfield && moved) a.vz[i] = vz[k];
-        if (DEP && deposit_ok(p[k].x, p[k].y, pc.nx, pc.ny)) deposit_win(a.qacc, win, ox, oy, pc.nx, p[k].x, p[k].y, w[k]);
-        f[0][k] = pc.steady ? outside_steady(p[k].x, p[k].y, pc.nx, pc.ny) : outside_absorbing(p[k].x, p[k].y, pc.nx, pc.ny);
+        if (DEP && deposit_ok(p[k].x, p[k].y, pc.nx, pc.ny, pc.ps))
+            deposit_win(a.qacc, win, ox, oy, pc.nx, pc.ps, p[k].x, p[k].y, w[k]);
+        f[0][k] = pc.steady ? outside_steady(p[k].x, p[k].y, pc.nx, pc.ny, pc.ps)
+                            : outside_absorbing(p[k].x, p[k].y, pc.nx, pc.ny, pc.ps);
     }
     int* const tl[1] = {a.tl_out};
     int* const tc[1] = {a.tc_out};
@@ -312,7 +314,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
 
 /* flag-only pass (wall classification without a push) */
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_flag(const float4* xv, DevState* ds, int s, int nx, int ny,
-                                                           int steady, int* tl, int* tc) {
+                                                           int ps, int steady, int* tl, int* tc) {
     pgb_pdl_entry();
     const long long n = ds->n[s];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
@@ -326,7 +328,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_flag(const float4* xv, Dev
             if (i >= n) continue;
             float4 p = xv[i];
             if (is_dead(p.x)) continue;
-            f[0][k] = steady ? outside_steady(p.x, p.y, nx, ny) : outside_absorbing(p.x, p.y, nx, ny);
+            f[0][k] = steady ? outside_steady(p.x, p.y, nx, ny, ps) : outside_absorbing(p.x, p.y, nx, ny, ps);
         }
         int* const tla[1] = {tl};
         int* const tca[1] = {tc};
@@ -336,12 +338,12 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_flag(const float4* xv, Dev
 
 /* standalone deposit (particle::collect_charge) */
 __global__ void __launch_bounds__(256) k_deposit(const float4* xv, const float* w, DevState* ds, int s, int nx, int ny,
-                                                 unsigned long long* qacc) {
+                                                 int ps, unsigned long long* qacc) {
     pgb_pdl_entry();
     const long long n = ds->n[s];
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float4 p = xv[i];
-        if (deposit_ok(p.x, p.y, nx, ny)) deposit_cell(qacc, nx, p.x, p.y, w[i]);
+        if (deposit_ok(p.x, p.y, nx, ny, ps)) deposit_cell(qacc, nx, ps, p.x, p.y, w[i]);
     }
 }
 
@@ -391,7 +393,7 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
             long long i = base + k * PGB_PUSH_THREADS + t;
-            pa[k] = make_float4(-INFINITY, 0.0f, 0.0f, 0.0f);
+            pa[k] = make_float4(pos_dead(), 0.0f, 0.0f, 0.0f);
             vza[k] = 0.0f;
             ida[k] = 0u;
             if (i < n) {
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
             if (!is_dead(pa[k].x)) {
                 float energy;
                 pgb_stream st;
-                ev = mcc_test(a.cc, ida[k], step, a.pc.nx, a.pc.ny, pa[k], vza[k], &energy, &st);
+                ev = mcc_test(a.cc, ida[k], step, a.pc.nx, a.pc.ny, a.pc.ps, pa[k], vza[k], &energy, &st);
             }
             const bool sc = (ev & MCC_SCATTER) != 0;
             f[k] = (ev & MCC_IONIZE) != 0;
@@ -610,14 +612,14 @@ __global__ void k_inject(InjectArgs a) {
     double y = (a.dy + ry * (a.ylength - 2.0 * a.dy));
     float vt = (float)S.vt;
     float vx = maxwell_f32(&st, vt), vy = maxwell_f32(&st, vt), vz = maxwell_f32(&st, vt);
-    float4 p = make_float4((float)(x / a.dx), (float)(y / a.dy), vx, vy);
+    float4 p = make_float4(pos_from_m(x, a.dx, a.pce.ps), pos_from_m(y, a.dy, a.pce.ps), vx, vy);
     bool out = false;
     if (s == 0 && a.push_e) {
         bool moved;
         gather_push_one(a.pce, a.exy, p, vz, moved);
         /* weight 0: the deposit adds nothing (particle.cpp:497) */
-        out = a.pce.steady ? outside_steady(p.x, p.y, a.pce.nx, a.pce.ny)
-                           : outside_absorbing(p.x, p.y, a.pce.nx, a.pce.ny);
+        out = a.pce.steady ? outside_steady(p.x, p.y, a.pce.nx, a.pce.ny, a.pce.ps)
+                           : outside_absorbing(p.x, p.y, a.pce.nx, a.pce.ny, a.pce.ps);
     }
     S.xv[slot] = p;
     S.vz[slot] = vz;
@@ -665,6 +667,7 @@ struct IonizeAppendArgs {
     CollConsts cc;
     const float* neut;
     double dx, dy;
+    int ps;
     int store_e, store_i;
 };
 __global__ void k_ionize_append(IonizeAppendArgs a) {
@@ -682,12 +685,13 @@ __global__ void k_ionize_append(IonizeAppendArgs a) {
         pgb_stream si;
         pgb_stream_init(&si, a.cc.seed, pid, (unsigned int)a.ds->t, PGB_STREAM_IONIZE, 0);
         float4 pp = a.e.xv[slot];
-        double xe = (double)pp.x * a.dx, ye = (double)pp.y * a.dy;
+        double xe = pos_m(pp.x, a.ps, a.dx), ye = pos_m(pp.y, a.ps, a.dy);
         IonizeOut o = ionize_f32(&si, a.neut, a.cc.n_neutral, a.cc, xe, ye, 0.0f, 0.0f, 0.0f);
         if (a.store_i) {
             long long s2 = ni0 + r;
             if (s2 < a.i.cap) {
-                a.i.xv[s2] = make_float4((float)(o.ix / a.dx), (float)(o.iy / a.dy), (float)o.ivx, (float)o.ivy);
+                a.i.xv[s2] = make_float4(pos_from_m(o.ix, a.dx, a.ps), pos_from_m(o.iy, a.dy, a.ps), (float)o.ivx,
+                                         (float)o.ivy);
                 a.i.vz[s2] = (float)o.ivz;
                 a.i.w[s2] = a.e.w[slot];
                 a.i.id[s2] = idi0 + (unsigned int)r;
@@ -698,7 +702,8 @@ __global__ void k_ionize_append(IonizeAppendArgs a) {
         if (a.store_e) {
             long long s2 = ne0 + r;
             if (s2 < a.e.cap) {
-                a.e.xv[s2] = make_float4((float)(o.nx_ / a.dx), (float)(o.ny_ / a.dy), (float)o.nvx, (float)o.nvy);
+                a.e.xv[s2] = make_float4(pos_from_m(o.nx_, a.dx, a.ps), pos_from_m(o.ny_, a.dy, a.ps), (float)o.nvx,
+                                         (float)o.nvy);
                 a.e.vz[s2] = (float)o.nvz;
                 a.e.w[s2] = a.e.w[slot];
                 a.e.id[s2] = ide0 + (unsigned int)r;
@@ -786,11 +791,11 @@ __global__ void k_compact_commit(DevState* ds, int s, const long long* total) {
 
 /* ------------------------------------------------------------ load / dump */
 /* slots [i0, i1) from records aos[6 i ..] */
-__global__ void k_load(Species S, const double* aos, long long i0, long long i1, double dx, double dy) {
+__global__ void k_load(Species S, const double* aos, long long i0, long long i1, double dx, double dy, int ps) {
     pgb_pdl_entry();
     for (long long i = i0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < i1; i += (long long)gridDim.x * blockDim.x) {
         const double* r = aos + 6 * i;
-        S.xv[i] = make_float4((float)(r[0] / dx), (float)(r[1] / dy), (float)r[2], (float)r[3]);
+        S.xv[i] = make_float4(pos_from_m(r[0], dx, ps), pos_from_m(r[1], dy, ps), (float)r[2], (float)r[3]);
         S.vz[i] = (float)r[4];
         S.w[i] = (float)r[5];
         S.id[i] = (unsigned int)i;
@@ -802,8 +807,8 @@ __global__ void k_load(Species S, const double* aos, long long i0, long long i1,
 /* out (6 doubles per particle) and ids (the particle's id) are each
  * written when not null                                                  */
 __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_dump(Species S, DevState* ds, int s, const int* toff, double dx,
-                                                           double dy, double* out, unsigned int* ids, long long cap,
-                                                           int t0, int t1) {
+                                                           double dy, int ps, double* out, unsigned int* ids,
+                                                           long long cap, int t0, int t1) {
     pgb_pdl_entry();
     const long long n = ds->n[s];
     const int ntiles = min(t1, (int)((n + PGB_TILE - 1) / PGB_TILE));
@@ -832,7 +837,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_dump(Species S, DevState* 
                 if (pos < cap && out) {
                     float4 p = S.xv[i];
                     double* o = out + 6 * pos;
-                    o[0] = (double)p.x * dx; o[1] = (double)p.y * dy;
+                    o[0] = pos_m(p.x, ps, dx); o[1] = pos_m(p.y, ps, dy);
                     o[2] = p.z; o[3] = p.w; o[4] = S.vz[i]; o[5] = S.w[i];
                 }
                 if (pos < cap && ids) ids[pos] = S.id[i];
@@ -848,8 +853,9 @@ static PushConsts push_consts(pgb_run* r, int s) {
     PushConsts pc;
     const Species& S = r->sp[s];
     pc.nx = r->nx; pc.ny = r->ny;
-    pc.dtdx = (float)(S.dt / r->dx);
-    pc.dtdy = (float)(S.dt / r->dy);
+    pc.ps = r->ps;
+    pc.dtdx = (float)ldexp(S.dt / r->dx, r->ps);
+    pc.dtdy = (float)ldexp(S.dt / r->dy, r->ps);
     pc.coef = (float)(0.5 * S.dt * S.q_over_m);
     double omega_dt = S.dt * S.q_over_m * r->p.magnetic_field;
     pc.ca = (float)cos(r->p.angle); pc.sa = (float)sin(r->p.angle);
@@ -920,7 +926,7 @@ int pgb_launch_push(pgb_run* r, int s, bool deposit) {
 
 int pgb_launch_flag_outside(pgb_run* r, int s) {
     int l = s == 0 ? LIST_OUT_E : LIST_OUT_I;
-    PGB_CK(r, pgb_launch_pdl(k_flag, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, r->sp[s].xv, r->ds, s, r->nx, r->ny, r->p.steadystate,
+    PGB_CK(r, pgb_launch_pdl(k_flag, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, r->sp[s].xv, r->ds, s, r->nx, r->ny, r->ps, r->p.steadystate,
                                                                r->tile_list[l], r->tile_cnt[l]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
@@ -976,7 +982,7 @@ int pgb_build_list(pgb_run* r, int which, int s) {
 }
 
 int pgb_launch_deposit(pgb_run* r, int s) {
-    PGB_CK(r, pgb_launch_pdl(k_deposit, dim3(grid_for(r, 8)), dim3(256), 0, r->stream, r->sp[s].xv, r->sp[s].w, r->ds, s, r->nx, r->ny, r->qacc[s]));
+    PGB_CK(r, pgb_launch_pdl(k_deposit, dim3(grid_for(r, 8)), dim3(256), 0, r->stream, r->sp[s].xv, r->sp[s].w, r->ds, s, r->nx, r->ny, r->ps, r->qacc[s]));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -1004,7 +1010,7 @@ int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i) {
     IonizeAppendArgs a;
     a.e = r->sp[0]; a.i = r->sp[1]; a.ds = r->ds; a.ev = r->list[LIST_ION_EV];
     a.cc = pgb_coll_consts(r); a.neut = r->neut[0];
-    a.dx = r->dx; a.dy = r->dy;
+    a.dx = r->dx; a.dy = r->dy; a.ps = r->ps;
     a.store_e = store_e;
     a.store_i = store_i;
     PGB_CK(r, pgb_launch_pdl(k_ionize_append, dim3(r->sms * 2), dim3(256), 0, r->stream, a));
@@ -1038,7 +1044,7 @@ int pgb_launch_compact(pgb_run* r, int s) {
 }
 
 int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long i0, long long i1) {
-    PGB_CK(r, pgb_launch_pdl(k_load, dim3(grid_for(r, 4)), dim3(256), 0, r->stream, r->sp[s], d_aos, i0, i1, r->dx, r->dy));
+    PGB_CK(r, pgb_launch_pdl(k_load, dim3(grid_for(r, 4)), dim3(256), 0, r->stream, r->sp[s], d_aos, i0, i1, r->dx, r->dy, r->ps));
     r->launches++;
     PGB_CK(r, cudaGetLastError());
     return 0;
@@ -1057,7 +1063,7 @@ int pgb_launch_dump_offsets(pgb_run* r, int s) {
 }
 
 int pgb_launch_dump(pgb_run* r, int s, double* d_out, unsigned int* d_ids, long long cap, int t0, int t1) {
-    PGB_CK(r, pgb_launch_pdl(k_dump, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, r->sp[s], r->ds, s, r->aux_j, r->dx, r->dy, d_out,
+    PGB_CK(r, pgb_launch_pdl(k_dump, dim3(grid_for(r, 8)), dim3(PGB_PUSH_THREADS), 0, r->stream, r->sp[s], r->ds, s, r->aux_j, r->dx, r->dy, r->ps, d_out,
                              d_ids, cap, t0, t1));
     r->launches++;
     PGB_CK(r, cudaGetLastError());

@@ -27,16 +27,77 @@ __device__ __forceinline__ int celld(double v) {
     return (v > -2147483649.0 && v < 2147483648.0) ? (int)v : INT32_MIN;
 }
 
-/* tombstone: a removed particle */
-__device__ __forceinline__ bool is_dead(float xs) { return xs == -INFINITY; }
+/* ------------------------------------------------------------ positions
+ * A particle position is a signed 32-bit fixed-point number of cells with
+ * ps fraction bits (2^-ps of a cell: ps = 20 at 513 nodes, see
+ * pgb_pos_shift), kept as a bit pattern in the x and y lanes of xv; no
+ * floating-point operation ever touches those lanes.  The push adds the
+ * rounded displacement exactly, so a position keeps 2^-ps of a cell
+ * wherever it is (an FP32 cell coordinate keeps 2^-15 of a cell at 256-512
+ * cells).  The cell index (int)(x/DX) and the CIC fraction are bit fields.
+ * Two codes below the range: a removed particle (a tombstone) and a NaN
+ * position (ionization products, a push with a NaN velocity), which keeps
+ * the reference's x86 meaning: not pushed, not deposited, outside the
+ * absorbing walls (its cell index is INT_MIN), never re-inserted by the
+ * steady walls.  Positions saturate at +-2^30, far outside any grid.      */
+#define PGB_POS_DEAD INT32_MIN
+#define PGB_POS_NAN (INT32_MIN + 1)
+#define PGB_POS_LIM (1 << 30)
+__device__ __forceinline__ int pbits(float lane) { return __float_as_int(lane); }
+__device__ __forceinline__ float plane(int x) { return __int_as_float(x); }
+__device__ __forceinline__ float pos_dead() { return __int_as_float(PGB_POS_DEAD); }
+__device__ __forceinline__ bool is_dead(float lane) { return __float_as_int(lane) == PGB_POS_DEAD; }
+__device__ __forceinline__ bool pos_is_nan(float lane) { return __float_as_int(lane) == PGB_POS_NAN; }
+/* (int)(x/DX): truncation toward zero; INT_MIN for NaN (x86-64)            */
+__device__ __forceinline__ int pcell(float lane, int ps) {
+    const int x = __float_as_int(lane);
+    return x <= PGB_POS_NAN ? INT32_MIN : (x >= 0 ? (x >> ps) : -((-x) >> ps));
+}
+/* x > 0 and x < 0 (NaN is neither)                                        */
+__device__ __forceinline__ bool pos_gt0(float lane) { return __float_as_int(lane) > 0; }
+__device__ __forceinline__ bool pos_lt0(float lane) {
+    const int x = __float_as_int(lane);
+    return x < 0 && x != PGB_POS_NAN;
+}
+/* x/DX - (int)(x/DX) for x >= 0: exact (ps <= 23 bits)                   */
+__device__ __forceinline__ float pfrac(float lane, int ps) {
+    return (float)(__float_as_int(lane) & ((1 << ps) - 1)) * __int_as_float((127 - ps) << 23);
+}
+/* the position in cells (exact in FP64) and in metres                    */
+__device__ __forceinline__ double pos_cells(float lane, int ps) {
+    const int x = __float_as_int(lane);
+    return x == PGB_POS_NAN ? __longlong_as_double(0x7ff8000000000000ll) : ldexp((double)x, -ps);
+}
+__device__ __forceinline__ double pos_m(float lane, int ps, double d) { return pos_cells(lane, ps) * d; }
+/* FP32 cells, for plots and histograms                                   */
+__device__ __forceinline__ float pos_cellsf(float lane, int ps) {
+    const int x = __float_as_int(lane);
+    return x == PGB_POS_NAN ? __int_as_float(0x7fffffff) : (float)x * __int_as_float((127 - ps) << 23);
+}
+/* a position from cells (c = x/DX), rounded to 2^-ps, saturated          */
+__device__ __forceinline__ float pos_from_cells(double c, int ps) {
+    if (c != c) return __int_as_float(PGB_POS_NAN);
+    double v = ldexp(c, ps);
+    v = fmin(fmax(v, -(double)PGB_POS_LIM), (double)PGB_POS_LIM);
+    return __int_as_float(__double2int_rn(v));
+}
+__device__ __forceinline__ float pos_from_m(double x, double d, int ps) { return pos_from_cells(x / d, ps); }
+/* x + d with d in units of 2^-ps of a cell (the push: d = dt*v/DX*2^ps) */
+__device__ __forceinline__ float pos_step(float lane, float d) {
+    if (d != d) return __int_as_float(PGB_POS_NAN);
+    const float lim = (float)PGB_POS_LIM;
+    long long v = (long long)__float_as_int(lane) + __float2ll_rn(fminf(fmaxf(d, -2.0f * lim), 2.0f * lim));
+    v = v < -(long long)PGB_POS_LIM ? -(long long)PGB_POS_LIM : (v > PGB_POS_LIM ? PGB_POS_LIM : v);
+    return __int_as_float((int)v);
+}
 
 /* CIC deposit of one particle (pic.cl:36-49) as int64 fixed point:
  * round(a*w*2^19) per node (1e-6 of a unit weight, below the FP32
  * rounding of a); integer sums are exact and order-free, so the grid is
  * identical run to run.  Caller checks deposit_ok().                     */
-__device__ __forceinline__ void deposit_cell(unsigned long long* qacc, int nx, float xs, float ys, float w) {
-    int jp = cellf(xs), kp = cellf(ys);
-    float wj = xs - (float)jp, wk = ys - (float)kp;
+__device__ __forceinline__ void deposit_cell(unsigned long long* qacc, int nx, int ps, float xl, float yl, float w) {
+    int jp = pcell(xl, ps), kp = pcell(yl, ps);
+    float wj = pfrac(xl, ps), wk = pfrac(yl, ps);
     float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
     float a2 = wk * (1.0f - wj), a1 = wj * wk;
     const float S = PGB_FIX_SCALE_F;
@@ -49,25 +110,26 @@ __device__ __forceinline__ void deposit_cell(unsigned long long* qacc, int nx, f
     atomicAdd(q + nx + 1, (unsigned long long)c1);
 }
 
-__device__ __forceinline__ bool deposit_ok(float xs, float ys, int nx, int ny) {
-    int jp = cellf(xs), kp = cellf(ys);
-    return jp < nx - 1 && xs > 0.0f && kp < ny - 1 && ys > 0.0f;
+/* collect_charge's test: jp < nx-1 && x > 0 && kp < ny-1 && y > 0 (pic.cl:35) */
+__device__ __forceinline__ bool deposit_ok(float xl, float yl, int nx, int ny, int ps) {
+    return pos_gt0(xl) && pos_gt0(yl) && pcell(xl, ps) < nx - 1 && pcell(yl, ps) < ny - 1;
 }
 
-__device__ __forceinline__ void maybe_deposit(unsigned long long* qacc, int nx, int ny, float xs, float ys, float w) {
-    if (deposit_ok(xs, ys, nx, ny)) deposit_cell(qacc, nx, xs, ys, w);
+__device__ __forceinline__ void maybe_deposit(unsigned long long* qacc, int nx, int ny, int ps, float xl, float yl,
+                                              float w) {
+    if (deposit_ok(xl, yl, nx, ny, ps)) deposit_cell(qacc, nx, ps, xl, yl, w);
 }
 
 /* ---------------------------------------------------------- wall classes */
 /* e_boundary / ion_boundary: outside iff jp<0 || jp>=nx || kp<0 || kp>=ny
  * (boundary.cpp:595-599, 774-778)                                         */
-__device__ __forceinline__ bool outside_absorbing(float xs, float ys, int nx, int ny) {
-    int jp = cellf(xs), kp = cellf(ys);
+__device__ __forceinline__ bool outside_absorbing(float xl, float yl, int nx, int ny, int ps) {
+    int jp = pcell(xl, ps), kp = pcell(yl, ps);
     return jp < 0 || jp >= nx || kp < 0 || kp >= ny;
 }
 /* steady walls: x < 0 or (int)(x/DX) >= nx, same for y (boundary.cpp:906-1013) */
-__device__ __forceinline__ bool outside_steady(float xs, float ys, int nx, int ny) {
-    return xs < 0.0f || cellf(xs) >= nx || ys < 0.0f || cellf(ys) >= ny;
+__device__ __forceinline__ bool outside_steady(float xl, float yl, int nx, int ny, int ps) {
+    return pos_lt0(xl) || pcell(xl, ps) >= nx || pos_lt0(yl) || pcell(yl, ps) >= ny;
 }
 
 /* ------------------------------------------------------- cross sections */
@@ -152,20 +214,31 @@ __device__ __forceinline__ float sigma_cx(const CollConsts& c, float e) {
 
 /* ------------------------------------------------ electron collisions */
 /* collisions::scattered_velocity (collisions.cpp:107-171) in FP32.  The
- * scattering angle cosChi = 2(1-(1+E)^R)/E + 1 is evaluated as
- * 1 - t with t = 2*expm1(R*log1p(E))/E, and sinChi = sqrt(t(2-t)): the same
- * values without the cancellation of 1-(1+E)^R and of 1-cosChi^2 that FP32
- * would otherwise suffer near forward scattering.  Events are rare (a few
- * per cent of the particles per step), and FP64 here would run at 1/64 rate
- * on a divergent warp.                                                    */
+ * scattering angle cosChi = 2(1-(1+E)^R)/E + 1 (cosChi = sqrt(1-R) below
+ * 0.01 eV) enters as t = 1 - cosChi and s = 1 + cosChi, sinChi = sqrt(t s):
+ *   t = 2 expm1(R log1p(E)) / E,    s = -2 (1+E) expm1(-(1-R) log1p(E)) / E
+ *   (below 0.01 eV: t = R / (1 + sqrt(1-R)),  s = 1 + sqrt(1-R)),
+ * the same values without the cancellations FP32 would suffer in
+ * 1-(1+E)^R, 1-sqrt(1-R) and 1-cosChi^2 near forward (R -> 0) and backward
+ * (R -> 1) scattering; 1-R is exact in FP32 for these draws.  The scattered
+ * velocity then keeps 2e-6 of the speed.  Events are rare (a few per cent
+ * of the particles per step), and FP64 here would run at 1/64 rate on a
+ * divergent warp.                                                         */
 __device__ __forceinline__ void scatter_f32(pgb_stream* st, const float* neut, int nn, float energy, float cf,
                                             float& vx, float& vy, float& vz) {
     const float two_pi = (float)(2.0 * PGB_PI);
     float R = pgb_u01f(pgb_stream_u32(st));
-    float t;   /* 1 - cosChi */
-    if (energy < 1.0e-2f) t = 1.0f - sqrtf(1.0f - R);
-    else t = 2.0f * expm1f(R * log1pf(energy)) / energy;
-    float sinChi = sqrtf(fmaxf(t * (2.0f - t), 0.0f));
+    float t, s;   /* 1 - cosChi, 1 + cosChi */
+    if (energy < 1.0e-2f) {
+        const float c = sqrtf(1.0f - R);
+        t = R / (1.0f + c);
+        s = 1.0f + c;
+    } else {
+        const float l = log1pf(energy);
+        t = 2.0f * expm1f(R * l) / energy;
+        s = -2.0f * (1.0f + energy) * expm1f(-(1.0f - R) * l) / energy;
+    }
+    float sinChi = sqrtf(fmaxf(t * s, 0.0f));
     float sinPhi, cosPhi;
     sincosf(two_pi * R, &sinPhi, &cosPhi);
     int index = (int)(pgb_stream_u32(st) % (uint32_t)(nn - 1));

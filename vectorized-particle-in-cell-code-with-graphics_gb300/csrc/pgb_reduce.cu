@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(256) k_kh_apply(KhArgs a) {
         if (is_dead(p.x)) continue;
         int g = kh_group(p, a);
         if (a.active[g] && kh_key(a, a.S.id[i], step) <= a.prefix[g]) {
-            a.S.xv[i].x = -INFINITY;
+            a.S.xv[i].x = pos_dead();
             rm++;
         } else if (a.gwd[g] != 1.0) {
             a.S.w[i] = (float)((double)a.S.w[i] * a.gwd[g]);

@@ -73,7 +73,7 @@ struct PointArgs {
     const float4* xv;
     const unsigned int* id;
     const DevState* ds;
-    int s, nx, ny, width, height, max_points, phase;
+    int s, nx, ny, ps, width, height, max_points, phase;
     uint32_t seed;
     const unsigned int* vmax;   /* phase: bits of max |vx|, |vy| */
     unsigned int* vmax_out;     /* k_rd_vmax */
@@ -92,6 +92,9 @@ __device__ __forceinline__ long long rd_tile(long long t, long long ntiles) {
 __device__ __forceinline__ bool rd_candidate(const PointArgs& a, long long i, long long nlive, float4& p) {
     p = a.xv[i];
     if (is_dead(p.x)) return false;
+    /* the position in FP32 cells (NaN for a NaN position) */
+    p.x = pos_cellsf(p.x, a.ps);
+    p.y = pos_cellsf(p.y, a.ps);
     if (!(p.x > 0.0f && p.x < (float)(a.nx - 1) && p.y > 0.0f && p.y < (float)(a.ny - 1))) return false;
     return rd_keep(a.id[i], a.seed, nlive, a.max_points);
 }
@@ -296,7 +299,7 @@ extern "C" int pgb_render(pgb_run* r, int plot, int32_t width, int32_t height, i
         unsigned char* layer = img + bytes;
         PGB_CK(r, cudaMemsetAsync(layer, 0, (size_t)npx, r->stream));
         PointArgs a;
-        a.ds = r->ds; a.nx = r->nx; a.ny = r->ny; a.width = width; a.height = height;
+        a.ds = r->ds; a.nx = r->nx; a.ny = r->ny; a.ps = r->ps; a.width = width; a.height = height;
         a.max_points = max_points; a.seed = seed; a.layer = layer;
         a.vmax = (const unsigned int*)r->rd_scratch;
         a.vmax_out = (unsigned int*)r->rd_scratch;

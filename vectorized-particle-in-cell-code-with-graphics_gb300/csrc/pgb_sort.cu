@@ -30,6 +30,7 @@ struct SortArgs {
     DevState* ds;
     int s;
     int nx, ny;              /* nodes */
+    int ps;                  /* fraction bits of the positions */
     int nbx, nby, nbins;     /* bins; key nbins = not in the deposit region */
     long long nchunks_cap;
     int* counts;             /* [key][chunk] */
@@ -41,11 +42,11 @@ struct SortArgs {
     int piece_tiles;
 };
 
-__device__ __forceinline__ int bin_key(float4 p, int nx, int ny, int nbx, int nbins) {
+__device__ __forceinline__ int bin_key(float4 p, int nx, int ny, int ps, int nbx, int nbins) {
     if (is_dead(p.x)) return -1;
-    int jp = cellf(p.x), kp = cellf(p.y);
+    int jp = pcell(p.x, ps), kp = pcell(p.y, ps);
     /* the deposit region of collectCharge (pic.cl:35) */
-    if (!(jp < nx - 1 && p.x > 0.0f && kp < ny - 1 && p.y > 0.0f)) return nbins;
+    if (!deposit_ok(p.x, p.y, nx, ny, ps)) return nbins;
     return (kp / PGB_BIN) * nbx + (jp / PGB_BIN);
 }
 
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(256) k_sort_count(SortArgs a) {
         for (int k = threadIdx.x; k < SORT_CHUNK; k += blockDim.x) {
             long long i = (long long)c * SORT_CHUNK + k;
             if (i >= n) break;
-            int key = bin_key(a.S.xv[i], a.nx, a.ny, a.nbx, a.nbins);
+            int key = bin_key(a.S.xv[i], a.nx, a.ny, a.ps, a.nbx, a.nbins);
             if (key >= 0) atomicAdd(&s_hist[key], 1);
         }
         __syncthreads();
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(256) k_sort_scatter(SortArgs a) {
                     vz[u] = a.S.vz[i];
                     w[u] = a.S.w[i];
                     id[u] = a.S.id[i];
-                    key[u] = bin_key(p[u], a.nx, a.ny, a.nbx, a.nbins);
+                    key[u] = bin_key(p[u], a.nx, a.ny, a.ps, a.nbx, a.nbins);
                 }
             }
 #pragma unroll
@@ -245,7 +246,7 @@ __global__ void k_sort_pad(SortArgs a) {
     for (int key = blockIdx.x; key <= a.nbins; key += gridDim.x) {
         long long s0 = a.key_start[key] + a.key_total[key], s1 = a.key_start[key + 1];
         for (long long i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-            a.S.xv2[i] = make_float4(-INFINITY, 0.f, 0.f, 0.f);
+            a.S.xv2[i] = make_float4(pos_dead(), 0.f, 0.f, 0.f);
             a.S.vz2[i] = 0.f;
             a.S.w2[i] = 0.f;
             a.S.id2[i] = 0u;
@@ -268,7 +269,7 @@ void pgb_bins(pgb_run* r, int* nbx, int* nby) {
 
 int pgb_launch_sort(pgb_run* r, int s) {
     SortArgs a;
-    a.S = r->sp[s]; a.ds = r->ds; a.s = s; a.nx = r->nx; a.ny = r->ny;
+    a.S = r->sp[s]; a.ds = r->ds; a.s = s; a.nx = r->nx; a.ny = r->ny; a.ps = r->ps;
     pgb_bins(r, &a.nbx, &a.nby);
     a.nbins = a.nbx * a.nby;
     a.nchunks_cap = r->sort_chunks_cap;

@@ -32,6 +32,9 @@
  *     array's address with cudaGetSymbolAddress and caches it.  This loads
  *     the module on that device if it is not loaded yet.  Make that first
  *     call before any stream capture begins.
+ *   - The cached address belongs to the device's primary context.  After
+ *     cudaDeviceReset on a device the module may load elsewhere, so the
+ *     entry point must not be called on that device again in this process.
  */
 #include <cuda_runtime.h>
 #include <mutex>
@@ -59,18 +62,20 @@ __global__ void k_static_clear(unsigned long long* acc, int nodes) {
 }
 
 /* Each record is a particleVec {x, y, vx, vy, vz, w} (particleVec.h:26-35).
- * x and y are converted to cell units exactly as pgb_load_species converts
- * them, so the deposit is bit-identical to the run handle's.             */
+ * x and y become fixed-point positions exactly as pgb_load_species makes
+ * them (pgb_pos_shift of the grid), so the deposit is bit-identical to the
+ * run handle's.                                                          */
 __global__ void __launch_bounds__(256) k_static_deposit(const double* aos6, long long n, int nx, int ny, double dx,
-                                                        double dy, unsigned long long* acc) {
+                                                        double dy, int ps, unsigned long long* acc) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double* r = aos6 + 6 * i;
-        float xs = (float)(r[0] / dx), ys = (float)(r[1] / dy), w = (float)r[5];
-        if (deposit_ok(xs, ys, nx, ny)) deposit_cell(acc, nx, xs, ys, w);
+        float xl = pos_from_m(r[0], dx, ps), yl = pos_from_m(r[1], dy, ps), w = (float)r[5];
+        if (deposit_ok(xl, yl, nx, ny, ps)) deposit_cell(acc, nx, ps, xl, yl, w);
     }
 }
 
-/* q = (sum * 2^-32 * qc/(DX*DY)) * edge factor (particle.cpp:829-845) */
+/* q = (sum / PGB_FIX_SCALE * qc/(DX*DY)) * edge factor, the sum being in
+ * units of 2^-19 of a unit weight (particle.cpp:829-845)                 */
 __global__ void k_static_finish(const unsigned long long* acc, int nx, int ny, double qcdxdy, double* q) {
     const int nodes = nx * ny;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nodes; k += gridDim.x * blockDim.x) {
@@ -137,7 +142,7 @@ extern "C" int pgb_deposit_static(const double* d_aos6, int64_t n, int32_t nx, i
     if (n > 0) {
         long long want = (n + 255) / 256;
         int pblocks = want < (long long)s.sms * 8 ? (int)want : s.sms * 8;
-        k_static_deposit<<<pblocks, 256, 0, st>>>(d_aos6, (long long)n, nx, ny, dx, dy, s.acc);
+        k_static_deposit<<<pblocks, 256, 0, st>>>(d_aos6, (long long)n, nx, ny, dx, dy, pgb_pos_shift(nx, ny), s.acc);
     }
     k_static_finish<<<gblocks, 256, 0, st>>>(s.acc, nx, ny, qc / (dx * dy), d_q);
     cudaError_t e = cudaGetLastError();

@@ -39,6 +39,7 @@ struct WallArgs {
     unsigned long long* qacc_e;
     unsigned long long* qacc_i;
     int nx, ny;
+    int ps;                    /* fraction bits of the positions */
     double dx, dy, dt;         /* boundary objects use DT (boundary.h:62) */
     double me, mi;
     double threshold, work_function;
@@ -49,8 +50,8 @@ struct WallArgs {
 };
 
 __device__ __forceinline__ void store_particle(const Species& S, long long slot, double x, double y, double vx,
-                                               double vy, double vz, double dx, double dy) {
-    S.xv[slot] = make_float4((float)(x / dx), (float)(y / dy), (float)vx, (float)vy);
+                                               double vy, double vz, double dx, double dy, int ps) {
+    S.xv[slot] = make_float4(pos_from_m(x, dx, ps), pos_from_m(y, dy, ps), (float)vx, (float)vy);
     S.vz[slot] = (float)vz;
 }
 
@@ -130,7 +131,7 @@ __global__ void k_iwall2(WallArgs a) {
         int c = a.aux[k];
         if (c > 0) {
             double w = a.i.w[slot];
-            int jp = cellf(p.x), kp = cellf(p.y);
+            int jp = pcell(p.x, a.ps), kp = pcell(p.y, a.ps);
             for (int j = 0; j < c; ++j) {
                 long long es = ne0 + a.off[k] + j;
                 if (es >= a.e.cap) { atomicOr(&a.ds->err, ERR_CAP_E); break; }
@@ -170,14 +171,14 @@ __global__ void k_iwall2(WallArgs a) {
                     y = (double)R * a.dt * fabs((double)vy);
                     if (kp >= a.ny) { y = lengthY - y; vy = -fabsf(velocity * cc); }
                 }
-                store_particle(a.e, es, x, y, vx, vy, vz, a.dx, a.dy);
+                store_particle(a.e, es, x, y, vx, vy, vz, a.dx, a.dy, a.ps);
                 a.e.w[es] = ww;
                 a.e.id[es] = id;
                 float4 q = a.e.xv[es];
-                maybe_deposit(a.qacc_e, a.nx, a.ny, q.x, q.y, (float)ww);
+                maybe_deposit(a.qacc_e, a.nx, a.ny, a.ps, q.x, q.y, (float)ww);
             }
         }
-        a.i.xv[slot].x = -INFINITY;
+        a.i.xv[slot].x = pos_dead();
     }
 }
 
@@ -248,23 +249,23 @@ __global__ void k_ewall1(WallArgs a) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
         int slot = a.list_e[k];
         float4 p = a.e.xv[slot];
-        double x = (double)p.x * a.dx, y = (double)p.y * a.dy;
+        double x = pos_m(p.x, a.ps, a.dx), y = pos_m(p.y, a.ps, a.dy);
         float vx = p.z, vy = p.w, vz = a.e.vz[slot];
         pgb_stream st;
         pgb_stream_init(&st, a.seed, a.e.id[slot], (unsigned int)a.ds->t, PGB_STREAM_EWALL, 0);
         int res = EW_RETRY, nsec = 0, kind = 0;
-        const int jp = cellf(p.x), kp = cellf(p.y);
+        const int jp = pcell(p.x, a.ps), kp = pcell(p.y, a.ps);
         for (int attempt = 0; attempt < 64 && res == EW_RETRY; ++attempt)
             res = e_wall_event(a, &st, x, y, vx, vy, vz, jp, kp, nsec, kind);
         if (res == EW_RETRY) res = EW_ABSORB;
         int c = 0;
         if (res == EW_STAY) {
-            store_particle(a.e, slot, x, y, vx, vy, vz, a.dx, a.dy);
+            store_particle(a.e, slot, x, y, vx, vy, vz, a.dx, a.dy, a.ps);
             float4 q = a.e.xv[slot];
-            maybe_deposit(a.qacc_e, a.nx, a.ny, q.x, q.y, a.e.w[slot]);
+            maybe_deposit(a.qacc_e, a.nx, a.ny, a.ps, q.x, q.y, a.e.w[slot]);
             cnt[kind == ST_REFL ? 1 : 2]++;
         } else if (res == EW_ABSORB) {
-            a.e.xv[slot].x = -INFINITY;
+            a.e.xv[slot].x = pos_dead();
             cnt[0]++;
         } else {
             c = nsec;
@@ -294,9 +295,9 @@ __global__ void k_ewall2(WallArgs a) {
         if (c == 0) continue;
         int slot = a.list_e[k];
         float4 p = a.e.xv[slot];
-        double px = (double)p.x * a.dx, py = (double)p.y * a.dy;
+        double px = pos_m(p.x, a.ps, a.dx), py = pos_m(p.y, a.ps, a.dy);
         float w = a.e.w[slot];
-        int jpp = cellf(p.x);
+        int jpp = pcell(p.x, a.ps);
         for (int j = 0; j < c; ++j) {
             long long es = ne0 + a.off[k] + j;
             if (es >= a.e.cap) { atomicOr(&a.ds->err, ERR_CAP_E); break; }
@@ -311,15 +312,15 @@ __global__ void k_ewall2(WallArgs a) {
             float velocity = see_velocity(a, R);
             /* the new electron sits at the parent's x (left/right wall) or y */
             int jp = (jpp < 0 || jpp >= a.nx) ? jpp : 0;
-            int kp = (jpp < 0 || jpp >= a.nx) ? 0 : cellf(p.y);
+            int kp = (jpp < 0 || jpp >= a.nx) ? 0 : pcell(p.y, a.ps);
             secondary_vel_f(a, &st, x, y, vx, vy, vz, velocity, jp, kp);
-            store_particle(a.e, es, x, y, vx, vy, vz, a.dx, a.dy);
+            store_particle(a.e, es, x, y, vx, vy, vz, a.dx, a.dy, a.ps);
             a.e.w[es] = w;
             a.e.id[es] = id;
             float4 q = a.e.xv[es];
-            maybe_deposit(a.qacc_e, a.nx, a.ny, q.x, q.y, w);
+            maybe_deposit(a.qacc_e, a.nx, a.ny, a.ps, q.x, q.y, w);
         }
-        a.e.xv[slot].x = -INFINITY;
+        a.e.xv[slot].x = pos_dead();
     }
 }
 
@@ -340,9 +341,9 @@ __global__ void k_wall_commit(DevState* ds, const long long* total, int which, l
  * outside electron in list order is paired with the r-th outside ion, and
  * both are re-inserted at one random point (plop_particles,
  * boundary.cpp:854-878).  One CTA; lists are a small fraction of N.       */
-__device__ __forceinline__ int steady_class(float c, int ncells) {
-    if (c < 0.0f) return 1;                 /* left / bottom  */
-    if (cellf(c) >= ncells) return 2;       /* right / top    */
+__device__ __forceinline__ int steady_class(float c, int ncells, int ps) {
+    if (pos_lt0(c)) return 1;               /* left / bottom  */
+    if (pcell(c, ps) >= ncells) return 2;   /* right / top    */
     return 0;
 }
 
@@ -380,7 +381,7 @@ __global__ void __launch_bounds__(1024) k_steady(WallArgs a, int* ion_by_rank) {
             if (k < mi_) {
                 slot = a.list_i[k];
                 float4 p = a.i.xv[slot];
-                cls = steady_class(axis == 0 ? p.x : p.y, nc);
+                cls = steady_class(axis == 0 ? p.x : p.y, nc, a.ps);
             }
             int ea, eb, ta, tb;
             block_scan2(cls == 1, cls == 2, ea, eb, ta, tb);
@@ -398,7 +399,7 @@ __global__ void __launch_bounds__(1024) k_steady(WallArgs a, int* ion_by_rank) {
             if (k < me_) {
                 slot = a.list_e[k];
                 float4 p = a.e.xv[slot];
-                cls = steady_class(axis == 0 ? p.x : p.y, nc);
+                cls = steady_class(axis == 0 ? p.x : p.y, nc, a.ps);
             }
             int ea, eb, ta, tb;
             block_scan2(cls == 1, cls == 2, ea, eb, ta, tb);
@@ -414,12 +415,12 @@ __global__ void __launch_bounds__(1024) k_steady(WallArgs a, int* ion_by_rank) {
                 double evx = maxwell_fp64(&st, a.vte), ivx = maxwell_fp64(&st, a.vti);
                 double evy = maxwell_fp64(&st, a.vte), ivy = maxwell_fp64(&st, a.vti);
                 double evz = maxwell_fp64(&st, a.vte), ivz = maxwell_fp64(&st, a.vti);
-                store_particle(a.e, slot, x, y, evx, evy, evz, a.dx, a.dy);
-                store_particle(a.i, partner, x, y, ivx, ivy, ivz, a.dx, a.dy);
+                store_particle(a.e, slot, x, y, evx, evy, evz, a.dx, a.dy, a.ps);
+                store_particle(a.i, partner, x, y, ivx, ivy, ivz, a.dx, a.dy, a.ps);
                 float4 q = a.e.xv[slot];
-                maybe_deposit(a.qacc_e, a.nx, a.ny, q.x, q.y, a.e.w[slot]);
+                maybe_deposit(a.qacc_e, a.nx, a.ny, a.ps, q.x, q.y, a.e.w[slot]);
                 q = a.i.xv[partner];
-                maybe_deposit(a.qacc_i, a.nx, a.ny, q.x, q.y, a.i.w[partner]);
+                maybe_deposit(a.qacc_i, a.nx, a.ny, a.ps, q.x, q.y, a.i.w[partner]);
                 atomicAdd(&s_plops, 1);
             }
             rlo += ta;
@@ -446,6 +447,7 @@ struct CxArgs {
     Species i;
     DevState* ds;
     int nx, ny;
+    int ps;                  /* fraction bits of the positions */
     float pcoef, ecoef;      /* DTI*1e-20*n_g, (0.5/CHARGE)*MI */
     CollConsts cc;
     long long* tile_sum;     /* [column][tile] fixed point */
@@ -458,7 +460,7 @@ struct CxArgs {
 __device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, float vz, int& col) {
     col = -1;
     if (is_dead(p.x)) return 0;
-    int jp = cellf(p.x), kp = cellf(p.y);
+    int jp = pcell(p.x, a.ps), kp = pcell(p.y, a.ps);
     if (!(jp >= 0 && jp < a.nx && kp >= 0 && kp < a.ny)) return 0;
     col = jp;
     float u2 = __fadd_rn(__fadd_rn(__fmul_rn(p.z, p.z), __fmul_rn(p.w, p.w)), __fmul_rn(vz, vz));
@@ -486,7 +488,7 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 long long i = (long long)t * CX_TILE + k0 + q * blockDim.x;
-                p[q] = make_float4(-INFINITY, 0.f, 0.f, 0.f);
+                p[q] = make_float4(pos_dead(), 0.f, 0.f, 0.f);
                 vz[q] = 0.f;
                 if (k0 + q * blockDim.x < CX_TILE && i < n) {
                     p[q] = a.i.xv[i];
@@ -590,7 +592,7 @@ static WallArgs wall_args(pgb_run* r) {
     a.list_e = r->list[LIST_OUT_E]; a.list_i = r->list[LIST_OUT_I];
     a.aux = r->aux_i; a.off = r->aux_j;
     a.qacc_e = r->qacc[0]; a.qacc_i = r->qacc[1];
-    a.nx = r->nx; a.ny = r->ny; a.dx = r->dx; a.dy = r->dy; a.dt = r->p.dt;
+    a.nx = r->nx; a.ny = r->ny; a.ps = r->ps; a.dx = r->dx; a.dy = r->dy; a.dt = r->p.dt;
     a.me = r->p.electron_mass; a.mi = r->p.ion_mass;
     a.threshold = r->p.threshold; a.work_function = r->p.work_function;
     a.e0 = r->p.see_e0; a.emax0 = r->p.see_emax0; a.max_yield = r->p.see_max_yield;
@@ -639,7 +641,7 @@ int pgb_launch_walls(pgb_run* r, int which) {
 
 int pgb_launch_cx(pgb_run* r) {
     CxArgs a;
-    a.i = r->sp[1]; a.ds = r->ds; a.nx = r->nx; a.ny = r->ny;
+    a.i = r->sp[1]; a.ds = r->ds; a.nx = r->nx; a.ny = r->ny; a.ps = r->ps;
     a.cc = pgb_coll_consts(r);
     a.pcoef = a.cc.i_pcoef; a.ecoef = a.cc.i_energy_coef;
     a.tile_sum = (long long*)r->cx_tile_sum;
