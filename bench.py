@@ -54,6 +54,9 @@ ELECTRON_KERNELS = {
                  "alg_bytes": 36, "bytes_note": "read x, y, vx, vy, w (20 B); write x, y, vx, vy (16 B)"},
 }
 METRIC = "particle-steps/s"
+POISSON_DESC = {"FMG32": "full multigrid, the reference's schedule, FP32",
+                "FMG_REF": "full multigrid, the reference's schedule, FP64 (bit-identical to the reference)",
+                "FP32_DC": "FP32 full multigrid + FP64 defect correction (FP32 V-cycles)"}
 # FP32_DC passes: the FP32 full-multigrid pass and three FP64 defect
 # corrections, each an FP32 V-cycle (phi within 3e-7 and E within 2e-6 of the
 # converged FP64 solution on this workload's charge)
@@ -74,6 +77,36 @@ def workload_params(picgb, seed=1003, n_per_species=N_PER_SPECIES, poisson="FP32
     L = picgb.make_params(**kw).xlength
     size = 1.0e15 * L * L / n_per_species
     return picgb.make_params(E_MACROPARTICLE_SIZE=size, ION_MACROPARTICLE_SIZE=size, **kw)
+
+
+def argon_params(picgb, nodes, n_per_species, poisson="FP32_DC", dc_passes=5, sort_interval=12, seed=1002,
+                 torr=0.01, te=2.0):
+    """Ar plasma in a square box with absorbing walls (the small and mid
+    configurations): energy-dependent e-Ar and Ar+-Ar fits at `torr`,
+    Te = `te`, no secondary emission; the macro-particle size gives the design
+    density 1e15 m^-3 for n_per_species particles."""
+    kw = dict(X_NO_OF_CELLS=nodes, TEMPERATURE=te, GAS_PRESSURE_TORR=torr, HAVE_COLLISIONS=True,
+              SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT", SIGMA_IONIZATION="ENERGY_DEPENDENT",
+              STEADYSTATE="NO", SIZE_TO_CHECK=2**31 - 1, RAND_SEED=seed, POISSON=poisson, DC_MAX_ITERS=dc_passes,
+              SORT_INTERVAL=sort_interval)
+    L = picgb.make_params(**kw).xlength
+    size = 1.0e15 * L * L / n_per_species
+    return picgb.make_params(E_MACROPARTICLE_SIZE=size, ION_MACROPARTICLE_SIZE=size, **kw)
+
+
+def uniform_state(p, n, te, ti, seed):
+    """Positions uniform in (0, L)^2; Maxwellian velocities (sigma = sqrt(kT/m))."""
+    rng = np.random.default_rng(seed)
+    L = p.xlength
+    out = []
+    for m, T in ((9.10939e-31, te), (p.ion_mass, ti)):
+        a = np.empty((n, 6))
+        a[:, 0] = rng.uniform(0.0, L, n)
+        a[:, 1] = rng.uniform(0.0, L, n)
+        a[:, 2:5] = rng.normal(0.0, math.sqrt(T * 1.602177e-19 / m), (n, 3))
+        a[:, 5] = 1.0
+        out.append(a)
+    return out
 
 
 def gaussian_state(p, n, te, ti, seed, ion_mass):
@@ -164,24 +197,28 @@ def ncu_traffic():
 
 
 # ------------------------------------------------------------------ CPU path
-def cpu_sample(n_per_species, steps, threads):
-    """The CPU oracle on a bounded sample of the workload: particle-steps/s."""
+def cpu_sample(n_per_species, steps, threads, warmup=1, params=None, state=None):
+    """The CPU path (the oracle: the reference's algorithm restated in FP64,
+    OpenMP over the gather/push and deposit loops, its serial collisions,
+    walls and one-pass FP64 multigrid) on the workload: warm-up steps, then
+    particle-steps/s over `steps` steps."""
     sys.path.insert(0, os.path.join(REPO, "tests"))
     import orc
     import picgb
     orc.build_port()
-    p = workload_params(picgb, n_per_species=n_per_species, poisson="FMG_REF")
-    e, i = gaussian_state(p, n_per_species, 3.0, 0.026, 1003, p.ion_mass)
+    p = params or workload_params(picgb, n_per_species=n_per_species, poisson="FMG_REF", sort_interval=0)
+    e, i = state or gaussian_state(p, n_per_species, 3.0, 0.026, 1003, p.ion_mass)
     o = orc.Oracle(p, threads=threads)
     o.load_particles(0, e)
     o.load_particles(1, i)
     o.initial_boundary()
-    o.step(1)
+    o.step(max(warmup, 0))
     c0 = o.counters()
     t0 = time.perf_counter()
     o.step(steps)
     dt = time.perf_counter() - t0
     c1 = o.counters()
+    o.close()
     ps = 0.5 * (c0["n_e"] + c0["n_i"] + c1["n_e"] + c1["n_i"]) * steps
     return ps / dt, dt
 
@@ -460,27 +497,129 @@ def run_gpu(args, rank, world):
         ni = run.dump_particles_ptr(1, hi.data_ptr(), hi.shape[0])
         h2d = d2h = 0
         tot = 0.0
+        parts = {"load": 0.0, "step": 0.0, "dump": 0.0}
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
+            ta = time.perf_counter()
             run.load_particles_ptr(0, he.data_ptr(), ne)
             run.load_particles_ptr(1, hi.data_ptr(), ni)
             h2d += 48 * (ne + ni)
+            tb = time.perf_counter()
             run.step(1)
+            tc = time.perf_counter()
             ne2 = run.dump_particles_ptr(0, he.data_ptr(), he.shape[0])
             ni2 = run.dump_particles_ptr(1, hi.data_ptr(), hi.shape[0])
+            td = time.perf_counter()
+            parts["load"] += tb - ta
+            parts["step"] += tc - tb
+            parts["dump"] += td - tc
             d2h += 48 * (min(ne2, he.shape[0]) + min(ni2, hi.shape[0]))
             tot += 0.5 * (ne + ni + ne2 + ni2)
             ne, ni = min(ne2, he.shape[0]), min(ni2, hi.shape[0])
         wall = time.perf_counter() - t0
         e2e = {"value": tot / wall, "unit": METRIC, "h2d_bytes_per_step": h2d // args.e2e_steps,
-               "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps}
+               "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps,
+               "ms_per_step": {k: 1000.0 * v / args.e2e_steps for k, v in parts.items()},
+               "note": "wall time per call: pgb_load_species (both species, pinned AoS doubles to device SoA), "
+                       "pgb_step(1), pgb_dump_species (both)"}
     render = run_render(run, args, picgb) if args.render_frames > 0 else None
+    # accuracy against the FP64 oracle, from the bench state (replaces the run's state)
+    accuracy = None
+    if args.accuracy_steps > 0 and world == 1:
+        accuracy = run_accuracy(args, picgb, p, e, i, run)
+        accuracy["poisson"] = POISSON_DESC[args.poisson] + (f", {p.dc_max_iters} passes"
+                                                            if args.poisson == "FP32_DC" else "")
     run.close()
+    modes = run_modes(args, picgb, e, i, n) if (args.mode_steps > 0 and world == 1) else None
+    del e, i
+    configs = run_configs(args, picgb, os.cpu_count() or 1) if (args.configs and world == 1) else None
     batched = run_batched(args) if (args.batch_runs > 0 and world == 1) else None
     served = run_served(args) if (args.serve_requests > 0 and world == 1) else None
     return dict(ms=ms, ps=ps, counts=(c0, c1), prof=prof, launches=launches, clocks=clk.summary(), e2e=e2e, n=n,
-                batched=batched, served=served, render=render)
+                batched=batched, served=served, render=render, accuracy=accuracy, modes=modes, configs=configs)
+
+
+def time_steps(run, steps):
+    """CUDA-event time of `steps` steps on the run's stream (ms) and the
+    particle-steps they did."""
+    import torch
+    st = torch.cuda.ExternalStream(run.stream())
+    c0 = run.counters()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    run.step(steps)
+    b.record(st)
+    torch.cuda.synchronize()
+    c1 = run.counters()
+    return a.elapsed_time(b), 0.5 * (c0["n_e"] + c0["n_i"] + c1["n_e"] + c1["n_i"]) * steps
+
+
+def run_modes(args, picgb, e, i, n):
+    """The step with the other Poisson modes, same state and schedule:
+    FMG_REF (the reference's one-pass FP64 full multigrid, bit-identical to
+    it) and FMG32 (that schedule in FP32, 1e-5-2e-5 of phi from it)."""
+    out = {}
+    for mode in ("FMG_REF", "FMG32"):
+        p = workload_params(picgb, n_per_species=n, poisson=mode, sort_interval=args.sort)
+        with picgb.Run(p) as r:
+            r.load_particles(0, e)
+            r.load_particles(1, i)
+            r.initial_boundary()
+            r.step(args.warmup)
+            ms, ps = time_steps(r, args.mode_steps)
+        out[mode] = {"ms_per_step": ms / args.mode_steps, "value": ps / (ms / 1000.0), "steps": args.mode_steps}
+    return out
+
+
+def run_accuracy(args, picgb, p, e, i, run):
+    """Errors against the FP64 oracle (the checker: tests/fullsize.py) after
+    args.accuracy_steps steps of the bench state, outside every timed region."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import fullsize
+    d = fullsize.compare(p, e, i, args.accuracy_steps, run=run, reference_solver=True)
+    pt = d["particles"]
+    return {"vs": "FP64 oracle: the reference's algorithm restated in FP64 with the same Philox draws and particle "
+                  "order, its Poisson solve converged; tie particles (FP32-vs-FP64 threshold decisions that went "
+                  "the other way) matched by id and counted",
+            "steps": d["steps"], "norm": "max |d| / max |oracle|",
+            "fields": d["grids_away_from_ties"], "fields_tie_corrected": d["grids_tie_corrected"],
+            "fields_raw": d["grids"], "nodes_near_ties": d["nodes_near_ties"],
+            "poisson_solver": d["solver"], "reference_one_pass_fmg": d["reference_solver"],
+            "mean_energy_rel": {k: v["mean_energy_rel"] for k, v in pt.items()},
+            "mean_energy_ev": {k: v["mean_energy_ev"] for k, v in pt.items()},
+            "positions_cells": {k: v["pos_cells"] for k, v in pt.items()},
+            "velocities_vt": {k: v["vel_vt"] for k, v in pt.items()},
+            "ties": d["ties"], "count_diffs": {k: v for k, v in d["counts"].items() if v}}
+
+
+def run_configs(args, picgb, threads):
+    """The other single-run configurations.  C1: 65^2 nodes, 200k particles per
+    species, Ar at 0.01 Torr, absorbing walls, Te = 2 eV, the reference's FP64
+    Poisson solve, 1000 steps, on the GPU and on the CPU path (all host
+    threads).  C2: 257^2 nodes, 4Mi per species, the same Ar setup, FP32
+    multigrid with FP64 defect correction (5 passes), on the GPU."""
+    out = {}
+    for name, nodes, n, mode, steps, seed in (("C1_65_200k", 65, 200000, "FMG_REF", args.c1_steps, 1001),
+                                              ("C2_257_4Mi", 257, 4 * 1024 * 1024, "FP32_DC", args.c2_steps, 1002)):
+        p = argon_params(picgb, nodes, n, poisson=mode, sort_interval=args.sort, seed=seed)
+        e, i = uniform_state(p, n, 2.0, 0.026, seed)
+        with picgb.Run(p) as r:
+            r.load_particles(0, e)
+            r.load_particles(1, i)
+            r.initial_boundary()
+            r.step(args.warmup)
+            ms, ps = time_steps(r, steps)
+        out[name] = {"gpu": {"value": ps / (ms / 1000.0), "ms_per_step": ms / steps, "steps": steps},
+                     "poisson": POISSON_DESC[mode]}
+        if name.startswith("C1") and not args.no_cpu and args.c1_cpu_steps > 0:
+            p0 = argon_params(picgb, nodes, n, poisson="FMG_REF", sort_interval=0, seed=seed)
+            v, dt = cpu_sample(n, args.c1_cpu_steps, threads, warmup=5, params=p0, state=(e, i))
+            out[name]["cpu"] = {"value": v, "seconds": dt, "steps": args.c1_cpu_steps, "cores": threads,
+                                "kind": "port"}
+            out[name]["ratio_gpu_cpu"] = out[name]["gpu"]["value"] / v
+    return out
 
 
 def combine_ranks(ms: float, ps: float):
@@ -505,12 +644,19 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the 16Mi particles per species")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-sample", type=int, default=2 * 1024 * 1024)
-    ap.add_argument("--cpu-steps", type=int, default=6)
+    ap.add_argument("--cpu-steps", type=int, default=4, help="timed steps of the CPU baseline (bench workload)")
+    ap.add_argument("--ref-max-steps", type=int, default=50,
+                    help="the reference arm times at most this many of --steps (stated in its line)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--poisson", default="FMG32", choices=["FMG32", "FMG_REF", "FP32_DC"])
+    ap.add_argument("--poisson", default="FP32_DC", choices=["FMG32", "FMG_REF", "FP32_DC"])
     ap.add_argument("--sort", type=int, default=12,
                     help="spatial sort of the electrons every k steps, of the ions every 4k (0 = off)")
+    ap.add_argument("--mode-steps", type=int, default=40, help="steps timed per other Poisson mode (0 = skip)")
+    ap.add_argument("--accuracy-steps", type=int, default=2, help="steps of the oracle comparison (0 = skip)")
+    ap.add_argument("--no-configs", dest="configs", action="store_false", help="skip the C1/C2 configurations")
+    ap.add_argument("--c1-steps", type=int, default=1000)
+    ap.add_argument("--c1-cpu-steps", type=int, default=1000)
+    ap.add_argument("--c2-steps", type=int, default=200)
     ap.add_argument("--batch-runs", type=int, default=64, help="runs of the batched workload (0 = skip it)")
     ap.add_argument("--batch-steps", type=int, default=200, help="steps per run of the batched workload")
     ap.add_argument("--serve-requests", type=int, default=16, help="requests of the served workload (0 = skip it)")
@@ -521,32 +667,32 @@ def main():
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    n = int(N_PER_SPECIES * args.scale)
     config = {"workload": "H plasma, collisional boundary (SEE+reflection+backscatter, e-H elastic+ionization, "
-                          "H+-H CX), 512x512 cells (513^2 nodes), 16Mi particles/species, Gaussian density "
-                          "sigma=L/4, Te=3 eV, Ti=0.026 eV",
-              "grid_nodes": GRID_NODES, "particles_per_species": int(N_PER_SPECIES * args.scale),
-              "l2": "inputs larger than L2 (particle state 0.9 GB)",
-              "poisson": {"FMG32": "full multigrid, reference schedule, FP32",
-                          "FMG_REF": "full multigrid, reference schedule, FP64 (bit-identical)",
-                          "FP32_DC": "FP32 full multigrid + FP64 defect correction"}[args.poisson],
+                          "H+-H CX), 512x512 cells (513^2 nodes), Gaussian density sigma=L/4, Te=3 eV, Ti=0.026 eV",
+              "grid_nodes": GRID_NODES, "particles_per_species": n,
+              "l2": "inputs larger than L2 (particle state 0.9 GB at 16Mi per species)",
+              "poisson": POISSON_DESC[args.poisson] + (f", {DC_PASSES} passes" if args.poisson == "FP32_DC" else ""),
               "macro_particle_size": "mean density 1e15 m^-3", "sort_interval": args.sort,
               "parallelism": "replicas" if world > 1 else "single"}
     threads = os.cpu_count() or 1
     if args.impl == "reference":
+        # the reference's algorithm (the FP64 restatement pinned bit for bit to
+        # the reference's own code) on the host cores, on the bench workload
         if rank != 0:
             return
-        sample = max(64 * 1024, int(args.cpu_sample * args.scale)) if args.scale < 1 else args.cpu_sample // 4
-        steps = max(1, min(args.steps, 20))
-        for _ in range(min(args.warmup, 1)):
-            pass
-        v, dt = cpu_sample(sample, steps, threads)
+        steps = max(1, min(args.steps, args.ref_max_steps))
+        v, dt = cpu_sample(n, steps, threads, warmup=args.warmup)
+        rconfig = dict(config, poisson="the reference's one-pass full multigrid, FP64", sort_interval=0)
         line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus, "steps": steps,
-                "warmup": 1, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": config,
-                "impl": "reference",
+                "warmup": args.warmup, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": rconfig, "impl": "reference",
                 "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
-                                 "sample": f"{sample} particles/species on the workload's grid and physics, "
-                                           f"{steps} steps (CPU oracle: FP64 restatement of the reference path)"},
+                                 "sample": f"the bench workload at {n} particles per species on 513^2 nodes, "
+                                           f"{args.warmup} warm-up and {steps} timed steps; the reference's "
+                                           "algorithm restated in FP64 (bit-identical to the reference's own code "
+                                           "on x86-64), OpenMP on the gather/push and deposit loops"},
                 "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -581,20 +727,26 @@ def main():
                                       ("ms_push_e", "ms_collide_e", "ms_scatter_e", "ms_push_e_kernel", "ms_push_i",
                                        "ms_collide_ions", "ms_walls", "ms_fields")}}
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and world == 1:
         try:
-            v, dt = cpu_sample(args.cpu_sample, args.cpu_steps, threads)
+            v, dt = cpu_sample(n, args.cpu_steps, threads, warmup=1)
             cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
-                   "sample": f"{args.cpu_sample} particles/species, {args.cpu_steps} steps of the same workload "
-                             f"({dt:.1f} s CPU wall)"}
+                   "sample": f"the bench workload at {n} particles per species, 1 warm-up and {args.cpu_steps} "
+                             f"timed steps ({dt:.1f} s CPU wall); the reference's algorithm restated in FP64 with "
+                             "its one-pass FP64 multigrid"}
         except Exception as ex:  # the CPU baseline never blocks the GPU line
             cpu = {"value": None, "unit": METRIC, "cores": threads, "kind": "port", "sample": f"failed: {ex}"}
     c0, c1 = res["counts"]
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 particles / f64 fields", "data": "synthetic (seeded)",
+            "vs_baseline": None,
+            "dtype": ("f32 velocities and multigrid, int32 fixed-point positions, int64 fixed-point charge, "
+                      "f64 defect correction and fields") if args.poisson == "FP32_DC" else
+                     "f32 velocities, int32 fixed-point positions; " + POISSON_DESC[args.poisson],
+            "data": "synthetic (seeded)",
             "config": config, "e2e": res["e2e"], "roofline": roofline, "cpu_baseline": cpu,
             "gpu_launches": res["launches"], "clocks": res["clocks"],
+            "accuracy": res.get("accuracy"), "poisson_modes": res.get("modes"), "configs": res.get("configs"),
             "particles": {"start": [c0["n_e"], c0["n_i"]], "end": [c1["n_e"], c1["n_i"]]},
             "batched": res.get("batched"), "served": res.get("served"), "render": res.get("render")}
     print(json.dumps(line), flush=True)

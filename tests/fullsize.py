@@ -229,9 +229,31 @@ def _solver_only(p, t, gg):
         o.close()
 
 
-def compare(p, e, i, steps, threads=None, run=None):
+def _reference_solver(p, t, gg):
+    """The reference's own solver (its one-pass FP64 full multigrid) on the
+    device's rho against the converged FP64 solve: the algebraic error the
+    reference carries, for scale."""
+    out = {}
+    for mode in (picgb.PGB_POISSON_FMG_REF, picgb.PGB_POISSON_FP32_DC):
+        q = type(p).from_buffer_copy(p)
+        q.poisson_mode = mode
+        o = orc.Oracle(q, rng=orc.ORC_RNG_PHILOX, order=orc.ORC_ORDER_STABLE)
+        try:
+            o.set_rho(gg["rho"].reshape(p.y_no_of_cells, p.x_no_of_cells))
+            o.poisson(t)
+            o.efield()
+            out[mode] = {g: o.get_grid(g) for g in ("phi", "ex", "ey")}
+        finally:
+            o.close()
+    a, b = out[picgb.PGB_POISSON_FMG_REF], out[picgb.PGB_POISSON_FP32_DC]
+    return {g: rel_err(a[g], b[g]) for g in a}
+
+
+def compare(p, e, i, steps, threads=None, run=None, reference_solver=False):
     """Step the same state on the device and in the oracle; return the errors.
-    `run`: an existing picgb.Run to reuse (its state is replaced)."""
+    `run`: an existing picgb.Run to reuse (its state is replaced).
+    `reference_solver`: also report the reference's one-pass FP64 multigrid
+    against the converged solve on the device's rho."""
     threads = threads or (os.cpu_count() or 1)
     o = orc.Oracle(p, rng=orc.ORC_RNG_PHILOX, order=orc.ORC_ORDER_STABLE, threads=threads)
     r = run or picgb.Run(p)
@@ -272,6 +294,8 @@ def compare(p, e, i, steps, threads=None, run=None):
             scale = np.max(np.abs(b_))
             out["grids_away_from_ties"][g] = float(np.max(np.abs(a_[m] - b_[m])) / scale) if scale > 0 else 0.0
         out["solver"] = _solver_only(p, steps - 1, gg)
+        if reference_solver:
+            out["reference_solver"] = _reference_solver(p, steps - 1, gg)
         return out
     finally:
         o.close()
