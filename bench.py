@@ -524,13 +524,13 @@ def run_gpu(args, rank, world):
                "note": "wall time per call: pgb_load_species (both species, pinned AoS doubles to device SoA), "
                        "pgb_step(1), pgb_dump_species (both)"}
     render = run_render(run, args, picgb) if args.render_frames > 0 else None
-    # accuracy against the FP64 oracle, from the bench state (replaces the run's state)
+    run.close()
+    # accuracy against the FP64 oracle, from the bench state, on a fresh run
     accuracy = None
     if args.accuracy_steps > 0 and world == 1:
-        accuracy = run_accuracy(args, picgb, p, e, i, run)
+        accuracy = run_accuracy(args, picgb, p, e, i)
         accuracy["poisson"] = POISSON_DESC[args.poisson] + (f", {p.dc_max_iters} passes"
                                                             if args.poisson == "FP32_DC" else "")
-    run.close()
     modes = run_modes(args, picgb, e, i, n) if (args.mode_steps > 0 and world == 1) else None
     del e, i
     configs = run_configs(args, picgb, os.cpu_count() or 1) if (args.configs and world == 1) else None
@@ -573,12 +573,14 @@ def run_modes(args, picgb, e, i, n):
     return out
 
 
-def run_accuracy(args, picgb, p, e, i, run):
+def run_accuracy(args, picgb, p, e, i):
     """Errors against the FP64 oracle (the checker: tests/fullsize.py) after
-    args.accuracy_steps steps of the bench state, outside every timed region."""
+    args.accuracy_steps steps of the bench state on a fresh run (a used run
+    keeps its counters and the field of its last step), outside every timed
+    region."""
     sys.path.insert(0, os.path.join(REPO, "tests"))
     import fullsize
-    d = fullsize.compare(p, e, i, args.accuracy_steps, run=run, reference_solver=True)
+    d = fullsize.compare(p, e, i, args.accuracy_steps, reference_solver=True)
     pt = d["particles"]
     return {"vs": "FP64 oracle: the reference's algorithm restated in FP64 with the same Philox draws and particle "
                   "order, its Poisson solve converged; tie particles (FP32-vs-FP64 threshold decisions that went "

@@ -251,7 +251,8 @@ def _reference_solver(p, t, gg):
 
 def compare(p, e, i, steps, threads=None, run=None, reference_solver=False):
     """Step the same state on the device and in the oracle; return the errors.
-    `run`: an existing picgb.Run to reuse (its state is replaced).
+    `run`: a fresh picgb.Run to use (one that has stepped keeps its counters
+    and the field of its last step, which the comparison would inherit).
     `reference_solver`: also report the reference's one-pass FP64 multigrid
     against the converged solve on the device's rho."""
     threads = threads or (os.cpu_count() or 1)

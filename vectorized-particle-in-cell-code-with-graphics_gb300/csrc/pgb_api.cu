@@ -181,7 +181,13 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
         drop_graphs(r);
     }
     if (need > S.cap) {
+        /* a species that already has storage grows by at least a quarter:
+         * a load or a step that needs a few more slots than last time (ions
+         * gain NUMBER_TO_INJECT a step) would otherwise reallocate every
+         * buffer and re-capture the step graphs each time.  The first
+         * allocation is exact, as pgb_footprint counts it.                  */
         long long cap = std::max<long long>(need, 1024);
+        if (S.cap > 0) cap = std::min<long long>(std::max<long long>(cap, S.cap + S.cap / 4), 0x7fffffffLL);
         Species T;   /* the new storage; S keeps the old until it is copied */
         T.qc = S.qc; T.q_over_m = S.q_over_m; T.mass = S.mass; T.vt = S.vt; T.dt = S.dt;
         T.cap = cap;
