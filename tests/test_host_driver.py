@@ -149,7 +149,18 @@ def test_parameters_h_reader_rejects_missing_file(lib):
     assert lib.pgb_params_from_header(b"/nonexistent/parameters.h", 1, C.byref(got)) == -6
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference presets not mounted")
+def _reference_dir():
+    """The reference's source directory that oracle/Makefile built oracle/_ref
+    from (recorded there), or None where it was not built."""
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "refdir")
+    try:
+        d = open(path).read().strip()
+    except OSError:
+        return None
+    return d if os.path.isdir(d) else None
+
+
+@pytest.mark.skipif(_reference_dir() is None, reason="reference presets not present")
 def test_reference_presets_parse(lib):
     import picgb
     lib.pgb_params_from_header.argtypes = [C.c_char_p, C.c_uint64, C.POINTER(picgb.PgbParams)]
@@ -157,6 +168,6 @@ def test_reference_presets_parse(lib):
                                ("parameter file for Ar with coll-boundary", 0, 0),
                                ("parameter file for H with coll-boundary", 1, 0)):
         got = picgb.PgbParams()
-        path = os.path.join("/root/reference", d, "parameters.h")
+        path = os.path.join(_reference_dir(), d, "parameters.h")
         assert lib.pgb_params_from_header(path.encode(), 1, C.byref(got)) == 0, path
         assert got.x_no_of_cells == 257 and got.species == species and got.steadystate == steady
