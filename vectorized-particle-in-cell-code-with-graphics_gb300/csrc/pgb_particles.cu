@@ -100,9 +100,13 @@ __device__ __forceinline__ int mcc_test(const CollConsts& cc, unsigned int id, u
     pgb_stream_init(st, cc.seed, id, step, PGB_STREAM_EMCC, 0);
     float R = pgb_u01f(pgb_stream_u32(st));
     int ev = 0;
-    /* P = 1 - exp(-x) is at most 1, so P > 2R cannot hold for R >= 1/2:
-     * the cross-section and the exponential are needed only below      */
-    if (R < 0.5f) {
+    /* P = 1 - exp(-x) is at most 1, so P > 2R cannot hold for R >= 1/2;
+     * and P <= x <= u*pcoef*el_max, so with that bound (times 1 + 1e-6,
+     * above the FP32 roundings of x and of expm1) at most 2R the event is
+     * ruled out: the cross-section and the exponential are needed only
+     * for the few electrons left, and every decision is the one the full
+     * test would take                                                    */
+    if (R < 0.5f && (u * cc.e_pcoef) * cc.el_max * 1.000001f > 2.0f * R) {
         float sel = sigma_el(cc, energy);
         float P = -expm1f(-(u * cc.e_pcoef * sel));
         if (P > 2.0f * R) ev |= MCC_SCATTER;
@@ -368,7 +372,9 @@ __global__ void __launch_bounds__(256) k_deposit(const float4* xv, const float* 
 #define MCC_THREADS (MCC_GROUPS * PGB_PUSH_THREADS)
 #define MCC_ION_BIT 0x80000000u
 struct MccGroupSmem {
-    int off[PGB_ITEMS][PGB_PUSH_THREADS / 32];
+    int off[PGB_ITEMS][PGB_PUSH_THREADS / 32];    /* ionization events per (item, warp) */
+    int soff[PGB_ITEMS][PGB_PUSH_THREADS / 32];   /* scattering events per (item, warp) */
+    unsigned long long sbase;                      /* the tile's first scattering-list entry */
 };
 __device__ __forceinline__ void group_sync(int g) {
     asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "n"(PGB_PUSH_THREADS) : "memory");
@@ -402,7 +408,7 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
                 ida[k] = a.id[i];
             }
         }
-        bool f[PGB_ITEMS];
+        bool f[PGB_ITEMS], sc[PGB_ITEMS];
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
             const int i = (int)(base + k * PGB_PUSH_THREADS + t);
@@ -412,21 +418,12 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
                 pgb_stream st;
                 ev = mcc_test(a.cc, ida[k], step, a.pc.nx, a.pc.ny, a.pc.ps, pa[k], vza[k], &energy, &st);
             }
-            const bool sc = (ev & MCC_SCATTER) != 0;
+            sc[k] = (ev & MCC_SCATTER) != 0;
             f[k] = (ev & MCC_IONIZE) != 0;
-            st_loc[0] += sc ? 1 : 0;
+            st_loc[0] += sc[k] ? 1 : 0;
             st_loc[1] += f[k] ? 1 : 0;
-            /* scattering events: one counter update per warp */
-            const unsigned ms = __ballot_sync(0xffffffffu, sc);
-            if (ms) {
-                const int leader = __ffs(ms) - 1;
-                unsigned long long b0 = 0;
-                if (lane == leader) b0 = atomicAdd(&a.ds->scat_n, (unsigned long long)__popc(ms));
-                b0 = __shfl_sync(0xffffffffu, b0, leader);
-                if (sc) scat[b0 + __popc(ms & lt)] = (int)((unsigned)i | (f[k] ? MCC_ION_BIT : 0u));
-            }
             /* an ionization without scattering is applied here */
-            if (f[k] && !sc) {
+            if (f[k] && !sc[k]) {
                 float4 p = pa[k];
                 float vz = vza[k];
                 mcc_ionize(a.cc, a.neut, ida[k], step, p, vz);
@@ -434,28 +431,48 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
                 a.vz[i] = vz;
             }
         }
-        /* the tile's ionization events in slot order (as tile_lists) */
-        unsigned m[PGB_ITEMS];
+        /* the tile's ionization events in slot order (as tile_lists), and its
+         * scattering events appended to the dense list with one counter
+         * update for the tile (a counter update per warp serialised some
+         * 400k atomics on one address per launch)                        */
+        unsigned m[PGB_ITEMS], ms[PGB_ITEMS];
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
             m[k] = __ballot_sync(0xffffffffu, f[k]);
-            if (lane == 0) S.off[k][warp] = __popc(m[k]);
+            ms[k] = __ballot_sync(0xffffffffu, sc[k]);
+            if (lane == 0) {
+                S.off[k][warp] = __popc(m[k]);
+                S.soff[k][warp] = __popc(ms[k]);
+            }
         }
         group_sync(g);
-        if (t == 0) {
-            int acc = 0;
-            for (int k = 0; k < PGB_ITEMS; ++k)
-                for (int w = 0; w < PGB_PUSH_THREADS / 32; ++w) {
-                    int c = S.off[k][w];
-                    S.off[k][w] = acc;
-                    acc += c;
-                }
-            a.tc_ev[tile] = acc;
+        /* exclusive scans of the group's 32 (item, warp) counts by its first
+         * warp, in (item, warp) order, which is slot order                */
+        static_assert(PGB_ITEMS * (PGB_PUSH_THREADS / 32) == 32, "one count per lane");
+        if (warp == 0) {
+            int* const io = &S.off[0][0];
+            int* const so = &S.soff[0][0];
+            const int c = io[lane], d = so[lane];
+            int x = c, y = d;
+#pragma unroll
+            for (int dd = 1; dd < 32; dd <<= 1) {
+                const int xu = __shfl_up_sync(0xffffffffu, x, dd), yu = __shfl_up_sync(0xffffffffu, y, dd);
+                if (lane >= dd) { x += xu; y += yu; }
+            }
+            io[lane] = x - c;
+            so[lane] = y - d;
+            if (lane == 31) {
+                a.tc_ev[tile] = x;
+                S.sbase = y ? atomicAdd(&a.ds->scat_n, (unsigned long long)y) : 0ull;
+            }
         }
         group_sync(g);
 #pragma unroll
-        for (int k = 0; k < PGB_ITEMS; ++k)
-            if (f[k]) a.tl_ev[(long long)tile * PGB_TILE + S.off[k][warp] + __popc(m[k] & lt)] = (int)(base + k * PGB_PUSH_THREADS + t);
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            const int i = (int)(base + k * PGB_PUSH_THREADS + t);
+            if (f[k]) a.tl_ev[(long long)tile * PGB_TILE + S.off[k][warp] + __popc(m[k] & lt)] = i;
+            if (sc[k]) scat[S.sbase + S.soff[k][warp] + __popc(ms[k] & lt)] = (int)((unsigned)i | (f[k] ? MCC_ION_BIT : 0u));
+        }
         group_sync(g);
     }
     flush_stats(st_loc, a.ds->stats);
@@ -876,6 +893,7 @@ CollConsts pgb_coll_consts(pgb_run* r) {
     c.ion_value = (float)p.ionization_sigma_value;
     c.cx_value = (float)p.sigma_value;
     c.e_energy_coef = (float)((0.5 / PGB_CHARGE) * p.electron_mass);
+    c.el_max = c.el_const ? c.el_value : (c.species == PGB_ARGON ? 25.5f : 50.5f);
     c.i_energy_coef = (float)((0.5 / PGB_CHARGE) * p.ion_mass);
     c.e_pcoef = (float)(p.dt * 1.0e-20 * p.neutral_density);
     c.i_pcoef = (float)(p.dti * 1.0e-20 * p.neutral_density);

@@ -195,6 +195,11 @@ struct CollConsts {
     /* electron speed below which e_collisions::ionization certainly gives
      * a negative excess energy, hence NaN velocities (see mcc_ionize)  */
     float ion_vcap;
+    /* an upper bound of sigma_el over every energy: 50.5 for the H fit
+     * (largest 49.23 at 0.01 eV), 25.5 for the Ar fit (largest 24.81 near
+     * 13.9 eV; its low-energy polynomial goes negative), the value itself
+     * for a constant cross-section                                        */
+    float el_max;
     int n_neutral;
     uint64_t seed;
 };
