@@ -60,6 +60,9 @@ enum { PGB_GRID_Q_E = 0, PGB_GRID_Q_I = 1, PGB_GRID_RHO = 2, PGB_GRID_PHI = 3,
  * FP32 full multigrid inside an FP64 defect-correction loop, which converges
  * to the exact discrete solution (dc_max_iters passes).                    */
 enum { PGB_POISSON_FMG_REF = 0, PGB_POISSON_FP32_DC = 1, PGB_POISSON_FMG32 = 2 };
+/* energy-dependent cross-section fits, for pgb_cross_sections()          */
+enum { PGB_XS_AR_ELASTIC = 0, PGB_XS_AR_IONIZE = 1, PGB_XS_H_ELASTIC = 2, PGB_XS_H_IONIZE = 3,
+       PGB_XS_AR_CX = 4, PGB_XS_H_CX = 5 };
 /* boundary selector for pgb_boundary(): the two member-function pointers
  * implement_i_boundary / implement_e_boundary (boundary.h:372-383)          */
 enum { PGB_BOUNDARY_IONS = 0, PGB_BOUNDARY_ELECTRONS = 1 };
@@ -180,6 +183,15 @@ PGB_API int pgb_dump_species(pgb_run* run, int species, double* aos6, int64_t ca
  * particle's random streams: loaded particles get 0..n-1, new ones the next
  * ids in creation order.  *n_out = live count; at most cap ids are written. */
 PGB_API int pgb_dump_ids(pgb_run* run, int species, uint32_t* ids, int64_t cap, int64_t* n_out);
+/* No reference counterpart: the library's FP32 forms of the cross-section
+ * fits that the collision kernels use (e_collisions::sigma_Ar_elastic,
+ * sigma_Ar_ionize, sigma_H_elastic, sigma_H_ionize at e_collisions.cpp:
+ * 205-308; ion_collisions::sigma_Ar_cx, sigma_H_cx at ion_collisions.cpp:
+ * 170-199), evaluated on the GPU at n energies (eV, host array; each is
+ * converted to FP32 as the kernels hold it) into out (host, 1e-20 m^2).
+ * which is a PGB_XS_* index.  For checking the fits against the
+ * reference's FP64 functions.                                              */
+PGB_API int pgb_cross_sections(int32_t which, const double* energies, int64_t n, double* out);
 /* particle::particle_size */
 PGB_API int pgb_species_count(pgb_run* run, int species, int64_t* n_out);
 

@@ -618,6 +618,18 @@ static double sigma_h_cx(double e) {
     if (e < 1.0e-4) return 0.0;
     return (A1 * log((A2 / e) + A6)) / (1.0 + A3 * e + A4 * pow(e, 3.5) + A5 * pow(e, 5.4));
 }
+/* the six energy-dependent fits by PGB_XS_* index (tabulated by the tests) */
+double orc_sigma(int which, double e) {
+    switch (which) {
+        case PGB_XS_AR_ELASTIC: return sigma_ar_elastic(e);
+        case PGB_XS_AR_IONIZE: return sigma_ar_ionize(e);
+        case PGB_XS_H_ELASTIC: return sigma_h_elastic(e);
+        case PGB_XS_H_IONIZE: return sigma_h_ionize(e);
+        case PGB_XS_AR_CX: return sigma_ar_cx(e);
+        case PGB_XS_H_CX: return sigma_h_cx(e);
+        default: return 0.0;
+    }
+}
 static double sigma_el(orc_run* r, double e) {
     if (r->prm.sigma_elastic_mode == PGB_SIGMA_CONSTANT) return r->prm.elastic_sigma_value;
     return r->prm.species == PGB_ARGON ? sigma_ar_elastic(e) : sigma_h_elastic(e);

@@ -71,6 +71,8 @@ int  orc_graphs_get(orc_run* r, int which, int species, double* out, int64_t n);
 /* headless viewer plots, the rules of pgb_render (RGB8, row 0 at the top) */
 int  orc_render(orc_run* r, int plot, int W, int H, int max_points, uint32_t seed, unsigned char* img, int64_t cap);
 void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* one of the energy-dependent cross-section fits (PGB_XS_*) at e eV      */
+double orc_sigma(int which, double e);
 
 #ifdef __cplusplus
 }

@@ -24,6 +24,13 @@
  *   fields <dir>         read rho.bin (ny*nx doubles) from dir, run
  *                        fields::grid_potential(step 0) and grid_electric_field
  *                        (fields.cpp:169-268, Mglin) and write phi.bin, ex.bin, ey.bin.
+ *   sigma <dir>          read energies.bin (doubles, eV) from dir and write
+ *                        sigma.bin: per energy the reference's six energy-
+ *                        dependent cross-sections (units of 1e-20 m^2), in the
+ *                        order e-Ar elastic, e-Ar ionization, e-H elastic, e-H
+ *                        ionization, Ar+-Ar charge exchange, H+-H charge
+ *                        exchange (e_collisions.cpp:205-308,
+ *                        ion_collisions.cpp:170-199).
  *
  * The reference keeps its state in private members; this file alone widens
  * access so that the state can be read without modifying the reference.
@@ -87,7 +94,7 @@ static void write_fields(fields& f) {
 
 int main(int argc, char** argv) {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: %s run <dir> <nsteps> | fields <dir>\n", argv[0]);
+        std::fprintf(stderr, "usage: %s run <dir> <nsteps> | fields <dir> | sigma <dir>\n", argv[0]);
         return 2;
     }
     std::string mode = argv[1];
@@ -140,6 +147,25 @@ int main(int argc, char** argv) {
         fl->grid_electric_field();
         write_fields(*fl);
         delete fl;
+    } else if (mode == "sigma") {
+        FILE* f = std::fopen("energies.bin", "rb");
+        if (!f) { std::perror("energies.bin"); return 3; }
+        std::vector<double> e;
+        double v;
+        while (std::fread(&v, sizeof v, 1, f) == 1) e.push_back(v);
+        std::fclose(f);
+        e_collisions ec;
+        ion_collisions ic;
+        std::vector<double> out(6 * e.size());
+        for (size_t k = 0; k < e.size(); ++k) {
+            ec.energy = e[k]; out[6 * k + 0] = ec.sigma_Ar_elastic();
+            ec.energy = e[k]; out[6 * k + 1] = ec.sigma_Ar_ionize();
+            ec.energy = e[k]; out[6 * k + 2] = ec.sigma_H_elastic();
+            ec.energy = e[k]; out[6 * k + 3] = ec.sigma_H_ionize();
+            ic.energy = e[k]; out[6 * k + 4] = ic.sigma_Ar_cx();
+            ic.energy = e[k]; out[6 * k + 5] = ic.sigma_H_cx();   /* rescales its energy member */
+        }
+        write_bin("sigma.bin", out.data(), out.size() * sizeof(double));
     } else {
         std::cout.rdbuf(saved);
         std::fprintf(stderr, "unknown mode %s\n", mode.c_str());

@@ -24,6 +24,8 @@ def golden_cases(mode=None):
     for f in sorted(os.listdir(GOLDEN)):
         if f.endswith(".npz"):
             with np.load(os.path.join(GOLDEN, f)) as z:
+                if "mode" not in z.files:   # a table, not a run or field case
+                    continue
                 if mode is None or str(z["mode"]) == mode:
                     out.append(f[:-4])
     return out

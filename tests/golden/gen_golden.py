@@ -5,7 +5,7 @@ oracle/_ref/ref_<config> with oracle/Makefile, i.e. the reference's
 pic::pic_run, particle, fields, Mglin, collision and boundary classes
 compiled unchanged from their sources behind an in-process OpenCL stand-in).
 
-    python tests/golden/gen_golden.py
+    PIC_REFERENCE_DIR=<reference sources> python tests/golden/gen_golden.py [case ...]
 
 For every case it writes tests/golden/<case>.npz holding
   params   JSON of the parameters.h-style inputs (picgb.make_params keywords)
@@ -17,6 +17,9 @@ Field-only cases (mode "fields") hold rho and the reference's phi, ex, ey
 for one fields::grid_potential + grid_electric_field call.  Cases with a
 graph window also hold graph_window (start, end) and graph_<file> for every
 text file the reference's graphs class wrote at the end of the window.
+
+sigma_fits.npz holds the reference's six energy-dependent cross-section fits
+(e_collisions.cpp:205-308, ion_collisions.cpp:170-199) on a fixed energy list.
 
 The states are seeded synthetic plasmas sized so that every code path of the
 case is exercised in a few steps (particles crossing walls, collisions,
@@ -150,10 +153,43 @@ def run_case(name, cfg, kw, recipe, nsteps, refdir):
     return rec
 
 
+SIGMA_COLUMNS = ("ar_elastic", "ar_ionize", "h_elastic", "h_ionize", "ar_cx", "h_cx")
+# branch edges of the fits (eV); at the first four the reference leaves sigma
+# uninitialised (e_collisions.cpp:208-253), so only the points around them
+# are tabulated
+SIGMA_EDGES_UNDEFINED = (0.35, 15.0, 15.755, 100.0)
+SIGMA_EDGES = (0.01, 20.0, 13.6, 4.0, 1.0e-4 * 1000.0 * 1.66054e-27, 2.0e10 * 1000.0 * 1.66054e-27)
+
+
+def sigma_energies():
+    """10^4 log-spaced energies from 1e-5 to 1e5 eV, and points on both sides
+    of every branch edge (one FP64 step and a relative 1e-6 away), the edge
+    itself where the reference defines it."""
+    e = list(np.geomspace(1e-5, 1e5, 10000))
+    for b in SIGMA_EDGES + SIGMA_EDGES_UNDEFINED:
+        e += [np.nextafter(b, 0.0), np.nextafter(b, np.inf), b * (1 - 1e-6), b * (1 + 1e-6)]
+    e += list(SIGMA_EDGES)
+    return np.array(sorted(set(e)), dtype=np.float64)
+
+
+def sigma_table(refdir):
+    """The reference's six cross-section fits on sigma_energies()."""
+    e = sigma_energies()
+    with tempfile.TemporaryDirectory() as d:
+        e.tofile(os.path.join(d, "energies.bin"))
+        subprocess.run([os.path.join(refdir, "ref_core33"), "sigma", d], check=True)
+        sig = np.fromfile(os.path.join(d, "sigma.bin")).reshape(-1, 6)
+    np.savez_compressed(os.path.join(HERE, "sigma_fits.npz"), energies=e, sigma=sig,
+                        columns=np.array(SIGMA_COLUMNS))
+    return e.size
+
+
 def main():
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref"], check=True)
     refdir = os.path.join(REPO, "oracle", "_ref")
     only = sys.argv[1:]
+    if not only or "sigma_fits" in only:
+        print(f"sigma_fits: {sigma_table(refdir)} energies")
     for name, (cfg, kw, recipe, nsteps) in CASES.items():
         if only and name not in only:
             continue

@@ -65,6 +65,7 @@ def load():
         "orc_graphs_enable": (C.c_int, [R, C.POINTER(picgb.PgbGraphsParams)]),
         "orc_graphs_get": (C.c_int, [R, C.c_int, C.c_int, dp, i64]),
         "orc_render": (C.c_int, [R, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32, C.POINTER(C.c_uint8), i64]),
+        "orc_sigma": (C.c_double, [C.c_int, C.c_double]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -72,6 +73,12 @@ def load():
         f.argtypes = args
     _LIB = lib
     return lib
+
+
+def sigma(which, energies):
+    """The oracle's FP64 form of one cross-section fit (picgb.PGB_XS_*)."""
+    lib = load()
+    return np.array([lib.orc_sigma(which, float(e)) for e in energies])
 
 
 def _dp(a):

@@ -94,3 +94,35 @@ def test_collisions_match_the_reference_random_source_statistically():
     edges[-1] *= 1.0 + 1e-12
     chi2, pv = _chi2_two_sample(speed["gpu"], speed["ref"], edges)
     assert pv > 1e-4, ("exchanged-ion speed", chi2, pv)
+
+
+def test_energy_distributions_after_ten_steps_match_the_reference_random_source():
+    """Ten steps of elastic e-Ar scattering and Ar+-Ar charge exchange: the
+    electron and ion energy distributions of the device (Philox) and of the
+    reference's algorithm with its own rand() pass a two-sample chi-square
+    test at p > 1e-4 over 20 equal-count bins, and the mean energies agree
+    within 5 standard errors.  Charge exchange replaces an ion's energy by a
+    neutral's, so after ten steps a large share of the ions carries the
+    neutral temperature; for the electrons the test checks that scattering
+    leaves the same (nearly elastic) distribution on both sides."""
+    steps = 10
+    p = _params()
+    e, i = _state(p, 12)
+    o = orc.Oracle(p, rng=orc.ORC_RNG_LIBC, order=orc.ORC_ORDER_STABLE)
+    with picgb.Run(p) as r:
+        for x in (o, r):
+            x.load_particles(0, e)
+            x.load_particles(1, i)
+            x.step(steps)
+        out = {"gpu": (r.get_particles(0), r.get_particles(1)), "ref": (o.get_particles(0), o.get_particles(1))}
+        cg, co = r.counters(), o.counters()
+    assert cg["charge_exchange"] > 5000 and co["charge_exchange"] > 5000
+    for s, m in ((0, picgb.ELECTRON_MASS), (1, p.ion_mass)):
+        en = {k: 0.5 * m * np.sum(v[s][:, 2:5] ** 2, axis=1) / picgb.CHARGE for k, v in out.items()}
+        a, b = en["gpu"], en["ref"]
+        edges = np.quantile(np.concatenate([a, b]), np.linspace(0, 1, 21))
+        edges[-1] *= 1.0 + 1e-12
+        chi2, pv = _chi2_two_sample(a, b, edges)
+        assert pv > 1e-4, ("energy distribution", s, chi2, pv)
+        se = math.sqrt(a.var() / a.size + b.var() / b.size)
+        assert abs(a.mean() - b.mean()) <= 5 * se, ("mean energy", s, a.mean(), b.mean(), se)

@@ -9,6 +9,7 @@ host the fixtures were written on -- the match is exact; elsewhere the C
 library's transcendental functions may differ in the last bit, so a 1e-9
 relative tolerance applies there.
 """
+import os
 import platform
 
 import numpy as np
@@ -142,3 +143,14 @@ def test_port_graphs_match_reference_files():
     m = o.graphs_get("maxima")
     assert m[0] == np.max(mine["phi2d"]) and m[3] == np.max(mine["density2d_e"])
 
+
+
+def test_port_cross_sections_match_reference():
+    """The oracle's six cross-section fits equal the reference's own
+    functions (e_collisions.cpp:205-308, ion_collisions.cpp:170-199) on the
+    fixture's 10^4 energies and around every branch edge."""
+    import picgb
+    with np.load(os.path.join(os.path.dirname(__file__), "golden", "sigma_fits.npz")) as z:
+        e, sig, cols = z["energies"], z["sigma"], [str(c) for c in z["columns"]]
+    for k, name in enumerate(cols):
+        _close(orc.sigma(picgb.XS[name], e), sig[:, k], f"sigma {name}")

@@ -600,6 +600,22 @@ extern "C" int pgb_dump_ids(pgb_run* r, int s, uint32_t* ids, int64_t cap, int64
     return 0;
 }
 
+extern "C" int pgb_cross_sections(int32_t which, const double* energies, int64_t n, double* out) {
+    if (which < PGB_XS_AR_ELASTIC || which > PGB_XS_H_CX || n < 0 || (n > 0 && (!energies || !out)))
+        return fail(nullptr, PGB_ERR_ARG, "pgb_cross_sections: bad argument");
+    if (n == 0) return 0;
+    double* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(double) * 2 * (size_t)n);
+    if (e != cudaSuccess) return fail(nullptr, PGB_ERR_CUDA, std::string("pgb_cross_sections: ") + cudaGetErrorString(e));
+    int rc = 0;
+    if (cudaMemcpy(d, energies, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        pgb_launch_cross_sections(which, d, n, d + n, nullptr) != 0 ||
+        cudaMemcpy(out, d + n, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = fail(nullptr, PGB_ERR_CUDA, "pgb_cross_sections: evaluation failed");
+    cudaFree(d);
+    return rc;
+}
+
 extern "C" int pgb_set_time_step(pgb_run* r, int64_t t) {
     if (!r) return PGB_ERR_ARG;
     r->time_step = t;

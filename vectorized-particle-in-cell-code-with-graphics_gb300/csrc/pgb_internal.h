@@ -287,3 +287,4 @@ int pgb_launch_graphs(pgb_run* r);
 int pgb_poisson_solve(pgb_run* r);
 int pgb_launch_efield(pgb_run* r, int advance);
 int pgb_launch_rhs(pgb_run* r);
+int pgb_launch_cross_sections(int which, const double* d_e, long long n, double* d_out, cudaStream_t st);

@@ -882,6 +882,27 @@ static PushConsts push_consts(pgb_run* r, int s) {
     return pc;
 }
 
+/* the FP32 fits at the given energies (pgb_cross_sections) */
+__global__ void k_cross_sections(int which, const double* e, long long n, double* out) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const float x = (float)e[k];
+        float s = 0.0f;
+        switch (which) {
+            case PGB_XS_AR_ELASTIC: s = sig_ar_el(x); break;
+            case PGB_XS_AR_IONIZE: s = sig_ar_ion(x); break;
+            case PGB_XS_H_ELASTIC: s = sig_h_el(x); break;
+            case PGB_XS_H_IONIZE: s = sig_h_ion(x); break;
+            case PGB_XS_AR_CX: s = sig_ar_cx(x); break;
+            default: s = sig_h_cx(x); break;
+        }
+        out[k] = (double)s;
+    }
+}
+int pgb_launch_cross_sections(int which, const double* d_e, long long n, double* d_out, cudaStream_t st) {
+    k_cross_sections<<<(int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, st>>>(which, d_e, n, d_out);
+    return cudaGetLastError() == cudaSuccess ? 0 : PGB_ERR_CUDA;
+}
+
 CollConsts pgb_coll_consts(pgb_run* r) {
     CollConsts c;
     const pgb_params& p = r->p;

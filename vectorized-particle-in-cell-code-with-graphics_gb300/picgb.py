@@ -310,6 +310,7 @@ def load_library():
         "pgb_dump_species": (C.c_int, [R, C.c_int, dp, i64, C.POINTER(i64)]),
         "pgb_species_count": (C.c_int, [R, C.c_int, C.POINTER(i64)]),
         "pgb_dump_ids": (C.c_int, [R, C.c_int, C.POINTER(C.c_uint32), i64, C.POINTER(i64)]),
+        "pgb_cross_sections": (C.c_int, [C.c_int32, dp, i64, dp]),
         "pgb_set_time_step": (C.c_int, [R, i64]),
         "pgb_initial_boundary": (C.c_int, [R]),
         "pgb_step": (C.c_int, [R, i32]),
@@ -363,6 +364,22 @@ def _dptr(a: np.ndarray):
 
 
 PGB_ERR_ARG, PGB_ERR_CUDA, PGB_ERR_NOMEM, PGB_ERR_CAPACITY, PGB_ERR_STATE, PGB_ERR_IO = -1, -2, -3, -4, -5, -6
+# cross-section fits (pgb_cross_sections)
+XS = {"ar_elastic": 0, "ar_ionize": 1, "h_elastic": 2, "h_ionize": 3, "ar_cx": 4, "h_cx": 5}
+PGB_XS_AR_ELASTIC, PGB_XS_AR_IONIZE, PGB_XS_H_ELASTIC, PGB_XS_H_IONIZE, PGB_XS_AR_CX, PGB_XS_H_CX = range(6)
+
+
+def cross_sections(which, energies) -> np.ndarray:
+    """The library's FP32 cross-section fit `which` (a key of XS or a
+    PGB_XS_* index) evaluated on the GPU at the energies (eV)."""
+    lib = load_library()
+    w = XS[which] if isinstance(which, str) else int(which)
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    out = np.empty_like(e)
+    rc = lib.pgb_cross_sections(w, _dptr(e), e.size, _dptr(out))
+    if rc != 0:
+        raise PicError(f"pgb_cross_sections failed ({rc}): {lib.pgb_last_error(None).decode()}", rc)
+    return out
 
 
 class PicError(RuntimeError):
