@@ -37,6 +37,11 @@ import time
 
 import numpy as np
 
+# many runs on their own streams (the batched and served forms): 32 hardware
+# work queues instead of the default 8, so that unrelated streams do not
+# queue behind one another (read when the CUDA context is created)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 REPO = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(REPO, "vectorized-particle-in-cell-code-with-graphics_gb300")
 sys.path.insert(0, PKG)
@@ -389,15 +394,19 @@ def run_served(args):
     srv.close()
     res["served"] = {"seconds": wall, "particle_steps_per_s": s["particle_steps"] / wall,
                      "step_ms_p50": s["step_ms_p50"], "step_ms_p99": s["step_ms_p99"],
+                     "host_seconds": {k: s[k] for k in ("busy_seconds", "admit_seconds", "retire_seconds",
+                                                        "issue_seconds")},
                      "ttc_s_p50": _quantile([(finish[k] - arrival[k], 1) for k in finish], 0.5),
                      "ttc_s_p99": _quantile([(finish[k] - arrival[k], 1) for k in finish], 0.99)}
     # plain: one request at a time in arrival order
     steps_ms, ttc, ps = [], [], 0.0
+    solo = []
     t0 = time.perf_counter()
     for t, p, st, steps, _ in reqs:
         now = time.perf_counter() - t0
         if now < t:
             time.sleep(t - now)
+        ta = time.perf_counter()
         with picgb.Run(p) as r:
             r.load_particles(0, st[0])
             r.load_particles(1, st[1])
@@ -411,12 +420,15 @@ def run_served(args):
             r.get_particles(1)
         steps_ms.append((1000.0 * (b - a) / steps, steps))
         ps += 0.5 * (n0 + n1) * steps
+        solo.append(time.perf_counter() - ta)
         ttc.append((time.perf_counter() - t0 - t, 1))
     wall = time.perf_counter() - t0
     res["plain"] = {"seconds": wall, "particle_steps_per_s": ps / wall, "step_ms_p50": _quantile(steps_ms, 0.5),
                     "step_ms_p99": _quantile(steps_ms, 0.99), "ttc_s_p50": _quantile(ttc, 0.5),
                     "ttc_s_p99": _quantile(ttc, 0.99)}
     res["speedup"] = res["served"]["particle_steps_per_s"] / res["plain"]["particle_steps_per_s"]
+    # no schedule can finish before every request's arrival plus its time alone
+    res["critical_path_s"] = max(r[0] + d for r, d in zip(reqs, solo))
     res["config"] = {"requests": len(reqs), "arrivals": "Poisson, mean 20 per second (seeded)",
                      "grid_nodes": sorted(set(r[4] for r in reqs)),
                      "particles_per_species": [min(r[2][0].shape[0] for r in reqs), max(r[2][0].shape[0] for r in reqs)],
@@ -661,7 +673,7 @@ def main():
     ap.add_argument("--c2-steps", type=int, default=200)
     ap.add_argument("--batch-runs", type=int, default=64, help="runs of the batched workload (0 = skip it)")
     ap.add_argument("--batch-steps", type=int, default=200, help="steps per run of the batched workload")
-    ap.add_argument("--serve-requests", type=int, default=16, help="requests of the served workload (0 = skip it)")
+    ap.add_argument("--serve-requests", type=int, default=32, help="requests of the served workload (0 = skip it)")
     ap.add_argument("--serve-max-steps", type=int, default=5000, help="longest request of the served workload")
     ap.add_argument("--serve-round", type=int, default=10, help="steps per server round")
     ap.add_argument("--render-frames", type=int, default=10, help="frames per viewer plot timed (0 = skip)")

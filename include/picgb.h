@@ -261,9 +261,11 @@ PGB_API int pgb_footprint(const pgb_params* p, int64_t ne, int64_t ni, int64_t* 
  *     step count) into the server's queue.
  *   - pgb_server_round admits queued requests, first fit in submission
  *     order, while their pgb_footprint fits the HBM budget and fewer than
- *     max_active runs are resident.  It then steps every resident run
- *     min(round_steps, steps left) steps with pgb_step_batch and retires the
- *     runs that are done.
+ *     max_active runs are resident.  It gives every idle resident run its
+ *     next chunk of min(round_steps, steps left) steps (pgb_step_async, so
+ *     the chunks of all runs overlap), returns once at least one chunk has
+ *     finished (at once when none is in flight), and retires the runs that
+ *     are done.  A run never waits for the others' chunks.
  *   - pgb_server_result hands back a finished request's particles and frees
  *     them.
  * A request's result does not depend on the other requests it ran with.
@@ -275,9 +277,13 @@ typedef struct pgb_server_stats {
     int64_t run_steps;             /* steps executed, summed over runs            */
     double  particle_steps;        /* particles x steps, summed over runs         */
     double  busy_seconds;          /* wall time spent inside rounds               */
-    double  step_ms_p50, step_ms_p99;  /* time per step of a resident run          */
+    double  step_ms_p50, step_ms_p99;  /* time per step of a resident run, from
+                                          issuing a chunk to seeing it finished   */
     double  ttc_s_p50, ttc_s_p99;  /* submission to completion                     */
     int64_t hbm_in_use, hbm_budget;
+    double  admit_seconds;         /* wall time creating and loading admitted runs */
+    double  retire_seconds;        /* wall time reading back and freeing finished runs */
+    double  issue_seconds;         /* wall time queueing chunks                    */
 } pgb_server_stats;
 PGB_API int pgb_server_create(int64_t hbm_budget_bytes, int32_t round_steps, int32_t max_active, pgb_server** out);
 PGB_API int pgb_server_destroy(pgb_server* server);

@@ -533,9 +533,10 @@ def test_batched_runs_equal_runs_alone(nsteps):
 
 
 def test_served_requests_equal_runs_alone():
-    """Requests submitted to the server at different times, stepped together
-    in rounds with others, end exactly as the same runs stepped alone
-    (restart load, the pre-loop boundary pass, nsteps steps)."""
+    """Requests submitted to the server at different times, stepped beside
+    the others in chunks that overlap on the GPU, end exactly as the same
+    runs stepped alone (restart load, the pre-loop boundary pass, nsteps
+    steps)."""
     reqs = [("core33", 12), ("arcoll33", 7), ("hsee33", 20), ("core65", 9)]
     alone = []
     for c, n in reqs:

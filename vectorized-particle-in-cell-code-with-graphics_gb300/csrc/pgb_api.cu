@@ -328,6 +328,7 @@ extern "C" int pgb_create(const pgb_params* p, pgb_run** out) {
     int prio_lo = 0, prio_hi = 0;
     if (cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) == cudaSuccess &&
         cudaStreamCreateWithPriority(&r->side, cudaStreamNonBlocking, prio_hi) == cudaSuccess) {
+        r->prio_hi = prio_hi;
         if (cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming) == cudaSuccess) {
             if (cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming) == cudaSuccess) r->side_ok = true;
             else cudaEventDestroy(r->ev_fork);
@@ -899,8 +900,12 @@ static void drop_graphs(pgb_run* r) {
         if (r->graph[k]) { cudaGraphExecDestroy(r->graph[k]); r->graph[k] = nullptr; }
         if (r->graph_a[k]) { cudaGraphExecDestroy(r->graph_a[k]); r->graph_a[k] = nullptr; }
         if (r->graph_b[k]) { cudaGraphExecDestroy(r->graph_b[k]); r->graph_b[k] = nullptr; }
+        if (r->graph_m[k]) { cudaGraphExecDestroy(r->graph_m[k]); r->graph_m[k] = nullptr; }
+        if (r->tmpl_a[k]) { cudaGraphDestroy(r->tmpl_a[k]); r->tmpl_a[k] = nullptr; }
+        if (r->tmpl_b[k]) { cudaGraphDestroy(r->tmpl_b[k]); r->tmpl_b[k] = nullptr; }
     }
     if (r->graph_f) { cudaGraphExecDestroy(r->graph_f); r->graph_f = nullptr; }
+    if (r->tmpl_f) { cudaGraphDestroy(r->tmpl_f); r->tmpl_f = nullptr; }
 }
 
 /* graphs are usable when no step needs a host decision: no profiling and
@@ -911,8 +916,10 @@ static bool graphs_ok(pgb_run* r) {
     return true;
 }
 
-/* capture fn(r, ion_step) as a graph; -1 if the launches cannot be captured */
-static int capture(pgb_run* r, int (*fn)(pgb_run*, bool), bool ion_step, cudaGraphExec_t* out, long long* nl) {
+/* capture fn(r, ion_step) as a graph; -1 if the launches cannot be captured.
+ * keep: where to keep the captured template (else it is destroyed)     */
+static int capture(pgb_run* r, int (*fn)(pgb_run*, bool), bool ion_step, cudaGraphExec_t* out, long long* nl,
+                   cudaGraph_t* keep = nullptr) {
     cudaGraph_t g = nullptr;
     PGB_CK(r, cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
     long long l0 = r->launches;
@@ -927,7 +934,12 @@ static int capture(pgb_run* r, int (*fn)(pgb_run*, bool), bool ion_step, cudaGra
     *nl = r->launches - l0;
     r->launches = l0;
     e = cudaGraphInstantiate(out, g, 0);
-    cudaGraphDestroy(g);
+    if (keep && e == cudaSuccess) {
+        if (*keep) cudaGraphDestroy(*keep);
+        *keep = g;
+    } else {
+        cudaGraphDestroy(g);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         *out = nullptr;
@@ -938,8 +950,9 @@ static int capture(pgb_run* r, int (*fn)(pgb_run*, bool), bool ion_step, cudaGra
 
 /* run fn as graph *slot (captured on first use), or launch it directly
  * when graphs are off or cannot be captured                            */
-static int replay(pgb_run* r, int (*fn)(pgb_run*, bool), bool ion_step, cudaGraphExec_t* slot, long long* nl) {
-    if (graphs_ok(r) && !*slot && capture(r, fn, ion_step, slot, nl)) r->use_graphs = 0;
+static int replay(pgb_run* r, int (*fn)(pgb_run*, bool), bool ion_step, cudaGraphExec_t* slot, long long* nl,
+                  cudaGraph_t* keep = nullptr) {
+    if (graphs_ok(r) && !*slot && capture(r, fn, ion_step, slot, nl, keep)) r->use_graphs = 0;
     if (!*slot || !graphs_ok(r)) return fn(r, ion_step);
     PGB_CK(r, cudaGraphLaunch(*slot, r->stream));
     r->launches += *nl;
@@ -957,7 +970,7 @@ static int launch_step(pgb_run* r, bool ion_step) {
 static int flush_fields(pgb_run* r) {
     if (!r->fields_pending) return 0;
     r->fields_pending = false;
-    return replay(r, step_fields, false, &r->graph_f, &r->graph_f_launches);
+    return replay(r, step_fields, false, &r->graph_f, &r->graph_f_launches, &r->tmpl_f);
 }
 
 /* pipelining needs collisions to overlap and graphs to replay the parts */
@@ -970,14 +983,81 @@ static bool pipelined(pgb_run* r) { return r->side_ok && r->p.have_collisions &&
  * stream while this step's collisions (graph A) run on the run's stream;
  * the rest of the step (graph B) waits for both, and this step's field
  * solve is left pending.                                                */
+/* a step that needs a host decision before its collisions: a spatial sort
+ * or a compaction (both launch kernels between F and A)                  */
+static bool host_work_due(pgb_run* r) {
+    if (r->p.sort_interval > 0) return r->time_step % r->p.sort_interval == 0;
+    for (int s = 0; s < 2; ++s)
+        if (r->hs->dead[s] * 8 > r->hs->n[s] && r->hs->dead[s] > 0) return true;
+    return false;
+}
+
+/* The pipelined step as one graph launch: the previous step's field solve
+ * (F, its kernels at the side stream's top priority) beside this step's
+ * collisions (A), then the other particle phases (B), built once per key
+ * from the captured templates.  0: launched; 1: not available (graphs off
+ * or a capture failed), use the separate graphs.                         */
+static int launch_merged(pgb_run* r, bool ion_step) {
+    const int key = graph_key(r, ion_step);
+    if (!r->graph_m[key]) {
+        if (!r->graph_f && capture(r, step_fields, false, &r->graph_f, &r->graph_f_launches, &r->tmpl_f)) return 1;
+        if (!r->graph_a[key] &&
+            capture(r, step_mcc_beside, ion_step, &r->graph_a[key], &r->graph_a_launches[key], &r->tmpl_a[key]))
+            return 1;
+        if (!r->graph_b[key] &&
+            capture(r, step_particles, ion_step, &r->graph_b[key], &r->graph_b_launches[key], &r->tmpl_b[key]))
+            return 1;
+        if (!r->tmpl_f || !r->tmpl_a[key] || !r->tmpl_b[key]) return 1;
+        /* F's kernels at the top priority, as on the side stream */
+        size_t nn = 0;
+        if (cudaGraphGetNodes(r->tmpl_f, nullptr, &nn) != cudaSuccess) return 1;
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (nn && cudaGraphGetNodes(r->tmpl_f, nodes.data(), &nn) != cudaSuccess) return 1;
+        for (cudaGraphNode_t nd : nodes) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) {
+                cudaLaunchAttributeValue v = {};
+                v.priority = r->prio_hi;
+                cudaGraphKernelNodeSetAttribute(nd, cudaLaunchAttributePriority, &v);
+            }
+        }
+        cudaGetLastError();
+        cudaGraph_t g = nullptr;
+        cudaGraphNode_t nf, na, nb;
+        bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+                  cudaGraphAddChildGraphNode(&nf, g, nullptr, 0, r->tmpl_f) == cudaSuccess &&
+                  cudaGraphAddChildGraphNode(&na, g, nullptr, 0, r->tmpl_a[key]) == cudaSuccess;
+        if (ok) {
+            cudaGraphNode_t deps[2] = {nf, na};
+            ok = cudaGraphAddChildGraphNode(&nb, g, deps, 2, r->tmpl_b[key]) == cudaSuccess &&
+                 cudaGraphInstantiate(&r->graph_m[key], g, 0) == cudaSuccess;
+        }
+        if (g) cudaGraphDestroy(g);
+        if (!ok) {
+            cudaGetLastError();
+            r->graph_m[key] = nullptr;
+            return 1;
+        }
+    }
+    PGB_CK(r, cudaGraphLaunch(r->graph_m[key], r->stream));
+    r->launches += r->graph_f_launches + r->graph_a_launches[key] + r->graph_b_launches[key];
+    return 0;
+}
+
 static int issue_one_step(pgb_run* r) {
     Range range("step");
     int rc;
     const bool pipe = pipelined(r);
-    bool forked = false;
-    if (r->fields_pending) {
+    bool forked = false, merged = false;
+    if (pipe && r->fields_pending && !host_work_due(r)) {
+        rc = launch_merged(r, (r->time_step % r->dt_dti) == 0);
+        if (rc < 0) return rc;
+        merged = rc == 0;
+        if (merged) r->fields_pending = true;   /* this step's field solve */
+    }
+    if (!merged && r->fields_pending) {
         if (pipe && !r->graph_f &&
-            capture(r, step_fields, false, &r->graph_f, &r->graph_f_launches))
+            capture(r, step_fields, false, &r->graph_f, &r->graph_f_launches, &r->tmpl_f))
             r->use_graphs = 0;
         if (pipe && r->graph_f && pipelined(r)) {
             PGB_CK(r, cudaEventRecord(r->ev_fork, r->stream));
@@ -991,7 +1071,9 @@ static int issue_one_step(pgb_run* r) {
             return rc;
         }
     }
-    if (r->p.sort_interval > 0) {
+    if (merged) {
+        /* no sort or compaction is due: the step is queued */
+    } else if (r->p.sort_interval > 0) {
         /* spatial sort (drops tombstones too): electrons every sort_interval
          * steps, ions every PGB_ION_SORT_FACTOR * sort_interval           */
         for (int s = 0; s < 2; ++s)
@@ -1024,11 +1106,14 @@ static int issue_one_step(pgb_run* r) {
         r->prof.slots_i += r->hs->n[1];
     }
     const bool ion_step = (r->time_step % r->dt_dti) == 0;
-    if (pipe || forked) {
+    if (merged) {
+        /* A and B went with F in the step graph */
+    } else if (pipe || forked) {
         const int key = graph_key(r, ion_step);
-        if ((rc = replay(r, step_mcc_beside, ion_step, &r->graph_a[key], &r->graph_a_launches[key]))) return rc;
+        if ((rc = replay(r, step_mcc_beside, ion_step, &r->graph_a[key], &r->graph_a_launches[key], &r->tmpl_a[key])))
+            return rc;
         if (forked) PGB_CK(r, cudaStreamWaitEvent(r->stream, r->ev_join, 0));
-        if ((rc = replay(r, step_particles, ion_step, &r->graph_b[key], &r->graph_b_launches[key])))
+        if ((rc = replay(r, step_particles, ion_step, &r->graph_b[key], &r->graph_b_launches[key], &r->tmpl_b[key])))
             return rc;
         r->fields_pending = true;
     } else {

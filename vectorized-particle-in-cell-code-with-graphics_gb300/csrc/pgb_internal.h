@@ -167,6 +167,12 @@ struct pgb_run {
      * the side stream while A of step t+1 runs on the run's stream        */
     cudaGraphExec_t graph_a[8] = {}, graph_b[8] = {}, graph_f = nullptr;
     long long graph_a_launches[8] = {}, graph_b_launches[8] = {}, graph_f_launches = 0;
+    /* the captured templates of A, B and F, and per key one step graph
+     * built from them: F of the previous step beside A, then B -- one
+     * launch for a step that needs no host decision                      */
+    cudaGraph_t tmpl_a[8] = {}, tmpl_b[8] = {}, tmpl_f = nullptr;
+    cudaGraphExec_t graph_m[8] = {};
+    int prio_hi = 0;                       /* the side stream's priority      */
     bool fields_pending = false;           /* last step's field solve not yet issued */
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork, ev_join;

@@ -5,13 +5,17 @@
  * pic::pic from a restart state, the boundary pass before the loop, and
  * nsteps iterations of pic_run's loop body.
  *
- * A round admits queued requests in submission order, first fit, while
- * their pgb_footprint fits the HBM budget and fewer than max_active runs
- * are resident; steps every resident run together with pgb_step_batch
- * (each run on its own stream); and retires the runs that are done,
- * keeping their particles and counters on the host until they are taken.
- * Runs never share device state, so a request's result does not depend on
- * the requests it ran with.
+ * Continuous batching.  A round admits queued requests in submission
+ * order, first fit, while their pgb_footprint fits the HBM budget and
+ * fewer than max_active runs are resident; gives every resident run that
+ * is idle its next chunk of at most round_steps steps (pgb_step_async: the
+ * run's own stream, so the chunks of all runs overlap on the GPU); waits
+ * until at least one chunk has finished; and retires the runs that are
+ * done, keeping their particles and counters on the host until they are
+ * taken.  No run waits for another: a small run steps at its own pace
+ * beside a large one, and a run that finishes frees its memory for the
+ * queue at once.  Runs never share device state, so a request's result
+ * does not depend on the requests it ran with.
  */
 #include <algorithm>
 #include <chrono>
@@ -19,6 +23,7 @@
 #include <deque>
 #include <map>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 #include "picgb.h"
@@ -45,7 +50,10 @@ struct Request {
 struct Resident {
     Request req;
     pgb_run* run = nullptr;
-    int32_t done = 0;
+    int32_t done = 0;              /* steps finished                        */
+    int32_t inflight = 0;          /* steps of the chunk on the GPU (0: idle) */
+    int64_t n_before = -1;         /* particles when the chunk was issued (-1: not read yet) */
+    Clock::time_point issued;
 };
 
 struct Result {
@@ -84,8 +92,8 @@ struct pgb_server {
     std::map<int64_t, Result> results;
     std::deque<int64_t> done_ids;
     int64_t submitted = 0, admitted = 0, completed = 0, run_steps = 0;
-    double particle_steps = 0.0, busy = 0.0;
-    std::vector<std::pair<double, int64_t>> step_ms;   /* (ms per step, run-steps) per round */
+    double particle_steps = 0.0, busy = 0.0, t_admit = 0.0, t_retire = 0.0, t_issue = 0.0;
+    std::vector<std::pair<double, int64_t>> step_ms;   /* (ms per step, steps) per finished chunk */
     std::vector<std::pair<double, int64_t>> ttc;       /* (seconds, 1) per request */
 };
 
@@ -170,6 +178,13 @@ static int retire(pgb_server* s, Resident& r) {
     return 0;
 }
 
+static int64_t particles_of(pgb_run* run) {
+    int64_t a = 0, b = 0;
+    pgb_species_count(run, PGB_ELECTRONS, &a);
+    pgb_species_count(run, PGB_IONS, &b);
+    return a + b;
+}
+
 extern "C" int pgb_server_round(pgb_server* s, int32_t* completed) {
     if (!s) return fail("pgb_server_round: bad argument", PGB_ERR_ARG);
     if (completed) *completed = 0;
@@ -183,54 +198,60 @@ extern "C" int pgb_server_round(pgb_server* s, int32_t* completed) {
         Resident r;
         r.req = std::move(*it);
         it = s->queue.erase(it);
+        const Clock::time_point ta = Clock::now();
         int rc = start_run(r);
+        s->t_admit += seconds_between(ta, Clock::now());
         if (rc) return fail("pgb_server_round: starting request " + std::to_string(r.req.id) + " failed: " +
                                 pgb_last_error(nullptr), rc);
         s->in_use += r.req.footprint;
         s->admitted++;
         s->resident.push_back(std::move(r));
     }
-    if (s->resident.empty()) return 0;
-    /* every resident run advances the same number of steps */
-    int32_t k = s->round_steps;
-    for (auto& r : s->resident) k = std::min(k, r.req.nsteps - r.done);
-    int64_t before = 0, after = 0;
-    std::vector<pgb_run*> runs;
-    for (auto& r : s->resident) runs.push_back(r.run);
-    for (auto* run : runs) {
-        int64_t a = 0, b = 0;
-        pgb_species_count(run, PGB_ELECTRONS, &a);
-        pgb_species_count(run, PGB_IONS, &b);
-        before += a + b;
+    /* every idle run gets its next chunk */
+    int inflight = 0;
+    const Clock::time_point ti = Clock::now();
+    for (auto& r : s->resident) {
+        if (r.inflight == 0 && r.done < r.req.nsteps) {
+            const int32_t k = std::min(s->round_steps, r.req.nsteps - r.done);
+            if (r.n_before < 0) r.n_before = particles_of(r.run);
+            r.issued = Clock::now();
+            int rc = pgb_step_async(r.run, k);
+            if (rc) return fail("pgb_server_round: stepping request " + std::to_string(r.req.id) + " failed: " +
+                                    pgb_last_error(r.run), rc);
+            r.inflight = k;
+        }
+        if (r.inflight) inflight++;
     }
-    if (k > 0) {
-        const Clock::time_point t1 = Clock::now();
-        int rc = pgb_step_batch(runs.data(), (int32_t)runs.size(), k);
-        if (rc) {
-            std::string msg = "pgb_server_round: stepping failed";
-            for (auto& r : s->resident) {
-                const char* m = pgb_last_error(r.run);
-                if (m && *m && std::strcmp(m, "no error") != 0) msg += std::string("; request ") + std::to_string(r.req.id) + ": " + m;
-            }
-            return fail(msg, rc);
+    s->t_issue += seconds_between(ti, Clock::now());
+    /* wait until at least one chunk has finished */
+    bool any = false;
+    while (inflight > 0 && !any) {
+        for (auto& r : s->resident) {
+            if (!r.inflight) continue;
+            int32_t idle = 0;
+            int rc = pgb_query(r.run, &idle);
+            if (rc) return fail("pgb_server_round: request " + std::to_string(r.req.id) + " failed: " +
+                                    pgb_last_error(r.run), rc);
+            if (!idle) continue;
+            const double ms = 1000.0 * seconds_between(r.issued, Clock::now()) / r.inflight;
+            s->step_ms.push_back({ms, (int64_t)r.inflight});
+            const int64_t n_after = particles_of(r.run);
+            s->particle_steps += 0.5 * (double)(r.n_before + n_after) * r.inflight;
+            r.n_before = n_after;   /* the next chunk starts from here */
+            s->run_steps += r.inflight;
+            r.done += r.inflight;
+            r.inflight = 0;
+            any = true;
         }
-        const double ms = 1000.0 * seconds_between(t1, Clock::now()) / k;
-        s->step_ms.push_back({ms, (int64_t)k * (int64_t)runs.size()});
-        for (auto* run : runs) {
-            int64_t a = 0, b = 0;
-            pgb_species_count(run, PGB_ELECTRONS, &a);
-            pgb_species_count(run, PGB_IONS, &b);
-            after += a + b;
-        }
-        s->particle_steps += 0.5 * (double)(before + after) * k;
-        s->run_steps += (int64_t)k * (int64_t)runs.size();
+        if (!any) std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
     /* retire the finished runs */
     for (size_t j = 0; j < s->resident.size();) {
         Resident& r = s->resident[j];
-        r.done += k;
-        if (r.done >= r.req.nsteps) {
+        if (r.inflight == 0 && r.done >= r.req.nsteps) {
+            const Clock::time_point tr = Clock::now();
             int rc = retire(s, r);
+            s->t_retire += seconds_between(tr, Clock::now());
             if (rc) return rc;
             if (completed) (*completed)++;
             s->resident.erase(s->resident.begin() + (long)j);
@@ -294,5 +315,8 @@ extern "C" int pgb_server_get_stats(pgb_server* s, pgb_server_stats* out) {
     out->ttc_s_p99 = weighted_quantile(s->ttc, 0.99);
     out->hbm_in_use = s->in_use;
     out->hbm_budget = s->budget;
+    out->admit_seconds = s->t_admit;
+    out->retire_seconds = s->t_retire;
+    out->issue_seconds = s->t_issue;
     return 0;
 }

@@ -91,7 +91,8 @@ class PgbServerStats(C.Structure):
                 ("queued", C.c_int64), ("run_steps", C.c_int64), ("particle_steps", C.c_double),
                 ("busy_seconds", C.c_double), ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double),
                 ("ttc_s_p50", C.c_double), ("ttc_s_p99", C.c_double), ("hbm_in_use", C.c_int64),
-                ("hbm_budget", C.c_int64)]
+                ("hbm_budget", C.c_int64), ("admit_seconds", C.c_double), ("retire_seconds", C.c_double),
+                ("issue_seconds", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
