@@ -48,10 +48,12 @@ __device__ __forceinline__ float plane(int x) { return __int_as_float(x); }
 __device__ __forceinline__ float pos_dead() { return __int_as_float(PGB_POS_DEAD); }
 __device__ __forceinline__ bool is_dead(float lane) { return __float_as_int(lane) == PGB_POS_DEAD; }
 __device__ __forceinline__ bool pos_is_nan(float lane) { return __float_as_int(lane) == PGB_POS_NAN; }
-/* (int)(x/DX): truncation toward zero; INT_MIN for NaN (x86-64)            */
+/* (int)(x/DX): truncation toward zero (a negative x first gains 2^ps - 1,
+ * then the arithmetic shift rounds down); INT_MIN for NaN (x86-64)       */
 __device__ __forceinline__ int pcell(float lane, int ps) {
     const int x = __float_as_int(lane);
-    return x <= PGB_POS_NAN ? INT32_MIN : (x >= 0 ? (x >> ps) : -((-x) >> ps));
+    const int c = (x + ((x >> 31) & ((1 << ps) - 1))) >> ps;
+    return x <= PGB_POS_NAN ? INT32_MIN : c;
 }
 /* x > 0 and x < 0 (NaN is neither)                                        */
 __device__ __forceinline__ bool pos_gt0(float lane) { return __float_as_int(lane) > 0; }
@@ -59,9 +61,11 @@ __device__ __forceinline__ bool pos_lt0(float lane) {
     const int x = __float_as_int(lane);
     return x < 0 && x != PGB_POS_NAN;
 }
-/* x/DX - (int)(x/DX) for x >= 0: exact (ps <= 23 bits)                   */
+/* x/DX - (int)(x/DX) for x >= 0, exact: the ps fraction bits placed in the
+ * mantissa of 1.0 (ps <= 23), minus 1                                     */
 __device__ __forceinline__ float pfrac(float lane, int ps) {
-    return (float)(__float_as_int(lane) & ((1 << ps) - 1)) * __int_as_float((127 - ps) << 23);
+    const unsigned m = ((unsigned)__float_as_int(lane) & ((1u << ps) - 1u)) << (23 - ps);
+    return __int_as_float(0x3f800000 | (int)m) - 1.0f;
 }
 /* the position in cells (exact in FP64) and in metres                    */
 __device__ __forceinline__ double pos_cells(float lane, int ps) {
@@ -82,13 +86,13 @@ __device__ __forceinline__ float pos_from_cells(double c, int ps) {
     return __int_as_float(__double2int_rn(v));
 }
 __device__ __forceinline__ float pos_from_m(double x, double d, int ps) { return pos_from_cells(x / d, ps); }
-/* x + d with d in units of 2^-ps of a cell (the push: d = dt*v/DX*2^ps) */
+/* x + d with d in units of 2^-ps of a cell (the push: d = dt*v/DX*2^ps),
+ * in 32-bit integers: |x| <= 2^30 and |d| < 2^30 cannot overflow           */
 __device__ __forceinline__ float pos_step(float lane, float d) {
-    if (d != d) return __int_as_float(PGB_POS_NAN);
-    const float lim = (float)PGB_POS_LIM;
-    long long v = (long long)__float_as_int(lane) + __float2ll_rn(fminf(fmaxf(d, -2.0f * lim), 2.0f * lim));
-    v = v < -(long long)PGB_POS_LIM ? -(long long)PGB_POS_LIM : (v > PGB_POS_LIM ? PGB_POS_LIM : v);
-    return __int_as_float((int)v);
+    const float lim = 1073741760.0f;   /* the largest float below 2^30 */
+    const int v = __float_as_int(lane) + __float2int_rn(fminf(fmaxf(d, -lim), lim));
+    const int c = min(max(v, -PGB_POS_LIM), PGB_POS_LIM);
+    return d != d ? __int_as_float(PGB_POS_NAN) : __int_as_float(c);
 }
 
 /* CIC deposit of one particle (pic.cl:36-49) as int64 fixed point:
