@@ -438,7 +438,7 @@ extern "C" int pgb_destroy(pgb_run* r) {
     cudaFree(r->rd_img);
     cudaFree(r->rd_scratch);
     if (r->prof_ev_ok)
-        for (int k = 0; k < 12; ++k) cudaEventDestroy(r->prof_ev[k]);
+        for (int k = 0; k < 13; ++k) cudaEventDestroy(r->prof_ev[k]);
     if (r->copy_ev_ok)
         for (int k = 0; k < PGB_COPY_EVENTS; ++k) cudaEventDestroy(r->copy_ev[k]);
     if (r->side_ok) { cudaEventDestroy(r->ev_fork); cudaEventDestroy(r->ev_join); }
@@ -715,7 +715,7 @@ extern "C" int pgb_collide_ions(pgb_run* r) {
     int rc = need_particles(r);
     if (rc) return rc;
     if ((rc = set_device_step(r, r->time_step, 1))) return rc;
-    if (pgb_launch_cx(r)) return PGB_ERR_CUDA;
+    if (pgb_launch_cx(r, 0, 0)) return PGB_ERR_CUDA;
     return sync_state(r);
 }
 
@@ -773,10 +773,13 @@ extern "C" int pgb_efield(pgb_run* r) {
  * CUDA graphs for every step.
  *   step_mcc:       e_collisions::collision (pic.cpp:1071-1075): collision
  *                   tests, scattering and the list of ionization events;
- *                   reads no field
+ *                   on an ion step, charge exchange of the ions present
+ *                   (ion_collisions::collision, pic.cpp:1102-1104, which
+ *                   reads only ions and comes before their push); reads
+ *                   no field
  *   step_particles: charge reset, electron push and deposit, ionization
- *                   products, injection,
- *                   ion charge exchange and push, walls, population control
+ *                   products, injection, charge exchange of the ions they
+ *                   appended, ion push, walls, population control
  *                   (pic.cpp:1080-1141), then ds->t += 1
  *   step_fields:    charge finalisation, grid_rho, grid_potential,
  *                   grid_electric_field (pic.cpp:1143-1161), then ds->tf += 1
@@ -784,19 +787,22 @@ extern "C" int pgb_efield(pgb_run* r) {
  * t+1 need the particles after step t's walls, not step t's fields, so the
  * pipelined path (issue_one_step) runs them while step t's field solve is
  * still in flight on the run's side stream.                              */
-static int mcc_part(pgb_run* r, int leave_sms) {
+static int mcc_part(pgb_run* r, int leave_sms, bool ion_step) {
     if (!r->p.have_collisions) return 0;
     if (pgb_launch_mcc(r, leave_sms)) return PGB_ERR_CUDA;
     PROF_MARK(r, 9);
     if (pgb_launch_scatter(r, leave_sms)) return PGB_ERR_CUDA;
     PROF_MARK(r, 10);
     if (pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
+    PROF_MARK(r, 11);
+    if (ion_step && pgb_launch_cx(r, 0, leave_sms)) return PGB_ERR_CUDA;
+    PROF_MARK(r, 12);
     return 0;
 }
-static int step_mcc(pgb_run* r, bool) { return mcc_part(r, 0); }
+static int step_mcc(pgb_run* r, bool ion_step) { return mcc_part(r, 0, ion_step); }
 /* beside a field solve: the one-CTA multigrid needs SMs of its own */
 #define PGB_FIELD_SMS 32
-static int step_mcc_beside(pgb_run* r, bool) { return mcc_part(r, PGB_FIELD_SMS); }
+static int step_mcc_beside(pgb_run* r, bool ion_step) { return mcc_part(r, PGB_FIELD_SMS, ion_step); }
 
 static int step_particles(pgb_run* r, bool ion_step) {
     const bool coll = r->p.have_collisions != 0;
@@ -820,7 +826,9 @@ static int step_particles(pgb_run* r, bool ion_step) {
     if (r->p.number_to_inject > 0 && pgb_launch_inject(r, 3, true)) return PGB_ERR_CUDA;
     PROF_MARK(r, 2);
     if (ion_step) {
-        if (coll && pgb_launch_cx(r)) return PGB_ERR_CUDA;
+        /* charge exchange of the ions appended since the collision pass */
+        const bool appended = r->p.number_to_inject > 0 || r->p.steadystate;
+        if (coll && appended && pgb_launch_cx(r, 1, 0)) return PGB_ERR_CUDA;
         PROF_MARK(r, 3);
         if (pgb_launch_push(r, 1, true)) return PGB_ERR_CUDA;
         if (pgb_build_list(r, LIST_OUT_I, 1)) return PGB_ERR_CUDA;
@@ -886,6 +894,8 @@ static int profile_collect(pgb_run* r) {
         r->prof.ms_collide_e += mk;
         PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[9], r->prof_ev[10]));
         r->prof.ms_scatter_e += mk;
+        PGB_CK(r, cudaEventElapsedTime(&mk, r->prof_ev[11], r->prof_ev[12]));
+        r->prof.ms_collide_ions += mk;
     }
     r->prof.ms_walls += ms[1] + ms[4];
     r->prof.ms_collide_ions += ms[2];
@@ -1282,7 +1292,7 @@ extern "C" int pgb_get_stream(pgb_run* r, void** stream) {
 extern "C" int pgb_set_profiling(pgb_run* r, int on) {
     if (!r) return PGB_ERR_ARG;
     if (on && !r->prof_ev_ok) {
-        for (int k = 0; k < 12; ++k) PGB_CK(r, cudaEventCreate(&r->prof_ev[k]));
+        for (int k = 0; k < 13; ++k) PGB_CK(r, cudaEventCreate(&r->prof_ev[k]));
         r->prof_ev_ok = true;
     }
     memset(&r->prof, 0, sizeof(r->prof));

@@ -67,6 +67,8 @@ struct DevState {
                                 potential); trails t while a solve overlaps the next
                                 step's collisions                                      */
     unsigned long long scat_n;   /* scattering events queued by the collision pass */
+    long long n_cx;          /* ion slots whose charge exchange was tested before this
+                                step's appends (the rest are tested after them)       */
 };
 
 /* dense event lists (ordered by slot) */
@@ -221,7 +223,7 @@ struct pgb_run {
     int fault_alloc = 0, alloc_events = 0;
     int prof_on = 0;
     pgb_profile prof;
-    cudaEvent_t prof_ev[12];
+    cudaEvent_t prof_ev[13];
     bool prof_ev_ok = false;
 };
 
@@ -275,7 +277,8 @@ int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e);
 int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i);
 int pgb_launch_mcc(pgb_run* r, int leave_sms);
 int pgb_launch_scatter(pgb_run* r, int leave_sms);
-int pgb_launch_cx(pgb_run* r);
+/* tail 0: the ions present (records their count); 1: those appended since */
+int pgb_launch_cx(pgb_run* r, int tail, int leave_sms);
 int pgb_launch_walls(pgb_run* r, int which);
 int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long i0, long long i1);
 int pgb_launch_dump_offsets(pgb_run* r, int s);

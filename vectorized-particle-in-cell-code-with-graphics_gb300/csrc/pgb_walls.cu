@@ -455,7 +455,21 @@ struct CxArgs {
     long long* col_acc;      /* per-column accumulator carried across steps (fixed point) */
     const float* neut_i;     /* ion-neutral table (FP32) */
     uint64_t seed;
+    int tail;                /* 0: slots [0, n), recording n in ds->n_cx;
+                                1: the slots appended since, [ds->n_cx, n)  */
 };
+
+/* The slots one pass tests.  Charge exchange (ion_collisions.cpp:255-308)
+ * walks the ions in slot order with one accumulator per column, so a pass
+ * over the ions present when the step starts, run beside the previous
+ * step's field solve, followed by a pass over the ions appended by
+ * ionization and injection, continues every column's sum in the same order
+ * and makes the same decisions as one pass over all of them.             */
+__device__ __forceinline__ void cx_range(const CxArgs& a, long long& i0, long long& n) {
+    n = a.ds->n[1];
+    i0 = a.tail ? a.ds->n_cx : 0;
+    if (i0 > n) i0 = n;
+}
 
 __device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, float vz, int& col) {
     col = -1;
@@ -476,8 +490,9 @@ __device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, fl
 __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
     pgb_pdl_entry();
     extern __shared__ unsigned long long s_sum[];
-    const long long n = a.ds->n[1];
-    const int ntiles = (int)((n + CX_TILE - 1) / CX_TILE);
+    long long i0, n;
+    cx_range(a, i0, n);
+    const int ntiles = (int)((n - i0 + CX_TILE - 1) / CX_TILE);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         for (int c = threadIdx.x; c < a.nx; c += blockDim.x) s_sum[c] = 0ull;
         __syncthreads();
@@ -487,7 +502,7 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
             float vz[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                long long i = (long long)t * CX_TILE + k0 + q * blockDim.x;
+                long long i = i0 + (long long)t * CX_TILE + k0 + q * blockDim.x;
                 p[q] = make_float4(pos_dead(), 0.f, 0.f, 0.f);
                 vz[q] = 0.f;
                 if (k0 + q * blockDim.x < CX_TILE && i < n) {
@@ -512,9 +527,12 @@ __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
     pgb_pdl_entry();
     const int lane = threadIdx.x & 31;
     const int col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    long long i0, n;
+    cx_range(a, i0, n);
+    /* the tail pass starts where this one ends (k_cx_tiles has read n) */
+    if (!a.tail && blockIdx.x == 0 && threadIdx.x == 0) a.ds->n_cx = n;
     if (col >= a.nx) return;
-    const long long n = a.ds->n[1];
-    const int ntiles = (int)((n + CX_TILE - 1) / CX_TILE);
+    const int ntiles = (int)((n - i0 + CX_TILE - 1) / CX_TILE);
     long long acc = a.col_acc[col];
     int fired = 0;
     const long long* row = a.tile_sum + (long long)col * a.ntl;
@@ -547,7 +565,7 @@ __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
         /* scan tile t0+first element by element, then continue after it */
         int tt = t0 + first;
         for (int b = 0; b < CX_TILE; b += 32) {
-            long long i = (long long)tt * CX_TILE + b + lane;
+            long long i = i0 + (long long)tt * CX_TILE + b + lane;
             int c = -1;
             long long pf = 0;
             if (i < n) pf = cx_prob_fixed(a, a.i.xv[i], a.i.vz[i], c);
@@ -639,8 +657,9 @@ int pgb_launch_walls(pgb_run* r, int which) {
     return 0;
 }
 
-int pgb_launch_cx(pgb_run* r) {
+int pgb_launch_cx(pgb_run* r, int tail, int leave_sms) {
     CxArgs a;
+    a.tail = tail;
     a.i = r->sp[1]; a.ds = r->ds; a.nx = r->nx; a.ny = r->ny; a.ps = r->ps;
     a.cc = pgb_coll_consts(r);
     a.pcoef = a.cc.i_pcoef; a.ecoef = a.cc.i_energy_coef;
@@ -649,7 +668,8 @@ int pgb_launch_cx(pgb_run* r) {
     a.col_acc = (long long*)r->prob_cx;
     a.neut_i = r->neut[1];
     a.seed = r->p.seed;
-    PGB_CK(r, pgb_launch_pdl(k_cx_tiles, dim3(r->sms * 4), dim3(256), sizeof(unsigned long long) * r->nx, r->stream, a));
+    const int sms = r->sms - leave_sms > 8 ? r->sms - leave_sms : 8;
+    PGB_CK(r, pgb_launch_pdl(k_cx_tiles, dim3(sms * 4), dim3(256), sizeof(unsigned long long) * r->nx, r->stream, a));
     r->launches++;
     int warps = 8;
     PGB_CK(r, pgb_launch_pdl(k_cx_walk, dim3((r->nx + warps - 1) / warps), dim3(warps * 32), 0, r->stream, a));
