@@ -49,9 +49,10 @@ struct PushArgs {
 /* gather (pic.cl:56-92) + push (pic.cl:95-149) of one particle in cell units */
 __device__ __forceinline__ void gather_push_one(const PushConsts& pc, const float2* exy, float4& p, float& vz,
                                                 bool& moved) {
-    int jp = pcell(p.x, pc.ps), kp = pcell(p.y, pc.ps);
     moved = false;
-    if (jp < pc.nx && pos_gt0(p.x) && kp < pc.ny && pos_gt0(p.y)) {
+    /* jp < nx && x > 0 && kp < ny && y > 0; then the cell is a shift */
+    if (pos_open_in(p.x, pc.nx, pc.ps) && pos_open_in(p.y, pc.ny, pc.ps)) {
+        const int jp = pbits(p.x) >> pc.ps, kp = pbits(p.y) >> pc.ps;
         float wj = pfrac(p.x, pc.ps), wk = pfrac(p.y, pc.ps);
         float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
         float a2 = wk * (1.0f - wj), a1 = wj * wk;
@@ -158,11 +159,12 @@ __device__ __forceinline__ void flush_stats(int (&st)[2], long long* stats) {
 /* ordered compaction of per-thread flags of one tile into its list.
  * Item k of thread t is slot tile*TILE + k*THREADS + t, so (k, warp, lane)
  * order is slot order.                                                    */
+static_assert(PGB_ITEMS * (PGB_PUSH_THREADS / 32) == 32, "one warp scans a tile's (item, warp) counts");
 template <int NL>
 __device__ __forceinline__ void tile_lists(const bool (&f)[NL][PGB_ITEMS], long long tile_base, int tile,
                                            int* const (&tl)[NL], int* const (&tc)[NL]) {
+    static_assert(NL <= PGB_PUSH_THREADS / 32, "one warp per list");
     __shared__ int s_off[NL][PGB_ITEMS][PGB_PUSH_THREADS / 32];
-    __shared__ int s_tot[NL];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
     unsigned m[NL][PGB_ITEMS];
@@ -174,16 +176,18 @@ __device__ __forceinline__ void tile_lists(const bool (&f)[NL][PGB_ITEMS], long 
             if (lane == 0) s_off[l][k][warp] = __popc(m[l][k]);
         }
     __syncthreads();
-    if (threadIdx.x < NL) {
-        int l = threadIdx.x, acc = 0;
-        for (int k = 0; k < PGB_ITEMS; ++k)
-            for (int w = 0; w < PGB_PUSH_THREADS / 32; ++w) {
-                int c = s_off[l][k][w];
-                s_off[l][k][w] = acc;
-                acc += c;
-            }
-        s_tot[l] = acc;
-        tc[l][tile] = acc;
+    if (warp < NL) {
+        /* lane = k * warps + w: the 32 counts in slot order, one shuffle scan */
+        int* so = &s_off[warp][0][0];
+        const int c = so[lane];
+        int incl = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        so[lane] = incl - c;
+        if (lane == 31) tc[warp][tile] = incl;
     }
     __syncthreads();
 #pragma unroll
@@ -208,25 +212,35 @@ __device__ __forceinline__ void tile_lists(const bool (&f)[NL][PGB_ITEMS], long 
 #define WIN_MAX_WEIGHT 1.99f
 static_assert(PGB_PIECE_TILES * PGB_TILE <= 4096, "window sums are sized for 4096 particles per piece");
 static_assert((PGB_FIX_SCALE * 1.99 + 1.0) * 4096.0 < 4294967296.0, "window sums must fit 32 bits");
-__device__ __forceinline__ unsigned long long win_get(const unsigned int* win, int k) { return win[k]; }
+
+/* round(v) to nearest even for 0 <= v < 2^22, as __float2int_rn: adding
+ * 1.5 * 2^23 leaves v's integer part in the low mantissa bits, rounded by
+ * the addition itself (1.5 * 2^23 is even, so ties go the same way)      */
+__device__ __forceinline__ unsigned int round_small(float v) {
+    return (unsigned int)__float_as_int(__fadd_rn(v, 12582912.0f)) - 0x4b400000u;
+}
 
 /* deposit into the CTA's shared window when the four nodes fall inside it,
- * else into the global grid                                               */
+ * else into the global grid.  Caller checks deposit_ok (x, y > 0).       */
 __device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned int* win, int ox, int oy, int nx,
                                             int ps, float xs, float ys, float w) {
-    int jp = pcell(xs, ps), kp = pcell(ys, ps);
-    int lx = jp - ox, ly = kp - oy;
-    if (win && lx >= 0 && ly >= 0 && lx < PGB_WIN - 1 && ly < PGB_WIN - 1 && w >= 0.0f && w < WIN_MAX_WEIGHT) {
+    const int jp = pbits(xs) >> ps, kp = pbits(ys) >> ps;
+    const int lx = jp - ox, ly = kp - oy;
+    if (win && (unsigned)lx < (unsigned)(PGB_WIN - 1) && (unsigned)ly < (unsigned)(PGB_WIN - 1) && w >= 0.0f &&
+        w < WIN_MAX_WEIGHT) {
         float wj = pfrac(xs, ps), wk = pfrac(ys, ps);
         float a4 = (1.0f - wj) * (1.0f - wk), a3 = wj * (1.0f - wk);
         float a2 = wk * (1.0f - wj), a1 = wj * wk;
-        const float S = PGB_FIX_SCALE_F;
+        /* (a*w)*2^19 == a*(w*2^19) exactly: scaling by a power of two
+         * commutes with rounding (w < 2: no overflow; a product below
+         * FP32's normal range rounds to 0 either way)                     */
+        const float wS = w * PGB_FIX_SCALE_F;
         const int k = ly * PGB_WIN + lx;
-        /* below 2^20: the 32-bit conversion gives the same integer */
-        atomicAdd(&win[k], (unsigned int)__float2int_rn(a4 * w * S));
-        atomicAdd(&win[k + 1], (unsigned int)__float2int_rn(a3 * w * S));
-        atomicAdd(&win[k + PGB_WIN], (unsigned int)__float2int_rn(a2 * w * S));
-        atomicAdd(&win[k + PGB_WIN + 1], (unsigned int)__float2int_rn(a1 * w * S));
+        /* below 2^21: the same integer as __float2ll_rn in deposit_cell */
+        atomicAdd(&win[k], round_small(__fmul_rn(a4, wS)));
+        atomicAdd(&win[k + 1], round_small(__fmul_rn(a3, wS)));
+        atomicAdd(&win[k + PGB_WIN], round_small(__fmul_rn(a2, wS)));
+        atomicAdd(&win[k + PGB_WIN + 1], round_small(__fmul_rn(a1, wS)));
     } else {
         deposit_cell(qacc, nx, ps, xs, ys, w);
     }
@@ -284,6 +298,11 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
     const int tile0 = (int)a.ds->sorted_tiles[a.s];
     const int nitems = npieces + (ntiles > tile0 ? ntiles - tile0 : 0);
     const PushConsts pc = a.pc;
+    /* the window starts zeroed; each flush leaves it zeroed again */
+    if (DEP && npieces > 0) {
+        for (int k = threadIdx.x; k < WIN_NODES; k += blockDim.x) s_win[k] = 0u;
+        __syncthreads();
+    }
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         if (item < npieces) {
             int4 pc4 = a.pieces[item];
@@ -293,19 +312,25 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
                 win = s_win;
                 ox = (pc4.z % a.nbx) * PGB_BIN - PGB_HALO;
                 oy = (pc4.z / a.nbx) * PGB_BIN - PGB_HALO;
-                for (int k = threadIdx.x; k < WIN_NODES; k += blockDim.x) s_win[k] = 0u;
-                __syncthreads();
             }
             for (int t = pc4.x; t < pc4.x + pc4.y && t < ntiles; ++t)
                 push_tile<DEP>(a, pc, t, n, win, ox, oy);
             if (win) {
                 __syncthreads();
-                for (int k = threadIdx.x; k < WIN_NODES; k += blockDim.x) {
-                    unsigned long long v = win_get(s_win, k);
-                    if (v) {
-                        int gx = ox + k % PGB_WIN, gy = oy + k / PGB_WIN;
-                        if (gx >= 0 && gy >= 0 && gx < pc.nx && gy < pc.ny)
-                            atomicAdd(&a.qacc[(long long)gy * pc.nx + gx], v);
+                /* a warp per window row, a lane per node: add the non-zero
+                 * sums to the grid and zero them for the next piece        */
+                const int lane = threadIdx.x & 31;
+                for (int ry = threadIdx.x >> 5; ry < PGB_WIN; ry += PGB_PUSH_THREADS / 32) {
+                    const int gy = oy + ry;
+                    unsigned long long* qrow = a.qacc + (long long)gy * pc.nx;
+                    for (int rx = lane; rx < PGB_WIN; rx += 32) {
+                        const unsigned int v = s_win[ry * PGB_WIN + rx];
+                        if (v) {
+                            s_win[ry * PGB_WIN + rx] = 0u;
+                            const int gx = ox + rx;
+                            if (gx >= 0 && gy >= 0 && gx < pc.nx && gy < pc.ny)
+                                atomicAdd(qrow + gx, (unsigned long long)v);
+                        }
                     }
                 }
                 __syncthreads();

@@ -55,6 +55,16 @@ __device__ __forceinline__ int pcell(float lane, int ps) {
     const int c = (x + ((x >> 31) & ((1 << ps) - 1))) >> ps;
     return x <= PGB_POS_NAN ? INT32_MIN : c;
 }
+/* x > 0 and (int)(x/DX) < n, in one unsigned compare: 0 < x < n*2^ps
+ * (false for the tombstone and NaN codes)                                */
+__device__ __forceinline__ bool pos_open_in(float lane, int n, int ps) {
+    return (unsigned)(__float_as_int(lane) - 1) < (unsigned)((n << ps) - 1);
+}
+/* 0 <= (int)(x/DX) < n (truncation toward zero): -2^ps < x < n*2^ps; false
+ * for the tombstone and NaN codes, whose cell index is INT_MIN           */
+__device__ __forceinline__ bool pos_trunc_in(float lane, int n, int ps) {
+    return (unsigned)(__float_as_int(lane) + (1 << ps) - 1) < (unsigned)((n << ps) + (1 << ps) - 1);
+}
 /* x > 0 and x < 0 (NaN is neither)                                        */
 __device__ __forceinline__ bool pos_gt0(float lane) { return __float_as_int(lane) > 0; }
 __device__ __forceinline__ bool pos_lt0(float lane) {
@@ -116,7 +126,7 @@ __device__ __forceinline__ void deposit_cell(unsigned long long* qacc, int nx, i
 
 /* collect_charge's test: jp < nx-1 && x > 0 && kp < ny-1 && y > 0 (pic.cl:35) */
 __device__ __forceinline__ bool deposit_ok(float xl, float yl, int nx, int ny, int ps) {
-    return pos_gt0(xl) && pos_gt0(yl) && pcell(xl, ps) < nx - 1 && pcell(yl, ps) < ny - 1;
+    return pos_open_in(xl, nx - 1, ps) && pos_open_in(yl, ny - 1, ps);
 }
 
 __device__ __forceinline__ void maybe_deposit(unsigned long long* qacc, int nx, int ny, int ps, float xl, float yl,
@@ -128,12 +138,14 @@ __device__ __forceinline__ void maybe_deposit(unsigned long long* qacc, int nx, 
 /* e_boundary / ion_boundary: outside iff jp<0 || jp>=nx || kp<0 || kp>=ny
  * (boundary.cpp:595-599, 774-778)                                         */
 __device__ __forceinline__ bool outside_absorbing(float xl, float yl, int nx, int ny, int ps) {
-    int jp = pcell(xl, ps), kp = pcell(yl, ps);
-    return jp < 0 || jp >= nx || kp < 0 || kp >= ny;
+    return !(pos_trunc_in(xl, nx, ps) && pos_trunc_in(yl, ny, ps));
 }
-/* steady walls: x < 0 or (int)(x/DX) >= nx, same for y (boundary.cpp:906-1013) */
+/* steady walls: x < 0 or (int)(x/DX) >= nx, same for y (boundary.cpp:906-1013);
+ * as unsigned, a negative x is above n*2^ps; NaN is neither               */
 __device__ __forceinline__ bool outside_steady(float xl, float yl, int nx, int ny, int ps) {
-    return pos_lt0(xl) || pcell(xl, ps) >= nx || pos_lt0(yl) || pcell(yl, ps) >= ny;
+    const int x = __float_as_int(xl), y = __float_as_int(yl);
+    return (x != PGB_POS_NAN && (unsigned)x >= (unsigned)(nx << ps)) ||
+           (y != PGB_POS_NAN && (unsigned)y >= (unsigned)(ny << ps));
 }
 
 /* ------------------------------------------------------- cross sections */
