@@ -81,9 +81,9 @@ __device__ __forceinline__ void gather_push_one(const PushConsts& pc, const floa
 }
 
 /* electron-neutral collision test (e_collisions.cpp:504-551): both
- * probabilities come from the energy before any event.  Returns a bit set
- * MCC_SCATTER | MCC_IONIZE; *energy is the electron's energy (eV) and *st
- * the EMCC stream after its first draw, as the scattering continues it.  */
+ * probabilities come from the energy before any event; the decisions are
+ * a bit set MCC_SCATTER | MCC_IONIZE.  The scattering continues the EMCC
+ * stream after the test's first draw.                                    */
 #define MCC_SCATTER 1
 #define MCC_IONIZE 2
 /* |v|^2 with its roundings spelled out: the collision test and the
@@ -91,15 +91,31 @@ __device__ __forceinline__ void gather_push_one(const PushConsts& pc, const floa
 __device__ __forceinline__ float speed2(const float4& p, float vz) {
     return __fmaf_rn(vz, vz, __fmaf_rn(p.w, p.w, __fmul_rn(p.z, p.z)));
 }
-__device__ __forceinline__ int mcc_test(const CollConsts& cc, unsigned int id, unsigned int step, int nx, int ny,
-                                        int ps, const float4& p, float vz, float* energy_out, pgb_stream* st) {
-    int jp = pcell(p.x, ps), kp = pcell(p.y, ps);
-    if (!(jp >= 0 && jp < nx && kp >= 0 && kp < ny)) return 0;
-    float u2 = speed2(p, vz);
+/* The test in two parts.  mcc_draw: in the domain (0 <= jp < nx,
+ * 0 <= kp < ny), |v|^2 and the elastic test's uniform R, the first draw
+ * of the electron's EMCC stream; false outside (no event).              */
+__device__ __forceinline__ bool mcc_draw(const CollConsts& cc, unsigned int id, unsigned int step, int nx, int ny,
+                                         int ps, const float4& p, float vz, float& u2, float& R) {
+    if (!(pos_trunc_in(p.x, nx, ps) && pos_trunc_in(p.y, ny, ps))) return false;
+    u2 = speed2(p, vz);
+    pgb_stream st;
+    pgb_stream_init(&st, cc.seed, id, step, PGB_STREAM_EMCC, 0);
+    R = pgb_u01f(pgb_stream_u32(&st));
+    return true;
+}
+/* whether mcc_decide can find an event: the elastic bound below with a
+ * margin of 1e-5 over its own (about 3e-7 of FP32 rounding, the square
+ * root included), written without the square root as u^2 K^2 > 4 R^2
+ * (K^2 = cc.el_bound2), or an energy at or above the lowest at which the
+ * ionization fit is non-zero (cc.ion_emin).  A false here is a decision
+ * of no event that mcc_decide would take too.                           */
+__device__ __forceinline__ bool mcc_candidate(const CollConsts& cc, float u2, float R) {
+    return (R < 0.5f && u2 * cc.el_bound2 > (2.0f * R) * (2.0f * R)) || cc.e_energy_coef * u2 >= cc.ion_emin;
+}
+/* the decisions from |v|^2 and R (bit set MCC_SCATTER | MCC_IONIZE) */
+__device__ __forceinline__ int mcc_decide(const CollConsts& cc, float u2, float R) {
     float energy = cc.e_energy_coef * u2;
     float u = sqrtf(u2);
-    pgb_stream_init(st, cc.seed, id, step, PGB_STREAM_EMCC, 0);
-    float R = pgb_u01f(pgb_stream_u32(st));
     int ev = 0;
     /* P = 1 - exp(-x) is at most 1, so P > 2R cannot hold for R >= 1/2;
      * and P <= x <= u*pcoef*el_max, so with that bound (times 1 + 1e-6,
@@ -116,7 +132,6 @@ __device__ __forceinline__ int mcc_test(const CollConsts& cc, unsigned int id, u
      * which holds exactly when x > 0 (for NaN x neither holds)          */
     float sio = sigma_ion(cc, energy);
     if (u * cc.e_pcoef * sio > 0.0f) ev |= MCC_IONIZE;
-    *energy_out = energy;
     return ev;
 }
 
@@ -400,10 +415,23 @@ struct MccGroupSmem {
     int off[PGB_ITEMS][PGB_PUSH_THREADS / 32];    /* ionization events per (item, warp) */
     int soff[PGB_ITEMS][PGB_PUSH_THREADS / 32];   /* scattering events per (item, warp) */
     unsigned long long sbase;                      /* the tile's first scattering-list entry */
+    int qn;                                        /* candidates queued                      */
+    float qu2[PGB_TILE];                           /* candidate |v|^2, R and tile position   */
+    float qr[PGB_TILE];
+    unsigned short qi[PGB_TILE];
+    unsigned char ev[PGB_TILE];                    /* decisions by tile position             */
 };
+static_assert(MCC_GROUPS * sizeof(MccGroupSmem) <= 48 * 1024, "static shared memory");
 __device__ __forceinline__ void group_sync(int g) {
     asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "n"(PGB_PUSH_THREADS) : "memory");
 }
+/* A tile in three passes.  (1) Every electron: the domain test, |v|^2,
+ * the Philox draw R and mcc_candidate; the candidates (about one in ten
+ * at a few eV) are queued.  (2) The queue, one candidate per thread: the
+ * cross-sections, the exponential and the decisions of mcc_decide, so
+ * that the fits run densely instead of in every warp that holds one
+ * candidate.  (3) Every electron takes its decisions back in slot order
+ * for the lists.                                                         */
 __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
     pgb_pdl_entry();
     __shared__ MccGroupSmem s_grp[MCC_GROUPS];
@@ -415,9 +443,11 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     const unsigned step = (unsigned)a.ds->t;
     int st_loc[2] = {0, 0};
+    if (t == 0) S.qn = 0;
+    group_sync(g);
     for (int tile = blockIdx.x * MCC_GROUPS + g; tile < ntiles; tile += gridDim.x * MCC_GROUPS) {
         const long long base = (long long)tile * PGB_TILE;
-        /* all loads of the thread's items first, then the tests */
+        /* (1) all loads of the thread's items first, then the draws */
         float4 pa[PGB_ITEMS];
         float vza[PGB_ITEMS];
         unsigned int ida[PGB_ITEMS];
@@ -433,25 +463,49 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
                 ida[k] = a.id[i];
             }
         }
+        unsigned cand = 0;   /* bit k: item k is queued */
+#pragma unroll
+        for (int k = 0; k < PGB_ITEMS; ++k) {
+            float u2 = 0.0f, R = 1.0f;
+            bool c = false;
+            if (!is_dead(pa[k].x) && mcc_draw(a.cc, ida[k], step, a.pc.nx, a.pc.ny, a.pc.ps, pa[k], vza[k], u2, R))
+                c = mcc_candidate(a.cc, u2, R);
+            const unsigned cm = __ballot_sync(0xffffffffu, c);
+            int qb = 0;
+            if (lane == 0 && cm) qb = atomicAdd(&S.qn, __popc(cm));
+            qb = __shfl_sync(0xffffffffu, qb, 0);
+            if (c) {
+                const int q = qb + __popc(cm & lt);
+                S.qu2[q] = u2;
+                S.qr[q] = R;
+                S.qi[q] = (unsigned short)(k * PGB_PUSH_THREADS + t);
+                cand |= 1u << k;
+            }
+        }
+        group_sync(g);
+        /* (2) the queued candidates, densely */
+        {
+            const int qn = S.qn;
+            for (int q = t; q < qn; q += PGB_PUSH_THREADS) S.ev[S.qi[q]] = (unsigned char)mcc_decide(a.cc, S.qu2[q], S.qr[q]);
+        }
+        group_sync(g);
+        /* (3) decisions back in slot order */
+        if (t == 0) S.qn = 0;   /* every thread has read it before the barrier */
         bool f[PGB_ITEMS], sc[PGB_ITEMS];
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
             const int i = (int)(base + k * PGB_PUSH_THREADS + t);
-            int ev = 0;
-            if (!is_dead(pa[k].x)) {
-                float energy;
-                pgb_stream st;
-                ev = mcc_test(a.cc, ida[k], step, a.pc.nx, a.pc.ny, a.pc.ps, pa[k], vza[k], &energy, &st);
-            }
+            const int ev = (cand >> k) & 1u ? S.ev[k * PGB_PUSH_THREADS + t] : 0;
             sc[k] = (ev & MCC_SCATTER) != 0;
             f[k] = (ev & MCC_IONIZE) != 0;
             st_loc[0] += sc[k] ? 1 : 0;
             st_loc[1] += f[k] ? 1 : 0;
-            /* an ionization without scattering is applied here */
+            /* an ionization without scattering is applied here (rare: the
+             * electron is read again rather than held through the passes) */
             if (f[k] && !sc[k]) {
-                float4 p = pa[k];
-                float vz = vza[k];
-                mcc_ionize(a.cc, a.neut, ida[k], step, p, vz);
+                float4 p = a.xv[i];
+                float vz = a.vz[i];
+                mcc_ionize(a.cc, a.neut, a.id[i], step, p, vz);
                 a.xv[i] = p;
                 a.vz[i] = vz;
             }
@@ -943,6 +997,13 @@ CollConsts pgb_coll_consts(pgb_run* r) {
     c.i_energy_coef = (float)((0.5 / PGB_CHARGE) * p.ion_mass);
     c.e_pcoef = (float)(p.dt * 1.0e-20 * p.neutral_density);
     c.i_pcoef = (float)(p.dti * 1.0e-20 * p.neutral_density);
+    {
+        const double k = (double)c.e_pcoef * (double)c.el_max * 1.000001 * (1.0 + 1.0e-5);
+        c.el_bound2 = (float)(k * k * (1.0 + 1.0e-6));
+        if (!(c.el_bound2 >= 0.0f)) c.el_bound2 = INFINITY;   /* a negative or NaN bound tests everyone */
+    }
+    if (c.ion_const) c.ion_emin = c.ion_value > 0.0f ? -INFINITY : INFINITY;
+    else c.ion_emin = c.species == PGB_ARGON ? 15.755f : 13.6f;
     c.me = p.electron_mass; c.mi = p.ion_mass; c.dt = p.dt; c.dti = p.dti;
     c.threshold = p.threshold;
     c.reduced_mass = p.ion_mass / (p.electron_mass + p.ion_mass);

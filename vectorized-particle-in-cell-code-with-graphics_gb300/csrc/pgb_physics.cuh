@@ -216,6 +216,13 @@ struct CollConsts {
      * 13.9 eV; its low-energy polynomial goes negative), the value itself
      * for a constant cross-section                                        */
     float el_max;
+    /* (e_pcoef * el_max * 1.000001 * (1 + 1e-5))^2, rounded up: the
+     * collision kernel's square-root-free form of that bound            */
+    float el_bound2;
+    /* the lowest energy (eV) at which sigma_ion can be non-zero: 13.6 and
+     * 15.755 below which the H and Ar fits return 0; for a constant
+     * cross-section -inf if it is positive (any speed ionizes), else +inf */
+    float ion_emin;
     int n_neutral;
     uint64_t seed;
 };
