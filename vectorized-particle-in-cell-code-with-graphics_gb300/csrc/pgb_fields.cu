@@ -235,24 +235,27 @@ __global__ void k_restrict(T* uc, const T* uf, int nc) {
     }
 }
 /* --------------------------------------- one-CTA solver for coarse levels */
-/* Shared-memory image of levels 0..J (n_l = 2^(l+1)+1).  U/F: the current
- * level's solution and right-hand side at the top, V/R: correction and
- * restricted residual of the levels below.                              */
+/* Shared-memory image of levels 0..J (n_l = 2^(l+1)+1).  U/F: a level's
+ * solution and right-hand side when it is the top of a V-cycle (every
+ * level of a full multigrid), V/R: correction and restricted residual of
+ * the levels below the top, so levels 0..J-1 only (J = 5, 65 nodes:
+ * 2*5718 + 2*1493 values).                                               */
+__host__ __device__ __forceinline__ int small_nodes_below(int l) {
+    /* sum_{m<l} (2^(m+1)+1)^2 = 4(4^l-1)/3 + 4(2^l-1) + l */
+    return (4 * ((1 << (2 * l)) - 1)) / 3 + 4 * ((1 << l) - 1) + l;
+}
 template <class T>
 struct SmallMG {
     T* base;
     T length;
+    int J;
     __device__ __forceinline__ int n(int l) const { return (1 << (l + 1)) + 1; }
-    /* the levels below l hold sum_{m<l} (2^(m+1)+1)^2 = 4(4^l-1)/3 + 4(2^l-1) + l
-     * nodes per array, four arrays each: addresses are register arithmetic
-     * (a pointer table indexed by level would live in local memory)      */
-    __device__ __forceinline__ T* U(int l) const {
-        const int below = (4 * ((1 << (2 * l)) - 1)) / 3 + 4 * ((1 << l) - 1) + l;
-        return base + 4 * below;
-    }
+    /* addresses are register arithmetic (a pointer table indexed by level
+     * would live in local memory)                                        */
+    __device__ __forceinline__ T* U(int l) const { return base + 2 * small_nodes_below(l); }
     __device__ __forceinline__ T* F(int l) const { return U(l) + n(l) * n(l); }
-    __device__ __forceinline__ T* V(int l) const { return U(l) + 2 * n(l) * n(l); }
-    __device__ __forceinline__ T* R(int l) const { return U(l) + 3 * n(l) * n(l); }
+    __device__ __forceinline__ T* V(int l) const { return base + 2 * small_nodes_below(J + 1) + 2 * small_nodes_below(l); }
+    __device__ __forceinline__ T* R(int l) const { return V(l) + n(l) * n(l); }
 };
 
 /* Loops of the one-CTA solver run over flat point indices so that every
@@ -421,6 +424,7 @@ __global__ void __launch_bounds__(1024, 1) k_mg_small(int J, int mode, T length,
     SmallMG<T> s;
     s.base = reinterpret_cast<T*>(smem_raw);
     s.length = length;
+    s.J = J;
     if (mode == 0) {
         const T* gf = g_f[J];
         T* const fJ = s.F(J);
@@ -467,12 +471,7 @@ __global__ void __launch_bounds__(1024, 1) k_mg_small(int J, int mode, T length,
 }
 
 static size_t small_smem_bytes(int J, size_t elem) {
-    size_t tot = 0;
-    for (int l = 0; l <= J; ++l) {
-        size_t n = (size_t)(1 << (l + 1)) + 1;
-        tot += 4 * n * n;
-    }
-    return tot * elem;
+    return (size_t)(2 * small_nodes_below(J + 1) + 2 * small_nodes_below(J)) * elem;
 }
 
 /* ------------------------------------------------------- E field */
@@ -635,8 +634,10 @@ static int vcycle(pgb_run* r, const Levels<T>& L, int j, int jsmall, T* u, const
 }
 
 /* top level of the one-CTA solver.  FP32 levels up to 65 nodes are faster
- * in one CTA than as separate launches; FP64 runs at a small fraction of
- * the FP32 rate, and one SM is too slow for more than 33 nodes.          */
+ * in one CTA than as separate launches; at 129 nodes one SM is slower than
+ * the level's three launches (measured: 10 us more a V-cycle).  FP64 runs
+ * at a small fraction of the FP32 rate, and one SM is too slow for more
+ * than 33 nodes.                                                        */
 static int small_top(pgb_run* r, size_t elem) {
     const int lim = elem == sizeof(float) ? PGB_MG_SMALL : PGB_MG_SMALL64;
     int jsmall = 0;
