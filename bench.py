@@ -61,15 +61,18 @@ ELECTRON_KERNELS = {
 METRIC = "particle-steps/s"
 POISSON_DESC = {"FMG32": "full multigrid, the reference's schedule, FP32",
                 "FMG_REF": "full multigrid, the reference's schedule, FP64 (bit-identical to the reference)",
-                "FP32_DC": "FP32 full multigrid + FP64 defect correction (FP32 V-cycles)"}
-# FP32_DC passes: the FP32 full-multigrid pass and three FP64 defect
-# corrections, each an FP32 V-cycle (phi within 3e-7 and E within 2e-6 of the
-# converged FP64 solution on this workload's charge)
-DC_PASSES = 4
+                "FP32_DC": "FP32 full multigrid + FP64 defect correction (FP32 V-cycles)",
+                "DST_DC": "FP32 sine-transform solve of the discrete system + FP64 defect correction"}
+# defect-correction passes per mode.  FP32_DC: the FP32 full-multigrid pass
+# and three FP64 corrections, each an FP32 V-cycle (phi within 3e-7 and E
+# within 2e-6 of the converged FP64 solution on this workload's charge).
+# DST_DC: the FP32 sine-transform solve (exact up to FP32 rounding) and one
+# FP64 correction.
+DC_PASSES = {"FP32_DC": 4, "DST_DC": 2}
 
 
 def workload_params(picgb, seed=1003, n_per_species=N_PER_SPECIES, poisson="FP32_DC", sort_interval=0,
-                    dc_passes=DC_PASSES):
+                    dc_passes=None):
     """H preset ("H with coll-boundary") at 513^2 nodes and Te = 3 eV.  The
     macro-particle size is set so that the mean density equals the design
     density ELECTRON_PARTICLE_DENSITY = 1e15 m^-3 (parameters.h:71) for
@@ -78,7 +81,7 @@ def workload_params(picgb, seed=1003, n_per_species=N_PER_SPECIES, poisson="FP32
               HAVE_COLLISIONS=True, SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT",
               SIGMA_IONIZATION="ENERGY_DEPENDENT", E_IMPACT_SEE="YES", ION_IMPACT_SEE="NO", REFLECTION="YES",
               BACKSCATTER="YES", STEADYSTATE="NO", NUMBER_TO_INJECT=10, SIZE_TO_CHECK=2**31 - 1, RAND_SEED=seed,
-              POISSON=poisson, DC_MAX_ITERS=dc_passes, SORT_INTERVAL=sort_interval)
+              POISSON=poisson, DC_MAX_ITERS=dc_passes or DC_PASSES.get(poisson, 1), SORT_INTERVAL=sort_interval)
     L = picgb.make_params(**kw).xlength
     size = 1.0e15 * L * L / n_per_species
     return picgb.make_params(E_MACROPARTICLE_SIZE=size, ION_MACROPARTICLE_SIZE=size, **kw)
@@ -542,7 +545,7 @@ def run_gpu(args, rank, world):
     if args.accuracy_steps > 0 and world == 1:
         accuracy = run_accuracy(args, picgb, p, e, i)
         accuracy["poisson"] = POISSON_DESC[args.poisson] + (f", {p.dc_max_iters} passes"
-                                                            if args.poisson == "FP32_DC" else "")
+                                                            if args.poisson in DC_PASSES else "")
     modes = run_modes(args, picgb, e, i, n) if (args.mode_steps > 0 and world == 1) else None
     del e, i
     configs = run_configs(args, picgb, os.cpu_count() or 1) if (args.configs and world == 1) else None
@@ -571,9 +574,10 @@ def time_steps(run, steps):
 def run_modes(args, picgb, e, i, n):
     """The step with the other Poisson modes, same state and schedule:
     FMG_REF (the reference's one-pass FP64 full multigrid, bit-identical to
-    it) and FMG32 (that schedule in FP32, 1e-5-2e-5 of phi from it)."""
+    it), FMG32 (that schedule in FP32, 1e-5-2e-5 of phi from it), and the
+    two converged modes FP32_DC and DST_DC, whichever is not the headline."""
     out = {}
-    for mode in ("FMG_REF", "FMG32"):
+    for mode in [m for m in ("FMG_REF", "FMG32", "FP32_DC", "DST_DC") if m != args.poisson]:
         p = workload_params(picgb, n_per_species=n, poisson=mode, sort_interval=args.sort)
         with picgb.Run(p) as r:
             r.load_particles(0, e)
@@ -662,7 +666,7 @@ def main():
     ap.add_argument("--ref-max-steps", type=int, default=50,
                     help="the reference arm times at most this many of --steps (stated in its line)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--poisson", default="FP32_DC", choices=["FMG32", "FMG_REF", "FP32_DC"])
+    ap.add_argument("--poisson", default="FP32_DC", choices=["FMG32", "FMG_REF", "FP32_DC", "DST_DC"])
     ap.add_argument("--sort", type=int, default=12,
                     help="spatial sort of the electrons every k steps, of the ions every 4k (0 = off)")
     ap.add_argument("--mode-steps", type=int, default=40, help="steps timed per other Poisson mode (0 = skip)")
@@ -686,7 +690,8 @@ def main():
                           "H+-H CX), 512x512 cells (513^2 nodes), Gaussian density sigma=L/4, Te=3 eV, Ti=0.026 eV",
               "grid_nodes": GRID_NODES, "particles_per_species": n,
               "l2": "inputs larger than L2 (particle state 0.9 GB at 16Mi per species)",
-              "poisson": POISSON_DESC[args.poisson] + (f", {DC_PASSES} passes" if args.poisson == "FP32_DC" else ""),
+              "poisson": POISSON_DESC[args.poisson] + (f", {DC_PASSES[args.poisson]} passes"
+                                                       if args.poisson in DC_PASSES else ""),
               "macro_particle_size": "mean density 1e15 m^-3", "sort_interval": args.sort,
               "parallelism": "replicas" if world > 1 else "single"}
     threads = os.cpu_count() or 1
@@ -754,8 +759,8 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": ("f32 velocities and multigrid, int32 fixed-point positions, int64 fixed-point charge, "
-                      "f64 defect correction and fields") if args.poisson == "FP32_DC" else
+            "dtype": ("f32 velocities and Poisson solve, int32 fixed-point positions, int64 fixed-point charge, "
+                      "f64 defect correction and fields") if args.poisson in DC_PASSES else
                      "f32 velocities, int32 fixed-point positions; " + POISSON_DESC[args.poisson],
             "data": "synthetic (seeded)",
             "config": config, "e2e": res["e2e"], "roofline": roofline, "cpu_baseline": cpu,

@@ -58,8 +58,10 @@ enum { PGB_GRID_Q_E = 0, PGB_GRID_Q_I = 1, PGB_GRID_RHO = 2, PGB_GRID_PHI = 3,
  * (mglin.cpp:21-196) in FP64 with the same schedule -- bit-identical to the
  * reference for the same rho.  FMG32: the same schedule in FP32.  FP32_DC:
  * FP32 full multigrid inside an FP64 defect-correction loop, which converges
- * to the exact discrete solution (dc_max_iters passes).                    */
-enum { PGB_POISSON_FMG_REF = 0, PGB_POISSON_FP32_DC = 1, PGB_POISSON_FMG32 = 2 };
+ * to the exact discrete solution (dc_max_iters passes).  DST_DC: the same
+ * loop around an FP32 sine-transform solve of the discrete system (exact up
+ * to FP32 rounding), so that two passes reach FP64 rounding.             */
+enum { PGB_POISSON_FMG_REF = 0, PGB_POISSON_FP32_DC = 1, PGB_POISSON_FMG32 = 2, PGB_POISSON_DST_DC = 3 };
 /* energy-dependent cross-section fits, for pgb_cross_sections()          */
 enum { PGB_XS_AR_ELASTIC = 0, PGB_XS_AR_IONIZE = 1, PGB_XS_H_ELASTIC = 2, PGB_XS_H_IONIZE = 3,
        PGB_XS_AR_CX = 4, PGB_XS_H_CX = 5 };

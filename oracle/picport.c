@@ -490,9 +490,10 @@ static void apply_walls(orc_run* r, double* phi, double phi_right) {
     for (int i = 0; i < nx; i++) { phi[i] = r->prm.phi_bottom; phi[(ny - 1) * nx + i] = r->prm.phi_top; }
 }
 void orc_poisson(orc_run* r, int64_t t) {
-    /* PGB_POISSON_FP32_DC approximates the exact discrete solution: its
-     * FP64 oracle is that solution (defect correction to convergence)   */
-    if (r->prm.poisson_mode == PGB_POISSON_FP32_DC) {
+    /* PGB_POISSON_FP32_DC and PGB_POISSON_DST_DC approximate the exact
+     * discrete solution: their FP64 oracle is that solution (defect
+     * correction to convergence)                                        */
+    if (r->prm.poisson_mode == PGB_POISSON_FP32_DC || r->prm.poisson_mode == PGB_POISSON_DST_DC) {
         orc_poisson_converged(r, t, ORC_CONVERGED_PASSES);
         return;
     }

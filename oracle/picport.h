@@ -62,7 +62,7 @@ int  orc_get_neutral_table(orc_run* r, int which, double* out, int64_t n);
 void orc_poisson_residual(orc_run* r, double* max_res, double* max_rhs);
 /* solve the same discrete Poisson problem to convergence (FP64 defect
  * correction around the full multigrid pass) -- the "exact" reference for
- * PGB_POISSON_FP32_DC                                                        */
+ * PGB_POISSON_FP32_DC and PGB_POISSON_DST_DC                                  */
 void orc_poisson_converged(orc_run* r, int64_t t, int iters);
 /* the graphs class (graphs.cpp): sums over the window's steps, read as
  * the reference's averages; `which` and the layouts are PGB_GRAPH_*       */

@@ -365,6 +365,60 @@ def test_defect_correction_converges_to_exact_solution(n):
     assert e <= 1e-9
 
 
+@pytest.mark.parametrize("n", [65, 257, 513])
+def test_sine_transform_solve_reaches_exact_solution(n):
+    """DST_DC: the FP32 sine-transform solve is the discrete solution up to
+    FP32 rounding (one pass: within 1e-5 of the FP64 converged solution on
+    white noise, the hardest right-hand side for FP32 rounding: the FFT's
+    rounding spreads over every mode, and the smooth modes are amplified by
+    1/|lambda|).  Each FP64 defect correction divides the error by more than
+    1e3 (2500x measured at 257^2): two passes 1e-8, three 1e-11."""
+    rng = np.random.default_rng(n + 3)
+    rho = 1e-6 * rng.standard_normal((n, n))
+    p0 = picgb.make_params(X_NO_OF_CELLS=n, POISSON="DST_DC", DC_MAX_ITERS=1)
+    o = orc.Oracle(p0)
+    o.set_rho(rho)
+    o.poisson_converged(0, 30)
+    want = o.get_grid("phi")
+    errs = {}
+    bounds = ((1, 1e-5), (2, 1e-8), (3, 1e-11))
+    for passes, _ in bounds:
+        p = picgb.make_params(X_NO_OF_CELLS=n, POISSON="DST_DC", DC_MAX_ITERS=passes)
+        with picgb.Run(p) as r:
+            r.set_rho(rho)
+            r.poisson(0)
+            errs[passes] = rel_err(r.get_grid("phi"), want)
+    print(n, "dst errors by passes", errs)
+    for passes, tol in bounds:
+        assert errs[passes] <= tol, (passes, errs)
+
+
+def test_sine_transform_solve_of_one_mode():
+    """rho = one sine mode of the grid: the discrete solution is the mode
+    divided by its eigenvalue -(s_k + s_l)/h^2, s_k = 4 sin^2(pi k/2N).  One
+    FP32 pass returns a smooth mode within 1e-6; for a high-frequency mode
+    the FFT's rounding of its large coefficient reaches the smooth modes and
+    is amplified there by the ratio of the eigenvalues (about 700 for
+    (127, 3) at 129^2; FP32 FFTs in general: 4e-6), so 5e-5.  With one FP64
+    defect correction every mode is within 1e-10 (walls at 0 V)."""
+    n, N = 129, 128
+    j = np.arange(n)
+    for k, l, tol1 in ((1, 1, 1e-6), (5, 17, 1e-6), (127, 3, 5e-5)):
+        mode = np.outer(np.sin(np.pi * j * l / N), np.sin(np.pi * j * k / N))   # [i][j]
+        for passes, tol in ((1, tol1), (2, 1e-10)):
+            p = picgb.make_params(X_NO_OF_CELLS=n, POISSON="DST_DC", DC_MAX_ITERS=passes, PHI_LEFT=0.0,
+                                  PHI_RIGHT=0.0, PHI_TOP=0.0, PHI_BOTTOM=0.0, PHI_PERIOD=0.0)
+            h = p.xlength / N
+            lam = -(4 * np.sin(np.pi * k / (2 * N)) ** 2 + 4 * np.sin(np.pi * l / (2 * N)) ** 2) / h**2
+            with picgb.Run(p) as r:
+                r.set_rho(-picgb.EPSILON * mode)   # -eps0 * L phi = rho with L phi = mode
+                r.poisson(0)
+                got = r.get_grid("phi")
+            e = rel_err(got, mode / lam)
+            print((k, l), passes, e)
+            assert e <= tol, ((k, l), passes, e)
+
+
 # ------------------------------------------------------------- spatial sort
 @pytest.mark.parametrize("case", ["see33", "arcoll33", "steady33"])
 def test_binned_runs_match_oracle(case):

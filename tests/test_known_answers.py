@@ -151,8 +151,8 @@ def _laplacian_rho(phi, h):
 
 def test_poisson_recovers_a_manufactured_discrete_solution():
     """phi = 10 x(1-x) y(1-y) exp(x+2y) on the unit-scaled domain, walls at
-    0 V, and rho its discrete Laplacian.  The defect-corrected solve
-    returns phi to 1e-9.  The reference's single FMG pass (FP64 and FP32)
+    0 V, and rho its discrete Laplacian.  The defect-corrected solves
+    (multigrid and sine transform) return phi to 1e-9.  The reference's single FMG pass (FP64 and FP32)
     leaves its truncation error, 5e-5 at 65^2, and it shrinks by more than
     2.5x from 65^2 to 129^2.  (sin x sin is no test of the multigrid: it is
     an eigenfunction of the discrete Laplacian, which one pass solves
@@ -162,7 +162,7 @@ def test_poisson_recovers_a_manufactured_discrete_solution():
         s = np.linspace(0.0, 1.0, n)
         X, Y = np.meshgrid(s, s)
         phi = 10.0 * X * (1 - X) * Y * (1 - Y) * np.exp(X + 2 * Y)
-        for mode, tol in (("FP32_DC", 1e-9), ("FMG_REF", 1e-4), ("FMG32", 1e-4)):
+        for mode, tol in (("FP32_DC", 1e-9), ("DST_DC", 1e-9), ("FMG_REF", 1e-4), ("FMG32", 1e-4)):
             p = picgb.make_params(X_NO_OF_CELLS=n, POISSON=mode, DC_MAX_ITERS=12)
             h = p.xlength / (n - 1)
             with picgb.Run(p) as r:

@@ -34,6 +34,7 @@ UNITS = {
     "pgb_graphs.cu": [],
     "pgb_render.cu": ["--fmad=false"],
     "pgb_static.cu": [],
+    "pgb_dst.cu": [],
 }
 
 

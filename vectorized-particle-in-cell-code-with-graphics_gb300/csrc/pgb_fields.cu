@@ -689,6 +689,41 @@ __global__ void k_dc_final(double* __restrict__ phi, const double* __restrict__ 
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x)
         phi[k] = u[k] + (double)e[k];
 }
+/* DST_DC: the FP32 right-hand side of the charge alone, -rho/EPSILON on
+ * the interior (the walls' terms are in the wall solutions)             */
+__global__ void k_rho32(float* __restrict__ f32, const double* __restrict__ rho, int n, double coef) {
+    pgb_pdl_entry();
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n * n; k += gridDim.x * blockDim.x) {
+        int i = k / n, j = k - i * n;
+        f32[k] = (i > 0 && j > 0 && i < n - 1 && j < n - 1) ? (float)(-coef * rho[k]) : 0.0f;
+    }
+}
+/* DST_DC's first update: u = wc + phi_right(t) * wr + e (the walls' FP64
+ * solutions and the FP32 solve of the charge term), and the FP64 defect
+ * d = f - L u of the full right-hand side, as k_dc_update            */
+__global__ void k_dc_first(const double* __restrict__ wc, const double* __restrict__ wr, const double* phi_tab,
+                           const DevState* ds, const float* __restrict__ e, double* __restrict__ uout,
+                           const double* __restrict__ f, float* __restrict__ d, int n, double h2i) {
+    pgb_pdl_entry();
+    const double phirx = phi_tab[ds->tf - ds->t_base];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n * n; k += gridDim.x * blockDim.x) {
+        int i = k / n, j = k - i * n;
+        auto U = [&](int q) { return (wc[q] + phirx * wr[q]) + (double)e[q]; };
+        double c = U(k), v = 0.0;
+        if (i > 0 && j > 0 && i < n - 1 && j < n - 1)
+            v = f[k] - h2i * (U(k + n) + U(k - n) + U(k + 1) + U(k - 1) - 4.0 * c);
+        uout[k] = c;
+        d[k] = (float)v;
+    }
+}
+/* the walls' terms of the right-hand side alone (rhs_node at rho = 0) */
+__global__ void k_wall_rhs(FinalizeArgs a, double phirx) {
+    pgb_pdl_entry();
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nx * a.ny; k += gridDim.x * blockDim.x) {
+        int j = k / a.nx, i = k - j * a.nx;
+        a.f[k] = rhs_node(0.0, i, j, a, phirx);
+    }
+}
 __global__ void k_to32(float* d, const double* s, int count) {
     pgb_pdl_entry();
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) d[k] = (float)s[k];
@@ -696,6 +731,76 @@ __global__ void k_to32(float* d, const double* s, int count) {
 __global__ void k_to64(double* d, const float* s, int count) {
     pgb_pdl_entry();
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) d[k] = (double)s[k];
+}
+
+/* FP64 defect correction around the FP32 sine-transform solve of L u = f64
+ * (zero walls), `passes` solves in all; the result goes to out (FP64).
+ * lift: the first approximation is the walls' solution wc + phi_right(t) wr
+ * plus the FP32 solve of the charge term alone, which keeps the walls'
+ * terms (-phi/(DX DY) next to a wall, a thousand times the charge term at
+ * 1 V) out of the FP32 transform, whose rounding they would otherwise
+ * spread over every mode; each pass then divides the error by about 1e6
+ * instead of about 300.  Otherwise the first solve is of f64 itself.  */
+static int dst_dc(pgb_run* r, const double* f64, double* out, int passes, bool lift) {
+    const int top = r->ng - 1, n = r->nx, G = n * n, gb = blocks_for(G);
+    const double h = r->p.xlength / (n - 1), h2i = 1.0 / (h * h);
+    float* const f32 = r->mg32_f[top];   /* right-hand side, then each defect */
+    float* const e32 = r->mg32_u[top];   /* each FP32 solve                   */
+    if (lift) PGB_CK(r, pgb_launch_pdl(k_rho32, dim3(gb), dim3(256), 0, r->stream, f32, (const double*)r->rho, n,
+                                       1.0 / 8.854e-12));
+    else PGB_CK(r, pgb_launch_pdl(k_to32, dim3(gb), dim3(256), 0, r->stream, f32, f64, G));
+    r->launches++;
+    if (pgb_dst_solve(r, f32, e32)) return PGB_ERR_CUDA;
+    if (passes <= 1 && !lift) {
+        PGB_CK(r, pgb_launch_pdl(k_to64, dim3(gb), dim3(256), 0, r->stream, out, (const float*)e32, G));
+        r->launches++;
+        return 0;
+    }
+    double* ua = nullptr;   /* FP64 solution so far */
+    double* ub = passes <= 1 ? out : r->dc_u;
+    if (lift) {
+        PGB_CK(r, pgb_launch_pdl(k_dc_first, dim3(gb), dim3(256), 0, r->stream, (const double*)r->dst_wc,
+                                 (const double*)r->dst_wr, (const double*)r->phi_tab, (const DevState*)r->ds,
+                                 (const float*)e32, ub, f64, f32, n, h2i));
+        r->launches++;
+        if (passes <= 1) return 0;
+        ua = ub;
+        ub = r->dc_u2;
+        if (pgb_dst_solve(r, f32, e32)) return PGB_ERR_CUDA;
+    }
+    for (int it = lift ? 2 : 1; it < passes; ++it) {
+        PGB_CK(r, pgb_launch_pdl(k_dc_update, dim3(gb), dim3(256), 0, r->stream, (const double*)ua, (const float*)e32,
+                                 ub, f64, f32, n, h2i));
+        r->launches++;
+        ua = ub;
+        ub = (ub == r->dc_u) ? r->dc_u2 : r->dc_u;
+        if (pgb_dst_solve(r, f32, e32)) return PGB_ERR_CUDA;
+    }
+    PGB_CK(r, pgb_launch_pdl(k_dc_final, dim3(gb), dim3(256), 0, r->stream, out, (const double*)ua, (const float*)e32, G));
+    r->launches++;
+    return 0;
+}
+
+/* DST_DC's wall solutions: L u = (the walls' right-hand side terms), the
+ * left, bottom and top walls at their potentials, then the right wall at
+ * 1 V, each to FP64 rounding (eight passes; about 300x each without lift) */
+static int dst_wall_solutions(pgb_run* r) {
+    const size_t G = (size_t)r->nx * r->ny;
+    PGB_CK(r, cudaMalloc(&r->dst_wc, G * sizeof(double)));
+    PGB_CK(r, cudaMalloc(&r->dst_wr, G * sizeof(double)));
+    PGB_CK(r, cudaDeviceSynchronize());   /* the setup's memsets ran on the legacy stream */
+    double* const f64 = r->mg_w[r->ng - 1];   /* FP64 scratch of the top level */
+    for (int w = 0; w < 2; ++w) {
+        FinalizeArgs a = fin_args(r, 0, true);
+        a.f = f64;
+        if (w == 1) a.phi0x = a.phi0y = a.phily = 0.0;
+        PGB_CK(r, pgb_launch_pdl(k_wall_rhs, dim3(blocks_for((long long)G)), dim3(256), 0, r->stream, a,
+                                 w == 1 ? 1.0 : 0.0));
+        if (dst_dc(r, f64, w == 0 ? r->dst_wc : r->dst_wr, 8, false)) return PGB_ERR_CUDA;
+    }
+    PGB_CK(r, cudaMemsetAsync(f64, 0, G * sizeof(double), r->stream));   /* the level's walls stay 0 */
+    PGB_CK(r, cudaStreamSynchronize(r->stream));
+    return 0;
 }
 
 int pgb_mg_setup(pgb_run* r) {
@@ -738,6 +843,10 @@ int pgb_mg_setup(pgb_run* r) {
                                    (int)small_smem_bytes(small_top(r, sizeof(double)), sizeof(double))));
     PGB_CK(r, cudaFuncSetAttribute(k_mg_small<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)small_smem_bytes(small_top(r, sizeof(float)), sizeof(float))));
+    if (r->p.poisson_mode == PGB_POISSON_DST_DC) {
+        if (pgb_dst_setup(r)) return PGB_ERR_CUDA;
+        if (pgb_dst_ok(r) && dst_wall_solutions(r)) return PGB_ERR_CUDA;
+    }
     return 0;
 }
 
@@ -749,6 +858,9 @@ void pgb_mg_free(pgb_run* r) {
     cudaFree(r->mg32_tab);
     cudaFree(r->dc_u);
     cudaFree(r->dc_u2);
+    cudaFree(r->dst_wc);
+    cudaFree(r->dst_wr);
+    pgb_dst_free(r);
 }
 
 /* fields::grid_potential after the right-hand side is in mg_f[ng-1]:
@@ -759,7 +871,12 @@ void pgb_mg_free(pgb_run* r) {
  *            (FP64 defect of the FP64 solution, one FP32 V-cycle on it
  *            from zero, FP64 addition of that correction).  The FP32 pass
  *            leaves an error of a few 1e-5 of phi; each V-cycle divides it
- *            by about ten, down to the FP64 discrete solution.          */
+ *            by about ten, down to the FP64 discrete solution.
+ *   DST_DC   the same FP64 defect correction around the FP32 sine-transform
+ *            solve (pgb_dst.cu), which solves the discrete system exactly
+ *            up to FP32 rounding (about 1e-6 of phi): a first solve, then
+ *            dc_max_iters - 1 corrections, each dividing the error by
+ *            about 1e6.                                                  */
 int pgb_poisson_solve(pgb_run* r) {
     const int top = r->ng - 1, n = r->nx;
     const int G = n * n;
@@ -767,6 +884,9 @@ int pgb_poisson_solve(pgb_run* r) {
     if (r->p.poisson_mode == PGB_POISSON_FMG_REF) {
         if (fmg<double>(r, levels64(r))) return PGB_ERR_CUDA;
         PGB_CK(r, cudaMemcpyAsync(r->phi, r->mg_u[top], sizeof(double) * G, cudaMemcpyDeviceToDevice, r->stream));
+    } else if (r->p.poisson_mode == PGB_POISSON_DST_DC) {
+        if (!pgb_dst_ok(r)) return PGB_ERR_CUDA;
+        if (dst_dc(r, r->mg_f[top], r->phi, r->p.dc_max_iters > 1 ? r->p.dc_max_iters : 1, true)) return PGB_ERR_CUDA;
     } else {
         Levels<float> L = levels32(r);
         PGB_CK(r, pgb_launch_pdl(k_to32, dim3(gb), dim3(256), 0, r->stream, L.f[top], r->mg_f[top], G));

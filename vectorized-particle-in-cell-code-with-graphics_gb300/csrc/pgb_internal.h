@@ -134,6 +134,14 @@ struct pgb_run {
     double** mg_tab = nullptr;                       /* device table of the level pointers */
     float** mg32_tab = nullptr;
     double *dc_u = nullptr, *dc_u2 = nullptr;       /* FP32_DC: FP64 solution, two buffers */
+    /* DST_DC: sine-transform scratch ((N-1) rows of N floats), twiddles, s_k */
+    float* dst_t = nullptr;
+    float2* dst_tw = nullptr;
+    float* dst_s = nullptr;
+    /* DST_DC: FP64 solutions for the walls (zero charge): the left, bottom
+     * and top walls at their potentials, and the right wall at 1 V       */
+    double* dst_wc = nullptr;
+    double* dst_wr = nullptr;
     float *mg32_u[PGB_MAX_LEVELS], *mg32_f[PGB_MAX_LEVELS], *mg32_v[PGB_MAX_LEVELS], *mg32_r[PGB_MAX_LEVELS];
     /* the pre-smoothing result of each level (the tiled smoother reads one
      * buffer and writes another: blocks never see a neighbour's update)  */
@@ -285,6 +293,11 @@ int pgb_launch_dump_offsets(pgb_run* r, int s);
 int pgb_launch_dump(pgb_run* r, int s, double* d_out, unsigned int* d_ids, long long cap, int t0, int t1);
 int pgb_mg_setup(pgb_run* r);
 void pgb_mg_free(pgb_run* r);
+/* FP32 sine-transform Poisson solver (pgb_dst.cu) */
+int pgb_dst_setup(pgb_run* r);
+void pgb_dst_free(pgb_run* r);
+bool pgb_dst_ok(const pgb_run* r);
+int pgb_dst_solve(pgb_run* r, const float* f, float* u);
 CollConsts pgb_coll_consts(pgb_run* r);
 int pgb_launch_compact(pgb_run* r, int s);
 int pgb_launch_sort(pgb_run* r, int s);

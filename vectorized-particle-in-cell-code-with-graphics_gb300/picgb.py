@@ -33,8 +33,8 @@ PGB_ELECTRONS, PGB_IONS = 0, 1
 PGB_ARGON, PGB_HYDROGEN = 0, 1
 PGB_SIGMA_CONSTANT, PGB_SIGMA_ENERGY_DEPENDENT = 0, 1
 GRID = {"q_e": 0, "q_i": 1, "rho": 2, "phi": 3, "ex": 4, "ey": 5}
-PGB_POISSON_FMG_REF, PGB_POISSON_FP32_DC, PGB_POISSON_FMG32 = 0, 1, 2
-POISSON_MODES = {"FMG_REF": 0, "FP32_DC": 1, "FMG32": 2}
+PGB_POISSON_FMG_REF, PGB_POISSON_FP32_DC, PGB_POISSON_FMG32, PGB_POISSON_DST_DC = 0, 1, 2, 3
+POISSON_MODES = {"FMG_REF": 0, "FP32_DC": 1, "FMG32": 2, "DST_DC": 3}
 PGB_BOUNDARY_IONS, PGB_BOUNDARY_ELECTRONS = 0, 1
 
 
