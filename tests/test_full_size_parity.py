@@ -2,13 +2,14 @@
 
 The CUDA library (through its C ABI) and the oracle (oracle/picport.c in its
 library mode: the same Philox draws, the same stable particle order, OpenMP
-over the host cores; its Poisson solve for FP32_DC is the converged FP64
-solution) step the same seeded state for three steps, across a spatial sort
+over the host cores; its Poisson solve for DST_DC and FP32_DC is the
+converged FP64 solution) step the same seeded state for three steps, across a spatial sort
 step (the sort runs every 2 steps here), and tests/fullsize.py compares them.
 
 Workloads (tests/fullsize.py):
   hydrogen_513  the benchmark's state: 513^2 nodes, 16Mi particles per species,
-                H plasma with the collisional boundary
+                H plasma with the collisional boundary, in both converged
+                Poisson modes (DST_DC, the benchmark's, and FP32_DC)
   argon_257     257^2 nodes, 4Mi particles per species, Ar, absorbing walls
 
 Why ties are counted rather than forbidden: the device keeps particles in
@@ -85,11 +86,12 @@ def check(d, name):
         assert abs(dv) <= 2 + 1e-5 * oc[k], f"{name} {k}: device - oracle = {dv} (oracle {oc[k]})"
 
 
-def test_hydrogen_513_bench_state_matches_oracle():
+@pytest.mark.parametrize("poisson", ["DST_DC", "FP32_DC"])
+def test_hydrogen_513_bench_state_matches_oracle(poisson):
     n = bench.N_PER_SPECIES
-    p = bench.workload_params(picgb, n_per_species=n, sort_interval=2)
+    p = bench.workload_params(picgb, n_per_species=n, sort_interval=2, poisson=poisson)
     e, i = bench.gaussian_state(p, n, 3.0, 0.026, 1003, p.ion_mass)
-    check(fullsize.compare(p, e, i, STEPS), "hydrogen_513")
+    check(fullsize.compare(p, e, i, STEPS), f"hydrogen_513 {poisson}")
 
 
 def test_argon_257_matches_oracle():
