@@ -154,6 +154,9 @@ static void free_lists(pgb_run* r) {
         r->tile_list[l] = r->tile_cnt[l] = r->list[l] = nullptr;
     }
     cudaFree(r->aux_i); cudaFree(r->aux_j); cudaFree(r->cx_tile_sum);
+    cudaFree(r->cx_mask); cudaFree(r->cx_total);
+    r->cx_mask = nullptr;
+    r->cx_total = nullptr;
     for (int q = 0; q < 2; ++q) {
         cudaFree(r->tile_bin[q]); cudaFree(r->pieces[q]);
         r->tile_bin[q] = nullptr; r->pieces[q] = nullptr;
@@ -256,10 +259,15 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
         }
         long long cxt = (lc + 4096 - 1) / 4096 + 1;
         r->cx_tiles_cap = cxt;
-        if (cudaMalloc(&r->cx_tile_sum, sizeof(long long) * cxt * r->nx) != cudaSuccess) {
+        r->cx_mask_words = (int)((cxt + 63) / 64);
+        if (cudaMalloc(&r->cx_tile_sum, sizeof(long long) * cxt * r->nx) != cudaSuccess ||
+            cudaMalloc(&r->cx_mask, sizeof(unsigned long long) * r->cx_mask_words * r->nx) != cudaSuccess ||
+            cudaMalloc(&r->cx_total, sizeof(long long) * r->nx) != cudaSuccess) {
             cudaGetLastError();
             return fail(r, PGB_ERR_NOMEM, "device allocation of CX scratch failed");
         }
+        PGB_CK(r, cudaMemsetAsync(r->cx_mask, 0, sizeof(unsigned long long) * r->cx_mask_words * r->nx, r->stream));
+        PGB_CK(r, cudaMemsetAsync(r->cx_total, 0, sizeof(long long) * r->nx, r->stream));
         r->list_cap = lc;
         r->ntiles_cap = nt;
         /* the bin-piece tables of both species went with the old block

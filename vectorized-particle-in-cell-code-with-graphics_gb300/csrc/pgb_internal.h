@@ -190,6 +190,11 @@ struct pgb_run {
     float* cx_p = nullptr;                 /* per-ion CX probability          */
     float* cx_tile_sum = nullptr;          /* [column][tile] (int64)          */
     long long cx_tiles_cap = 0;
+    /* [column][tile / 64] bits of the tiles with a non-zero sum, and the
+     * per-column totals; zero between passes (the walk clears them)     */
+    unsigned long long* cx_mask = nullptr;
+    long long* cx_total = nullptr;
+    int cx_mask_words = 0;
     /* spatial sort */
     int* tile_bin[2] = {nullptr, nullptr};
     int4* pieces[2] = {nullptr, nullptr};

@@ -450,8 +450,11 @@ struct CxArgs {
     int ps;                  /* fraction bits of the positions */
     float pcoef, ecoef;      /* DTI*1e-20*n_g, (0.5/CHARGE)*MI */
     CollConsts cc;
-    long long* tile_sum;     /* [column][tile] fixed point */
+    long long* tile_sum;     /* [column][tile] fixed point, written where non-zero */
     long long ntl;           /* tiles capacity (row length of tile_sum) */
+    unsigned long long* mask;   /* [column][mw]: bit t of the tiles with a non-zero sum */
+    long long* total;        /* per-column sum of the pass                */
+    int mw;
     long long* col_acc;      /* per-column accumulator carried across steps (fixed point) */
     const float* neut_i;     /* ion-neutral table (FP32) */
     uint64_t seed;
@@ -518,7 +521,17 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
             }
         }
         __syncthreads();
-        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) a.tile_sum[(long long)c * a.ntl + t] = (long long)s_sum[c];
+        /* only non-zero sums are stored (marked in the column's bit mask and
+         * added to its total): where no ion can exchange (the H fit is 0 at
+         * any ion energy above 1e-14 eV) a pass writes nothing            */
+        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) {
+            const unsigned long long v = s_sum[c];
+            if (v) {
+                a.tile_sum[(long long)c * a.ntl + t] = (long long)v;
+                atomicOr(&a.mask[(long long)c * a.mw + (t >> 6)], 1ull << (t & 63));
+                atomicAdd((unsigned long long*)&a.total[c], v);
+            }
+        }
         __syncthreads();
     }
 }
@@ -536,17 +549,21 @@ __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
     long long acc = a.col_acc[col];
     int fired = 0;
     const long long* row = a.tile_sum + (long long)col * a.ntl;
+    unsigned long long* const mrow = a.mask + (long long)col * a.mw;
     /* most columns do not reach 1 in a step: test the column total first */
-    long long tot = 0;
-    for (int t = lane; t < ntiles; t += 32) tot += row[t];
-    for (int d = 16; d; d >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, d);
+    const long long tot = a.total[col];
     if (acc + tot <= CX_ONE) {
-        if (lane == 0) a.col_acc[col] = acc + tot;
+        if (lane == 0) {
+            a.col_acc[col] = acc + tot;
+            a.total[col] = 0;
+        }
+        if (tot)
+            for (int w = lane; w < (ntiles + 63) / 64; w += 32) mrow[w] = 0ull;
         return;
     }
     for (int t0 = 0; t0 < ntiles; t0 += 32) {
         int t = t0 + lane;
-        long long s = (t < ntiles) ? row[t] : 0;
+        long long s = (t < ntiles && ((mrow[t >> 6] >> (t & 63)) & 1ull)) ? row[t] : 0;
         /* inclusive prefix over the 32 tiles */
         long long ps = s;
         for (int d = 1; d < 32; d <<= 1) {
@@ -597,8 +614,11 @@ __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
         /* resume with the tiles after tt */
         t0 = tt + 1 - 32;
     }
+    __syncwarp();
+    for (int w = lane; w < (ntiles + 63) / 64; w += 32) mrow[w] = 0ull;
     if (lane == 0) {
         a.col_acc[col] = acc;
+        a.total[col] = 0;
         if (fired) atomicAdd((unsigned long long*)&a.ds->stats[ST_CX], (unsigned long long)fired);
     }
 }
@@ -665,6 +685,9 @@ int pgb_launch_cx(pgb_run* r, int tail, int leave_sms) {
     a.pcoef = a.cc.i_pcoef; a.ecoef = a.cc.i_energy_coef;
     a.tile_sum = (long long*)r->cx_tile_sum;
     a.ntl = r->cx_tiles_cap;
+    a.mask = r->cx_mask;
+    a.total = r->cx_total;
+    a.mw = r->cx_mask_words;
     a.col_acc = (long long*)r->prob_cx;
     a.neut_i = r->neut[1];
     a.seed = r->p.seed;
