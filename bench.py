@@ -477,10 +477,21 @@ def run_gpu(args, rank, world):
     n = int(N_PER_SPECIES * args.scale)
     p = workload_params(picgb, seed=1003 + rank, n_per_species=n, poisson=args.poisson, sort_interval=args.sort)
     e, i = gaussian_state(p, n, 3.0, 0.026, 1003 + rank, p.ion_mass)
+    # launch shapes (they change no result): pgb_autotune on a separate run
+    # of the same state, then the measured run uses the fastest candidate
+    tune = None
+    if args.autotune_steps > 0:
+        with picgb.Run(p) as tr:
+            tr.load_particles(0, e)
+            tr.load_particles(1, i)
+            tr.initial_boundary()
+            tune = tr.autotune(args.autotune_steps)
     run = picgb.Run(p)
     run.load_particles(0, e)
     run.load_particles(1, i)
     run.initial_boundary()
+    if tune:
+        run.set_launch_config(tune["push_blocks_per_sm"], tune["field_sms"])
     run.step(args.warmup)
     stream = torch.cuda.ExternalStream(run.stream())
     c0 = run.counters()
@@ -555,6 +566,7 @@ def run_gpu(args, rank, world):
     batched = run_batched(args) if (args.batch_runs > 0 and world == 1) else None
     served = run_served(args) if (args.serve_requests > 0 and world == 1) else None
     return dict(ms=ms, ps=ps, counts=(c0, c1), prof=prof, launches=launches, clocks=clk.summary(), e2e=e2e, n=n,
+                tune=tune,
                 batched=batched, served=served, render=render, accuracy=accuracy, modes=modes, configs=configs)
 
 
@@ -684,6 +696,8 @@ def main():
     ap.add_argument("--serve-max-steps", type=int, default=5000, help="longest request of the served workload")
     ap.add_argument("--serve-round", type=int, default=10, help="steps per server round")
     ap.add_argument("--render-frames", type=int, default=10, help="frames per viewer plot timed (0 = skip)")
+    ap.add_argument("--autotune-steps", type=int, default=16,
+                    help="timed steps per launch-shape candidate before the run (0 = default shapes)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -768,6 +782,7 @@ def main():
             "data": "synthetic (seeded)",
             "config": config, "e2e": res["e2e"], "roofline": roofline, "cpu_baseline": cpu,
             "gpu_launches": res["launches"], "clocks": res["clocks"],
+            "autotune": res.get("tune") or {"off": "default launch shapes (push 8 blocks/SM, 32 SMs for the field solve)"},
             "accuracy": res.get("accuracy"), "poisson_modes": res.get("modes"), "configs": res.get("configs"),
             "particles": {"start": [c0["n_e"], c0["n_i"]], "end": [c1["n_e"], c1["n_i"]]},
             "batched": res.get("batched"), "served": res.get("served"), "render": res.get("render")}

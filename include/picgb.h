@@ -246,6 +246,24 @@ PGB_API int pgb_get_counters(pgb_run* run, pgb_counters* out);
 /* The cudaStream_t every kernel of this run is launched on (so a caller
  * can record CUDA events around pgb_step).                               */
 PGB_API int pgb_get_stream(pgb_run* run, void** stream);
+/* Launch shapes (no reference counterpart).  They change no result, only
+ * speed: the push kernels' grid is the SM count times push_blocks_per_sm
+ * (four 256-thread blocks fit on an SM, default 8), and the collision
+ * kernels that run beside the previous step's field solve leave it
+ * field_sms SMs (default 32).                                             */
+typedef struct pgb_launch_config {
+    int32_t push_blocks_per_sm;
+    int32_t field_sms;
+} pgb_launch_config;
+PGB_API int pgb_get_launch_config(pgb_run* run, pgb_launch_config* out);
+/* From the next step on (waits for queued work; captured graphs are rebuilt). */
+PGB_API int pgb_set_launch_config(pgb_run* run, const pgb_launch_config* c);
+/* Time each candidate (push_blocks_per_sm 4, 8, 12 x field_sms 8, 16, 32,
+ * 48, in that order) on this run: 2 untimed steps, then `steps` steps timed
+ * with CUDA events on the run's stream; the fastest is kept, returned in
+ * *best, its milliseconds per step in *ms_best; ms_all (12 values, may be
+ * NULL) gets every candidate's.  The run advances 12 * (steps + 2) steps. */
+PGB_API int pgb_autotune(pgb_run* run, int32_t steps, pgb_launch_config* best, double* ms_best, double* ms_all);
 /* on = 1 resets and starts the per-phase profile of pgb_step; 0 stops it. */
 PGB_API int pgb_set_profiling(pgb_run* run, int on);
 PGB_API int pgb_get_profile(pgb_run* run, pgb_profile* out);

@@ -88,3 +88,45 @@ def test_pipelined_steps_equal_steps_in_order(name):
                 assert a == b, (m, name)
             else:
                 assert np.array_equal(a, b, equal_nan=True), (m, name, k)
+
+
+def test_launch_shapes_change_no_result():
+    """pgb_set_launch_config changes how the push grid and the collision
+    kernels beside the field solve are laid out, not what they compute:
+    the same state stepped under three shapes ends bit for bit the same
+    (particles, grids, counters)."""
+    p, e, i, n = _case("h_sorted_129")
+    res = []
+    for push, field in ((8, 32), (4, 8), (12, 48)):
+        with picgb.Run(p) as r:
+            r.load_particles(0, e)
+            r.load_particles(1, i)
+            r.initial_boundary()
+            r.set_launch_config(push, field)
+            assert r.launch_config() == {"push_blocks_per_sm": push, "field_sms": field}
+            r.step(n)
+            res.append([r.get_particles(0), r.get_particles(1)] + [r.get_grid(k) for k in ("q_e", "q_i", "phi")]
+                       + [r.counters()])
+    for got in res[1:]:
+        for k, (a, b) in enumerate(zip(res[0], got)):
+            if isinstance(a, dict):
+                assert a == b
+            else:
+                assert np.array_equal(a, b, equal_nan=True), k
+
+
+def test_autotune_keeps_the_fastest_candidate():
+    """pgb_autotune times the 12 candidates and keeps the fastest; the run's
+    launch configuration is then that candidate, and a bad shape is refused."""
+    p, e, i, _ = _case("h_sorted_129")
+    with picgb.Run(p) as r:
+        r.load_particles(0, e)
+        r.load_particles(1, i)
+        r.initial_boundary()
+        t = r.autotune(2)
+        assert len(t["candidates"]) == 12 and all(c["ms_per_step"] > 0 for c in t["candidates"])
+        fastest = min(t["candidates"], key=lambda c: c["ms_per_step"])
+        assert (t["push_blocks_per_sm"], t["field_sms"]) == (fastest["push_blocks_per_sm"], fastest["field_sms"])
+        assert r.launch_config() == {"push_blocks_per_sm": t["push_blocks_per_sm"], "field_sms": t["field_sms"]}
+        with pytest.raises(picgb.PicError):
+            r.set_launch_config(0, 8)

@@ -808,9 +808,8 @@ static int mcc_part(pgb_run* r, int leave_sms, bool ion_step) {
     return 0;
 }
 static int step_mcc(pgb_run* r, bool ion_step) { return mcc_part(r, 0, ion_step); }
-/* beside a field solve: the one-CTA multigrid needs SMs of its own */
-#define PGB_FIELD_SMS 32
-static int step_mcc_beside(pgb_run* r, bool ion_step) { return mcc_part(r, PGB_FIELD_SMS, ion_step); }
+/* beside a field solve, which needs SMs of its own (r->tune_field_sms) */
+static int step_mcc_beside(pgb_run* r, bool ion_step) { return mcc_part(r, r->tune_field_sms, ion_step); }
 
 static int step_particles(pgb_run* r, bool ion_step) {
     const bool coll = r->p.have_collisions != 0;
@@ -1294,6 +1293,66 @@ extern "C" int pgb_get_counters(pgb_run* r, pgb_counters* c) {
 extern "C" int pgb_get_stream(pgb_run* r, void** stream) {
     if (!r || !stream) return fail(r, PGB_ERR_ARG, "pgb_get_stream: bad argument");
     *stream = (void*)r->stream;
+    return 0;
+}
+
+/* ------------------------------------------------------ launch shapes */
+extern "C" int pgb_get_launch_config(pgb_run* r, pgb_launch_config* out) {
+    if (!r || !out) return fail(r, PGB_ERR_ARG, "pgb_get_launch_config: bad argument");
+    out->push_blocks_per_sm = r->tune_push_per_sm;
+    out->field_sms = r->tune_field_sms;
+    return 0;
+}
+
+extern "C" int pgb_set_launch_config(pgb_run* r, const pgb_launch_config* c) {
+    if (!r || !c) return fail(r, PGB_ERR_ARG, "pgb_set_launch_config: bad argument");
+    if (c->push_blocks_per_sm < 1 || c->push_blocks_per_sm > 64 || c->field_sms < 0 || c->field_sms >= r->sms)
+        return fail(r, PGB_ERR_ARG, "pgb_set_launch_config: push_blocks_per_sm in [1, 64], field_sms in [0, SMs)");
+    int rc = flush_fields(r);   /* a pending field solve was captured with the old shapes */
+    if (rc) return rc;
+    PGB_CK(r, cudaStreamSynchronize(r->stream));
+    r->tune_push_per_sm = c->push_blocks_per_sm;
+    r->tune_field_sms = c->field_sms;
+    drop_graphs(r);
+    return 0;
+}
+
+extern "C" int pgb_autotune(pgb_run* r, int32_t steps, pgb_launch_config* best, double* ms_best, double* ms_all) {
+    if (!r || steps < 1 || !best) return fail(r, PGB_ERR_ARG, "pgb_autotune: bad argument");
+    static const int pushes[3] = {4, 8, 12}, fields[4] = {8, 16, 32, 48};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    PGB_CK(r, cudaEventCreate(&e0));
+    PGB_CK(r, cudaEventCreate(&e1));
+    pgb_launch_config keep;
+    pgb_get_launch_config(r, &keep);
+    double bm = 1e300;
+    int rc = 0, k = 0;
+    for (int a = 0; a < 3 && !rc; ++a)
+        for (int b = 0; b < 4 && !rc; ++b, ++k) {
+            pgb_launch_config c;
+            c.push_blocks_per_sm = pushes[a];
+            c.field_sms = std::min(fields[b], r->sms - 1);
+            if ((rc = pgb_set_launch_config(r, &c)) || (rc = pgb_step(r, 2))) break;   /* graphs captured */
+            if (cudaEventRecord(e0, r->stream) != cudaSuccess) { rc = fail(r, PGB_ERR_CUDA, "pgb_autotune: event"); break; }
+            if ((rc = pgb_step_async(r, steps))) break;
+            float ms = 0.0f;
+            if (cudaEventRecord(e1, r->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+                rc = fail(r, PGB_ERR_CUDA, "pgb_autotune: event");
+                break;
+            }
+            const double per = (double)ms / steps;
+            if (ms_all) ms_all[k] = per;
+            if (per < bm) { bm = per; keep = c; }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!rc) rc = sync_state(r);
+    int rc2 = pgb_set_launch_config(r, &keep);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    *best = keep;
+    if (ms_best) *ms_best = bm;
     return 0;
 }
 

@@ -183,6 +183,11 @@ struct pgb_run {
     cudaGraph_t tmpl_a[8] = {}, tmpl_b[8] = {}, tmpl_f = nullptr;
     cudaGraphExec_t graph_m[8] = {};
     int prio_hi = 0;                       /* the side stream's priority      */
+    /* launch shapes (pgb_set_launch_config, pgb_autotune): they change no
+     * result.  push grid = SMs x tune_push_per_sm; the collision kernels
+     * beside a field solve leave it tune_field_sms SMs                   */
+    int tune_push_per_sm = 8;
+    int tune_field_sms = 32;
     bool fields_pending = false;           /* last step's field solve not yet issued */
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork, ev_join;

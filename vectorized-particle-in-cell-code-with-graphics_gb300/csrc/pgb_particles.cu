@@ -1041,7 +1041,7 @@ static PushArgs push_args(pgb_run* r, int s) {
 
 int pgb_launch_push(pgb_run* r, int s, bool deposit) {
     PushArgs a = push_args(r, s);
-    int g = grid_for(r, 8);
+    int g = grid_for(r, r->tune_push_per_sm);
     void (*kp)(PushArgs) = deposit ? k_push<true> : k_push<false>;
     PGB_CK(r, pgb_launch_pdl(kp, dim3(g), dim3(PGB_PUSH_THREADS), 0, r->stream, a));
     r->launches++;

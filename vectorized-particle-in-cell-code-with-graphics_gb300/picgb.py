@@ -154,6 +154,10 @@ def graph_size(which: str, p, gp: PgbGraphsParams) -> int:
     return {5: p.x_no_of_cells, 6: p.y_no_of_cells, 11: 5}.get(w, gp.no_bins)
 
 
+class PgbLaunchConfig(C.Structure):
+    _fields_ = [("push_blocks_per_sm", C.c_int32), ("field_sms", C.c_int32)]
+
+
 class PgbProfile(C.Structure):
     """ctypes image of `pgb_profile` (include/picgb.h)."""
 
@@ -349,6 +353,9 @@ def load_library():
         "pgb_get_stream": (C.c_int, [R, C.POINTER(C.c_void_p)]),
         "pgb_set_profiling": (C.c_int, [R, C.c_int]),
         "pgb_get_profile": (C.c_int, [R, C.POINTER(PgbProfile)]),
+        "pgb_get_launch_config": (C.c_int, [R, C.POINTER(PgbLaunchConfig)]),
+        "pgb_set_launch_config": (C.c_int, [R, C.POINTER(PgbLaunchConfig)]),
+        "pgb_autotune": (C.c_int, [R, i32, C.POINTER(PgbLaunchConfig), dp, dp]),
         "pgb_deposit_static": (C.c_int, [C.c_void_p, i64, i32, i32, C.c_double, C.c_double, C.c_double,
                                          C.c_void_p, C.c_void_p]),
     }
@@ -520,6 +527,27 @@ class Run:
         v = C.c_void_p()
         self._check(self.lib.pgb_get_stream(self.h, C.byref(v)), "pgb_get_stream")
         return int(v.value or 0)
+
+    def launch_config(self) -> dict:
+        c = PgbLaunchConfig()
+        self._check(self.lib.pgb_get_launch_config(self.h, C.byref(c)), "pgb_get_launch_config")
+        return {"push_blocks_per_sm": c.push_blocks_per_sm, "field_sms": c.field_sms}
+
+    def set_launch_config(self, push_blocks_per_sm: int, field_sms: int):
+        c = PgbLaunchConfig(push_blocks_per_sm, field_sms)
+        self._check(self.lib.pgb_set_launch_config(self.h, C.byref(c)), "pgb_set_launch_config")
+
+    def autotune(self, steps: int = 8) -> dict:
+        """pgb_autotune: time the 12 launch-shape candidates on this run (it
+        advances 12 * (steps + 2) steps) and keep the fastest."""
+        c = PgbLaunchConfig()
+        best = C.c_double()
+        allms = (C.c_double * 12)()
+        self._check(self.lib.pgb_autotune(self.h, steps, C.byref(c), C.byref(best), allms), "pgb_autotune")
+        cands = [{"push_blocks_per_sm": p, "field_sms": f, "ms_per_step": allms[k]}
+                 for k, (p, f) in enumerate((p, f) for p in (4, 8, 12) for f in (8, 16, 32, 48))]
+        return {"push_blocks_per_sm": c.push_blocks_per_sm, "field_sms": c.field_sms, "ms_per_step": best.value,
+                "candidates": cands}
 
     def set_profiling(self, on: bool):
         self._check(self.lib.pgb_set_profiling(self.h, 1 if on else 0), "pgb_set_profiling")
