@@ -171,49 +171,35 @@ __device__ __forceinline__ void flush_stats(int (&st)[2], long long* stats) {
     }
 }
 
-/* ordered compaction of per-thread flags of one tile into its list.
- * Item k of thread t is slot tile*TILE + k*THREADS + t, so (k, warp, lane)
- * order is slot order.                                                    */
-static_assert(PGB_ITEMS * (PGB_PUSH_THREADS / 32) == 32, "one warp scans a tile's (item, warp) counts");
-template <int NL>
-__device__ __forceinline__ void tile_lists(const bool (&f)[NL][PGB_ITEMS], long long tile_base, int tile,
-                                           int* const (&tl)[NL], int* const (&tc)[NL]) {
-    static_assert(NL <= PGB_PUSH_THREADS / 32, "one warp per list");
-    __shared__ int s_off[NL][PGB_ITEMS][PGB_PUSH_THREADS / 32];
+/* A tile's ordered list as bit masks: item k of thread t is slot
+ * tile*TILE + k*THREADS + t, so word k*warps + w of the tile (the ballot of
+ * warp w's item k) holds its slots in slot order, and the words in order
+ * are the tile's list.  The tile's count goes through a shared counter:
+ * one barrier per tile, and no scan (k_gather_lists expands the words).
+ * s_cnt: two shared counters, zero at the kernel's start, used by turns
+ * (it counts the calls of the block), so that a block's next tile can
+ * count while thread 0 reads and clears this one's after the barrier.   */
+static_assert(PGB_ITEMS * (PGB_PUSH_THREADS / 32) == 32, "a tile's list is 32 mask words");
+__device__ __forceinline__ void tile_masks(const bool (&f)[PGB_ITEMS], int tile, unsigned* masks, int* tc,
+                                           int* s_cnt, int& it) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
-    unsigned m[NL][PGB_ITEMS];
+    int c = 0;
 #pragma unroll
-    for (int l = 0; l < NL; ++l)
-#pragma unroll
-        for (int k = 0; k < PGB_ITEMS; ++k) {
-            m[l][k] = __ballot_sync(0xffffffffu, f[l][k]);
-            if (lane == 0) s_off[l][k][warp] = __popc(m[l][k]);
+    for (int k = 0; k < PGB_ITEMS; ++k) {
+        const unsigned m = __ballot_sync(0xffffffffu, f[k]);
+        if (lane == 0) {
+            masks[(long long)tile * 32 + k * (PGB_PUSH_THREADS / 32) + warp] = m;
+            c += __popc(m);
         }
-    __syncthreads();
-    if (warp < NL) {
-        /* lane = k * warps + w: the 32 counts in slot order, one shuffle scan */
-        int* so = &s_off[warp][0][0];
-        const int c = so[lane];
-        int incl = c;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= d) incl += y;
-        }
-        so[lane] = incl - c;
-        if (lane == 31) tc[warp][tile] = incl;
     }
+    int* const cnt = &s_cnt[it & 1];
+    if (lane == 0 && c) atomicAdd(cnt, c);
     __syncthreads();
-#pragma unroll
-    for (int l = 0; l < NL; ++l)
-#pragma unroll
-        for (int k = 0; k < PGB_ITEMS; ++k)
-            if (f[l][k]) {
-                int pos = s_off[l][k][warp] + __popc(m[l][k] & lt);
-                tl[l][(long long)tile * PGB_TILE + pos] = (int)(tile_base + k * PGB_PUSH_THREADS + threadIdx.x);
-            }
-    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc[tile] = *cnt;
+        *cnt = 0;
+    }
+    ++it;
 }
 
 /* The shared deposit window holds each node's sum as one 32-bit word
@@ -263,9 +249,9 @@ __device__ __forceinline__ void deposit_win(unsigned long long* qacc, unsigned i
 
 template <bool DEP>
 __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& pc, int tile, long long n,
-                                          unsigned int* win, int ox, int oy) {
+                                          unsigned int* win, int ox, int oy, int* s_cnt, int& it) {
     const long long base = (long long)tile * PGB_TILE;
-    bool f[1][PGB_ITEMS];
+    bool f[PGB_ITEMS];
     /* all loads of the thread's items first, so that they are in flight
      * together, then the pushes                                          */
     float4 p[PGB_ITEMS];
@@ -284,7 +270,7 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
     }
 #pragma unroll
     for (int k = 0; k < PGB_ITEMS; ++k) {
-        f[0][k] = false;
+        f[k] = false;
         long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
         if (is_dead(p[k].x)) continue;
         bool moved;
@@ -293,12 +279,10 @@ __device__ __forceinline__ void push_tile(const PushArgs& a, const PushConsts& p
         if (pc.bfield && moved) a.vz[i] = vz[k];
         if (DEP && deposit_ok(p[k].x, p[k].y, pc.nx, pc.ny, pc.ps))
             deposit_win(a.qacc, win, ox, oy, pc.nx, pc.ps, p[k].x, p[k].y, w[k]);
-        f[0][k] = pc.steady ? outside_steady(p[k].x, p[k].y, pc.nx, pc.ny, pc.ps)
-                            : outside_absorbing(p[k].x, p[k].y, pc.nx, pc.ny, pc.ps);
+        f[k] = pc.steady ? outside_steady(p[k].x, p[k].y, pc.nx, pc.ny, pc.ps)
+                         : outside_absorbing(p[k].x, p[k].y, pc.nx, pc.ny, pc.ps);
     }
-    int* const tl[1] = {a.tl_out};
-    int* const tc[1] = {a.tc_out};
-    tile_lists<1>(f, base, tile, tl, tc);
+    tile_masks(f, tile, (unsigned*)a.tl_out, a.tc_out, s_cnt, it);
 }
 
 /* Work items: the bin pieces of the last sort (tiles of one bin, deposited
@@ -313,11 +297,13 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
     const int tile0 = (int)a.ds->sorted_tiles[a.s];
     const int nitems = npieces + (ntiles > tile0 ? ntiles - tile0 : 0);
     const PushConsts pc = a.pc;
+    __shared__ int s_cnt[2];
+    int it = 0;
+    if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0;
     /* the window starts zeroed; each flush leaves it zeroed again */
-    if (DEP && npieces > 0) {
+    if (DEP && npieces > 0)
         for (int k = threadIdx.x; k < WIN_NODES; k += blockDim.x) s_win[k] = 0u;
-        __syncthreads();
-    }
+    __syncthreads();
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         if (item < npieces) {
             int4 pc4 = a.pieces[item];
@@ -329,7 +315,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
                 oy = (pc4.z / a.nbx) * PGB_BIN - PGB_HALO;
             }
             for (int t = pc4.x; t < pc4.x + pc4.y && t < ntiles; ++t)
-                push_tile<DEP>(a, pc, t, n, win, ox, oy);
+                push_tile<DEP>(a, pc, t, n, win, ox, oy, s_cnt, it);
             if (win) {
                 __syncthreads();
                 /* a warp per window row, a lane per node: add the non-zero
@@ -351,7 +337,7 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS, 4) k_push(PushArgs a) {
                 __syncthreads();
             }
         } else {
-            push_tile<DEP>(a, pc, tile0 + (item - npieces), n, nullptr, 0, 0);
+            push_tile<DEP>(a, pc, tile0 + (item - npieces), n, nullptr, 0, 0, s_cnt, it);
         }
     }
 }
@@ -362,21 +348,23 @@ __global__ void __launch_bounds__(PGB_PUSH_THREADS) k_flag(const float4* xv, Dev
     pgb_pdl_entry();
     const long long n = ds->n[s];
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
+    __shared__ int s_cnt[2];
+    int it = 0;
+    if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long base = (long long)tile * PGB_TILE;
-        bool f[1][PGB_ITEMS];
+        bool f[PGB_ITEMS];
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
             long long i = base + k * PGB_PUSH_THREADS + threadIdx.x;
-            f[0][k] = false;
+            f[k] = false;
             if (i >= n) continue;
             float4 p = xv[i];
             if (is_dead(p.x)) continue;
-            f[0][k] = steady ? outside_steady(p.x, p.y, nx, ny, ps) : outside_absorbing(p.x, p.y, nx, ny, ps);
+            f[k] = steady ? outside_steady(p.x, p.y, nx, ny, ps) : outside_absorbing(p.x, p.y, nx, ny, ps);
         }
-        int* const tla[1] = {tl};
-        int* const tca[1] = {tc};
-        tile_lists<1>(f, base, tile, tla, tca);
+        tile_masks(f, tile, (unsigned*)tl, tc, s_cnt, it);
     }
 }
 
@@ -510,7 +498,7 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
                 a.vz[i] = vz;
             }
         }
-        /* the tile's ionization events in slot order (as tile_lists), and its
+        /* the tile's ionization events in slot order (as tile_masks), and its
          * scattering events appended to the dense list with one counter
          * update for the tile (a counter update per warp serialised some
          * 400k atomics on one address per launch)                        */
@@ -549,7 +537,8 @@ __global__ void __launch_bounds__(MCC_THREADS, 1) k_mcc(PushArgs a, int* scat) {
 #pragma unroll
         for (int k = 0; k < PGB_ITEMS; ++k) {
             const int i = (int)(base + k * PGB_PUSH_THREADS + t);
-            if (f[k]) a.tl_ev[(long long)tile * PGB_TILE + S.off[k][warp] + __popc(m[k] & lt)] = i;
+            /* the ionization events as the tile's mask words (tile_masks) */
+            if (lane == 0) ((unsigned*)a.tl_ev)[(long long)tile * 32 + k * (PGB_PUSH_THREADS / 32) + warp] = m[k];
             if (sc[k]) scat[S.sbase + S.soff[k][warp] + __popc(ms[k] & lt)] = (int)((unsigned)i | (f[k] ? MCC_ION_BIT : 0u));
         }
         group_sync(g);
@@ -651,19 +640,36 @@ __global__ void __launch_bounds__(1024) k_scan_list(const int* cnt, int* off, co
     if (threadIdx.x == 0) *total = t;
 }
 
-/* gather per-tile lists into one dense list in slot order.  A warp per
- * tile: lists hold about one particle in a hundred, so a tile has a few
- * entries, and a block walking its tiles one after another would wait on
- * each tile's count and offset in turn.                                 */
+/* gather per-tile lists (32 mask words a tile, see tile_masks) into one
+ * dense list in slot order.  A warp per tile, a lane per word: a shuffle
+ * scan of the words' counts gives each word's place, then each lane writes
+ * the slots of its set bits.                                             */
 __global__ void k_gather_lists(const int* tl, const int* tc, const int* toff, const long long* n_ptr, int* out) {
     pgb_pdl_entry();
     const long long n = *n_ptr;
     const int ntiles = (int)((n + PGB_TILE - 1) / PGB_TILE);
     const int lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
+    const unsigned* masks = (const unsigned*)tl;
     for (int t = blockIdx.x * wpb + (threadIdx.x >> 5); t < ntiles; t += gridDim.x * wpb) {
-        const int c = tc[t], o = toff[t];
-        for (int k = lane; k < c; k += 32) out[o + k] = tl[(long long)t * PGB_TILE + k];
+        if (tc[t] == 0) continue;   /* the same for every lane */
+        unsigned m = masks[(long long)t * 32 + lane];
+        const int c = __popc(m);
+        int incl = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        int pos = toff[t] + incl - c;
+        /* word lane = k * warps + w holds slots tile*TILE + k*THREADS + w*32 + bit */
+        const int sb = t * PGB_TILE + (lane / (PGB_PUSH_THREADS / 32)) * PGB_PUSH_THREADS +
+                       (lane % (PGB_PUSH_THREADS / 32)) * 32;
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            out[pos++] = sb + b;
+        }
     }
 }
 
