@@ -257,7 +257,7 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
             cudaGetLastError();
             return fail(r, PGB_ERR_NOMEM, "device allocation of sort scratch failed");
         }
-        long long cxt = (lc + 4096 - 1) / 4096 + 1;
+        long long cxt = (lc + PGB_CX_TILE - 1) / PGB_CX_TILE + 1;
         r->cx_tiles_cap = cxt;
         r->cx_mask_words = (int)((cxt + 63) / 64);
         if (cudaMalloc(&r->cx_tile_sum, sizeof(long long) * cxt * r->nx) != cudaSuccess ||
@@ -536,7 +536,7 @@ extern "C" int pgb_footprint(const pgb_params* p, int64_t ne, int64_t ni, int64_
     b += 2 * (4 * nt + 16 * (nt + nkeys + 1));                            /* tile bins, pieces */
     const long long chunks = (lc + PGB_SORT_CHUNK - 1) / PGB_SORT_CHUNK + 1;
     b += 2 * 4 * nkeys * chunks + 4 * nkeys + 8 * (nkeys + 1);            /* sort scratch */
-    b += 8 * nx * ((lc + 4096 - 1) / 4096 + 1);                           /* CX tile sums */
+    b += 8 * nx * ((lc + PGB_CX_TILE - 1) / PGB_CX_TILE + 1) + 8 * nx * ((lc + PGB_CX_TILE - 1) / PGB_CX_TILE / 64 + 2); /* CX tile sums, masks */
     b += 48 * std::max(ne, ni);                                           /* load/dump staging */
     long long levels = 0;
     for (long long n = nx; n >= 3; n = n / 2 + 1) { levels += n * n; if (n == 3) break; }

@@ -31,6 +31,7 @@
 #define PGB_FIX_SCALE 524288.0      /* deposit fixed point: 2^19 per unit weight */
 #define PGB_FIX_SCALE_F 524288.0f
 #define PGB_MG_SMALL 65        /* levels with n <= 65 are solved by one CTA  */
+#define PGB_CX_TILE 2048       /* ions per charge-exchange tile sum            */
 #define PGB_MG_SMALL64 33      /* the same for the FP64 multigrid            */
 #define PGB_MAX_LEVELS 16
 #define PGB_BIN 32             /* bin edge in cells (spatial sort)            */

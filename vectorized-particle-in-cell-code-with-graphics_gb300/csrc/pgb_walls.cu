@@ -439,9 +439,17 @@ __global__ void __launch_bounds__(1024) k_steady(WallArgs a, int* ion_by_rank) {
  * kept in fixed point (2^40 per unit), so sums are exact and independent
  * of summation order.  Pass 1: per tile of CX_TILE slots, per-column sums.
  * Pass 2: one warp per column walks the tiles, skipping whole tiles whose
- * sum cannot cross 1 and scanning the others element by element.        */
-#define CX_TILE 4096
+ * sum cannot cross 1 and scanning the others element by element.
+ * The tile sums are built in shared memory from two 32-bit atomics per ion
+ * (the low 20 bits of its fixed-point probability, then the rest): 64-bit
+ * shared atomics are compare-and-swap loops on this GPU, and the ions of a
+ * sorted tile share a few dozen columns, so those loops contended (argon,
+ * where every ion has a probability: 0.22 ms of a 0.46 ms step at 129^2).
+ * A probability is at most 2^40, so with 2048 ions a tile neither 32-bit
+ * sum can reach 2^32.                                                     */
+#define CX_TILE PGB_CX_TILE
 #define CX_ONE (1ll << 40)
+static_assert((long long)CX_TILE << 20 <= (1ll << 31), "32-bit halves of the tile sums must not overflow");
 
 struct CxArgs {
     Species i;
@@ -492,12 +500,17 @@ __device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, fl
 
 __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
     pgb_pdl_entry();
-    extern __shared__ unsigned long long s_sum[];
+    extern __shared__ unsigned int s_sum32[];
+    unsigned int* const s_lo = s_sum32;          /* low 20 bits of the probabilities */
+    unsigned int* const s_hi = s_sum32 + a.nx;   /* the rest (>> 20)                  */
     long long i0, n;
     cx_range(a, i0, n);
     const int ntiles = (int)((n - i0 + CX_TILE - 1) / CX_TILE);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) s_sum[c] = 0ull;
+        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) {
+            s_lo[c] = 0u;
+            s_hi[c] = 0u;
+        }
         __syncthreads();
         /* four ions per thread in flight at a time */
         for (int k0 = threadIdx.x; k0 < CX_TILE; k0 += 4 * blockDim.x) {
@@ -517,7 +530,11 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
             for (int q = 0; q < 4; ++q) {
                 int col;
                 long long pf = cx_prob_fixed(a, p[q], vz[q], col);
-                if (col >= 0 && pf) atomicAdd(&s_sum[col], (unsigned long long)pf);
+                if (col >= 0 && pf) {
+                    atomicAdd(&s_lo[col], (unsigned int)(pf & 0xFFFFF));
+                    const unsigned int hi = (unsigned int)(pf >> 20);
+                    if (hi) atomicAdd(&s_hi[col], hi);
+                }
             }
         }
         __syncthreads();
@@ -525,7 +542,7 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
          * added to its total): where no ion can exchange (the H fit is 0 at
          * any ion energy above 1e-14 eV) a pass writes nothing            */
         for (int c = threadIdx.x; c < a.nx; c += blockDim.x) {
-            const unsigned long long v = s_sum[c];
+            const unsigned long long v = ((unsigned long long)s_hi[c] << 20) + s_lo[c];
             if (v) {
                 a.tile_sum[(long long)c * a.ntl + t] = (long long)v;
                 atomicOr(&a.mask[(long long)c * a.mw + (t >> 6)], 1ull << (t & 63));
@@ -692,7 +709,7 @@ int pgb_launch_cx(pgb_run* r, int tail, int leave_sms) {
     a.neut_i = r->neut[1];
     a.seed = r->p.seed;
     const int sms = r->sms - leave_sms > 8 ? r->sms - leave_sms : 8;
-    PGB_CK(r, pgb_launch_pdl(k_cx_tiles, dim3(sms * 4), dim3(256), sizeof(unsigned long long) * r->nx, r->stream, a));
+    PGB_CK(r, pgb_launch_pdl(k_cx_tiles, dim3(sms * 4), dim3(256), 2 * sizeof(unsigned int) * r->nx, r->stream, a));
     r->launches++;
     int warps = 8;
     PGB_CK(r, pgb_launch_pdl(k_cx_walk, dim3((r->nx + warps - 1) / warps), dim3(warps * 32), 0, r->stream, a));
