@@ -506,6 +506,8 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
     long long i0, n;
     cx_range(a, i0, n);
     const int ntiles = (int)((n - i0 + CX_TILE - 1) / CX_TILE);
+    /* H+-H with the fit: vz is read only for the rare ion that needs it */
+    const bool h_fit = a.cc.species == PGB_HYDROGEN && !a.cc.cx_const;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         for (int c = threadIdx.x; c < a.nx; c += blockDim.x) {
             s_lo[c] = 0u;
@@ -523,11 +525,21 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
                 vz[q] = 0.f;
                 if (k0 + q * blockDim.x < CX_TILE && i < n) {
                     p[q] = a.i.xv[i];
-                    vz[q] = a.i.vz[i];
+                    if (!h_fit) vz[q] = a.i.vz[i];
                 }
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
+                if (h_fit) {
+                    /* the H fit is 0 where e / (1000 AMU) >= 2e10 (sig_h_cx),
+                     * and e >= e_xy = ecoef (vx^2 + vy^2) also after rounding
+                     * (adding vz^2 >= 0 and scaling by ecoef > 0 are monotone):
+                     * such an ion's probability is 0 without its vz            */
+                    const float exy = __fmul_rn(a.ecoef, __fadd_rn(__fmul_rn(p[q].z, p[q].z), __fmul_rn(p[q].w, p[q].w)));
+                    if (exy * (1.0f / (1000.0f * 1.66054e-27f)) >= 2.0e10f) continue;
+                    const long long i = i0 + (long long)t * CX_TILE + k0 + q * blockDim.x;
+                    if (k0 + q * blockDim.x < CX_TILE && i < n) vz[q] = a.i.vz[i];
+                }
                 int col;
                 long long pf = cx_prob_fixed(a, p[q], vz[q], col);
                 if (col >= 0 && pf) {
