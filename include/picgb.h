@@ -249,7 +249,7 @@ PGB_API int pgb_get_stream(pgb_run* run, void** stream);
 /* Launch shapes (no reference counterpart).  They change no result, only
  * speed: the push kernels' grid is the SM count times push_blocks_per_sm
  * (four 256-thread blocks fit on an SM, default 8), and the collision
- * kernels that run beside the previous step's field solve leave it
+ * test, which runs beside the previous step's field solve, leaves it
  * field_sms SMs (default 32).                                             */
 typedef struct pgb_launch_config {
     int32_t push_blocks_per_sm;
