@@ -322,7 +322,7 @@ def test_phase_entry_points_equal_fused_step():
 
 # ------------------------------------------------------------ solver modes
 @pytest.mark.parametrize("n", [129, 513])
-def test_fmg32_within_1e5_of_reference_schedule(n):
+def test_fmg32_phi_within_2e5_e_within_1e5_of_reference_schedule(n):
     """FMG32 runs the reference's schedule in FP32: phi within 2e-5 and E
     within 1e-5 of the FP64 result (max norm relative to the max; the FP32
     rounding of ~16 sweep-equivalents at 513^2 reaches 1.4e-5 on phi, while
