@@ -837,9 +837,12 @@ static int step_particles(pgb_run* r, bool ion_step) {
     if (r->p.number_to_inject > 0 && pgb_launch_inject(r, 3, true)) return PGB_ERR_CUDA;
     PROF_MARK(r, 2);
     if (ion_step) {
-        /* charge exchange of the ions appended since the collision pass */
+        /* charge exchange of the ions appended since the collision pass:
+         * without steady-state re-insertion only the injected ones (the
+         * ionization products of an ion step are not stored), one block  */
         const bool appended = r->p.number_to_inject > 0 || r->p.steadystate;
-        if (coll && appended && pgb_launch_cx(r, 1, 0)) return PGB_ERR_CUDA;
+        const bool few = !r->p.steadystate && r->p.number_to_inject <= 4096;
+        if (coll && appended && pgb_launch_cx(r, few ? 2 : 1, 0)) return PGB_ERR_CUDA;
         PROF_MARK(r, 3);
         if (pgb_launch_push(r, 1, true)) return PGB_ERR_CUDA;
         if (pgb_build_list(r, LIST_OUT_I, 1)) return PGB_ERR_CUDA;

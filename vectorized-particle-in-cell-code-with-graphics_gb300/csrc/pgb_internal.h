@@ -296,7 +296,8 @@ int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e);
 int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i);
 int pgb_launch_mcc(pgb_run* r, int leave_sms);
 int pgb_launch_scatter(pgb_run* r, int leave_sms);
-/* tail 0: the ions present (records their count); 1: those appended since */
+/* tail 0: the ions present (records their count); 1: those appended since;
+ * 2: the same in one block, for a tail of a few thousand ions at most     */
 int pgb_launch_cx(pgb_run* r, int tail, int leave_sms);
 int pgb_launch_walls(pgb_run* r, int which);
 int pgb_launch_load(pgb_run* r, int s, const double* d_aos, long long i0, long long i1);

@@ -1144,9 +1144,11 @@ int pgb_launch_ionize_appends(pgb_run* r, int store_e, int store_i) {
     a.dx = r->dx; a.dy = r->dy; a.ps = r->ps;
     a.store_e = store_e;
     a.store_i = store_i;
-    PGB_CK(r, pgb_launch_pdl(k_ionize_append, dim3(r->sms * 2), dim3(256), 0, r->stream, a));
-    r->launches++;
-    PGB_CK(r, cudaGetLastError());
+    if (store_e || store_i) {   /* else the products are only counted */
+        PGB_CK(r, pgb_launch_pdl(k_ionize_append, dim3(r->sms * 2), dim3(256), 0, r->stream, a));
+        r->launches++;
+        PGB_CK(r, cudaGetLastError());
+    }
     PGB_CK(r, pgb_launch_pdl(k_ionize_commit, dim3(1), dim3(1), 0, r->stream, r->ds, a.store_e, a.store_i, r->sp[0].cap, r->sp[1].cap));
     r->launches++;
     PGB_CK(r, cudaGetLastError());

@@ -498,6 +498,21 @@ __device__ __forceinline__ long long cx_prob_fixed(const CxArgs& a, float4 p, fl
     return __float2ll_rn(P * 1099511627776.0f);   /* P * 2^40, exact scaling */
 }
 
+/* charge_exchange_velocity (ion_collisions.cpp:209-221): ion i takes a
+ * neutral's velocity from the table, picked by its CX stream            */
+__device__ __forceinline__ void cx_exchange(const CxArgs& a, long long i) {
+    pgb_stream st;
+    pgb_stream_init(&st, a.seed, a.i.id[i], (unsigned int)a.ds->t, PGB_STREAM_CX, 1);
+    (void)pgb_stream_u32(&st);
+    int nn = a.cc.n_neutral;
+    int index = (int)(pgb_stream_u32(&st) % (uint32_t)(nn - 1));
+    float4 p = a.i.xv[i];
+    p.z = a.neut_i[index];
+    p.w = a.neut_i[nn + index];
+    a.i.xv[i] = p;
+    a.i.vz[i] = a.neut_i[2 * nn + index];
+}
+
 __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
     pgb_pdl_entry();
     extern __shared__ unsigned int s_sum32[];
@@ -623,19 +638,7 @@ __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
                 acc += v;
                 if (acc > CX_ONE) {
                     acc = 0;
-                    if (lane == l) {
-                        /* charge_exchange_velocity (ion_collisions.cpp:209-221) */
-                        pgb_stream st;
-                        pgb_stream_init(&st, a.seed, a.i.id[i], (unsigned int)a.ds->t, PGB_STREAM_CX, 1);
-                        (void)pgb_stream_u32(&st);
-                        int nn = a.cc.n_neutral;
-                        int index = (int)(pgb_stream_u32(&st) % (uint32_t)(nn - 1));
-                        float4 p = a.i.xv[i];
-                        p.z = a.neut_i[index];
-                        p.w = a.neut_i[nn + index];
-                        a.i.xv[i] = p;
-                        a.i.vz[i] = a.neut_i[2 * nn + index];
-                    }
+                    if (lane == l) cx_exchange(a, i);
                     fired++;
                 }
             }
@@ -649,6 +652,58 @@ __global__ void __launch_bounds__(256) k_cx_walk(CxArgs a) {
         a.col_acc[col] = acc;
         a.total[col] = 0;
         if (fired) atomicAdd((unsigned long long*)&a.ds->stats[ST_CX], (unsigned long long)fired);
+    }
+}
+
+/* The charge exchange of the few ions appended since pass 1 (the injected
+ * ones), in one block: their probabilities go to shared memory 256 at a
+ * time, then each column's accumulator continues over them in slot order,
+ * as k_cx_tiles + k_cx_walk would take it.                               */
+__global__ void __launch_bounds__(256) k_cx_tail_small(CxArgs a) {
+    pgb_pdl_entry();
+    __shared__ long long s_pf[256];
+    __shared__ int s_col[256];
+    long long i0, n;
+    cx_range(a, i0, n);
+    int fired = 0;
+    for (long long b = i0; b < n; b += 256) {
+        const long long i = b + threadIdx.x;
+        int col = -1;
+        long long pf = 0;
+        if (i < n) pf = cx_prob_fixed(a, a.i.xv[i], a.i.vz[i], col);
+        s_pf[threadIdx.x] = pf;
+        s_col[threadIdx.x] = pf ? col : -1;
+        __syncthreads();
+        const int cnt = (int)(n - b < 256 ? n - b : 256);
+        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) {
+            long long acc = a.col_acc[c];
+            for (int j = 0; j < cnt; ++j)
+                if (s_col[j] == c) {
+                    acc += s_pf[j];
+                    if (acc > CX_ONE) {
+                        acc = 0;
+                        cx_exchange(a, b + j);
+                        fired++;
+                    }
+                }
+            a.col_acc[c] = acc;
+        }
+        __syncthreads();
+    }
+    for (int d = 16; d; d >>= 1) fired += __shfl_down_sync(0xffffffffu, fired, d);
+    if ((threadIdx.x & 31) == 0 && fired) atomicAdd((unsigned long long*)&a.ds->stats[ST_CX], (unsigned long long)fired);
+}
+
+/* the ion walls without ion-impact emission: every listed ion is removed
+ * (k_iwall1's yield is 0 there, so no secondary and nothing to scan)     */
+__global__ void k_iwall_absorb(WallArgs a) {
+    pgb_pdl_entry();
+    const long long m = a.ds->list_n[LIST_OUT_I];
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x)
+        a.i.xv[a.list_i[k]].x = pos_dead();
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.ds->stats[ST_ABS_I] += m;
+        a.ds->dead[1] += m;
     }
 }
 
@@ -683,7 +738,10 @@ int pgb_launch_walls(pgb_run* r, int which) {
         }
         return 0;
     }
-    if (which == PGB_BOUNDARY_IONS) {
+    if (which == PGB_BOUNDARY_IONS && !a.ion_see) {
+        PGB_CK(r, pgb_launch_pdl(k_iwall_absorb, dim3(g), dim3(256), 0, r->stream, a));
+        r->launches++;
+    } else if (which == PGB_BOUNDARY_IONS) {
         PGB_CK(r, pgb_launch_pdl(k_iwall1, dim3(g), dim3(256), 0, r->stream, a));
         r->launches++;
         PGB_CK(r, pgb_launch_pdl(k_scan_list, dim3(1), dim3(1024), 0, r->stream, r->aux_i, r->aux_j, &r->ds->list_n[LIST_OUT_I], &r->ds->list_n[LIST_SPARE]));
@@ -708,7 +766,7 @@ int pgb_launch_walls(pgb_run* r, int which) {
 
 int pgb_launch_cx(pgb_run* r, int tail, int leave_sms) {
     CxArgs a;
-    a.tail = tail;
+    a.tail = tail ? 1 : 0;
     a.i = r->sp[1]; a.ds = r->ds; a.nx = r->nx; a.ny = r->ny; a.ps = r->ps;
     a.cc = pgb_coll_consts(r);
     a.pcoef = a.cc.i_pcoef; a.ecoef = a.cc.i_energy_coef;
@@ -720,6 +778,12 @@ int pgb_launch_cx(pgb_run* r, int tail, int leave_sms) {
     a.col_acc = (long long*)r->prob_cx;
     a.neut_i = r->neut[1];
     a.seed = r->p.seed;
+    if (tail == 2) {
+        PGB_CK(r, pgb_launch_pdl(k_cx_tail_small, dim3(1), dim3(256), 0, r->stream, a));
+        r->launches++;
+        PGB_CK(r, cudaGetLastError());
+        return 0;
+    }
     const int sms = r->sms - leave_sms > 8 ? r->sms - leave_sms : 8;
     PGB_CK(r, pgb_launch_pdl(k_cx_tiles, dim3(sms * 4), dim3(256), 2 * sizeof(unsigned int) * r->nx, r->stream, a));
     r->launches++;
