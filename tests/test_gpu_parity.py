@@ -393,6 +393,34 @@ def test_sine_transform_solve_reaches_exact_solution(n):
         assert errs[passes] <= tol, (passes, errs)
 
 
+@pytest.mark.parametrize("n", [257, 513])
+def test_sine_transform_solve_with_wall_potentials(n):
+    """DST_DC with every wall at its own potential and the right wall
+    oscillating (PHI_PERIOD): the walls' FP64 solutions lifted out of the
+    FP32 transform, scaled by the right wall's value at each step, give the
+    converged FP64 solution of the oracle within 1e-9 (two passes) at two
+    different steps."""
+    kw = dict(X_NO_OF_CELLS=n, PHI_RIGHT=1.5, PHI_LEFT=-0.5, PHI_TOP=0.25, PHI_BOTTOM=0.1, PHI_PERIOD=0.02)
+    rng = np.random.default_rng(n + 4)
+    sgrid = np.linspace(0, 1, n)
+    X, Y = np.meshgrid(sgrid, sgrid)
+    rho = 1e-6 * np.sin(3 * X) * np.cos(2 * Y) + 1e-8 * rng.standard_normal((n, n))
+    p = picgb.make_params(POISSON="DST_DC", DC_MAX_ITERS=2, **kw)
+    with picgb.Run(p) as r:
+        for t in (7, 40):
+            o = orc.Oracle(p)
+            o.set_rho(rho)
+            o.poisson_converged(t, 30)
+            o.efield()
+            r.set_rho(rho)
+            r.poisson(t)
+            r.efield()
+            for grid in ("phi", "ex", "ey"):
+                e = rel_err(r.get_grid(grid), o.get_grid(grid))
+                print(n, t, grid, e)
+                assert e <= 1e-9, (n, t, grid, e)
+
+
 def test_sine_transform_solve_of_one_mode():
     """rho = one sine mode of the grid: the discrete solution is the mode
     divided by its eigenvalue -(s_k + s_l)/h^2, s_k = 4 sin^2(pi k/2N).  One

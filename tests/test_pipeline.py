@@ -35,12 +35,17 @@ def _gaussian(p, n, te, ti, seed):
     return out
 
 
+_H129 = dict(X_NO_OF_CELLS=129, TEMPERATURE=3.0, ION_MASS_AMU=1.0, THRESHOLD=13.6, SPECIES="HYDROGEN",
+             HAVE_COLLISIONS=True, SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT",
+             SIGMA_IONIZATION="ENERGY_DEPENDENT", E_IMPACT_SEE="YES", REFLECTION="YES", BACKSCATTER="YES",
+             STEADYSTATE="NO", NUMBER_TO_INJECT=10, SIZE_TO_CHECK=2**31 - 1, SORT_INTERVAL=4, POISSON="FMG32")
+
+
 def _case(name):
-    if name == "h_sorted_129":
-        kw = dict(X_NO_OF_CELLS=129, TEMPERATURE=3.0, ION_MASS_AMU=1.0, THRESHOLD=13.6, SPECIES="HYDROGEN",
-                  HAVE_COLLISIONS=True, SIGMA="ENERGY_DEPENDENT", SIGMA_ELASTIC="ENERGY_DEPENDENT",
-                  SIGMA_IONIZATION="ENERGY_DEPENDENT", E_IMPACT_SEE="YES", REFLECTION="YES", BACKSCATTER="YES",
-                  STEADYSTATE="NO", NUMBER_TO_INJECT=10, SIZE_TO_CHECK=2**31 - 1, SORT_INTERVAL=4, POISSON="FMG32")
+    if name in ("h_sorted_129", "h_sorted_129_dst"):
+        kw = dict(_H129)
+        if name.endswith("_dst"):
+            kw.update(POISSON="DST_DC", DC_MAX_ITERS=2)
         n = 60000
         L = picgb.make_params(**kw).xlength
         p = picgb.make_params(E_MACROPARTICLE_SIZE=1.0e15 * L * L / n, ION_MACROPARTICLE_SIZE=1.0e15 * L * L / n, **kw)
@@ -74,10 +79,10 @@ def _run(p, e, i, n, mode, window=None):
         return out
 
 
-@pytest.mark.parametrize("name", ["arcoll33", "arsee33", "hsee33", "arcoll33_dti2", "h_sorted_129"])
+@pytest.mark.parametrize("name", ["arcoll33", "arsee33", "hsee33", "arcoll33_dti2", "h_sorted_129", "h_sorted_129_dst"])
 def test_pipelined_steps_equal_steps_in_order(name):
     p, e, i, n = _case(name)
-    window = (2, n - 2) if name in ("arsee33", "h_sorted_129") else None
+    window = (2, n - 2) if name in ("arsee33", "h_sorted_129", "h_sorted_129_dst") else None
     res = {m: _run(p, e, i, n, m, window) for m in ("in order", "pipelined", "one call per step")}
     ref = res["in order"]
     assert ref[7]["n_e"] > 0
