@@ -223,7 +223,8 @@ static int ensure_capacity(pgb_run* r, int s, long long need) {
         free_lists(r);
         long long nt = (lc + PGB_TILE - 1) / PGB_TILE + 1;
         for (int l = 0; l < 4; ++l) {
-            if (cudaMalloc(&r->tile_list[l], sizeof(int) * nt * PGB_TILE) != cudaSuccess ||
+            /* a tile's list is its 32 ballot words (tile_masks) */
+            if (cudaMalloc(&r->tile_list[l], sizeof(int) * nt * 32) != cudaSuccess ||
                 cudaMalloc(&r->tile_cnt[l], sizeof(int) * nt) != cudaSuccess ||
                 cudaMalloc(&r->list[l], sizeof(int) * lc) != cudaSuccess) {
                 cudaGetLastError();
@@ -531,7 +532,7 @@ extern "C" int pgb_footprint(const pgb_params* p, int64_t ne, int64_t ni, int64_
     const long long nbx = (nx - 1 + PGB_BIN - 1) / PGB_BIN, nby = (ny - 1 + PGB_BIN - 1) / PGB_BIN, nkeys = nbx * nby + 1;
     long long b = 0;
     b += 2 * (16 + 4 + 4 + 4) * (ce + ci);                               /* particles, two copies */
-    b += 4 * (4 * nt * PGB_TILE + 4 * nt + 4 * lc);                      /* event lists */
+    b += 4 * (4 * nt * 32 + 4 * nt + 4 * lc);                            /* event lists (32 mask words a tile) */
     b += 2 * 4 * std::max(lc, nt);                                        /* aux_i, aux_j */
     b += 2 * (4 * nt + 16 * (nt + nkeys + 1));                            /* tile bins, pieces */
     const long long chunks = (lc + PGB_SORT_CHUNK - 1) / PGB_SORT_CHUNK + 1;

@@ -148,7 +148,8 @@ struct pgb_run {
      * buffer and writes another: blocks never see a neighbour's update)  */
     double* mg_w[PGB_MAX_LEVELS] = {};
     float* mg32_w[PGB_MAX_LEVELS] = {};
-    /* event lists */
+    /* event lists: per tile 32 ballot words (slot order) and a count, then
+     * the dense list in slot order                                       */
     int* tile_list[4] = {nullptr, nullptr, nullptr, nullptr};
     int* tile_cnt[4] = {nullptr, nullptr, nullptr, nullptr};
     int* list[4] = {nullptr, nullptr, nullptr, nullptr};
