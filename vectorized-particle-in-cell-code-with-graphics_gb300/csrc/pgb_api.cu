@@ -806,7 +806,10 @@ static int mcc_part(pgb_run* r, int leave_sms, bool ion_step) {
      * higher priority, when it has not ended)                             */
     if (pgb_launch_scatter(r, 0)) return PGB_ERR_CUDA;
     PROF_MARK(r, 10);
-    if (pgb_build_list(r, LIST_ION_EV, 0)) return PGB_ERR_CUDA;
+    /* the ionization products are stored (so the event list is read) only
+     * with steady-state walls or off ion steps; else only their number is */
+    const bool products = r->p.steadystate || !ion_step;
+    if (pgb_build_list(r, LIST_ION_EV, 0, !products)) return PGB_ERR_CUDA;
     PROF_MARK(r, 11);
     if (ion_step && pgb_launch_cx(r, 0, 0)) return PGB_ERR_CUDA;
     PROF_MARK(r, 12);

@@ -290,7 +290,8 @@ inline cudaError_t pgb_launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, si
 struct CollConsts;
 int pgb_launch_push(pgb_run* r, int s, bool deposit);
 int pgb_launch_flag_outside(pgb_run* r, int s);
-int pgb_build_list(pgb_run* r, int which, int species_for_tiles);
+/* count_only: the list's length alone (ds->list_n), not the list */
+int pgb_build_list(pgb_run* r, int which, int species_for_tiles, bool count_only = false);
 int pgb_launch_deposit(pgb_run* r, int s);
 int pgb_launch_finalize(pgb_run* r, int which_species_mask, bool make_rhs);
 int pgb_launch_inject(pgb_run* r, int species_mask, bool push_e);

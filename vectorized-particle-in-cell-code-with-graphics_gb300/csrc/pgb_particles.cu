@@ -1101,10 +1101,11 @@ int pgb_launch_scatter(pgb_run* r, int leave_sms) {
 }
 
 /* per-tile list `which` (tiles of species s) -> dense list + count */
-int pgb_build_list(pgb_run* r, int which, int s) {
+int pgb_build_list(pgb_run* r, int which, int s, bool count_only) {
     int* toff = r->aux_j;
     PGB_CK(r, pgb_launch_pdl(k_scan_small, dim3(1), dim3(1024), 0, r->stream, r->tile_cnt[which], toff, &r->ds->n[s], 0, &r->ds->list_n[which]));
     r->launches++;
+    if (count_only) return 0;
     PGB_CK(r, pgb_launch_pdl(k_gather_lists, dim3(grid_for(r, 4)), dim3(256), 0, r->stream, r->tile_list[which], r->tile_cnt[which], toff,
                                                            &r->ds->n[s], r->list[which]));
     r->launches++;
