@@ -550,8 +550,8 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
                      * and e >= e_xy = ecoef (vx^2 + vy^2) also after rounding
                      * (adding vz^2 >= 0 and scaling by ecoef > 0 are monotone):
                      * such an ion's probability is 0 without its vz            */
-                    const float exy = __fmul_rn(a.ecoef, __fadd_rn(__fmul_rn(p[q].z, p[q].z), __fmul_rn(p[q].w, p[q].w)));
-                    if (exy * (1.0f / (1000.0f * 1.66054e-27f)) >= 2.0e10f) continue;
+                    const float e_xy = __fmul_rn(a.ecoef, __fadd_rn(__fmul_rn(p[q].z, p[q].z), __fmul_rn(p[q].w, p[q].w)));
+                    if (e_xy * (1.0f / (1000.0f * 1.66054e-27f)) >= 2.0e10f) continue;
                     const long long i = i0 + (long long)t * CX_TILE + k0 + q * blockDim.x;
                     if (k0 + q * blockDim.x < CX_TILE && i < n) vz[q] = a.i.vz[i];
                 }
