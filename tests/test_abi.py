@@ -62,6 +62,18 @@ def test_create_rejects_bad_grid(lib):
     assert b"power of 2" in lib.pgb_last_error(None)
 
 
+def test_create_rejects_unknown_poisson_mode_and_pass_count(lib):
+    import picgb
+    for field, value, text in (("poisson_mode", 7, b"poisson_mode"), ("dc_max_iters", -1, b"dc_max_iters"),
+                               ("dc_max_iters", 65, b"dc_max_iters")):
+        p = picgb.make_params(X_NO_OF_CELLS=33)
+        setattr(p, field, value)
+        h = C.c_void_p()
+        rc = lib.pgb_create(C.byref(p), C.byref(h))
+        assert rc == -1 and not h.value, field
+        assert text in lib.pgb_last_error(None), field
+
+
 def test_no_silent_cpu_fallback_without_a_gpu(lib):
     """Without a usable GPU the library reports a CUDA error; it never
     computes on the host instead."""

@@ -137,6 +137,11 @@ static int validate(const pgb_params* p, std::string& why) {
     if (!(p->xlength > 0) || !(p->ylength > 0) || !(p->dt > 0) || !(p->dti > 0)) { why = "lengths and time steps must be positive"; return 0; }
     if (p->init_no_neutrals < 2) { why = "INIT_NO_NEUTRALS must be >= 2"; return 0; }
     if (p->no_groups < 1 || p->no_groups > 3) { why = "NO_GROUPS must be 1..3"; return 0; }
+    if (p->poisson_mode < PGB_POISSON_FMG_REF || p->poisson_mode > PGB_POISSON_DST_DC) {
+        why = "poisson_mode must be one of PGB_POISSON_FMG_REF, _FP32_DC, _FMG32, _DST_DC";
+        return 0;
+    }
+    if (p->dc_max_iters < 0 || p->dc_max_iters > 64) { why = "dc_max_iters must be 0..64"; return 0; }
     return 1;
 }
 
