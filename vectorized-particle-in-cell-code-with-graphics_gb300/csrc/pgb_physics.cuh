@@ -58,12 +58,13 @@ __device__ __forceinline__ int pcell(float lane, int ps) {
 /* x > 0 and (int)(x/DX) < n, in one unsigned compare: 0 < x < n*2^ps
  * (false for the tombstone and NaN codes)                                */
 __device__ __forceinline__ bool pos_open_in(float lane, int n, int ps) {
-    return (unsigned)(__float_as_int(lane) - 1) < (unsigned)((n << ps) - 1);
+    /* in unsigned arithmetic: x - 1 wraps for the codes at INT_MIN */
+    return (unsigned)__float_as_int(lane) - 1u < (unsigned)((n << ps) - 1);
 }
 /* 0 <= (int)(x/DX) < n (truncation toward zero): -2^ps < x < n*2^ps; false
  * for the tombstone and NaN codes, whose cell index is INT_MIN           */
 __device__ __forceinline__ bool pos_trunc_in(float lane, int n, int ps) {
-    return (unsigned)(__float_as_int(lane) + (1 << ps) - 1) < (unsigned)((n << ps) + (1 << ps) - 1);
+    return (unsigned)__float_as_int(lane) + (unsigned)((1 << ps) - 1) < (unsigned)((n << ps) + (1 << ps) - 1);
 }
 /* x > 0 and x < 0 (NaN is neither)                                        */
 __device__ __forceinline__ bool pos_gt0(float lane) { return __float_as_int(lane) > 0; }
