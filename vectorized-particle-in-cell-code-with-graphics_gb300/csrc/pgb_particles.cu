@@ -15,8 +15,8 @@
  * One pass of k_push then reads a particle once (16 B, plus 4 B vz with a
  * magnetic field and 4 B weight), gathers E bilinearly from the FP32 node
  * grid (L2 resident), pushes, deposits the new position into the int64
- * fixed-point charge grid and records wall crossings in per-tile lists
- * that keep slot order.  Grids are sized from the SM count and loop over
+ * fixed-point charge grid and records wall crossings as per-tile ballot
+ * words that keep slot order.  Grids are sized from the SM count and loop over
  * tiles, reading the particle count from device memory, so a step needs
  * no host round trip.
  */
