@@ -154,3 +154,34 @@ def test_port_cross_sections_match_reference():
         e, sig, cols = z["energies"], z["sigma"], [str(c) for c in z["columns"]]
     for k, name in enumerate(cols):
         _close(orc.sigma(picgb.XS[name], e), sig[:, k], f"sigma {name}")
+
+
+@pytest.mark.parametrize("n", [65, 129])
+def test_converged_poisson_is_the_exact_discrete_solution(n):
+    """The oracle's converged solve (FP64 defect correction around its full
+    multigrid, 30 passes), the reference that DST_DC and FP32_DC are tested
+    against, equals the exact solution of the 5-point system computed a
+    different way: FP64 type-I sine transforms (scipy), whose eigenvalues
+    are -(s_k + s_l)/h^2, s_k = 4 sin^2(pi k / 2N).  Walls at 0 V, a smooth
+    charge plus white noise; max difference within 1e-12 of max |phi|."""
+    sf = pytest.importorskip("scipy.fft")
+    import picgb
+    p = picgb.make_params(X_NO_OF_CELLS=n, POISSON="DST_DC", PHI_LEFT=0.0, PHI_RIGHT=0.0, PHI_TOP=0.0,
+                          PHI_BOTTOM=0.0, PHI_PERIOD=0.0)
+    rng = np.random.default_rng(n + 5)
+    s = np.linspace(0, 1, n)
+    X, Y = np.meshgrid(s, s)
+    rho = 1e-6 * np.sin(3 * X) * np.cos(2 * Y) + 1e-7 * rng.standard_normal((n, n))
+    o = orc.Oracle(p)
+    o.set_rho(rho)
+    o.poisson_converged(0, 30)
+    phi = o.get_grid("phi")
+    N = n - 1
+    h = p.xlength / N
+    f = -rho[1:-1, 1:-1] / picgb.EPSILON
+    sk = 4 * np.sin(np.pi * np.arange(1, N) / (2 * N)) ** 2
+    lam = -(sk[:, None] + sk[None, :]) / h**2
+    u = sf.idst(sf.idst(sf.dst(sf.dst(f, type=1, axis=0), type=1, axis=1) / lam, type=1, axis=0), type=1, axis=1)
+    err = np.max(np.abs(phi[1:-1, 1:-1] - u)) / np.max(np.abs(u))
+    assert np.max(np.abs(phi[0])) == 0.0 and np.max(np.abs(phi[:, 0])) == 0.0
+    assert err <= 1e-12, err
