@@ -148,3 +148,29 @@ def test_binary_datadump_round_trips_exactly(tmp_path):
     for bad in ("bad.bin", "cut.bin"):
         with pytest.raises(picgb.PicError):
             picgb.read_datadump_bin(str(tmp_path / bad))
+
+
+def test_header_is_plain_c_and_a_c_caller_links(lib, tmp_path):
+    """include/picgb.h compiles as strict C99, and a C program links against
+    libpicgb.so and calls an entry point that needs no GPU."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    import picgb
+    src = tmp_path / "caller.c"
+    src.write_text('#include "picgb.h"\n'
+                   "int main(void) {\n"
+                   "    pgb_params p;\n"
+                   "    pgb_launch_config c = {8, 32};\n"
+                   "    (void)c;\n"
+                   "    if (pgb_params_default(&p) != 0) return 2;\n"
+                   "    return p.x_no_of_cells > 2 && p.poisson_mode == PGB_POISSON_FMG_REF ? 0 : 3;\n"
+                   "}\n")
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(picgb.library_path())
+    inc = os.path.join(REPO, "include")
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{inc}", str(src), "-o", str(exe),
+                    f"-L{libdir}", "-lpicgb", f"-Wl,-rpath,{libdir}"], check=True)
+    assert subprocess.run([str(exe)]).returncode == 0
