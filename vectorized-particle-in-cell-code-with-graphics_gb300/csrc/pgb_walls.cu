@@ -523,12 +523,14 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
     const int ntiles = (int)((n - i0 + CX_TILE - 1) / CX_TILE);
     /* H+-H with the fit: vz is read only for the rare ion that needs it */
     const bool h_fit = a.cc.species == PGB_HYDROGEN && !a.cc.cx_const;
+    /* the sums start at zero, and the scan of each tile zeroes what it reads */
+    for (int c = threadIdx.x; c < a.nx; c += blockDim.x) {
+        s_lo[c] = 0u;
+        s_hi[c] = 0u;
+    }
+    __syncthreads();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) {
-            s_lo[c] = 0u;
-            s_hi[c] = 0u;
-        }
-        __syncthreads();
+        int any = 0;   /* an ion of this tile has a non-zero probability */
         /* four ions per thread in flight at a time */
         for (int k0 = threadIdx.x; k0 < CX_TILE; k0 += 4 * blockDim.x) {
             float4 p[4];
@@ -561,22 +563,26 @@ __global__ void __launch_bounds__(256) k_cx_tiles(CxArgs a) {
                     atomicAdd(&s_lo[col], (unsigned int)(pf & 0xFFFFF));
                     const unsigned int hi = (unsigned int)(pf >> 20);
                     if (hi) atomicAdd(&s_hi[col], hi);
+                    any = 1;
                 }
             }
         }
-        __syncthreads();
         /* only non-zero sums are stored (marked in the column's bit mask and
          * added to its total): where no ion can exchange (the H fit is 0 at
-         * any ion energy above 1e-14 eV) a pass writes nothing            */
-        for (int c = threadIdx.x; c < a.nx; c += blockDim.x) {
-            const unsigned long long v = ((unsigned long long)s_hi[c] << 20) + s_lo[c];
-            if (v) {
-                a.tile_sum[(long long)c * a.ntl + t] = (long long)v;
-                atomicOr(&a.mask[(long long)c * a.mw + (t >> 6)], 1ull << (t & 63));
-                atomicAdd((unsigned long long*)&a.total[c], v);
+         * any ion energy above 1e-14 eV) a tile has none and is not scanned */
+        if (__syncthreads_or(any)) {
+            for (int c = threadIdx.x; c < a.nx; c += blockDim.x) {
+                const unsigned long long v = ((unsigned long long)s_hi[c] << 20) + s_lo[c];
+                s_lo[c] = 0u;
+                s_hi[c] = 0u;
+                if (v) {
+                    a.tile_sum[(long long)c * a.ntl + t] = (long long)v;
+                    atomicOr(&a.mask[(long long)c * a.mw + (t >> 6)], 1ull << (t & 63));
+                    atomicAdd((unsigned long long*)&a.total[c], v);
+                }
             }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
